@@ -1,0 +1,353 @@
+"""gpview_gb300 -- GB300-native two-level voxelizer (Python bindings over libgpview.so).
+
+The compute path is the C ABI in include/gpview.h, implemented by hand-written sm_103a kernels in
+csrc/.  This module binds it with ctypes and mirrors the reference's Object interface
+(includes/Object.h:106-135: ReadObject, ReadOFFObject, CreateFlatTriangleData,
+PerformVoxelization, SaveVoxelization) so reference-shaped code reads the same.
+
+There is no CPU fallback: if libgpview.so is missing or no CUDA device is present, the
+voxelization calls raise.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "libgpview.so")
+
+GPV_OK = 0
+ERRORS = {
+    -1: "GPV_ERR_INVALID", -2: "GPV_ERR_CUDA", -3: "GPV_ERR_OOM", -4: "GPV_ERR_IO",
+    -5: "GPV_ERR_PARSE", -6: "GPV_ERR_DEVICE", -7: "GPV_ERR_BUDGET", -8: "GPV_ERR_PENDING",
+    -9: "GPV_ERR_NOTFOUND",
+}
+
+
+class GpvError(RuntimeError):
+    def __init__(self, code, msg=""):
+        self.code = code
+        super().__init__(f"{ERRORS.get(code, code)}: {msg}")
+
+
+class GridSpec(C.Structure):
+    _fields_ = [("bbox_min", C.c_float * 3), ("bbox_max", C.c_float * 3),
+                ("ndiv", C.c_int32 * 3), ("ndiv2", C.c_int32 * 3)]
+
+    def __repr__(self):
+        return (f"GridSpec(min={list(self.bbox_min)}, max={list(self.bbox_max)}, "
+                f"ndiv={list(self.ndiv)}, ndiv2={list(self.ndiv2)})")
+
+
+class Work(C.Structure):
+    _fields_ = [("sat1", C.c_int64), ("sat2", C.c_int64), ("ray1", C.c_int64), ("ray2", C.c_int64)]
+
+    def total(self):
+        return self.sat1 + self.sat2 + self.ray1 + self.ray2
+
+
+class Result(C.Structure):
+    _fields_ = [("spec", GridSpec), ("grid_size", C.c_float * 3), ("grid_size2", C.c_float * 3),
+                ("num_level1", C.c_int64), ("num_boundary", C.c_int64),
+                ("num_level1_inside", C.c_int64), ("num_level2_inside", C.c_int64),
+                ("num_level2_boundary", C.c_int64), ("num_pairs", C.c_int64), ("work", Work),
+                ("level1_inout", C.c_void_p), ("level1_prefix", C.c_void_p),
+                ("boundary_index", C.c_void_p), ("level2_inout", C.c_void_p),
+                ("handle", C.c_uint64)]
+
+
+class MeshC(C.Structure):
+    _fields_ = [("tris", C.POINTER(C.c_float)), ("num_triangles", C.c_int64),
+                ("bbox_min", C.c_float * 3), ("bbox_max", C.c_float * 3),
+                ("max_model_size", C.c_float)]
+
+
+_lib = None
+
+
+def lib():
+    """Loads libgpview.so (building it first if the sources are newer)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise GpvError(-2, f"{LIB_PATH} is missing; run gpview_gb300/build.py")
+    L = C.CDLL(LIB_PATH)
+    f3 = C.POINTER(C.c_float)
+    L.gpv_init.argtypes = [C.c_int, C.POINTER(C.c_void_p)]
+    L.gpv_destroy.argtypes = [C.c_void_p]
+    L.gpv_last_error.argtypes = [C.c_void_p]
+    L.gpv_last_error.restype = C.c_char_p
+    L.gpv_set_tile.argtypes = [C.c_void_p, C.c_int]
+    L.gpv_grid_padded.argtypes = [f3, f3, C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.POINTER(GridSpec)]
+    L.gpv_grid_reference.argtypes = [f3, f3, C.c_float, C.c_int32, C.c_int32, C.POINTER(GridSpec)]
+    L.gpv_voxelize.argtypes = [C.c_void_p, C.c_void_p, C.c_int64, C.POINTER(GridSpec),
+                               C.POINTER(Result), C.c_void_p]
+    L.gpv_voxelize_host.argtypes = [C.c_void_p, C.c_void_p, C.c_int64, C.POINTER(GridSpec),
+                                    C.POINTER(Result), C.c_void_p]
+    L.gpv_result_copy_to_host.argtypes = [C.c_void_p, C.POINTER(Result), C.c_void_p, C.c_void_p,
+                                          C.c_void_p, C.c_void_p, C.c_void_p]
+    L.gpv_result_release.argtypes = [C.c_void_p, C.POINTER(Result)]
+    L.gpv_load_obj.argtypes = [C.c_char_p, C.POINTER(MeshC)]
+    L.gpv_load_off.argtypes = [C.c_char_p, C.POINTER(MeshC)]
+    L.gpv_mesh_free.argtypes = [C.POINTER(MeshC)]
+    L.gpv_write_raw.argtypes = [C.c_char_p, C.POINTER(Result), C.c_void_p, C.c_void_p, C.c_void_p]
+    for name, extra in (("gpv_gen_uvsphere", [C.c_int32, C.c_int32, f3, C.c_float, C.c_float]),
+                        ("gpv_gen_torus", [C.c_int32, C.c_int32, f3, C.c_float, C.c_float, C.c_float]),
+                        ("gpv_gen_star", [C.c_int32, f3, C.c_float, C.c_float, f3]),
+                        ("gpv_gen_superellipsoid", [C.c_int32, C.c_int32, f3, f3, C.c_float,
+                                                    C.c_float, f3])):
+        fn = getattr(L, name)
+        fn.argtypes = [C.c_uint64, *extra, C.c_void_p]
+        fn.restype = C.c_int64
+    if hasattr(L, "gpv_voxelize_batch"):
+        L.gpv_voxelize_batch.argtypes = [C.c_void_p, C.c_int32, C.POINTER(C.c_void_p),
+                                         C.POINTER(C.c_int64), C.POINTER(GridSpec),
+                                         C.POINTER(Result), C.c_void_p]
+    _lib = L
+    return L
+
+
+def _f3(v):
+    return (C.c_float * 3)(*[float(x) for x in v])
+
+
+def _i3(v):
+    return (C.c_int32 * 3)(*[int(x) for x in v])
+
+
+# ---- grids ------------------------------------------------------------------------------------
+def grid_padded(mesh_min, mesh_max, ndiv, ndiv2=(0, 0, 0)):
+    """n^3 cells over the mesh box grown by one cell on each side."""
+    if np.isscalar(ndiv):
+        ndiv = (ndiv,) * 3
+    if np.isscalar(ndiv2):
+        ndiv2 = (ndiv2,) * 3
+    s = GridSpec()
+    rc = lib().gpv_grid_padded(_f3(mesh_min), _f3(mesh_max), _i3(ndiv), _i3(ndiv2), C.byref(s))
+    if rc:
+        raise GpvError(rc, "grid_padded")
+    return s
+
+
+def grid_reference(bbox_min, bbox_max, max_model_size, voxel_count=8, voxel_count2=4):
+    """GPView's own sizing from GLParameters::voxelCount / voxelCount2."""
+    s = GridSpec()
+    rc = lib().gpv_grid_reference(_f3(bbox_min), _f3(bbox_max), float(max_model_size),
+                                  int(voxel_count), int(voxel_count2), C.byref(s))
+    if rc:
+        raise GpvError(rc, "grid_reference")
+    return s
+
+
+def mesh_bounds(tris):
+    v = np.asarray(tris, dtype=np.float32).reshape(-1, 3)
+    return v.min(axis=0), v.max(axis=0)
+
+
+# ---- synthetic meshes -------------------------------------------------------------------------
+def _gen(name, seed, *args):
+    fn = getattr(lib(), name)
+    n = fn(C.c_uint64(seed), *args, None)
+    out = np.empty(9 * n, dtype=np.float32)
+    got = fn(C.c_uint64(seed), *args, out.ctypes.data_as(C.c_void_p))
+    assert got == n
+    return out
+
+
+def gen_uvsphere(seed, nlon=128, nlat=64, center=(0.5, 0.5, 0.5), radius=0.4, jitter=0.002):
+    return _gen("gpv_gen_uvsphere", seed, int(nlon), int(nlat), _f3(center), float(radius),
+                float(jitter))
+
+
+def gen_torus(seed, nu=512, nv=256, center=(0.5, 0.5, 0.5), R=0.35, r=0.12, noise=0.01):
+    return _gen("gpv_gen_torus", seed, int(nu), int(nv), _f3(center), float(R), float(r),
+                float(noise))
+
+
+def gen_star(seed, subdiv=8, center=(0.5, 0.5, 0.5), radius=0.3, amp=0.2, scale=(1, 1, 6)):
+    return _gen("gpv_gen_star", seed, int(subdiv), _f3(center), float(radius), float(amp),
+                _f3(scale))
+
+
+def gen_superellipsoid(seed, nlon, nlat, center, semi, e1, e2, rot=None):
+    rot = np.eye(3, dtype=np.float32) if rot is None else np.asarray(rot, np.float32)
+    return _gen("gpv_gen_superellipsoid", seed, int(nlon), int(nlat), _f3(center), _f3(semi),
+                float(e1), float(e2), (C.c_float * 9)(*rot.reshape(-1).tolist()))
+
+
+# ---- context ----------------------------------------------------------------------------------
+class Context:
+    """A libgpview context on one device: stream-ordered pool, pinned staging, results."""
+
+    def __init__(self, device=0):
+        self._h = C.c_void_p()
+        rc = lib().gpv_init(int(device), C.byref(self._h))
+        if rc:
+            raise GpvError(rc, "gpv_init (no CUDA device?)")
+        self.device = device
+
+    def close(self):
+        if self._h:
+            lib().gpv_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def error(self):
+        return lib().gpv_last_error(self._h).decode()
+
+    def set_tile(self, t):
+        rc = lib().gpv_set_tile(self._h, int(t))
+        if rc:
+            raise GpvError(rc, "set_tile")
+
+    def _check(self, rc, what):
+        if rc:
+            raise GpvError(rc, f"{what}: {self.error()}")
+
+    def voxelize_device(self, d_ptr, num_triangles, spec, stream=0):
+        """Plain path on device triangles (pointer to float[T*9], 16-byte aligned)."""
+        res = Result()
+        self._check(lib().gpv_voxelize(self._h, C.c_void_p(d_ptr), int(num_triangles),
+                                       C.byref(spec), C.byref(res), C.c_void_p(stream)),
+                    "gpv_voxelize")
+        return res
+
+    def voxelize_host(self, tris, spec, stream=0):
+        tris = np.ascontiguousarray(tris, dtype=np.float32).reshape(-1)
+        res = Result()
+        self._check(lib().gpv_voxelize_host(self._h, tris.ctypes.data_as(C.c_void_p),
+                                            tris.size // 9, C.byref(spec), C.byref(res),
+                                            C.c_void_p(stream)), "gpv_voxelize_host")
+        return res
+
+    def voxelize_batch(self, d_ptrs, counts, specs, stream=0):
+        n = len(d_ptrs)
+        ptrs = (C.c_void_p * n)(*[C.c_void_p(p) for p in d_ptrs])
+        cnts = (C.c_int64 * n)(*[int(c) for c in counts])
+        sp = (GridSpec * n)(*specs)
+        res = (Result * n)()
+        self._check(lib().gpv_voxelize_batch(self._h, n, ptrs, cnts, sp, res, C.c_void_p(stream)),
+                    "gpv_voxelize_batch")
+        return list(res)
+
+    def fetch(self, res, stream=0):
+        """Copies a result to host numpy arrays: (level1 u8, prefix i32, boundary i32, level2 u8)."""
+        cells = res.spec.ndiv2[0] * res.spec.ndiv2[1] * res.spec.ndiv2[2]
+        l1 = np.empty(res.num_level1, np.uint8)
+        pre = np.empty(res.num_level1, np.int32)
+        bi = np.empty(res.num_boundary, np.int32)
+        l2 = np.empty(res.num_boundary * cells, np.uint8)
+        self._check(lib().gpv_result_copy_to_host(
+            self._h, C.byref(res), l1.ctypes.data_as(C.c_void_p), pre.ctypes.data_as(C.c_void_p),
+            bi.ctypes.data_as(C.c_void_p), l2.ctypes.data_as(C.c_void_p), C.c_void_p(stream)),
+            "copy_to_host")
+        return l1, pre, bi, l2
+
+    def release(self, res):
+        self._check(lib().gpv_result_release(self._h, C.byref(res)), "release")
+
+
+# ---- reference-shaped host interface ----------------------------------------------------------
+class GLParameters:
+    """The voxelization knobs of GLParameters (src/GLParameters.cpp:28-69)."""
+
+    def __init__(self, voxelCount=8, voxelCount2=4, level2Voxels=True, saveVoxels=True):
+        self.voxelCount = voxelCount
+        self.voxelCount2 = voxelCount2
+        self.level2Voxels = level2Voxels
+        self.saveVoxels = saveVoxels
+
+
+class VoxelData:
+    """Result fields named as in the reference's VoxelData (includes/Utilities.h:79-154)."""
+
+    def __init__(self, res, l1, prefix, bindex, l2):
+        s = res.spec
+        self.numDivX, self.numDivY, self.numDivZ = (int(v) for v in s.ndiv)
+        self.numDivX2, self.numDivY2, self.numDivZ2 = (int(v) for v in s.ndiv2)
+        self.gridSizeX, self.gridSizeY, self.gridSizeZ = (float(v) for v in res.grid_size)
+        self.gridSizeX2, self.gridSizeY2, self.gridSizeZ2 = (float(v) for v in res.grid_size2)
+        self.level1InOut = l1            # uint8 .raw encoding (state*127)
+        self.boundaryPrefixSum = prefix
+        self.boundaryIndex = bindex
+        self.level2InOut = l2
+        self.numLevel1InsideVoxels = int(res.num_level1_inside)
+        self.numLevel1BoundaryVoxels = int(res.num_boundary)
+        self.numLevel2InsideVoxels = int(res.num_level2_inside)
+        self.numLevel2BoundaryVoxels = int(res.num_level2_boundary)
+
+
+class Object:
+    """Mirror of the reference's Object for the voxelization path (includes/Object.h:85-135)."""
+
+    def __init__(self, ctx=None, objID=-1):
+        self.ctx = ctx
+        self.objID = objID
+        self.flatCPUTriangleData = None
+        self.totalNumTriangles = 0
+        self.bBoxMin = None
+        self.bBoxMax = None
+        self.maxModelSize = 0.0
+        self.voxelData = None
+        self._result = None
+
+    def _load(self, fn, path):
+        m = MeshC()
+        rc = fn(path.encode(), C.byref(m))
+        if rc:
+            raise GpvError(rc, path)
+        try:
+            n = int(m.num_triangles)
+            self._tris = np.ctypeslib.as_array(m.tris, shape=(9 * n,)).copy() if n else np.zeros(0, np.float32)
+            self.bBoxMin = np.array(m.bbox_min, np.float32)
+            self.bBoxMax = np.array(m.bbox_max, np.float32)
+            self.maxModelSize = float(m.max_model_size)
+        finally:
+            lib().gpv_mesh_free(C.byref(m))
+
+    def ReadObject(self, path):
+        self._load(lib().gpv_load_obj, path)
+
+    def ReadOFFObject(self, path):
+        self._load(lib().gpv_load_off, path)
+
+    def CreateFlatTriangleData(self):
+        self.flatCPUTriangleData = self._tris
+        self.totalNumTriangles = self._tris.size // 9
+
+    def PerformVoxelization(self, glParam, bufferSize=-1, spec=None):
+        """Voxelizes on the GPU.  `spec` overrides the reference sizing (explicit grids)."""
+        del bufferSize  # the device path has no fixed per-voxel buffer
+        if self.flatCPUTriangleData is None:
+            self.CreateFlatTriangleData()
+        if self.ctx is None:
+            self.ctx = Context()
+        if spec is None:
+            spec = grid_reference(self.bBoxMin, self.bBoxMax, self.maxModelSize,
+                                  glParam.voxelCount, glParam.voxelCount2 if glParam.level2Voxels else 0)
+        res = self.ctx.voxelize_host(self.flatCPUTriangleData, spec)
+        try:
+            l1, pre, bi, l2 = self.ctx.fetch(res)
+        finally:
+            self._result = res
+        self.voxelData = VoxelData(res, l1, pre, bi, l2)
+        if glParam.saveVoxels:
+            self.SaveVoxelization(glParam)
+        self.ctx.release(res)
+        return self.voxelData
+
+    def SaveVoxelization(self, glParam, prefix=None):
+        vd = self.voxelData
+        prefix = prefix or f"Obj{self.objID}"
+        rc = lib().gpv_write_raw(prefix.encode(), C.byref(self._result),
+                                 vd.level1InOut.ctypes.data_as(C.c_void_p),
+                                 vd.boundaryPrefixSum.ctypes.data_as(C.c_void_p),
+                                 vd.level2InOut.ctypes.data_as(C.c_void_p))
+        if rc:
+            raise GpvError(rc, "SaveVoxelization")

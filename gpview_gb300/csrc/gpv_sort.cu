@@ -1,0 +1,216 @@
+// gpv_sort.cu -- hand-written device scan and LSD radix sort used to build the per-voxel
+// triangle lists (the reference builds them on the host, src/Object.cpp:2146-2180, and
+// compacts boundary voxels there too, :3271-3279).
+//
+// scan_u32:  reduce-then-scan, three launches, no inter-block waiting.
+// sort_pairs: stable LSD radix sort of (u32 key, u32 value), 8-bit digits; per pass a tile
+//             histogram, a scan of the digit-major histogram, and a stable scatter whose
+//             in-tile ranks come from __match_any_sync peer masks.
+#include "gpv_internal.h"
+
+namespace gpv {
+
+namespace {
+
+constexpr int kScanThreads = 256;
+constexpr int kScanItems = 8;
+constexpr int kScanTile = kScanThreads * kScanItems;
+
+__device__ __forceinline__ uint32_t warp_incl_scan(uint32_t v) {
+  const unsigned lane = threadIdx.x & 31u;
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    uint32_t o = __shfl_up_sync(0xffffffffu, v, d);
+    if (lane >= (unsigned)d) v += o;
+  }
+  return v;
+}
+
+// Block-wide exclusive scan of one value per thread; the block total goes to `total`.
+template <int NT>
+__device__ __forceinline__ uint32_t block_excl_scan(uint32_t v, uint32_t &total) {
+  __shared__ uint32_t s_w[NT / 32];
+  __shared__ uint32_t s_total;
+  const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+  const uint32_t inc = warp_incl_scan(v);
+  if (lane == 31) s_w[warp] = inc;
+  __syncthreads();
+  if (warp == 0) {
+    const uint32_t w = lane < NT / 32 ? s_w[lane] : 0u;
+    const uint32_t wi = warp_incl_scan(w);
+    if (lane < NT / 32) s_w[lane] = wi - w;
+    if (lane == 31) s_total = wi;
+  }
+  __syncthreads();
+  const uint32_t r = s_w[warp] + inc - v;
+  total = s_total;
+  __syncthreads();
+  return r;
+}
+
+__global__ void k_scan_reduce(const uint32_t *__restrict__ in, int64_t n,
+                              uint32_t *__restrict__ part) {
+  const int64_t base = (int64_t)blockIdx.x * kScanTile;
+  uint32_t s = 0;
+#pragma unroll
+  for (int k = 0; k < kScanItems; ++k) {
+    int64_t i = base + (int64_t)k * kScanThreads + threadIdx.x;
+    if (i < n) s += in[i];
+  }
+  uint32_t tot;
+  block_excl_scan<kScanThreads>(s, tot);
+  if (threadIdx.x == 0) part[blockIdx.x] = tot;
+}
+
+// Single block: exclusive scan of the partials in place; total to *total.
+__global__ void k_scan_partials(uint32_t *__restrict__ part, int64_t nb,
+                                uint32_t *__restrict__ total) {
+  uint32_t carry = 0;
+  for (int64_t b0 = 0; b0 < nb; b0 += 1024) {
+    int64_t i = b0 + threadIdx.x;
+    uint32_t v = i < nb ? part[i] : 0u;
+    uint32_t tot;
+    uint32_t ex = block_excl_scan<1024>(v, tot);
+    if (i < nb) part[i] = carry + ex;
+    carry += tot;
+  }
+  if (threadIdx.x == 0 && total) *total = carry;
+}
+
+__global__ void k_scan_down(const uint32_t *__restrict__ in, int64_t n,
+                            const uint32_t *__restrict__ part, uint32_t *__restrict__ out) {
+  const int64_t base = (int64_t)blockIdx.x * kScanTile;
+  // blocked arrangement: thread owns kScanItems consecutive items
+  uint32_t v[kScanItems];
+  uint32_t s = 0;
+  const int64_t tb = base + (int64_t)threadIdx.x * kScanItems;
+#pragma unroll
+  for (int k = 0; k < kScanItems; ++k) {
+    int64_t i = tb + k;
+    v[k] = i < n ? in[i] : 0u;
+    s += v[k];
+  }
+  uint32_t tot;
+  uint32_t ex = block_excl_scan<kScanThreads>(s, tot) + part[blockIdx.x];
+#pragma unroll
+  for (int k = 0; k < kScanItems; ++k) {
+    int64_t i = tb + k;
+    if (i < n) out[i] = ex;
+    ex += v[k];
+  }
+}
+
+// ---- radix sort ---------------------------------------------------------------------------
+constexpr int kSortThreads = 256;
+constexpr int kSortRounds = 8;
+constexpr int kSortTile = kSortThreads * kSortRounds;
+
+__global__ void k_radix_hist(const uint32_t *__restrict__ keys, int64_t n, int shift,
+                             uint32_t *__restrict__ hist, int64_t nb) {
+  __shared__ uint32_t s_h[256];
+  s_h[threadIdx.x] = 0;
+  __syncthreads();
+  const int64_t base = (int64_t)blockIdx.x * kSortTile;
+  for (int r = 0; r < kSortRounds; ++r) {
+    int64_t i = base + (int64_t)r * kSortThreads + threadIdx.x;
+    if (i < n) atomicAdd(&s_h[(keys[i] >> shift) & 255u], 1u);
+  }
+  __syncthreads();
+  hist[(int64_t)threadIdx.x * nb + blockIdx.x] = s_h[threadIdx.x];
+}
+
+__global__ void k_radix_scatter(const uint32_t *__restrict__ keys, const uint32_t *__restrict__ vals,
+                                int64_t n, int shift, const uint32_t *__restrict__ hoff, int64_t nb,
+                                uint32_t *__restrict__ kout, uint32_t *__restrict__ vout) {
+  __shared__ uint32_t s_off[256];
+  __shared__ uint32_t s_run[256];
+  __shared__ uint16_t s_w[kSortThreads / 32][256];
+  const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+  s_off[threadIdx.x] = hoff[(int64_t)threadIdx.x * nb + blockIdx.x];
+  s_run[threadIdx.x] = 0;
+  const int64_t base = (int64_t)blockIdx.x * kSortTile;
+  const unsigned lt_mask = (1u << lane) - 1u;
+  for (int r = 0; r < kSortRounds; ++r) {
+    if (base + (int64_t)r * kSortThreads >= n) break;  // block-uniform
+#pragma unroll
+    for (int w = 0; w < kSortThreads / 32; ++w) s_w[w][threadIdx.x] = 0;
+    __syncthreads();
+    const int64_t i = base + (int64_t)r * kSortThreads + threadIdx.x;
+    const bool valid = i < n;
+    uint32_t key = 0, val = 0, digit = 256u;
+    if (valid) {
+      key = keys[i];
+      val = vals[i];
+      digit = (key >> shift) & 255u;
+    }
+    const unsigned peers = __match_any_sync(0xffffffffu, digit);
+    const unsigned rank = __popc(peers & lt_mask);
+    if (valid && rank == 0) s_w[warp][digit] = (uint16_t)__popc(peers);
+    __syncthreads();
+    uint32_t acc = 0;
+    {
+      const unsigned d = threadIdx.x;
+#pragma unroll
+      for (int w = 0; w < kSortThreads / 32; ++w) {
+        uint32_t c = s_w[w][d];
+        s_w[w][d] = (uint16_t)acc;
+        acc += c;
+      }
+    }
+    __syncthreads();
+    if (valid) {
+      const uint32_t pos = s_off[digit] + s_run[digit] + s_w[warp][digit] + rank;
+      kout[pos] = key;
+      vout[pos] = val;
+    }
+    __syncthreads();
+    s_run[threadIdx.x] += acc;
+    __syncthreads();
+  }
+}
+
+}  // namespace
+
+int64_t scan_temp_words(int64_t n) { return (n + kScanTile - 1) / kScanTile + 1; }
+
+void scan_u32(const uint32_t *in, uint32_t *out, int64_t n, uint32_t *d_total, uint32_t *temp,
+              cudaStream_t s) {
+  if (n <= 0) {
+    if (d_total) cudaMemsetAsync(d_total, 0, sizeof(uint32_t), s);
+    return;
+  }
+  const int64_t nb = (n + kScanTile - 1) / kScanTile;
+  k_scan_reduce<<<(unsigned)nb, kScanThreads, 0, s>>>(in, n, temp);
+  k_scan_partials<<<1, 1024, 0, s>>>(temp, nb, d_total);
+  k_scan_down<<<(unsigned)nb, kScanThreads, 0, s>>>(in, n, temp, out);
+}
+
+int64_t sort_temp_words(int64_t n) {
+  const int64_t nb = (n + kSortTile - 1) / kSortTile;
+  return 2 * 256 * nb + scan_temp_words(256 * nb);
+}
+
+// Sorts (keys, vals) by the low key_bits bits.  Ping-pongs with (kalt, valt); returns true when
+// the sorted data ended in (kalt, valt).
+bool sort_pairs(uint32_t *keys, uint32_t *vals, uint32_t *kalt, uint32_t *valt, int64_t n,
+                int key_bits, uint32_t *temp, cudaStream_t s) {
+  if (n <= 1) return false;
+  const int64_t nb = (n + kSortTile - 1) / kSortTile;
+  uint32_t *hist = temp;
+  uint32_t *hoff = temp + 256 * nb;
+  uint32_t *stmp = temp + 2 * 256 * nb;
+  bool alt = false;
+  for (int shift = 0; shift < key_bits; shift += 8) {
+    const uint32_t *ki = alt ? kalt : keys;
+    const uint32_t *vi = alt ? valt : vals;
+    uint32_t *ko = alt ? keys : kalt;
+    uint32_t *vo = alt ? vals : valt;
+    k_radix_hist<<<(unsigned)nb, kSortThreads, 0, s>>>(ki, n, shift, hist, nb);
+    scan_u32(hist, hoff, 256 * nb, nullptr, stmp, s);
+    k_radix_scatter<<<(unsigned)nb, kSortThreads, 0, s>>>(ki, vi, n, shift, hoff, nb, ko, vo);
+    alt = !alt;
+  }
+  return alt;
+}
+
+}  // namespace gpv

@@ -1,0 +1,187 @@
+/*
+ * gpview.h -- C ABI of the GB300-native two-level voxelizer (libgpview.so).
+ *
+ * Two groups of entry points:
+ *
+ *  1. Reference-named shims.  Same names, signatures and "1 on success" return as the CUDA
+ *     wrappers GPView's Object class binds (includes/CUDAUtilities.h:63-64, :87-89).  All pointers
+ *     are DEVICE pointers owned by the caller; launches go to the legacy default stream, as in
+ *     the reference.  A reference-shaped caller relinks against this library unchanged.
+ *
+ *  2. The native API (gpv_*).  Plain pointers and sizes, an int status (0 = GPV_OK, negative =
+ *     error), an explicit cudaStream_t, a context that owns a stream-ordered device pool.  The
+ *     voxelization contract is the reference's CPU path: every Level1/Level2 state equals what
+ *     ClassifyInOutCPU + ClassifyTessellation + ClassifyInOutLevel2CPU + ClassifyTessellationLevel2
+ *     (src/Object.cpp) produce on the same triangles and grid, bit for bit.
+ *
+ * One context per host thread.  Device-side failures are reported through status words read
+ * back by the host, never by a trap.
+ */
+#ifndef GPVIEW_H
+#define GPVIEW_H
+
+#include <stddef.h>
+#include <stdint.h>
+#include <cuda_runtime_api.h> /* cudaStream_t */
+#include <vector_types.h>     /* float3, int3: the reference shim signatures use them by value */
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ---------------------------------------------------------------------- */
+#define GPV_OK 0
+#define GPV_ERR_INVALID (-1)  /* bad argument or grid */
+#define GPV_ERR_CUDA (-2)     /* a CUDA runtime call failed */
+#define GPV_ERR_OOM (-3)      /* device or host allocation refused */
+#define GPV_ERR_IO (-4)       /* file could not be opened / written */
+#define GPV_ERR_PARSE (-5)    /* malformed .obj / .off */
+#define GPV_ERR_DEVICE (-6)   /* a kernel raised its error status word (bounded wait expired) */
+#define GPV_ERR_BUDGET (-7)   /* request exceeds the serving memory budget */
+#define GPV_ERR_PENDING (-8)  /* serving: result not ready yet */
+#define GPV_ERR_NOTFOUND (-9) /* serving: unknown ticket */
+
+typedef struct gpv_ctx gpv_ctx;
+
+/* Grid of one voxelization.  bbox_min/bbox_max play the role of Object::bBoxMin/bBoxMax
+ * (includes/Object.h:95-96): Level1 cell sizes are float((max-min)/(n*1.0)) and every centre
+ * and ray origin follows the reference's formulas (src/Object.cpp:3108-3130, :743-745,
+ * :1132-1160, :2329-2331, :2389-2391).  ndiv2 = {0,0,0} disables Level2. */
+typedef struct {
+    float bbox_min[3];
+    float bbox_max[3];
+    int32_t ndiv[3];
+    int32_t ndiv2[3];
+} gpv_grid_spec;
+
+/* Algorithmic work of one voxelization, counted from the reference's own algorithm:
+ *   sat1 = sum over triangles of the Level1 candidate box size   (src/Object.cpp:2309-2325)
+ *   sat2 = sum over boundary voxels of |tris(b)| * n2^3          (src/Object.cpp:2374-2398)
+ *   ray1 = sum over triangles of (columns whose centre lies in the triangle's x/y box) * nz
+ *   ray2 = sum over boundary voxels of |column union(b)| * n2^3  (src/Object.cpp:1162-1193)
+ * ray1 counts the candidate pairs a column-binned fill must test; the reference's brute force
+ * (every voxel against every triangle) is not counted. */
+typedef struct {
+    int64_t sat1, sat2, ray1, ray2;
+} gpv_work;
+
+/* Result of one voxelization.  Device arrays are owned by the context until
+ * gpv_result_release().  State bytes are the reference's .raw encoding uint8(state*127):
+ * 0 = outside, 127 = inside, 254 = boundary (src/Object.cpp:3031). */
+typedef struct {
+    gpv_grid_spec spec;
+    float grid_size[3];
+    float grid_size2[3];
+    int64_t num_level1;          /* nx*ny*nz */
+    int64_t num_boundary;        /* Level1 boundary voxels (B) */
+    int64_t num_level1_inside;   /* Level1 voxels with state 1 */
+    int64_t num_level2_inside;   /* Level2 cells with state 1 */
+    int64_t num_level2_boundary; /* Level2 cells with state 2 */
+    int64_t num_pairs;           /* (Level1 voxel, triangle) records */
+    gpv_work work;
+    uint8_t *level1_inout;       /* device, num_level1 bytes, x fastest */
+    int32_t *level1_prefix;      /* device, num_level1 int32: boundaryPrefixSum */
+    int32_t *boundary_index;     /* device, num_boundary int32: boundaryIndex */
+    uint8_t *level2_inout;       /* device, num_boundary * n2x*n2y*n2z bytes */
+    uint64_t handle;             /* internal */
+} gpv_result;
+
+/* A triangle soup on the host, as Object::CreateFlatTriangleData builds it
+ * (src/Object.cpp:3496-3527): float[num_triangles*9], vertex-major, file face order.
+ * bbox_min/bbox_max are the loader's bounds padded by 0.001*|max-min| (src/Object.cpp:572-583). */
+typedef struct {
+    float *tris;
+    int64_t num_triangles;
+    float bbox_min[3];
+    float bbox_max[3];
+    float max_model_size;
+} gpv_mesh;
+
+/* ---- context ------------------------------------------------------------------------------ */
+int gpv_init(int device, gpv_ctx **out);
+void gpv_destroy(gpv_ctx *ctx);
+const char *gpv_last_error(gpv_ctx *ctx);
+/* Tunables (autotuner output): triangles per Level1 tile (32..256, power of two). */
+int gpv_set_tile(gpv_ctx *ctx, int tris_per_tile);
+
+/* ---- grids --------------------------------------------------------------------------------- */
+/* Explicit grid: n^3 cells over the mesh box grown by one cell on every side. */
+int gpv_grid_padded(const float mesh_min[3], const float mesh_max[3], const int32_t ndiv[3],
+                    const int32_t ndiv2[3], gpv_grid_spec *out);
+/* Reference sizing from GLParameters::voxelCount / voxelCount2 (src/Object.cpp:3094-3107). */
+int gpv_grid_reference(const float bbox_min[3], const float bbox_max[3], float max_model_size,
+                       int32_t voxel_count, int32_t voxel_count2, gpv_grid_spec *out);
+
+/* ---- voxelization ---------------------------------------------------------------------------- */
+/* Plain path: one mesh, device triangles (16-byte aligned), results stay on the device. */
+int gpv_voxelize(gpv_ctx *ctx, const float *d_tris, int64_t num_triangles,
+                 const gpv_grid_spec *spec, gpv_result *out, cudaStream_t stream);
+/* Same, from host triangles (copied in on the stream). */
+int gpv_voxelize_host(gpv_ctx *ctx, const float *h_tris, int64_t num_triangles,
+                      const gpv_grid_spec *spec, gpv_result *out, cudaStream_t stream);
+/* Copy a result's arrays to host buffers (any may be NULL) and wait for the stream. */
+int gpv_result_copy_to_host(gpv_ctx *ctx, const gpv_result *res, uint8_t *level1_inout,
+                            int32_t *level1_prefix, int32_t *boundary_index,
+                            uint8_t *level2_inout, cudaStream_t stream);
+int gpv_result_release(gpv_ctx *ctx, gpv_result *res);
+
+/* Batched path: n meshes in one launch sequence (persistent work-queue kernels).
+ * d_tris[i] are device pointers (16-byte aligned); results are filled like gpv_voxelize. */
+int gpv_voxelize_batch(gpv_ctx *ctx, int32_t n, const float *const *d_tris,
+                       const int64_t *num_triangles, const gpv_grid_spec *specs,
+                       gpv_result *results, cudaStream_t stream);
+
+/* ---- meshes and files (host) ---------------------------------------------------------------- */
+int gpv_load_obj(const char *path, gpv_mesh *out); /* Object::ReadObject (src/Object.cpp:395) */
+int gpv_load_off(const char *path, gpv_mesh *out); /* Object::ReadOFFObject (src/Object.cpp:171) */
+void gpv_mesh_free(gpv_mesh *mesh);
+/* Object::SaveVoxelization's files from host arrays (src/Object.cpp:2934-3075):
+ * <prefix>VoxelConfig.txt, Level1InOut.raw, Level1BoundaryPrefixSum.raw, Level2InOut.raw. */
+int gpv_write_raw(const char *prefix, const gpv_result *res, const uint8_t *level1_inout,
+                  const int32_t *level1_prefix, const uint8_t *level2_inout);
+
+/* ---- seeded synthetic meshes (host) ---------------------------------------------------------- */
+/* Each returns the triangle count; with tris == NULL only the count is returned. */
+int64_t gpv_gen_uvsphere(uint64_t seed, int32_t nlon, int32_t nlat, const float center[3],
+                         float radius, float jitter_sigma, float *tris);
+int64_t gpv_gen_torus(uint64_t seed, int32_t nu, int32_t nv, const float center[3], float R,
+                      float r, float noise_amp, float *tris);
+int64_t gpv_gen_star(uint64_t seed, int32_t subdiv, const float center[3], float radius,
+                     float amp, const float scale[3], float *tris);
+int64_t gpv_gen_superellipsoid(uint64_t seed, int32_t nlon, int32_t nlat, const float center[3],
+                               const float semi[3], float e1, float e2, const float rot[9],
+                               float *tris);
+
+/* ---- reference-named shims (includes/CUDAUtilities.h:63-64, :87-89) --------------------------- */
+void InitializeCUDA(void);                 /* src/CUDAUtilities.cpp:51-55 */
+void CUDACheckErrors(char const *label);   /* src/CUDAUtilities.cpp:33-49 */
+/* cuda/CUDAClassifyTessellation.cu:507-515.  Marks inOut[v]=2 for every voxel whose SAT test
+ * passes inside each triangle's candidate box, counts triangles per voxel in voxelTriCount and
+ * stores up to triBufferLen ids per voxel in voxelTriIndex[v*triBufferLen..] (never beyond;
+ * the count still reports the true number, so the caller's resize-and-retry works).  Centres
+ * are the reference CPU's: float((p+0.5)*boxExtents*2 + objBoxMin), evaluated in double. */
+int CUDAClassifyTessellation(float *trianglesCUDAData, int numTriangles, float *inOutCUDAData,
+                             int *voxelTriCountCUDAData, int *voxelTriIndexCUDAData,
+                             float3 objBoxMin, float3 objBoxMax, float3 boxExtents, int3 numDiv,
+                             int triBufferLen);
+/* cuda/CUDAClassifyTessellation.cu:518-527.  Level2 SAT of each boundary voxel b against the
+ * triangles listed for Level1 voxel level2Index[b]; writes 2 into level2InOut and accumulates
+ * unit face normals + a count into level2Normal (4 floats per cell), in list order. */
+int CUDAClassifyTessellationLevel2(float *trianglesCUDAData, float *level2InOutCUDAData,
+                                   float *level2NormalCUDAData, float *level1MidPointCUDAData,
+                                   int *level2IndexCUDAData, int *voxelTriCountCUDAData,
+                                   int *level1TriFlatIndexCUDAData, int *level1TriFlatCUDAData,
+                                   int numBoundary, int3 numDiv2, float3 boxExtentsLevel1,
+                                   float3 boxExtentsLevel2);
+/* cuda/CUDAClassifyTessellation.cu:531-540.  +z ray parity of every Level2 cell centre against
+ * the x/y-column triangle list of its Level1 voxel; odd -> level2InOut = 1. */
+int CUDAClassifyInOutLevel2(float *trianglesCUDAData, float *level2InOutCUDAData,
+                            float *level1MidPointCUDAData, int *level2IndexCUDAData,
+                            int *xyTriCountCUDAData, int *xyTriFlatIndexCUDAData,
+                            int *xyTriFlatCUDAData, int numBoundary, int3 numDiv, int3 numDiv2,
+                            float3 boxExtentsLevel1, float3 boxExtentsLevel2);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GPVIEW_H */

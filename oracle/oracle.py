@@ -1,0 +1,170 @@
+"""ctypes wrapper of the CPU oracle (gpv_oracle.c).  TEST INFRASTRUCTURE ONLY.
+
+Imported by tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg -- never by the
+gpview_gb300 package.  `Oracle(ref=True)` loads the build linked against the reference's own
+predicates (oracle/_ref/, present only where the reference sources were available at build time).
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+FILL_VOXEL, FILL_COLUMN, FILL_CAND = 0, 1, 2
+
+
+class Spec(C.Structure):
+    _fields_ = [("bmin", C.c_float * 3), ("bmax", C.c_float * 3),
+                ("n", C.c_int32 * 3), ("n2", C.c_int32 * 3)]
+
+
+def lib_path(ref=False):
+    return os.path.join(HERE, "_ref", "liboracle_ref.so") if ref else os.path.join(HERE, "liboracle.so")
+
+
+def available(ref=False):
+    return os.path.exists(lib_path(ref))
+
+
+_libs = {}
+
+
+def _load(ref=False):
+    if ref in _libs:
+        return _libs[ref]
+    path = lib_path(ref)
+    if not os.path.exists(path):
+        if ref:
+            raise FileNotFoundError(path)
+        from oracle import build_oracle  # noqa: WPS433  (build on demand)
+        build_oracle.build()
+    L = C.CDLL(path)
+    vp, i64 = C.c_void_p, C.c_int64
+    L.orc_create.argtypes = [vp, i64, C.POINTER(Spec), C.c_int, C.c_int]
+    L.orc_create.restype = vp
+    L.orc_free.argtypes = [vp]
+    for fn in ("orc_num_boundary", "orc_num_pairs", "orc_sat1_tests", "orc_ray1_candidates"):
+        getattr(L, fn).argtypes = [vp]
+        getattr(L, fn).restype = i64
+    L.orc_level1_state.argtypes = [vp, vp]
+    L.orc_prefix.argtypes = [vp, vp]
+    L.orc_boundary_index.argtypes = [vp, vp]
+    L.orc_voxel_tris.argtypes = [vp, i64, vp, i64]
+    L.orc_voxel_tris.restype = i64
+    L.orc_level2.argtypes = [vp, i64, i64, vp, C.c_int, C.POINTER(i64), C.POINTER(i64)]
+    L.orc_tri_box.argtypes = [vp, vp, vp]
+    L.orc_tri_ray.argtypes = [vp, vp, vp, vp, vp, C.POINTER(C.c_float)]
+    L.orc_tri_ray_z.argtypes = [vp, vp]
+    L.orc_grid_tables.argtypes = [C.POINTER(Spec), vp, vp, vp, vp, vp, vp, vp]
+    _libs[ref] = L
+    return L
+
+
+def spec_from(grid):
+    """Accepts a gpview_gb300.GridSpec or a (bmin, bmax, n, n2) tuple."""
+    s = Spec()
+    if hasattr(grid, "bbox_min"):
+        bmin, bmax, n, n2 = grid.bbox_min, grid.bbox_max, grid.ndiv, grid.ndiv2
+    else:
+        bmin, bmax, n, n2 = grid
+    s.bmin[:] = [float(x) for x in bmin]
+    s.bmax[:] = [float(x) for x in bmax]
+    s.n[:] = [int(x) for x in n]
+    s.n2[:] = [int(x) for x in n2]
+    return s
+
+
+def _p(a):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+class Run:
+    """One oracle voxelization (Level1 done at construction, Level2 on demand)."""
+
+    def __init__(self, tris, grid, fill=FILL_CAND, threads=0, ref=False):
+        self.L = _load(ref)
+        self.tris = np.ascontiguousarray(tris, dtype=np.float32).reshape(-1)
+        self.spec = spec_from(grid)
+        self.h = self.L.orc_create(_p(self.tris), self.tris.size // 9, C.byref(self.spec),
+                                   int(fill), int(threads))
+        self.N1 = int(np.prod(list(self.spec.n)))
+        self.cells = int(np.prod(list(self.spec.n2)))
+        self.B = int(self.L.orc_num_boundary(self.h))
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            self.L.orc_free(self.h)
+            self.h = None
+
+    def level1_state(self):
+        out = np.empty(self.N1, np.uint8)
+        self.L.orc_level1_state(self.h, _p(out))
+        return out
+
+    def level1_bytes(self):
+        return (self.level1_state() * 127).astype(np.uint8)
+
+    def prefix(self):
+        out = np.empty(self.N1, np.int32)
+        self.L.orc_prefix(self.h, _p(out))
+        return out
+
+    def boundary_index(self):
+        out = np.empty(self.B, np.int32)
+        self.L.orc_boundary_index(self.h, _p(out))
+        return out
+
+    def voxel_tris(self, v):
+        n = self.L.orc_voxel_tris(self.h, int(v), None, 0)
+        out = np.empty(n, np.int32)
+        self.L.orc_voxel_tris(self.h, int(v), _p(out), n)
+        return out
+
+    def num_pairs(self):
+        return int(self.L.orc_num_pairs(self.h))
+
+    def sat1_tests(self):
+        return int(self.L.orc_sat1_tests(self.h))
+
+    def ray1_candidates(self):
+        return int(self.L.orc_ray1_candidates(self.h))
+
+    def level2_state(self, b0=0, b1=None, threads=0):
+        """States (0/1/2) of boundary voxels [b0,b1), plus (sat2, ray2) work counts."""
+        b1 = self.B if b1 is None else b1
+        out = np.empty(max(b1 - b0, 0) * self.cells, np.uint8)
+        s2, r2 = C.c_int64(), C.c_int64()
+        if b1 > b0:
+            self.L.orc_level2(self.h, int(b0), int(b1), _p(out), int(threads), C.byref(s2), C.byref(r2))
+        return out, int(s2.value), int(r2.value)
+
+    def level2_bytes(self, b0=0, b1=None, threads=0):
+        st, _, _ = self.level2_state(b0, b1, threads)
+        return (st * 127).astype(np.uint8)
+
+
+def tri_box(c, h, tv, ref=False):
+    L = _load(ref)
+    c = np.asarray(c, np.float32); h = np.asarray(h, np.float32); tv = np.asarray(tv, np.float32)
+    return int(L.orc_tri_box(_p(c), _p(h), _p(tv)))
+
+
+def tri_ray(v1, v2, v3, o, d, ref=False):
+    L = _load(ref)
+    a = [np.ascontiguousarray(x, np.float32) for x in (v1, v2, v3, o, d)]
+    t = C.c_float(0.0)
+    hit = int(L.orc_tri_ray(*[_p(x) for x in a], C.byref(t)))
+    return hit, float(t.value)
+
+
+def grid_tables(grid):
+    L = _load(False)
+    s = spec_from(grid)
+    n = list(s.n)
+    n2 = [max(int(x), 1) for x in s.n2]
+    g, e1, g2, e2 = (np.empty(3, np.float32) for _ in range(4))
+    c1 = np.empty(sum(n), np.float32)
+    c2s = np.empty(sum(a * b for a, b in zip(n, n2)), np.float32)
+    o2 = np.empty_like(c2s)
+    L.orc_grid_tables(C.byref(s), _p(g), _p(e1), _p(g2), _p(e2), _p(c1), _p(c2s), _p(o2))
+    return dict(g=g, e1=e1, g2=g2, e2=e2, c1=c1, c2s=c2s, o2=o2)
