@@ -1,0 +1,350 @@
+#!/usr/bin/env python3
+"""Benchmark of the two-level voxelizer (prints one JSON line on rank 0).
+
+Default workload (one step = one voxelization of one mesh through the plain path):
+  torus262k -- torus R=0.35 r=0.12, 512x256 segments (262,144 triangles), 4-octave value-noise
+               displacement of amplitude 0.01, Level1 128^3 over the mesh box padded by one cell,
+               Level2 8^3 per boundary voxel.  Seeded synthetic data.
+
+value    tri-voxel tests/s on device-resident triangles (results stay on the device), timed with
+         CUDA events on the launching stream; L2 is flushed (256 MiB write) between steps,
+         outside the timed spans.
+e2e      the same metric through the public host API: H2D of the step's triangles from pinned
+         memory, voxelization, D2H of every result array, timed on the host around each step.
+tests    = sat1 + sat2 + ray1 + ray2 counted from the reference algorithm (see include/gpview.h).
+
+--impl reference times the reference's CPU path (the oracle restatement, all host threads) on a
+bounded sample of the same workload and reports the same metric.
+Multi-GPU: replicas only (each rank voxelizes its own copy; the path has no exchange step).
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "tests"))
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=10)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="gpv", choices=["gpv", "reference"])
+    p.add_argument("--workload", default="torus262k", choices=["sphere16k", "torus262k", "star1310k"])
+    p.add_argument("--tile", type=int, default=0)
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--cpu-seconds", type=float, default=15.0)
+    return p.parse_args()
+
+
+WORKLOADS = {
+    "sphere16k": dict(name="sphere16k", level1=64, level2=4,
+                      desc="UV-sphere r=0.4, 128x64 segments, 16,128 triangles, 64^3 / 4^3"),
+    "torus262k": dict(name="torus262k", level1=128, level2=8,
+                      desc="noisy torus R=0.35 r=0.12, 512x256 segments, 262,144 triangles, 128^3 / 8^3"),
+    "star1310k": dict(name="star1310k", level1=256, level2=16,
+                      desc="Y_lm star on an 8x subdivided icosphere, 1,310,720 triangles, 1:1:6, 256^3 / 16^3"),
+}
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={q}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        out = {"sm_mhz": None, "sm_max_mhz": None, "reasons": []}
+        if not self.proc:
+            return out
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sms, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sms.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        os.unlink(self.path)
+        out["sm_mhz"] = statistics.median(sms) if sms else None
+        out["sm_max_mhz"] = mx
+        out["reasons"] = sorted(reasons)
+        out["samples"] = len(sms)
+        return out
+
+
+def load_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f), "measured"
+    except Exception:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "sm_max_mhz": 2070.0}, "fallback"
+
+
+def cpu_baseline(tris, spec, work_total, seconds, threads):
+    """The oracle (port of the reference CPU path) on a bounded sample: Level1 in full, Level2 on
+    a contiguous range of boundary voxels sized to the time budget; extrapolated to the mesh."""
+    from oracle import oracle as orc
+
+    t0 = time.perf_counter()
+    run = orc.Run(tris, spec, fill=orc.FILL_CAND, threads=threads)
+    t_l1 = time.perf_counter() - t0
+    B = run.B
+    nb = min(B, 256)
+    t_l2 = 0.0
+    done = 0
+    while done < B:
+        t1 = time.perf_counter()
+        run.level2_state(done, done + nb, threads)
+        dt = time.perf_counter() - t1
+        t_l2 += dt
+        done += nb
+        if t_l1 + t_l2 > seconds:
+            break
+        nb = min(B - done, nb * 2)
+    t_full = t_l1 + (t_l2 * B / done if done else 0.0)
+    return {"value": work_total / t_full, "unit": "tests/s", "cores": threads, "kind": "port",
+            "sample": f"Level1 in full + Level2 on {done}/{B} boundary voxels, extrapolated "
+                      f"({t_l1 + t_l2:.1f} s of CPU work, est. {t_full:.2f} s per mesh)",
+            "sec_per_mesh": t_full}
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    import workloads as W
+
+    cfg = WORKLOADS[args.workload]
+    tris, spec = W.make(cfg)
+    from oracle import oracle as orc
+
+    threads = os.cpu_count() or 1
+    # per-mesh work counts from the oracle (Level1 exact; Level2 counted on the sample)
+    times = []
+    work_total = None
+    for step in range(args.warmup + args.steps):
+        base = cpu_baseline(tris, spec, 1.0, max(args.cpu_seconds / 3, 3.0), threads)
+        if work_total is None:
+            run = orc.Run(tris, spec, fill=orc.FILL_CAND, threads=threads)
+            _, s2, r2 = run.level2_state(0, run.B, threads)
+            work_total = run.sat1_tests() + run.ray1_candidates() + s2 + r2
+        if step >= args.warmup:
+            times.append(base["sec_per_mesh"])
+    t = sum(times) / len(times)
+    value = work_total / t
+    line = {"metric": "tri-voxel tests/s", "value": value, "unit": "tests/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic", "impl": "reference",
+            "config": {"workload": cfg["name"], "desc": cfg["desc"], "l2_flush": "n/a (CPU)"},
+            "cpu_baseline": {"value": value, "unit": "tests/s", "cores": threads, "kind": "port",
+                             "sample": base["sample"]},
+            "e2e": {"value": value, "unit": "tests/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+        return
+    import numpy as np
+    import torch
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    torch.cuda.set_device(local)
+
+    import gpview_gb300 as gpv
+    import workloads as W
+
+    cfg = WORKLOADS[args.workload]
+    tris, spec = W.make(cfg)
+    T = tris.size // 9
+    ctx = gpv.Context(local)
+    if args.tile:
+        ctx.set_tile(args.tile)
+    stream = torch.cuda.Stream(device=local)
+    sp = stream.cuda_stream
+    d_tris = torch.from_numpy(tris).to(f"cuda:{local}")
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=f"cuda:{local}")
+
+    def step_device():
+        res = ctx.voxelize_device(d_tris.data_ptr(), T, spec, sp)
+        return res
+
+    # warm-up
+    with torch.cuda.stream(stream):
+        for _ in range(args.warmup):
+            r = step_device()
+            ctx.release(r)
+    torch.cuda.synchronize()
+    peaks, peak_kind = load_peaks()
+
+    # timed region (device-resident inputs)
+    clocks = Clocks(local)
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(args.steps)]
+    ctx.set_timing(True)
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    launches0 = gpv.kernel_launches()
+    work = None
+    stats = None
+    with torch.cuda.stream(stream):
+        for k in range(args.steps):
+            flush.zero_()
+            ev[k][0].record(stream)
+            r = step_device()
+            ev[k][1].record(stream)
+            if work is None:
+                work = (r.work.sat1, r.work.sat2, r.work.ray1, r.work.ray2)
+                stats = dict(boundary=r.num_boundary, pairs=r.num_pairs,
+                             l1_inside=r.num_level1_inside, l2_inside=r.num_level2_inside,
+                             l2_boundary=r.num_level2_boundary, level1=r.num_level1)
+            ctx.release(r)
+    torch.cuda.synchronize()
+    launches = gpv.kernel_launches() - launches0
+    clk = clocks.stop()
+    calls, stage_ms = ctx.stage_times()
+    ctx.set_timing(False)
+    if dist:
+        dist.barrier()
+    step_ms = [a.elapsed_time(b) for a, b in ev]
+    t_total = sum(step_ms) / 1e3
+    if dist:
+        tt = torch.tensor([t_total], device=f"cuda:{local}", dtype=torch.float64)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t_total = float(tt.item())
+    tests_per_step = sum(work)
+    value = tests_per_step * args.steps * world / t_total
+
+    # e2e through the host API: pinned H2D, voxelize, D2H of all outputs
+    cells = spec.ndiv2[0] * spec.ndiv2[1] * spec.ndiv2[2]
+    h_tris = torch.from_numpy(tris).pin_memory()
+    h_l1 = torch.empty(stats["level1"], dtype=torch.uint8).pin_memory()
+    h_pre = torch.empty(stats["level1"], dtype=torch.int32).pin_memory()
+    h_bi = torch.empty(max(stats["boundary"], 1), dtype=torch.int32).pin_memory()
+    h_l2 = torch.empty(max(stats["boundary"] * cells, 1), dtype=torch.uint8).pin_memory()
+    e2e_times = []
+    import ctypes as C
+
+    for k in range(args.warmup + args.steps):
+        with torch.cuda.stream(stream):
+            flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        res = gpv.Result()
+        rc = gpv.lib().gpv_voxelize_host(ctx._h, C.c_void_p(h_tris.data_ptr()), T, C.byref(spec),
+                                          C.byref(res), C.c_void_p(sp))
+        if rc:
+            raise gpv.GpvError(rc, ctx.error())
+        rc = gpv.lib().gpv_result_copy_to_host(ctx._h, C.byref(res), C.c_void_p(h_l1.data_ptr()),
+                                               C.c_void_p(h_pre.data_ptr()), C.c_void_p(h_bi.data_ptr()),
+                                               C.c_void_p(h_l2.data_ptr()), C.c_void_p(sp))
+        if rc:
+            raise gpv.GpvError(rc, ctx.error())
+        t1 = time.perf_counter()
+        ctx.release(res)
+        if k >= args.warmup:
+            e2e_times.append(t1 - t0)
+    e2e_t = sum(e2e_times)
+    if dist:
+        tt = torch.tensor([e2e_t], device=f"cuda:{local}", dtype=torch.float64)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        e2e_t = float(tt.item())
+    e2e_value = tests_per_step * args.steps * world / e2e_t
+    h2d = T * 36
+    d2h = stats["level1"] * 5 + stats["boundary"] * (4 + cells)
+
+    # roofline of the dominant stage
+    per_call = {k: v / max(calls, 1) for k, v in stage_ms.items()}
+    dom = max(per_call, key=per_call.get)
+    N1 = stats["level1"]
+    B = stats["boundary"]
+    P = stats["pairs"]
+    hbm_bytes = {
+        "prep": T * (36 + 48 + 32),
+        "expand": N1 * 5 + B * 4 + (N1 // 8) * 2 + (N1 // 32) * 4,
+        "sort_lists": P * 8 * 3 * 3 + P * 16,
+        "level2": B * cells + P * 8 + P * 48,
+        "level1": T * 64 + P * 8 + N1 // 8,
+        "fill_finish": (N1 // 8) * 2,
+    }
+    ms = per_call[dom]
+    achieved = hbm_bytes[dom] / (ms / 1e3) / 1e9
+    roof = {"kernel_stage": dom, "bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"],
+            "unit": "GB/s", "frac": achieved / peaks["hbm_gbs"], "traffic": None,
+            "peak_source": peak_kind, "stage_ms_per_step": per_call}
+
+    line = {"metric": "tri-voxel tests/s", "value": value, "unit": "tests/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_total * 1e3 / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic",
+            "config": {"workload": cfg["name"], "desc": cfg["desc"], "triangles": T,
+                       "level1": cfg["level1"], "level2": cfg["level2"], "parallelism": "replicas",
+                       "l2_flush": "256 MiB write between steps (outside the timed spans)",
+                       "work_per_step": dict(zip(("sat1", "sat2", "ray1", "ray2"), work)),
+                       "stats": stats},
+            "meshes_per_s": args.steps * world / t_total,
+            "voxels_per_s": (N1 + B * cells) * args.steps * world / t_total,
+            "e2e": {"value": e2e_value, "unit": "tests/s", "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h, "ms_per_step": e2e_t * 1e3 / args.steps},
+            "gpu_launches": launches, "roofline": roof, "clocks": clk}
+    if rank == 0 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(tris, spec, tests_per_step, args.cpu_seconds,
+                                            os.cpu_count() or 1)
+        line["cpu_baseline"].pop("sec_per_mesh", None)
+    if rank == 0:
+        print(json.dumps(line))
+    ctx.close()
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -79,6 +79,9 @@ def lib():
     L.gpv_last_error.argtypes = [C.c_void_p]
     L.gpv_last_error.restype = C.c_char_p
     L.gpv_set_tile.argtypes = [C.c_void_p, C.c_int]
+    L.gpv_set_timing.argtypes = [C.c_void_p, C.c_int]
+    L.gpv_stage_times.argtypes = [C.c_void_p, C.POINTER(C.c_double), C.c_int]
+    L.gpv_kernel_launches.restype = C.c_uint64
     L.gpv_grid_padded.argtypes = [f3, f3, C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.POINTER(GridSpec)]
     L.gpv_grid_reference.argtypes = [f3, f3, C.c_float, C.c_int32, C.c_int32, C.POINTER(GridSpec)]
     L.gpv_voxelize.argtypes = [C.c_void_p, C.c_void_p, C.c_int64, C.POINTER(GridSpec),
@@ -106,6 +109,11 @@ def lib():
                                          C.POINTER(Result), C.c_void_p]
     _lib = L
     return L
+
+
+def kernel_launches():
+    """Kernels launched by libgpview.so in this process so far."""
+    return int(lib().gpv_kernel_launches())
 
 
 def _f3(v):
@@ -200,6 +208,17 @@ class Context:
 
     def error(self):
         return lib().gpv_last_error(self._h).decode()
+
+    STAGES = ("prep", "level1", "fill_finish", "expand", "sort_lists", "level2")
+
+    def set_timing(self, on=True):
+        self._check(lib().gpv_set_timing(self._h, int(bool(on))), "set_timing")
+
+    def stage_times(self):
+        """(calls, {stage: accumulated ms}) from the per-stage CUDA events."""
+        ms = (C.c_double * 8)()
+        calls = lib().gpv_stage_times(self._h, ms, 8)
+        return calls, {k: ms[i] for i, k in enumerate(self.STAGES)}
 
     def set_tile(self, t):
         rc = lib().gpv_set_tile(self._h, int(t))

@@ -12,7 +12,12 @@
 #include "gpv_internal.h"
 
 struct gpv_ctx {
+  static constexpr int kStages = 8;
   int device = 0;
+  bool timing = false;                 // record per-stage CUDA events on the launching stream
+  cudaEvent_t ev[kStages + 1] = {};
+  double stage_ms[kStages] = {};      // accumulated stage durations
+  uint64_t stage_calls = 0;
   std::string err;
   int tile = 128;
   gpv::MeshStats *h_stats = nullptr;  // pinned
@@ -237,8 +242,13 @@ static int voxelize_impl(gpv_ctx *ctx, const float *d_tris, int64_t T, const gpv
     if (l2) cudaFreeAsync(l2, s);
   };
 
+  auto mark = [&](int i) {
+    if (ctx->timing) cudaEventRecord(ctx->ev[i], s);
+  };
   // 1. per-triangle preparation and work counts
+  mark(0);
   launch_prep(g, b, s);
+  mark(1);
   GPV_CUDA(cudaMemcpyAsync(ctx->h_stats, b.stats, sizeof(MeshStats), cudaMemcpyDeviceToHost, s));
   GPV_CUDA(cudaStreamSynchronize(s));
   const uint64_t cap = std::max<uint64_t>(ctx->h_stats->sat1, 1);
@@ -249,10 +259,13 @@ static int voxelize_impl(gpv_ctx *ctx, const float *d_tris, int64_t T, const gpv
                            cudaMemcpyHostToDevice, s));
 
   // 2. Level1 SAT + fill, boundary counts
+  mark(2);
   launch_level1(g, b, ctx->tile, s);
+  mark(3);
   launch_fill_finish(g, b, s);
   launch_popc(g, b.bplane, wcnt, s);
   scan_u32(wcnt, wpre, N1w, d_tot, scan_tmp, s);
+  mark(4);
   GPV_CUDA(cudaGetLastError());
   GPV_CUDA(cudaMemcpyAsync(ctx->h_stats, b.stats, sizeof(MeshStats), cudaMemcpyDeviceToHost, s));
   GPV_CUDA(cudaMemcpyAsync(ctx->h_u32, d_tot, 4, cudaMemcpyDeviceToHost, s));
@@ -269,7 +282,9 @@ static int voxelize_impl(gpv_ctx *ctx, const float *d_tris, int64_t T, const gpv
   GPV_CUDA(cudaMallocAsync((void **)&bindex, 4 * std::max<int64_t>(B, 4), s));
   const int64_t l2bytes = gh.level2 ? B * gh.cells : 0;
   GPV_CUDA(cudaMallocAsync((void **)&l2, std::max<int64_t>(l2bytes, 16), s));
+  mark(5);
   launch_expand(g, b.bplane, b.iplane, wpre, l1, prefix, bindex, b.stats, s);
+  mark(6);
   if (gh.level2 && B > 0) {
     uint32_t *kalt, *valt, *flags, *uidx, *useg, *colend, *stmp;
     GPV_CUDA(ws.get(&kalt, (size_t)P));
@@ -286,12 +301,27 @@ static int voxelize_impl(gpv_ctx *ctx, const float *d_tris, int64_t T, const gpv
     scan_u32(flags, uidx, P, d_tot + 1, stmp, s);
     launch_useg(flags, uidx, P, useg, s);
     launch_colend(g, sk, useg, B, P, colend, s);
+    mark(7);
     launch_level2(g, b.ptri, b.fbox, sk, sv, useg, colend, prefix, B, l2, b.stats, s);
+  } else {
+    mark(7);
   }
+  mark(8);
   GPV_CUDA(cudaGetLastError());
   GPV_CUDA(cudaMemcpyAsync(ctx->h_stats, b.stats, sizeof(MeshStats), cudaMemcpyDeviceToHost, s));
   GPV_CUDA(cudaMemcpyAsync(ctx->h_u32 + 1, d_tot + 1, 4, cudaMemcpyDeviceToHost, s));
   GPV_CUDA(cudaStreamSynchronize(s));
+  if (ctx->timing) {
+    // stages: 0 prep, 1 level1, 2 fill finish + boundary scan, 3 expand, 4 sort + lists,
+    // 5 level2 (event pairs (0,1) (2,3) (3,4) (5,6) (6,7) (7,8))
+    const int pr[6][2] = {{0, 1}, {2, 3}, {3, 4}, {5, 6}, {6, 7}, {7, 8}};
+    for (int k = 0; k < 6; ++k) {
+      float ms = 0.f;
+      if (cudaEventElapsedTime(&ms, ctx->ev[pr[k][0]], ctx->ev[pr[k][1]]) == cudaSuccess)
+        ctx->stage_ms[k] += ms;
+    }
+    ctx->stage_calls++;
+  }
   const MeshStats &st = *ctx->h_stats;
   if (st.status) {
     drop_results();
@@ -366,6 +396,26 @@ void gpv_destroy(gpv_ctx *ctx) {
 }
 
 const char *gpv_last_error(gpv_ctx *ctx) { return ctx ? ctx->err.c_str() : "no context"; }
+
+int gpv_set_timing(gpv_ctx *ctx, int on) {
+  if (!ctx) return GPV_ERR_INVALID;
+  cudaSetDevice(ctx->device);
+  if (on && !ctx->ev[0])
+    for (int i = 0; i <= gpv_ctx::kStages; ++i)
+      if (cudaEventCreate(&ctx->ev[i]) != cudaSuccess) return GPV_ERR_CUDA;
+  ctx->timing = on != 0;
+  for (double &v : ctx->stage_ms) v = 0.0;
+  ctx->stage_calls = 0;
+  return GPV_OK;
+}
+
+int gpv_stage_times(gpv_ctx *ctx, double *ms, int n) {
+  if (!ctx || !ms) return GPV_ERR_INVALID;
+  for (int i = 0; i < n && i < gpv_ctx::kStages; ++i) ms[i] = ctx->stage_ms[i];
+  return (int)ctx->stage_calls;
+}
+
+uint64_t gpv_kernel_launches(void) { return gpv::launch_count(); }
 
 int gpv_set_tile(gpv_ctx *ctx, int t) {
   if (!ctx || (t != 32 && t != 64 && t != 128 && t != 256)) return GPV_ERR_INVALID;

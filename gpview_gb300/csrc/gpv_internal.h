@@ -10,6 +10,10 @@
 
 namespace gpv {
 
+// ---- launch accounting: every kernel launch of the library bumps this counter ----------------
+uint64_t launch_count();
+void count_launch(uint64_t n = 1);
+
 // ---- scan / sort (gpv_sort.cu) ---------------------------------------------------------------
 int64_t scan_temp_words(int64_t n);
 void scan_u32(const uint32_t *in, uint32_t *out, int64_t n, uint32_t *d_total, uint32_t *temp,

@@ -606,16 +606,17 @@ void launch_prep(const GridDev &g, const Level1Bufs &b, cudaStream_t s) {
   if (b.T <= 0) return;
   const unsigned nb = (unsigned)((b.T + 255) / 256);
   k_prep<<<nb, 256, 0, s>>>(g, b);
+  count_launch();
 }
 
 void launch_level1(const GridDev &g, const Level1Bufs &b, int tile, cudaStream_t s) {
   if (b.T <= 0) return;
   const unsigned nb = (unsigned)((b.T + tile - 1) / tile);
   switch (tile) {
-    case 32: k_level1<32><<<nb, kL1Threads, 0, s>>>(g, b); break;
-    case 64: k_level1<64><<<nb, kL1Threads, 0, s>>>(g, b); break;
-    case 128: k_level1<128><<<nb, kL1Threads, 0, s>>>(g, b); break;
-    default: k_level1<256><<<(unsigned)((b.T + 255) / 256), kL1Threads, 0, s>>>(g, b); break;
+    case 32: k_level1<32><<<nb, kL1Threads, 0, s>>>(g, b); count_launch(); break;
+    case 64: k_level1<64><<<nb, kL1Threads, 0, s>>>(g, b); count_launch(); break;
+    case 128: k_level1<128><<<nb, kL1Threads, 0, s>>>(g, b); count_launch(); break;
+    default: k_level1<256><<<(unsigned)((b.T + 255) / 256), kL1Threads, 0, s>>>(g, b); count_launch(); break;
   }
 }
 
@@ -623,11 +624,13 @@ void launch_fill_finish(const GridDev &g, const Level1Bufs &b, cudaStream_t s) {
   const int64_t warps = (int64_t)g.n[1] * g.nxw;
   const unsigned nb = (unsigned)((warps * 32 + 255) / 256);
   k_fill_finish<<<nb, 256, 0, s>>>(g, b);
+  count_launch();
 }
 
 void launch_popc(const GridDev &g, const uint32_t *bplane, uint32_t *cnt, cudaStream_t s) {
   const int64_t nw = (int64_t)g.n[2] * g.n[1] * g.nxw;
   k_popc<<<(unsigned)((nw + 255) / 256), 256, 0, s>>>(bplane, nw, cnt);
+  count_launch();
 }
 
 void launch_expand(const GridDev &g, const uint32_t *bplane, const uint32_t *iplane,
@@ -635,17 +638,20 @@ void launch_expand(const GridDev &g, const uint32_t *bplane, const uint32_t *ipl
                    MeshStats *st, cudaStream_t s) {
   const unsigned rows = (unsigned)((int64_t)g.n[2] * g.n[1]);
   k_expand<<<rows, 128, 0, s>>>(g, bplane, iplane, wpre, l1, prefix, bindex, st);
+  count_launch();
 }
 
 void launch_heads(const uint32_t *keys, int64_t P, uint32_t *flags, cudaStream_t s) {
   if (P <= 0) return;
   k_heads<<<(unsigned)((P + 255) / 256), 256, 0, s>>>(keys, P, flags);
+  count_launch();
 }
 
 void launch_useg(const uint32_t *flags, const uint32_t *uidx, int64_t P, uint32_t *useg,
                  cudaStream_t s) {
   if (P <= 0) return;
   k_useg<<<(unsigned)((P + 255) / 256), 256, 0, s>>>(flags, uidx, P, useg);
+  count_launch();
 }
 
 void launch_colend(const GridDev &g, const uint32_t *keys, const uint32_t *useg, int64_t B,
@@ -653,6 +659,7 @@ void launch_colend(const GridDev &g, const uint32_t *keys, const uint32_t *useg,
   (void)P;
   if (B <= 0) return;
   k_colend<<<(unsigned)((B + 255) / 256), 256, 0, s>>>(g, keys, useg, B, colend);
+  count_launch();
 }
 
 void launch_level2(const GridDev &g, const float4 *ptri, const float4 *fbox,

@@ -6,6 +6,8 @@
 // sort_pairs: stable LSD radix sort of (u32 key, u32 value), 8-bit digits; per pass a tile
 //             histogram, a scan of the digit-major histogram, and a stable scatter whose
 //             in-tile ranks come from __match_any_sync peer masks.
+#include <atomic>
+
 #include "gpv_internal.h"
 
 namespace gpv {
@@ -171,6 +173,12 @@ __global__ void k_radix_scatter(const uint32_t *__restrict__ keys, const uint32_
 
 }  // namespace
 
+namespace {
+std::atomic<uint64_t> g_launches{0};
+}
+uint64_t launch_count() { return g_launches.load(); }
+void count_launch(uint64_t n) { g_launches.fetch_add(n); }
+
 int64_t scan_temp_words(int64_t n) { return (n + kScanTile - 1) / kScanTile + 1; }
 
 void scan_u32(const uint32_t *in, uint32_t *out, int64_t n, uint32_t *d_total, uint32_t *temp,
@@ -183,6 +191,7 @@ void scan_u32(const uint32_t *in, uint32_t *out, int64_t n, uint32_t *d_total, u
   k_scan_reduce<<<(unsigned)nb, kScanThreads, 0, s>>>(in, n, temp);
   k_scan_partials<<<1, 1024, 0, s>>>(temp, nb, d_total);
   k_scan_down<<<(unsigned)nb, kScanThreads, 0, s>>>(in, n, temp, out);
+  count_launch(3);
 }
 
 int64_t sort_temp_words(int64_t n) {
@@ -208,6 +217,7 @@ bool sort_pairs(uint32_t *keys, uint32_t *vals, uint32_t *kalt, uint32_t *valt, 
     k_radix_hist<<<(unsigned)nb, kSortThreads, 0, s>>>(ki, n, shift, hist, nb);
     scan_u32(hist, hoff, 256 * nb, nullptr, stmp, s);
     k_radix_scatter<<<(unsigned)nb, kSortThreads, 0, s>>>(ki, vi, n, shift, hoff, nb, ko, vo);
+    count_launch(2);
     alt = !alt;
   }
   return alt;

@@ -103,6 +103,14 @@ void gpv_destroy(gpv_ctx *ctx);
 const char *gpv_last_error(gpv_ctx *ctx);
 /* Tunables (autotuner output): triangles per Level1 tile (32..256, power of two). */
 int gpv_set_tile(gpv_ctx *ctx, int tris_per_tile);
+/* Per-stage CUDA-event timing on the launching stream (off by default).  Stages:
+ * 0 prep, 1 Level1 SAT+fill, 2 fill finish + boundary scan, 3 Level1 expansion,
+ * 4 pair sort + lists, 5 Level2.  gpv_stage_times returns the number of timed calls and the
+ * accumulated milliseconds per stage. */
+int gpv_set_timing(gpv_ctx *ctx, int on);
+int gpv_stage_times(gpv_ctx *ctx, double *ms, int n);
+/* Number of kernels this library has launched in this process. */
+uint64_t gpv_kernel_launches(void);
 
 /* ---- grids --------------------------------------------------------------------------------- */
 /* Explicit grid: n^3 cells over the mesh box grown by one cell on every side. */

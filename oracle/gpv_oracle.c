@@ -373,17 +373,21 @@ static int orc_threads(int req)
 /* Conservative x/y candidate test used by ORC_FILL_CAND.  The margin is a generous multiple of
  * the float rounding bound of the u/v tests; triangles whose projection is ill-conditioned
  * (det rounding bound comparable to det) are tested against every column. */
-typedef struct { float lo[2], hi[2]; int all; } orc_xybox;
+typedef struct { float lo[2], hi[2]; int all, none; } orc_xybox;
 
 static void orc_xy_box(const float *tv, float gx, float gy, orc_xybox *b)
 {
     float e1x = tv[3] - tv[0], e1y = tv[4] - tv[1];
     float e2x = tv[6] - tv[0], e2y = tv[7] - tv[1];
-    double det = (double)e1x * (-(double)e2y) + (double)e1y * e2x;
+    /* the float determinant of the test itself: when it fails the 1e-6 test no column passes */
+    float detf = e1x * (-e2y) + e1y * e2x;
+    double det = detf;
     double sd = fabs((double)e1x * e2y) + fabs((double)e1y * e2x);
     const double eps = 5.9604644775390625e-08; /* 2^-24 */
     b->all = 0;
-    if (!(fabs(det) > 1e-7) || 64.0 * eps * sd >= fabs(det)) { b->all = 1; return; }
+    b->none = 0;
+    if (det > -0.000001 && det < 0.000001) { b->none = 1; return; }
+    if (64.0 * eps * sd >= fabs(det)) { b->all = 1; return; }
     double G = gx > gy ? gx : gy;
     double au = 64.0 * eps * G * (fabs(e2x) + fabs(e2y)) / fabs(det);
     double av = 64.0 * eps * G * (fabs(e1x) + fabs(e1y)) / fabs(det);
@@ -469,7 +473,8 @@ static void orc_fill_level1(orc_run *r, int mode, int nth)
     for (int64_t t = 0; t < T; ++t) {
         orc_xy_box(r->tris + 9 * t, r->t.g[0], r->t.g[1], &bx[t]);
         int *q = rng + 4 * t;
-        if (bx[t].all) { q[0] = 0; q[1] = nx - 1; q[2] = 0; q[3] = ny - 1; nall++; }
+        if (bx[t].none) { q[0] = 1; q[1] = 0; q[2] = 1; q[3] = 0; }
+        else if (bx[t].all) { q[0] = 0; q[1] = nx - 1; q[2] = 0; q[3] = ny - 1; nall++; }
         else {
             /* columns whose centre lies in [lo,hi] of the monotone centre tables */
             q[0] = orc_first_ge(cx, nx, bx[t].lo[0]);

@@ -43,3 +43,108 @@ def test_small_sphere_vs_brute_force(ctx):
     tris = gpv.gen_uvsphere(11, 24, 12, (0.5, 0.5, 0.5), 0.4, 0.002)
     mn, mx = gpv.mesh_bounds(tris)
     _check_full(ctx, tris, gpv.grid_padded(mn, mx, 20, 4), fill=orc.FILL_VOXEL)
+
+
+def test_torus262k_full(ctx):
+    tris, spec = W.make(W.C2)
+    _check_full(ctx, tris, spec)
+
+
+def test_star1310k_level1_full_level2_sampled(ctx):
+    """Level1 outputs in full; Level2 on three seeded ranges of boundary voxels."""
+    tris, spec = W.make(W.C3)
+    res = ctx.voxelize_host(tris, spec)
+    l1, pre, bi, l2 = ctx.fetch(res)
+    ref = orc.Run(tris, spec, fill=orc.FILL_CAND)
+    assert res.num_boundary == ref.B
+    np.testing.assert_array_equal(l1, ref.level1_bytes())
+    np.testing.assert_array_equal(pre, ref.prefix())
+    np.testing.assert_array_equal(bi, ref.boundary_index())
+    assert res.num_pairs == ref.num_pairs()
+    cells = ref.cells
+    rng = np.random.default_rng(1234)
+    for b0 in sorted(rng.integers(0, max(ref.B - 3000, 1), size=3)):
+        b1 = min(int(b0) + 3000, ref.B)
+        exp = ref.level2_bytes(int(b0), b1)
+        np.testing.assert_array_equal(l2[int(b0) * cells:b1 * cells], exp)
+    ctx.release(res)
+
+
+def _pad_spec(tris, n, n2):
+    import gpview_gb300 as gpv
+
+    mn, mx = gpv.mesh_bounds(tris)
+    return gpv.grid_padded(mn, mx, n, n2)
+
+
+def test_empty_mesh(ctx):
+    import gpview_gb300 as gpv
+
+    spec = gpv.grid_padded((0, 0, 0), (1, 1, 1), 16, 4)
+    res = ctx.voxelize_host(np.zeros(0, np.float32), spec)
+    l1, pre, bi, l2 = ctx.fetch(res)
+    assert res.num_boundary == 0 and not l1.any() and not pre.any() and l2.size == 0
+    ctx.release(res)
+
+
+def test_single_open_triangle(ctx):
+    tris = np.array([0.1, 0.2, 0.3, 0.9, 0.25, 0.5, 0.4, 0.8, 0.7], np.float32)
+    _check_full(ctx, tris, _pad_spec(tris, 12, 4), fill=orc.FILL_VOXEL)
+
+
+def test_axis_aligned_cube(ctx):
+    """Faces on cell boundaries and vertices on the box maximum (the reference's decrement)."""
+    v = np.array([[0, 0, 0], [1, 0, 0], [1, 1, 0], [0, 1, 0], [0, 0, 1], [1, 0, 1], [1, 1, 1], [0, 1, 1]],
+                 np.float32)
+    f = [(0, 2, 1), (0, 3, 2), (4, 5, 6), (4, 6, 7), (0, 1, 5), (0, 5, 4), (1, 2, 6), (1, 6, 5),
+         (2, 3, 7), (2, 7, 6), (3, 0, 4), (3, 4, 7)]
+    tris = np.concatenate([v[list(t)].reshape(-1) for t in f]).astype(np.float32)
+    import gpview_gb300 as gpv
+
+    for spec in (gpv.grid_padded((0, 0, 0), (1, 1, 1), 10, 2),
+                 _spec_exact((0, 0, 0), (1, 1, 1), (8, 8, 8), (4, 4, 4))):
+        _check_full(ctx, tris, spec, fill=orc.FILL_VOXEL)
+
+
+def _spec_exact(mn, mx, n, n2):
+    import gpview_gb300 as gpv
+
+    s = gpv.GridSpec()
+    s.bbox_min[:] = mn
+    s.bbox_max[:] = mx
+    s.ndiv[:] = n
+    s.ndiv2[:] = n2
+    return s
+
+
+def test_nonuniform_divisions_and_odd_sizes(ctx):
+    import gpview_gb300 as gpv
+
+    tris = gpv.gen_torus(5, 64, 32, (0.5, 0.5, 0.5), 0.3, 0.1, 0.01)
+    _check_full(ctx, tris, _pad_spec(tris, (37, 21, 70), (3, 5, 2)))
+    _check_full(ctx, tris, _pad_spec(tris, (33, 64, 40), (8, 8, 8)))
+
+
+def test_superellipsoids_and_tiles(ctx):
+    import gpview_gb300 as gpv
+
+    rng = np.random.default_rng(5)
+    for k, tile in enumerate((32, 64, 128, 256)):
+        ctx.set_tile(tile)
+        e1, e2 = rng.uniform(0.3, 2.0, 2)
+        semi = rng.uniform(0.2, 0.45, 3)
+        q, _ = np.linalg.qr(rng.normal(size=(3, 3)))
+        tris = gpv.gen_superellipsoid(k, 40, 20, (0.5, 0.5, 0.5), semi, e1, e2, q.astype(np.float32))
+        _check_full(ctx, tris, _pad_spec(tris, 40, 4))
+    ctx.set_tile(128)
+
+
+def test_reference_grid_sizing(ctx):
+    """GPView's own sizing (voxelCount=8 -> GetNextDiv4 divisions) on a generated mesh."""
+    import gpview_gb300 as gpv
+
+    tris = gpv.gen_uvsphere(3, 40, 20, (0.2, -0.3, 1.5), 2.0, 0.01)
+    mn, mx = gpv.mesh_bounds(tris)
+    pad = np.float32(0.001) * np.linalg.norm(mx - mn)
+    spec = gpv.grid_reference(mn - pad, mx + pad, float((mx - mn).max() + 2 * pad), 32, 4)
+    _check_full(ctx, tris, spec)
