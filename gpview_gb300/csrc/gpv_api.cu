@@ -96,6 +96,9 @@ int grid_derive(const gpv_grid_spec &spec, GridHost &gh, const float *ext1_overr
   while (kb < 32 && ((int64_t)1 << kb) < N1) ++kb;
   gh.key_bits = kb;
   gh.thr = eps_threshold();
+  gh.oz_monotone = true;
+  for (size_t q = 1; q < gh.o2[2].size(); ++q)
+    if (!(gh.o2[2][q] > gh.o2[2][q - 1])) gh.oz_monotone = false;
   return GPV_OK;
 }
 
@@ -132,6 +135,7 @@ GridDev make_griddev(const GridHost &gh, const float *dt) {
   g.nzw = gh.nzw;
   g.key_bits = gh.key_bits;
   g.thr = gh.thr;
+  g.oz_monotone = gh.oz_monotone ? 1 : 0;
   return g;
 }
 
@@ -286,23 +290,22 @@ static int voxelize_impl(gpv_ctx *ctx, const float *d_tris, int64_t T, const gpv
   launch_expand(g, b.bplane, b.iplane, wpre, l1, prefix, bindex, b.stats, s);
   mark(6);
   if (gh.level2 && B > 0) {
-    uint32_t *kalt, *valt, *flags, *uidx, *useg, *colend, *stmp;
+    uint32_t *kalt, *valt, *flags, *uidx, *useg, *stmp, *l2tmp;
     GPV_CUDA(ws.get(&kalt, (size_t)P));
     GPV_CUDA(ws.get(&valt, (size_t)P));
     GPV_CUDA(ws.get(&flags, (size_t)P));
     GPV_CUDA(ws.get(&uidx, (size_t)P));
     GPV_CUDA(ws.get(&useg, (size_t)B + 1));
-    GPV_CUDA(ws.get(&colend, (size_t)ncol));
     GPV_CUDA(ws.get(&stmp, (size_t)std::max(sort_temp_words(P), scan_temp_words(P))));
+    GPV_CUDA(ws.get(&l2tmp, (size_t)level2_temp_words(B)));
     const bool in_alt = sort_pairs(b.keys, b.vals, kalt, valt, P, gh.key_bits, stmp, s);
     const uint32_t *sk = in_alt ? kalt : b.keys;
     const uint32_t *sv = in_alt ? valt : b.vals;
     launch_heads(sk, P, flags, s);
     scan_u32(flags, uidx, P, d_tot + 1, stmp, s);
     launch_useg(flags, uidx, P, useg, s);
-    launch_colend(g, sk, useg, B, P, colend, s);
     mark(7);
-    launch_level2(g, b.ptri, b.fbox, sk, sv, useg, colend, prefix, B, l2, b.stats, s);
+    launch_level2c(g, b.ptri, b.fbox, sk, sv, useg, prefix, B, l2tmp, l2, b.stats, s);
   } else {
     mark(7);
   }

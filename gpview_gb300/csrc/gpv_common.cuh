@@ -49,6 +49,7 @@ struct GridDev {
   int nzw;              // 32-bit words per column of the toggle plane
   int key_bits;         // bits of the column-major voxel key
   float thr;            // largest float below 1e-6
+  int oz_monotone;      // Level2 ray-origin heights strictly increase along every column
 };
 
 __device__ __forceinline__ float fm(float a, float b) { return __fmul_rn(a, b); }
@@ -184,6 +185,17 @@ __device__ __forceinline__ void ray_tri(const float *V, float thr, RayTri &r) {
   const float det = fa(fm(r.e1x, -r.e2y), fm(r.e1y, r.e2x));
   r.ok = (det < -thr) || (det > thr);
   r.inv_det = __fdiv_rn(1.0f, det);
+}
+
+// Same constants with 1/det taken from the per-triangle record written by the prep kernel
+// (computed there with the same __fdiv_rn(1, det)); `ok` is not evaluated here -- callers skip
+// triangles whose conservative ray box is empty, which is the case exactly when det fails.
+__device__ __forceinline__ void ray_tri_pre(const float *V, float inv_det, RayTri &r) {
+  r.v1x = V[0]; r.v1y = V[1]; r.v1z = V[2];
+  r.e1x = fs(V[3], V[0]); r.e1y = fs(V[4], V[1]); r.e1z = fs(V[5], V[2]);
+  r.e2x = fs(V[6], V[0]); r.e2y = fs(V[7], V[1]); r.e2z = fs(V[8], V[2]);
+  r.inv_det = inv_det;
+  r.ok = true;
 }
 
 struct RayCol { float Tx, Ty; };

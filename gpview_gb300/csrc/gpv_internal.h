@@ -31,6 +31,7 @@ struct GridHost {
   int64_t N1 = 0, cells = 0;
   int nxw = 0, nzw = 0, key_bits = 0;
   bool level2 = false;
+  bool oz_monotone = false;
   float thr = 0.f;
 };
 // Derives sizes and coordinate tables exactly as the reference does (double then float).
@@ -62,12 +63,13 @@ void launch_expand(const GridDev &g, const uint32_t *bplane, const uint32_t *ipl
 void launch_heads(const uint32_t *keys, int64_t P, uint32_t *flags, cudaStream_t s);
 void launch_useg(const uint32_t *flags, const uint32_t *uidx, int64_t P, uint32_t *useg,
                  cudaStream_t s);
-void launch_colend(const GridDev &g, const uint32_t *keys, const uint32_t *useg, int64_t B,
-                   int64_t P, uint32_t *colend, cudaStream_t s);
-void launch_level2(const GridDev &g, const float4 *ptri, const float4 *fbox,
-                   const uint32_t *keys, const uint32_t *vals, const uint32_t *useg,
-                   const uint32_t *colend, const int32_t *prefix, int64_t B, uint8_t *l2,
-                   MeshStats *st, cudaStream_t s);
+int level2_chunk(const GridDev &g);
+size_t level2_smem(const GridDev &g);
+int64_t level2_temp_words(int64_t B);
+void launch_level2c(const GridDev &g, const float4 *ptri, const float4 *fbox,
+                    const uint32_t *keys, const uint32_t *vals, const uint32_t *useg,
+                    const int32_t *prefix, int64_t B, uint32_t *tmp, uint8_t *l2, MeshStats *st,
+                    cudaStream_t s);
 
 GridDev make_griddev(const GridHost &gh, const float *dtables);
 int64_t table_floats(const GridHost &gh);

@@ -15,8 +15,7 @@
 //                 the linear (x fastest) inside plane.
 //   sort          radix sort of the pairs by column-major voxel key (gpv_sort.cu).
 //   k_expand      .raw bytes of Level1, boundaryPrefixSum, boundaryIndex.
-//   k_level2      one warp per boundary voxel: Level2 SAT of its own triangles and +z parity
-//                 against the column union of triangles at z >= k, written as .raw bytes.
+//   Level2        gpv_level2.cu.
 #include "gpv_internal.h"
 
 namespace gpv {
@@ -156,7 +155,9 @@ __global__ void __launch_bounds__(256) k_prep(GridDev g, Level1Bufs b) {
     else { fx0 = 1; fx1 = 0; fy0 = 1; fy1 = 0; }
     b.ptri[3 * t + 0] = make_float4(V[0], V[1], V[2], __uint_as_float(pack2(fx0, fx1)));
     b.ptri[3 * t + 1] = make_float4(V[3], V[4], V[5], __uint_as_float(pack2(fy0, fy1)));
-    b.ptri[3 * t + 2] = make_float4(V[6], V[7], V[8], 0.f);
+    // 1/det of the +z ray test (src/TriRayIntersection.cpp:310), shared by every column
+    const float det = fa(fm(fs(V[3], V[0]), -fs(V[7], V[1])), fm(fs(V[4], V[1]), fs(V[6], V[0])));
+    b.ptri[3 * t + 2] = make_float4(V[6], V[7], V[8], __fdiv_rn(1.0f, det));
     b.rng[t] = make_int4((int)pack2(lo[0], hi[0]), (int)pack2(lo[1], hi[1]),
                          (int)pack2(lo[2], hi[2]), 0);
     b.fbox[t] = fb;
@@ -321,9 +322,9 @@ __global__ void __launch_bounds__(kL1Threads) k_level1(GridDev g, Level1Bufs b) 
       const int j = lo16(fyr) + (int)(c / (uint32_t)nxr);
       const float V[9] = {a0.x, a0.y, a0.z, a1.x, a1.y, a1.z, a2.x, a2.y, a2.z};
       RayTri rt;
-      ray_tri(V, g.thr, rt);
+      ray_tri_pre(V, a2.w, rt);  // fill units exist only for triangles passing the det test
       RayCol rc;
-      pass = rt.ok && ray_col(rt, __ldg(g.c1[0] + i), __ldg(g.c1[1] + j), rc);
+      pass = ray_col(rt, __ldg(g.c1[0] + i), __ldg(g.c1[1] + j), rc);
     }
     const unsigned qm = __ballot_sync(FULL, pass);
     if (pass) s_q[warp][__popc(qm & lt_mask)] = u;
@@ -340,7 +341,7 @@ __global__ void __launch_bounds__(kL1Threads) k_level1(GridDev g, Level1Bufs b) 
       const int j = lo16(fyr) + (int)(c / (uint32_t)nxr);
       const float V[9] = {a0.x, a0.y, a0.z, a1.x, a1.y, a1.z, a2.x, a2.y, a2.z};
       RayTri rt;
-      ray_tri(V, g.thr, rt);
+      ray_tri_pre(V, a2.w, rt);
       RayCol rc;
       ray_col(rt, __ldg(g.c1[0] + i), __ldg(g.c1[1] + j), rc);
       const size_t col = (size_t)j * nx + i;
@@ -449,156 +450,6 @@ __global__ void k_useg(const uint32_t *__restrict__ flags, const uint32_t *__res
   if (e == P - 1) useg[uidx[e] + flags[e]] = (uint32_t)P;
 }
 
-__global__ void k_colend(GridDev g, const uint32_t *__restrict__ keys,
-                         const uint32_t *__restrict__ useg, int64_t B,
-                         uint32_t *__restrict__ colend) {
-  const int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (u >= B) return;
-  const uint32_t nz = (uint32_t)g.n[2];
-  const uint32_t col = keys[useg[u]] / nz;
-  const bool last = (u == B - 1) || (keys[useg[u + 1]] / nz != col);
-  if (last) colend[col] = useg[u + 1];
-}
-
-// ---------------------------------------------------------------------------------------------
-constexpr int kL2Warps = 8;
-
-__device__ __forceinline__ void l2_range(float tmin, float tmax, float c0, float h, float g2,
-                                         int n2, int &lo, int &hi) {
-  const float vmin = c0 - h;
-  const float delta = 8.f * EPS24 * (fabsf(tmin) + fabsf(tmax) + fabsf(vmin) + h);
-  float f0 = (tmin - delta - vmin) / g2;
-  float f1 = (tmax + delta - vmin) / g2;
-  f0 = fminf(fmaxf(f0, -4.f), (float)n2 + 4.f);
-  f1 = fminf(fmaxf(f1, -4.f), (float)n2 + 4.f);
-  lo = max((int)floorf(f0) - 1, 0);
-  hi = min((int)floorf(f1) + 1, n2 - 1);
-}
-
-__global__ void __launch_bounds__(kL2Warps * 32) k_level2(
-    GridDev g, const float4 *__restrict__ ptri, const float4 *__restrict__ fbox,
-    const uint32_t *__restrict__ keys, const uint32_t *__restrict__ vals,
-    const uint32_t *__restrict__ useg, const uint32_t *__restrict__ colend,
-    const int32_t *__restrict__ prefix, int64_t B, uint8_t *__restrict__ l2, MeshStats *st) {
-  extern __shared__ uint32_t sm[];
-  const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
-  const int n2x = g.n2[0], n2y = g.n2[1], n2z = g.n2[2];
-  const int cells = n2x * n2y * n2z;
-  const int W = (cells + 31) >> 5;
-  uint32_t *sat = sm + (size_t)warp * 2 * W;
-  uint32_t *par = sat + W;
-  const int64_t u = (int64_t)blockIdx.x * kL2Warps + warp;
-  if (u >= B) return;
-  for (int w = lane; w < W; w += 32) { sat[w] = 0; par[w] = 0; }
-  __syncwarp();
-
-  const int nx = g.n[0], ny = g.n[1], nz = g.n[2];
-  const uint32_t e0 = useg[u], e1 = useg[u + 1];
-  const uint32_t key = keys[e0];
-  const uint32_t col = key / (uint32_t)nz;
-  const int k = (int)(key - col * (uint32_t)nz);
-  const int i = (int)(col % (uint32_t)nx), j = (int)(col / (uint32_t)nx);
-  const int64_t vlin = ((int64_t)k * ny + j) * nx + i;
-  const int32_t bidx = prefix[vlin];
-  const uint32_t cend = colend[col];
-  const float *sx = g.c2s[0] + (size_t)i * n2x, *sy = g.c2s[1] + (size_t)j * n2y,
-              *sz = g.c2s[2] + (size_t)k * n2z;
-  const float *ox = g.o2[0] + (size_t)i * n2x, *oy = g.o2[1] + (size_t)j * n2y,
-              *oz = g.o2[2] + (size_t)k * n2z;
-
-  // Level2 SAT: the voxel's own triangles against the sub-cells near each triangle's box.
-  for (uint32_t e = e0; e < e1; ++e) {
-    const uint32_t t = vals[e] & 0x7fffffffu;
-    const float4 a0 = __ldg(ptri + 3 * (size_t)t), a1 = __ldg(ptri + 3 * (size_t)t + 1),
-                 a2 = __ldg(ptri + 3 * (size_t)t + 2);
-    const float V[9] = {a0.x, a0.y, a0.z, a1.x, a1.y, a1.z, a2.x, a2.y, a2.z};
-    int p0, p1, q0, q1, r0, r1;
-    l2_range(fminf(V[0], fminf(V[3], V[6])), fmaxf(V[0], fmaxf(V[3], V[6])), __ldg(sx), g.e2[0],
-             g.g2[0], n2x, p0, p1);
-    l2_range(fminf(V[1], fminf(V[4], V[7])), fmaxf(V[1], fmaxf(V[4], V[7])), __ldg(sy), g.e2[1],
-             g.g2[1], n2y, q0, q1);
-    l2_range(fminf(V[2], fminf(V[5], V[8])), fmaxf(V[2], fmaxf(V[5], V[8])), __ldg(sz), g.e2[2],
-             g.g2[2], n2z, r0, r1);
-    if (p0 > p1 || q0 > q1 || r0 > r1) continue;
-    const int np = p1 - p0 + 1;
-    const int ncol = np * (q1 - q0 + 1);
-    for (int cc = lane; cc < ncol; cc += 32) {
-      const int p = p0 + cc % np, q = q0 + cc / np;
-      SatCol s;
-      if (!sat_col(V, __ldg(sx + p), __ldg(sy + q), g.e2, s)) continue;
-      for (int r = r0; r <= r1; ++r)
-        if (sat_z(s, V, __ldg(sz + r), g.e2)) {
-          const int c = (r * n2y + q) * n2x + p;
-          atomicOr(&sat[c >> 5], 1u << (c & 31));
-        }
-    }
-  }
-
-  // Level2 fill: +z parity against the union of the column's triangles at z >= k; each triangle
-  // appears once (the entry flagged as its topmost occurrence in the column).
-  uint32_t nun = 0;
-  const int ncols2 = n2x * n2y;
-  for (uint32_t e = e0; e < cend; ++e) {
-    const uint32_t vv = vals[e];
-    if (!(vv & 0x80000000u)) continue;
-    ++nun;
-    const uint32_t t = vv & 0x7fffffffu;
-    const float4 a0 = __ldg(ptri + 3 * (size_t)t), a1 = __ldg(ptri + 3 * (size_t)t + 1),
-                 a2 = __ldg(ptri + 3 * (size_t)t + 2);
-    const float V[9] = {a0.x, a0.y, a0.z, a1.x, a1.y, a1.z, a2.x, a2.y, a2.z};
-    RayTri rt;
-    ray_tri(V, g.thr, rt);
-    if (!rt.ok) continue;
-    const float4 fb = __ldg(fbox + t);
-    for (int cc = lane; cc < ncols2; cc += 32) {
-      const int p = cc % n2x, q = cc / n2x;
-      const float x = __ldg(ox + p), y = __ldg(oy + q);
-      if (x < fb.x || x > fb.z || y < fb.y || y > fb.w) continue;
-      RayCol rc;
-      if (!ray_col(rt, x, y, rc)) continue;
-      uint32_t bits = 0;
-      for (int r = 0; r < n2z; ++r)
-        if (ray_t(rt, rc, __ldg(oz + r), g.thr)) bits |= 1u << r;
-      if (bits) {
-        const int off = cc * n2z;  // (q*n2x + p) * n2z
-        const int sh = off & 31;
-        atomicXor(&par[off >> 5], bits << sh);
-        if (sh + n2z > 32) atomicXor(&par[(off >> 5) + 1], bits >> (32 - sh));
-      }
-    }
-  }
-  __syncwarp();
-
-  uint8_t *out = l2 + (size_t)bidx * cells;
-  unsigned long long nin = 0, nbd = 0;
-  const bool vec = (cells & 3) == 0;
-  for (int c4 = lane * 4; c4 < cells; c4 += 128) {
-    uint32_t word = 0;
-#pragma unroll
-    for (int d = 0; d < 4; ++d) {
-      const int c = c4 + d;
-      if (c >= cells) break;
-      const int p = c % n2x, q = (c / n2x) % n2y, r = c / (n2x * n2y);
-      const uint32_t sb = (sat[c >> 5] >> (c & 31)) & 1u;
-      const int pi = (q * n2x + p) * n2z + r;
-      const uint32_t pb = (par[pi >> 5] >> (pi & 31)) & 1u;
-      const uint32_t s = sb ? 254u : (pb ? 127u : 0u);
-      nin += (!sb && pb);
-      nbd += sb;
-      if (vec) word |= s << (8 * d);
-      else out[c] = (uint8_t)s;
-    }
-    if (vec) *reinterpret_cast<uint32_t *>(out + c4) = word;
-  }
-  nin = warp_sum(nin);
-  nbd = warp_sum(nbd);
-  if (lane == 0) {
-    if (nin) atomicAdd(&st->l2_inside, nin);
-    if (nbd) atomicAdd(&st->l2_boundary, nbd);
-    if (nun) atomicAdd(&st->ray2, (unsigned long long)nun * cells);
-  }
-}
-
 }  // namespace
 
 // ---- launchers --------------------------------------------------------------------------------
@@ -652,32 +503,6 @@ void launch_useg(const uint32_t *flags, const uint32_t *uidx, int64_t P, uint32_
   if (P <= 0) return;
   k_useg<<<(unsigned)((P + 255) / 256), 256, 0, s>>>(flags, uidx, P, useg);
   count_launch();
-}
-
-void launch_colend(const GridDev &g, const uint32_t *keys, const uint32_t *useg, int64_t B,
-                   int64_t P, uint32_t *colend, cudaStream_t s) {
-  (void)P;
-  if (B <= 0) return;
-  k_colend<<<(unsigned)((B + 255) / 256), 256, 0, s>>>(g, keys, useg, B, colend);
-  count_launch();
-}
-
-void launch_level2(const GridDev &g, const float4 *ptri, const float4 *fbox,
-                   const uint32_t *keys, const uint32_t *vals, const uint32_t *useg,
-                   const uint32_t *colend, const int32_t *prefix, int64_t B, uint8_t *l2,
-                   MeshStats *st, cudaStream_t s) {
-  if (B <= 0) return;
-  const int cells = g.n2[0] * g.n2[1] * g.n2[2];
-  const int W = (cells + 31) >> 5;
-  const size_t smem = (size_t)kL2Warps * 2 * W * sizeof(uint32_t);
-  static bool attr_set = false;
-  if (!attr_set) {
-    cudaFuncSetAttribute(k_level2, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-    attr_set = true;
-  }
-  const unsigned nb = (unsigned)((B + kL2Warps - 1) / kL2Warps);
-  k_level2<<<nb, kL2Warps * 32, smem, s>>>(g, ptri, fbox, keys, vals, useg, colend, prefix, B,
-                                           l2, st);
 }
 
 }  // namespace gpv

@@ -1,0 +1,450 @@
+// gpv_level2.cu -- Level2 refinement of the boundary voxels, organised per Level1 column.
+//
+// Reference semantics (src/Object.cpp:1111-1207 and :2344-2400): for boundary voxel b at
+// (i,j,k), a Level2 cell is 2 if the SAT passes for any triangle recorded in b; otherwise 1 if
+// the +z ray from the cell's origin crosses an odd number of distinct triangles among those
+// recorded in voxels (i,j,z) with z >= k; otherwise 0.
+//
+// Work unit: a chunk of up to CH consecutive boundary voxels of one Level1 column (one warp).
+//   SAT   -- (triangle, sub-column) items of each voxel, flattened over the 32 lanes; the cells
+//            of a sub-column are tested only inside the plane slab that can pass the SAT's own
+//            plane test (PlaneSlab), and one atomic per sub-column writes the z bits.
+//   fill  -- the column's triangle entries flagged as topmost occurrences are the union sets
+//            of all voxels of the chunk at once (voxel k sees the triangles whose topmost z is
+//            >= k).  The u/v part of each ray test depends only on the sub-column, so it runs
+//            once per (triangle, sub-column) for the whole chunk.  Voxels that lie certainly below
+//            the triangle (t at their top origin exceeds 1e-6 by twice a float error bound) are
+//            entirely hit: one "full hit" toggle marks the highest of them and a suffix XOR over
+//            the chunk's voxels expands it.  The remaining voxels evaluate t per origin.
+#include "gpv_internal.h"
+
+namespace gpv {
+
+namespace {
+
+constexpr unsigned FULL = 0xffffffffu;
+constexpr float EPS24 = 5.9604644775390625e-08f;  // 2^-24
+constexpr int kWarps = 4;
+constexpr int kMaskWords = 512;  // words of one mask kind per warp (sets the chunk length)
+
+__device__ __forceinline__ uint32_t warp_incl_scan(uint32_t v) {
+  const unsigned lane = threadIdx.x & 31u;
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    uint32_t o = __shfl_up_sync(FULL, v, d);
+    if (lane >= (unsigned)d) v += o;
+  }
+  return v;
+}
+
+template <typename T>
+__device__ __forceinline__ T warp_sum(T v) {
+#pragma unroll
+  for (int d = 16; d > 0; d >>= 1) v += __shfl_xor_sync(FULL, v, d);
+  return v;
+}
+
+// Sub-cells along one axis whose box can meet [tmin, tmax]: every cell outside the returned
+// range is rejected by the SAT's own box-axis test (the range is widened by several ulps and
+// one cell on each side).
+__device__ __forceinline__ void l2_range(float tmin, float tmax, float c0, float h, float g2,
+                                         int n2, int &lo, int &hi) {
+  const float vmin = c0 - h;
+  const float delta = 8.f * EPS24 * (fabsf(tmin) + fabsf(tmax) + fabsf(vmin) + h);
+  float f0 = (tmin - delta - vmin) / g2;
+  float f1 = (tmax + delta - vmin) / g2;
+  f0 = fminf(fmaxf(f0, -4.f), (float)n2 + 4.f);
+  f1 = fminf(fmaxf(f1, -4.f), (float)n2 + 4.f);
+  lo = max((int)floorf(f0) - 1, 0);
+  hi = min((int)floorf(f1) + 1, n2 - 1);
+}
+
+// Slab of cell centres the triangle's plane test can accept.  For a cell centre c the SAT's
+// plane test (planeBoxOverlap on the box-relative, rounded edges) can only pass when
+//   |n_f . (V0 - c)| <= |n_f| . h + E,
+// with n_f the float normal (V1-V0) x (V2-V1) and E a bound on the float deviations of both
+// sides from exact arithmetic.  With R the largest |V_i,q - c_q| over the voxel's centres and
+// h the largest half size, the deviations sum to less than 736 eps R^2 (h + R); E uses 1024.
+struct PlaneSlab { float nx, ny, nz, H; };
+
+__device__ __forceinline__ PlaneSlab plane_slab(const float *V, float cx0, float cx1, float cy0,
+                                                float cy1, float cz0, float cz1, const float h[3]) {
+  const float a0 = fs(V[3], V[0]), a1 = fs(V[4], V[1]), a2 = fs(V[5], V[2]);
+  const float b0 = fs(V[6], V[3]), b1 = fs(V[7], V[4]), b2 = fs(V[8], V[5]);
+  PlaneSlab ps;
+  ps.nx = fs(fm(a1, b2), fm(a2, b1));
+  ps.ny = fs(fm(a2, b0), fm(a0, b2));
+  ps.nz = fs(fm(a0, b1), fm(a1, b0));
+  const float lo[3] = {cx0 - h[0], cy0 - h[1], cz0 - h[2]};
+  const float hi[3] = {cx1 + h[0], cy1 + h[1], cz1 + h[2]};
+  float R = 0.f;
+#pragma unroll
+  for (int q = 0; q < 3; ++q) {
+    const float vmn = fminf(V[q], fminf(V[3 + q], V[6 + q]));
+    const float vmx = fmaxf(V[q], fmaxf(V[3 + q], V[6 + q]));
+    R = fmaxf(R, fmaxf(fabsf(vmx - lo[q]), fabsf(hi[q] - vmn)));
+  }
+  R *= 1.0001f;
+  const float hm = fmaxf(h[0], fmaxf(h[1], h[2]));
+  const float E = 1024.f * EPS24 * R * R * (hm + R);
+  ps.H = fabsf(ps.nx) * h[0] + fabsf(ps.ny) * h[1] + fabsf(ps.nz) * h[2] + E;
+  return ps;
+}
+
+// Bits of one Level2 column (n2z cells along z) start at bit (q*n2x + p)*n2z of a voxel's mask.
+__device__ __forceinline__ void or_column(uint32_t *m, int colidx, int n2z, uint32_t bits) {
+  const int off = colidx * n2z, sh = off & 31;
+  atomicOr(&m[off >> 5], bits << sh);
+  if (sh + n2z > 32) atomicOr(&m[(off >> 5) + 1], bits >> (32 - sh));
+}
+__device__ __forceinline__ void xor_column(uint32_t *m, int colidx, int n2z, uint32_t bits) {
+  const int off = colidx * n2z, sh = off & 31;
+  atomicXor(&m[off >> 5], bits << sh);
+  if (sh + n2z > 32) atomicXor(&m[(off >> 5) + 1], bits >> (32 - sh));
+}
+
+// t of the +z test for one origin height (same operations as ray_t).
+__device__ __forceinline__ float ray_tval(const RayTri &r, const RayCol &c, float oz) {
+  const float Tz = fs(oz, r.v1z);
+  const float q0 = fs(fm(c.Ty, r.e1z), fm(Tz, r.e1y));
+  const float q1 = fs(fm(Tz, r.e1x), fm(c.Tx, r.e1z));
+  const float q2 = fs(fm(c.Tx, r.e1y), fm(c.Ty, r.e1x));
+  return fm(fa(fa(fm(r.e2x, q0), fm(r.e2y, q1)), fm(r.e2z, q2)), r.inv_det);
+}
+
+// last index tl in [0,31] with pre[tl] <= it (pre nondecreasing, pre[0] = 0)
+__device__ __forceinline__ int batch_search(const uint32_t *pre, uint32_t it) {
+  int lo = 0, hi = 31;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (pre[mid] <= it) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
+
+struct WarpScratch {
+  float v[32][9];     // triangle vertices of the current batch
+  float x[32][4];     // slab (SAT) or (1/det, well-conditioned flag) (fill)
+  uint32_t rng[32];   // packed sub-cell ranges
+  uint32_t pre[33];   // exclusive prefix of item counts
+  int jm[32];         // fill: voxels of the chunk below the triangle's topmost voxel
+};
+
+// ---- item construction -----------------------------------------------------------------------
+__global__ void k_colflags(const uint32_t *__restrict__ keys, const uint32_t *__restrict__ useg,
+                           int64_t B, uint32_t nz, uint32_t *__restrict__ cflag) {
+  const int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (u >= B) return;
+  const uint32_t col = keys[useg[u]] / nz;
+  cflag[u] = (u == 0 || keys[useg[u - 1]] / nz != col) ? 1u : 0u;
+}
+
+__global__ void k_colheads(const uint32_t *__restrict__ cflag, const uint32_t *__restrict__ cord,
+                           int64_t B, uint32_t *__restrict__ colhead) {
+  const int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (u >= B) return;
+  if (cflag[u]) colhead[cord[u]] = (uint32_t)u;
+  if (u == B - 1) colhead[cord[u] + cflag[u]] = (uint32_t)B;
+}
+
+__global__ void k_itemflags(const uint32_t *__restrict__ cflag, const uint32_t *__restrict__ cord,
+                            const uint32_t *__restrict__ colhead, int64_t B, int CH,
+                            uint32_t *__restrict__ iflag) {
+  const int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (u >= B) return;
+  const uint32_t c = cord[u] + cflag[u] - 1u;
+  iflag[u] = ((u - colhead[c]) % CH == 0) ? 1u : 0u;
+}
+
+__global__ void k_itemstarts(const uint32_t *__restrict__ iflag, const uint32_t *__restrict__ iord,
+                             int64_t B, uint32_t *__restrict__ istart, uint32_t *__restrict__ nitems) {
+  const int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (u >= B) return;
+  if (iflag[u]) istart[iord[u]] = (uint32_t)u;
+  if (u == B - 1) *nitems = iord[u] + iflag[u];
+}
+
+// ---- Level2 ------------------------------------------------------------------------------------
+__global__ void __launch_bounds__(kWarps * 32) k_level2c(
+    GridDev g, const float4 *__restrict__ ptri, const float4 *__restrict__ fbox,
+    const uint32_t *__restrict__ keys, const uint32_t *__restrict__ vals,
+    const uint32_t *__restrict__ useg, const uint32_t *__restrict__ cflag,
+    const uint32_t *__restrict__ cord, const uint32_t *__restrict__ colhead,
+    const uint32_t *__restrict__ istart, const uint32_t *__restrict__ nitems,
+    const int32_t *__restrict__ prefix, int CH, uint8_t *__restrict__ l2, MeshStats *st) {
+  extern __shared__ uint32_t sm[];
+  const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+  const int n2x = g.n2[0], n2y = g.n2[1], n2z = g.n2[2];
+  const int cells = n2x * n2y * n2z;
+  const int W = (cells + 31) >> 5;
+  const int ncol2 = n2x * n2y;
+  const int FW = (ncol2 + 31) >> 5;
+  const int per_warp = 2 * CH * W + CH * FW + CH + FW + (int)(sizeof(WarpScratch) / 4);
+  uint32_t *base = sm + (size_t)warp * per_warp;
+  uint32_t *sat = base;
+  uint32_t *par = sat + CH * W;
+  uint32_t *ft = par + CH * W;
+  int *kz = (int *)(ft + CH * FW);
+  uint32_t *ftacc = (uint32_t *)(kz + CH);
+  WarpScratch &ws = *reinterpret_cast<WarpScratch *>(ftacc + FW);
+
+  const int64_t it = (int64_t)blockIdx.x * kWarps + warp;
+  if (it >= (int64_t)*nitems) return;
+  const uint32_t ua = istart[it];
+  const uint32_t ucol_end = colhead[cord[ua] + cflag[ua]];  // first voxel of the next column
+  const int m = (int)min((uint32_t)CH, ucol_end - ua);
+  for (int w = lane; w < 2 * CH * W + CH * FW; w += 32) sat[w] = 0;
+  const int nx = g.n[0], ny = g.n[1], nz = g.n[2];
+  const uint32_t col = keys[useg[ua]] / (uint32_t)nz;
+  const int ci = (int)(col % (uint32_t)nx), cj = (int)(col / (uint32_t)nx);
+  if ((int)lane < m) kz[lane] = (int)(keys[useg[ua + lane]] - col * (uint32_t)nz);
+  __syncwarp();
+
+  const float *sx = g.c2s[0] + (size_t)ci * n2x, *sy = g.c2s[1] + (size_t)cj * n2y;
+  const float *ox = g.o2[0] + (size_t)ci * n2x, *oy = g.o2[1] + (size_t)cj * n2y;
+  const float sx0 = __ldg(sx), sx1 = __ldg(sx + n2x - 1), sy0 = __ldg(sy), sy1 = __ldg(sy + n2y - 1);
+
+  // ---------------- SAT of each voxel's own triangles
+  for (int jv = 0; jv < m; ++jv) {
+    const int k = kz[jv];
+    const float *sz = g.c2s[2] + (size_t)k * n2z;
+    const float sz0 = __ldg(sz), sz1 = __ldg(sz + n2z - 1);
+    const uint32_t s0 = useg[ua + jv], s1 = useg[ua + jv + 1];
+    uint32_t *satj = sat + jv * W;
+    for (uint32_t b0 = s0; b0 < s1; b0 += 32) {
+      const uint32_t e = b0 + lane;
+      uint32_t cnt = 0;
+      if (e < s1) {
+        const uint32_t t = vals[e] & 0x7fffffffu;
+        const float4 a0 = __ldg(ptri + 3 * (size_t)t), a1 = __ldg(ptri + 3 * (size_t)t + 1),
+                     a2 = __ldg(ptri + 3 * (size_t)t + 2);
+        const float V[9] = {a0.x, a0.y, a0.z, a1.x, a1.y, a1.z, a2.x, a2.y, a2.z};
+        int p0, p1, q0, q1, r0, r1;
+        l2_range(fminf(V[0], fminf(V[3], V[6])), fmaxf(V[0], fmaxf(V[3], V[6])), sx0, g.e2[0],
+                 g.g2[0], n2x, p0, p1);
+        l2_range(fminf(V[1], fminf(V[4], V[7])), fmaxf(V[1], fmaxf(V[4], V[7])), sy0, g.e2[1],
+                 g.g2[1], n2y, q0, q1);
+        l2_range(fminf(V[2], fminf(V[5], V[8])), fmaxf(V[2], fmaxf(V[5], V[8])), sz0, g.e2[2],
+                 g.g2[2], n2z, r0, r1);
+        if (p0 <= p1 && q0 <= q1 && r0 <= r1) {
+          const PlaneSlab ps = plane_slab(V, sx0, sx1, sy0, sy1, sz0, sz1, g.e2);
+#pragma unroll
+          for (int q = 0; q < 9; ++q) ws.v[lane][q] = V[q];
+          ws.x[lane][0] = ps.nx; ws.x[lane][1] = ps.ny; ws.x[lane][2] = ps.nz; ws.x[lane][3] = ps.H;
+          const int np = p1 - p0 + 1;
+          ws.rng[lane] = (uint32_t)p0 | ((uint32_t)np << 6) | ((uint32_t)q0 << 12) |
+                         ((uint32_t)r0 << 18) | ((uint32_t)r1 << 24);
+          cnt = (uint32_t)(np * (q1 - q0 + 1));
+        }
+      }
+      const uint32_t inc = warp_incl_scan(cnt);
+      ws.pre[lane] = inc - cnt;
+      const uint32_t tot = __shfl_sync(FULL, inc, 31);
+      __syncwarp();
+      for (uint32_t w = lane; w < tot; w += 32) {
+        const int tl = batch_search(ws.pre, w);
+        const uint32_t loc = w - ws.pre[tl];
+        const uint32_t rg = ws.rng[tl];
+        const int np = (int)((rg >> 6) & 63u);
+        const int p = (int)(rg & 63u) + (int)(loc % (uint32_t)np);
+        const int q = (int)((rg >> 12) & 63u) + (int)(loc / (uint32_t)np);
+        const int r0 = (int)((rg >> 18) & 63u), r1 = (int)((rg >> 24) & 63u);
+        float V[9];
+#pragma unroll
+        for (int qq = 0; qq < 9; ++qq) V[qq] = ws.v[tl][qq];
+        const float cx = __ldg(sx + p), cy = __ldg(sy + q);
+        SatCol s;
+        if (!sat_col(V, cx, cy, g.e2, s)) continue;
+        const float nxs = ws.x[tl][0], nys = ws.x[tl][1], nzs = ws.x[tl][2], H = ws.x[tl][3];
+        const float sxy = fa(fm(nxs, fs(V[0], cx)), fm(nys, fs(V[1], cy)));
+        uint32_t bits = 0;
+        for (int r = r0; r <= r1; ++r) {
+          const float cz = __ldg(sz + r);
+          if (fabsf(fa(sxy, fm(nzs, fs(V[2], cz)))) > H) continue;  // plane misses the cell
+          if (sat_z(s, V, cz, g.e2)) bits |= 1u << r;
+        }
+        if (bits) or_column(satj, q * n2x + p, n2z, bits);
+      }
+      __syncwarp();
+    }
+  }
+
+  // ---------------- fill: u/v once per (triangle, sub-column) for the whole chunk
+  const uint32_t f0 = useg[ua], f1 = useg[ucol_end];
+  const float *ozt = g.o2[2];
+  const float oz_lo = __ldg(ozt + (size_t)kz[0] * n2z);
+  const float oz_hi = __ldg(ozt + (size_t)kz[m - 1] * n2z + n2z - 1);
+  uint64_t nun = 0;
+  for (uint32_t b0 = f0; b0 < f1; b0 += 32) {
+    const uint32_t e = b0 + lane;
+    const uint32_t vv = e < f1 ? vals[e] : 0u;
+    uint32_t cnt = 0;
+    if (vv & 0x80000000u) {
+      const uint32_t t = vv & 0x7fffffffu;
+      const int zt = (int)(keys[e] - col * (uint32_t)nz);
+      int jm = 0;
+      while (jm < m && kz[jm] <= zt) ++jm;
+      nun += (uint64_t)jm;
+      const float4 fb = __ldg(fbox + t);
+      if (jm > 0 && fb.x <= fb.z) {
+        int p0 = 0, p1 = n2x - 1, q0 = 0, q1 = n2y - 1;
+        while (p0 <= p1 && __ldg(ox + p0) < fb.x) ++p0;
+        while (p1 >= p0 && __ldg(ox + p1) > fb.z) --p1;
+        while (q0 <= q1 && __ldg(oy + q0) < fb.y) ++q0;
+        while (q1 >= q0 && __ldg(oy + q1) > fb.w) --q1;
+        if (p0 <= p1 && q0 <= q1) {
+          const float4 a0 = __ldg(ptri + 3 * (size_t)t), a1 = __ldg(ptri + 3 * (size_t)t + 1),
+                       a2 = __ldg(ptri + 3 * (size_t)t + 2);
+          ws.v[lane][0] = a0.x; ws.v[lane][1] = a0.y; ws.v[lane][2] = a0.z;
+          ws.v[lane][3] = a1.x; ws.v[lane][4] = a1.y; ws.v[lane][5] = a1.z;
+          ws.v[lane][6] = a2.x; ws.v[lane][7] = a2.y; ws.v[lane][8] = a2.z;
+          ws.x[lane][0] = a2.w;  // 1/det
+          // an unbounded box marks an ill-conditioned x/y projection: no certification there
+          ws.x[lane][1] = (isinf(fb.x) || isinf(fb.z)) ? 0.f : 1.f;
+          const int np = p1 - p0 + 1;
+          ws.rng[lane] = (uint32_t)p0 | ((uint32_t)np << 6) | ((uint32_t)q0 << 12);
+          ws.jm[lane] = jm;
+          cnt = (uint32_t)(np * (q1 - q0 + 1));
+        }
+      }
+    }
+    const uint32_t inc = warp_incl_scan(cnt);
+    ws.pre[lane] = inc - cnt;
+    const uint32_t tot = __shfl_sync(FULL, inc, 31);
+    __syncwarp();
+    for (uint32_t w = lane; w < tot; w += 32) {
+      const int tl = batch_search(ws.pre, w);
+      const uint32_t loc = w - ws.pre[tl];
+      const uint32_t rg = ws.rng[tl];
+      const int np = (int)((rg >> 6) & 63u);
+      const int p = (int)(rg & 63u) + (int)(loc % (uint32_t)np);
+      const int q = (int)((rg >> 12) & 63u) + (int)(loc / (uint32_t)np);
+      float V[9];
+#pragma unroll
+      for (int qq = 0; qq < 9; ++qq) V[qq] = ws.v[tl][qq];
+      RayTri rt;
+      ray_tri_pre(V, ws.x[tl][0], rt);
+      RayCol rc;
+      if (!ray_col(rt, __ldg(ox + p), __ldg(oy + q), rc)) continue;
+      const int pq = q * n2x + p;
+      const bool well = g.oz_monotone && ws.x[tl][1] != 0.f;
+      float E2 = 0.f;
+      if (well) {
+        // |t - t*| <= 8.2 eps M1 |1/det| for every origin with |Tz| <= Zm (t* exact, affine and
+        // decreasing in the origin height); 16 eps gives the float evaluation room.
+        const float Zm = fmaxf(fabsf(oz_lo - rt.v1z), fabsf(oz_hi - rt.v1z)) * 1.0001f;
+        const float atx = fabsf(rc.Tx), aty = fabsf(rc.Ty);
+        const float M1 = fabsf(rt.e2x) * (aty * fabsf(rt.e1z) + Zm * fabsf(rt.e1y)) +
+                         fabsf(rt.e2y) * (Zm * fabsf(rt.e1x) + atx * fabsf(rt.e1z)) +
+                         fabsf(rt.e2z) * (atx * fabsf(rt.e1y) + aty * fabsf(rt.e1x));
+        E2 = 2.f * 16.f * EPS24 * M1 * fabsf(rt.inv_det) * 1.0001f;
+      }
+      for (int jv = ws.jm[tl] - 1; jv >= 0; --jv) {
+        const float *oz = ozt + (size_t)kz[jv] * n2z;
+        if (well && ray_tval(rt, rc, __ldg(oz + n2z - 1)) > g.thr + E2) {
+          // this voxel and every lower voxel of the chunk are hit at every origin
+          atomicXor(&ft[jv * FW + (pq >> 5)], 1u << (pq & 31));
+          break;
+        }
+        uint32_t bits = 0;
+        for (int r = 0; r < n2z; ++r)
+          if (ray_t(rt, rc, __ldg(oz + r), g.thr)) bits |= 1u << r;
+        if (bits) xor_column(par + jv * W, pq, n2z, bits);
+      }
+    }
+    __syncwarp();
+  }
+
+  // ---------------- output, top voxel first so the full-hit toggles accumulate downwards
+  for (int w = lane; w < FW; w += 32) ftacc[w] = 0;
+  __syncwarp();
+  unsigned long long nin = 0, nbd = 0;
+  const bool vec = (cells & 3) == 0;
+  for (int jv = m - 1; jv >= 0; --jv) {
+    for (int w = lane; w < FW; w += 32) ftacc[w] ^= ft[jv * FW + w];
+    __syncwarp();
+    const int64_t vlin = ((int64_t)kz[jv] * ny + cj) * nx + ci;
+    uint8_t *out = l2 + (size_t)prefix[vlin] * cells;
+    const uint32_t *satj = sat + jv * W, *parj = par + jv * W;
+    for (int c4 = lane * 4; c4 < cells; c4 += 128) {
+      uint32_t word = 0;
+#pragma unroll
+      for (int d = 0; d < 4; ++d) {
+        const int c = c4 + d;
+        if (c >= cells) break;
+        const int p = c % n2x, q = (c / n2x) % n2y, r = c / ncol2;
+        const int pq = q * n2x + p;
+        const int bi = pq * n2z + r;
+        const uint32_t sb = (satj[bi >> 5] >> (bi & 31)) & 1u;
+        const uint32_t pb = ((parj[bi >> 5] >> (bi & 31)) ^ (ftacc[pq >> 5] >> (pq & 31))) & 1u;
+        const uint32_t s = sb ? 254u : (pb ? 127u : 0u);
+        nin += (!sb && pb);
+        nbd += sb;
+        if (vec) word |= s << (8 * d);
+        else out[c] = (uint8_t)s;
+      }
+      if (vec) *reinterpret_cast<uint32_t *>(out + c4) = word;
+    }
+    __syncwarp();
+  }
+  nin = warp_sum(nin);
+  nbd = warp_sum(nbd);
+  nun = warp_sum(nun);
+  if (lane == 0) {
+    if (nin) atomicAdd(&st->l2_inside, nin);
+    if (nbd) atomicAdd(&st->l2_boundary, nbd);
+    if (nun) atomicAdd(&st->ray2, (unsigned long long)nun * (unsigned long long)cells);
+  }
+}
+
+}  // namespace
+
+int level2_chunk(const GridDev &g) {
+  const int cells = g.n2[0] * g.n2[1] * g.n2[2];
+  const int W = (cells + 31) >> 5;
+  return std::max(1, std::min(32, kMaskWords / W));
+}
+
+size_t level2_smem(const GridDev &g) {
+  const int cells = g.n2[0] * g.n2[1] * g.n2[2];
+  const int W = (cells + 31) >> 5;
+  const int FW = (g.n2[0] * g.n2[1] + 31) >> 5;
+  const int CH = level2_chunk(g);
+  const size_t per_warp = 2 * CH * W + CH * FW + CH + FW + sizeof(WarpScratch) / 4;
+  return per_warp * 4 * kWarps;
+}
+
+// Builds the chunk items from the sorted pair lists and runs the Level2 kernel.
+// tmp must hold 6*B + 2 words plus the scan temporaries (level2_temp_words).
+int64_t level2_temp_words(int64_t B) { return 6 * B + 8 + scan_temp_words(B); }
+
+void launch_level2c(const GridDev &g, const float4 *ptri, const float4 *fbox,
+                    const uint32_t *keys, const uint32_t *vals, const uint32_t *useg,
+                    const int32_t *prefix, int64_t B, uint32_t *tmp, uint8_t *l2, MeshStats *st,
+                    cudaStream_t s) {
+  if (B <= 0) return;
+  uint32_t *cflag = tmp, *cord = cflag + B, *colhead = cord + B, *iflag = colhead + B + 1,
+           *iord = iflag + B, *istart = iord + B, *nitems = istart + B + 1,
+           *stmp = nitems + 4;
+  const unsigned nb = (unsigned)((B + 255) / 256);
+  const int CH = level2_chunk(g);
+  k_colflags<<<nb, 256, 0, s>>>(keys, useg, B, (uint32_t)g.n[2], cflag);
+  scan_u32(cflag, cord, B, nullptr, stmp, s);
+  k_colheads<<<nb, 256, 0, s>>>(cflag, cord, B, colhead);
+  k_itemflags<<<nb, 256, 0, s>>>(cflag, cord, colhead, B, CH, iflag);
+  scan_u32(iflag, iord, B, nullptr, stmp, s);
+  k_itemstarts<<<nb, 256, 0, s>>>(iflag, iord, B, istart, nitems);
+  count_launch(4);
+  const size_t smem = level2_smem(g);
+  static bool attr_set = false;
+  if (!attr_set) {
+    cudaFuncSetAttribute(k_level2c, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    attr_set = true;
+  }
+  const unsigned nblk = (unsigned)((B + kWarps - 1) / kWarps);  // items <= B
+  k_level2c<<<nblk, kWarps * 32, smem, s>>>(g, ptri, fbox, keys, vals, useg, cflag, cord, colhead,
+                                            istart, nitems, prefix, CH, l2, st);
+  count_launch();
+}
+
+}  // namespace gpv
