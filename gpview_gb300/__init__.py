@@ -103,6 +103,10 @@ def lib():
         fn = getattr(L, name)
         fn.argtypes = [C.c_uint64, *extra, C.c_void_p]
         fn.restype = C.c_int64
+    L.gpv_voxelize_level1_noalloc.argtypes = [C.c_void_p, C.c_int64, C.POINTER(GridSpec),
+                                              C.c_void_p, C.c_void_p, C.c_void_p,
+                                              C.POINTER(C.c_int64), C.c_void_p]
+    L.gpv_noalloc_last_error.restype = C.c_char_p
     if hasattr(L, "gpv_voxelize_batch"):
         L.gpv_voxelize_batch.argtypes = [C.c_void_p, C.c_int32, C.POINTER(C.c_void_p),
                                          C.POINTER(C.c_int64), C.POINTER(GridSpec),

@@ -139,6 +139,24 @@ int gpv_voxelize_batch(gpv_ctx *ctx, int32_t n, const float *const *d_tris,
                        const int64_t *num_triangles, const gpv_grid_spec *specs,
                        gpv_result *results, cudaStream_t stream);
 
+/* Level1 voxelization that allocates nothing (no counterpart in the reference).  For callers
+ * that cannot call cudaMalloc -- code running inside another allocator's or memory pool's
+ * hooks, host paths that must not take the device synchronisation cudaMalloc/cudaFree can cause,
+ * plugin hosts that forbid a library its own device memory.  The caller passes device triangles
+ * (16-byte aligned) and three device outputs: level1_inout (nx*ny*nz bytes), level1_prefix
+ * (nx*ny*nz int32) and boundary_index (room for nx*ny*nz int32); the boundary count is returned
+ * in *num_boundary and the call waits for `stream`.  Results equal gpv_voxelize's Level1 outputs.
+ * All intermediates live in one file-scope device array of 32 MiB that every GPU loading the
+ * library holds until exit; larger inputs are rejected with GPV_ERR_INVALID (reason in
+ * gpv_noalloc_last_error()).  The first call on each device looks up that array's address
+ * (cudaGetSymbolAddress); make it before any stream capture.  Calls share the array and clear
+ * it themselves; calls whose GPU work overlaps race on it and must be serialised. */
+int gpv_voxelize_level1_noalloc(const float *d_tris, int64_t num_triangles,
+                                const gpv_grid_spec *spec, uint8_t *d_level1_inout,
+                                int32_t *d_level1_prefix, int32_t *d_boundary_index,
+                                int64_t *num_boundary, cudaStream_t stream);
+const char *gpv_noalloc_last_error(void);
+
 /* ---- meshes and files (host) ---------------------------------------------------------------- */
 int gpv_load_obj(const char *path, gpv_mesh *out); /* Object::ReadObject (src/Object.cpp:395) */
 int gpv_load_off(const char *path, gpv_mesh *out); /* Object::ReadOFFObject (src/Object.cpp:171) */
