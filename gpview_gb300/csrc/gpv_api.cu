@@ -9,27 +9,7 @@
 #include <string>
 #include <unordered_map>
 
-#include "gpv_internal.h"
-
-struct gpv_ctx {
-  static constexpr int kStages = 8;
-  int device = 0;
-  bool timing = false;                 // record per-stage CUDA events on the launching stream
-  cudaEvent_t ev[kStages + 1] = {};
-  double stage_ms[kStages] = {};      // accumulated stage durations
-  uint64_t stage_calls = 0;
-  std::string err;
-  int tile = 128;
-  gpv::MeshStats *h_stats = nullptr;  // pinned
-  uint32_t *h_u32 = nullptr;          // pinned scratch (small)
-  float *h_tables = nullptr;          // pinned staging for coordinate tables
-  size_t h_tables_cap = 0;
-  uint64_t next_handle = 1;
-  struct Owned {
-    void *l1, *prefix, *bindex, *l2;
-  };
-  std::unordered_map<uint64_t, Owned> owned;
-};
+#include "gpv_ctx.h"
 
 namespace gpv {
 
@@ -143,222 +123,11 @@ GridDev make_griddev(const GridHost &gh, const float *dt) {
 
 using namespace gpv;
 
-namespace {
-
-int fail(gpv_ctx *ctx, int code, const char *what) {
-  if (ctx) ctx->err = what;
-  return code;
-}
-
-int cuda_fail(gpv_ctx *ctx, cudaError_t e, const char *where) {
-  if (ctx) ctx->err = std::string(where) + ": " + cudaGetErrorString(e);
-  return GPV_ERR_CUDA;
-}
-
-#define GPV_CUDA(call)                                  \
-  do {                                                  \
-    cudaError_t e_ = (call);                            \
-    if (e_ != cudaSuccess) return cuda_fail(ctx, e_, #call); \
+#define GPV_CUDA(call)                                        \
+  do {                                                        \
+    cudaError_t e_ = (call);                                  \
+    if (e_ != cudaSuccess) return ctx_cuda_fail(ctx, e_, #call); \
   } while (0)
-
-// Stream-ordered allocation list freed together.
-struct Arena {
-  std::vector<void *> ptrs;
-  cudaStream_t s;
-  explicit Arena(cudaStream_t st) : s(st) {}
-  template <typename T>
-  cudaError_t get(T **p, size_t count) {
-    void *q = nullptr;
-    cudaError_t e = cudaMallocAsync(&q, std::max<size_t>(count * sizeof(T), 16), s);
-    if (e == cudaSuccess) ptrs.push_back(q);
-    *p = (T *)q;
-    return e;
-  }
-  ~Arena() {
-    for (void *p : ptrs) cudaFreeAsync(p, s);
-  }
-};
-
-int ensure_tables(gpv_ctx *ctx, size_t n) {
-  if (ctx->h_tables_cap >= n) return GPV_OK;
-  if (ctx->h_tables) cudaFreeHost(ctx->h_tables);
-  ctx->h_tables = nullptr;
-  GPV_CUDA(cudaMallocHost(&ctx->h_tables, n * sizeof(float)));
-  ctx->h_tables_cap = n;
-  return GPV_OK;
-}
-
-}  // namespace
-
-// ---- plain pipeline -----------------------------------------------------------------------------
-static int voxelize_impl(gpv_ctx *ctx, const float *d_tris, int64_t T, const gpv_grid_spec *spec,
-                         gpv_result *out, cudaStream_t s) {
-  GridHost gh;
-  int rc = grid_derive(*spec, gh);
-  if (rc) return fail(ctx, rc, "invalid grid specification");
-  if (T < 0 || T >= ((int64_t)1 << 31)) return fail(ctx, GPV_ERR_INVALID, "bad triangle count");
-  if (T > 0 && (reinterpret_cast<uintptr_t>(d_tris) & 15u))
-    return fail(ctx, GPV_ERR_INVALID, "triangle buffer must be 16-byte aligned");
-
-  Arena ws(s);
-  const int64_t nt = table_floats(gh);
-  rc = ensure_tables(ctx, (size_t)nt);
-  if (rc) return rc;
-  float *d_tab;
-  GPV_CUDA(ws.get(&d_tab, nt));
-  pack_tables(gh, ctx->h_tables);
-  GPV_CUDA(cudaMemcpyAsync(d_tab, ctx->h_tables, nt * sizeof(float), cudaMemcpyHostToDevice, s));
-  const GridDev g = make_griddev(gh, d_tab);
-
-  const int64_t N1 = gh.N1;
-  const int64_t N1w = (int64_t)gh.n[2] * gh.n[1] * gh.nxw;
-  const int64_t ncol = (int64_t)gh.n[0] * gh.n[1];
-  Level1Bufs b{};
-  b.tris = d_tris;
-  b.T = T;
-  GPV_CUDA(ws.get(&b.ptri, 3 * (size_t)std::max<int64_t>(T, 1)));
-  GPV_CUDA(ws.get(&b.rng, (size_t)std::max<int64_t>(T, 1)));
-  GPV_CUDA(ws.get(&b.fbox, (size_t)std::max<int64_t>(T, 1)));
-  GPV_CUDA(ws.get(&b.bplane, (size_t)N1w));
-  GPV_CUDA(ws.get(&b.iplane, (size_t)N1w));
-  GPV_CUDA(ws.get(&b.toggles, (size_t)(ncol * gh.nzw)));
-  GPV_CUDA(ws.get(&b.stats, 1));
-  uint32_t *wcnt, *wpre, *d_tot, *scan_tmp;
-  GPV_CUDA(ws.get(&wcnt, (size_t)N1w));
-  GPV_CUDA(ws.get(&wpre, (size_t)N1w));
-  GPV_CUDA(ws.get(&d_tot, 4));
-  GPV_CUDA(ws.get(&scan_tmp, (size_t)scan_temp_words(N1w)));
-  GPV_CUDA(cudaMemsetAsync(b.stats, 0, sizeof(MeshStats), s));
-  GPV_CUDA(cudaMemsetAsync(b.bplane, 0, N1w * 4, s));
-  GPV_CUDA(cudaMemsetAsync(b.toggles, 0, ncol * gh.nzw * 4, s));
-
-  // results with sizes known up front
-  uint8_t *l1 = nullptr;
-  int32_t *prefix = nullptr;
-  GPV_CUDA(cudaMallocAsync((void **)&l1, std::max<int64_t>(N1, 16), s));
-  GPV_CUDA(cudaMallocAsync((void **)&prefix, 4 * std::max<int64_t>(N1, 4), s));
-  int32_t *bindex = nullptr;
-  uint8_t *l2 = nullptr;
-  auto drop_results = [&]() {
-    cudaFreeAsync(l1, s);
-    cudaFreeAsync(prefix, s);
-    if (bindex) cudaFreeAsync(bindex, s);
-    if (l2) cudaFreeAsync(l2, s);
-  };
-
-  auto mark = [&](int i) {
-    if (ctx->timing) cudaEventRecord(ctx->ev[i], s);
-  };
-  // 1. per-triangle preparation and work counts
-  mark(0);
-  launch_prep(g, b, s);
-  mark(1);
-  GPV_CUDA(cudaMemcpyAsync(ctx->h_stats, b.stats, sizeof(MeshStats), cudaMemcpyDeviceToHost, s));
-  GPV_CUDA(cudaStreamSynchronize(s));
-  const uint64_t cap = std::max<uint64_t>(ctx->h_stats->sat1, 1);
-  GPV_CUDA(ws.get(&b.keys, cap));
-  GPV_CUDA(ws.get(&b.vals, cap));
-  ctx->h_stats->pair_cap = cap;
-  GPV_CUDA(cudaMemcpyAsync(&b.stats->pair_cap, &ctx->h_stats->pair_cap, sizeof(uint64_t),
-                           cudaMemcpyHostToDevice, s));
-
-  // 2. Level1 SAT + fill, boundary counts
-  mark(2);
-  launch_level1(g, b, ctx->tile, s);
-  mark(3);
-  launch_fill_finish(g, b, s);
-  launch_popc(g, b.bplane, wcnt, s);
-  scan_u32(wcnt, wpre, N1w, d_tot, scan_tmp, s);
-  mark(4);
-  GPV_CUDA(cudaGetLastError());
-  GPV_CUDA(cudaMemcpyAsync(ctx->h_stats, b.stats, sizeof(MeshStats), cudaMemcpyDeviceToHost, s));
-  GPV_CUDA(cudaMemcpyAsync(ctx->h_u32, d_tot, 4, cudaMemcpyDeviceToHost, s));
-  GPV_CUDA(cudaStreamSynchronize(s));
-  if (ctx->h_stats->status) {
-    drop_results();
-    return fail(ctx, (ctx->h_stats->status & ST_BAD_INPUT) ? GPV_ERR_INVALID : GPV_ERR_DEVICE,
-                (ctx->h_stats->status & ST_BAD_INPUT) ? "non-finite vertex" : "device status raised");
-  }
-  const int64_t P = (int64_t)ctx->h_stats->pairs;
-  const int64_t B = (int64_t)ctx->h_u32[0];
-
-  // 3. outputs of Level1, sorted pair lists, Level2
-  GPV_CUDA(cudaMallocAsync((void **)&bindex, 4 * std::max<int64_t>(B, 4), s));
-  const int64_t l2bytes = gh.level2 ? B * gh.cells : 0;
-  GPV_CUDA(cudaMallocAsync((void **)&l2, std::max<int64_t>(l2bytes, 16), s));
-  mark(5);
-  launch_expand(g, b.bplane, b.iplane, wpre, l1, prefix, bindex, b.stats, s);
-  mark(6);
-  if (gh.level2 && B > 0) {
-    uint32_t *kalt, *valt, *flags, *uidx, *useg, *stmp, *l2tmp;
-    GPV_CUDA(ws.get(&kalt, (size_t)P));
-    GPV_CUDA(ws.get(&valt, (size_t)P));
-    GPV_CUDA(ws.get(&flags, (size_t)P));
-    GPV_CUDA(ws.get(&uidx, (size_t)P));
-    GPV_CUDA(ws.get(&useg, (size_t)B + 1));
-    GPV_CUDA(ws.get(&stmp, (size_t)std::max(sort_temp_words(P), scan_temp_words(P))));
-    GPV_CUDA(ws.get(&l2tmp, (size_t)level2_temp_words(B)));
-    const bool in_alt = sort_pairs(b.keys, b.vals, kalt, valt, P, gh.key_bits, stmp, s);
-    const uint32_t *sk = in_alt ? kalt : b.keys;
-    const uint32_t *sv = in_alt ? valt : b.vals;
-    launch_heads(sk, P, flags, s);
-    scan_u32(flags, uidx, P, d_tot + 1, stmp, s);
-    launch_useg(flags, uidx, P, useg, s);
-    mark(7);
-    launch_level2c(g, b.ptri, b.fbox, sk, sv, useg, prefix, B, l2tmp, l2, b.stats, s);
-  } else {
-    mark(7);
-  }
-  mark(8);
-  GPV_CUDA(cudaGetLastError());
-  GPV_CUDA(cudaMemcpyAsync(ctx->h_stats, b.stats, sizeof(MeshStats), cudaMemcpyDeviceToHost, s));
-  GPV_CUDA(cudaMemcpyAsync(ctx->h_u32 + 1, d_tot + 1, 4, cudaMemcpyDeviceToHost, s));
-  GPV_CUDA(cudaStreamSynchronize(s));
-  if (ctx->timing) {
-    // stages: 0 prep, 1 level1, 2 fill finish + boundary scan, 3 expand, 4 sort + lists,
-    // 5 level2 (event pairs (0,1) (2,3) (3,4) (5,6) (6,7) (7,8))
-    const int pr[6][2] = {{0, 1}, {2, 3}, {3, 4}, {5, 6}, {6, 7}, {7, 8}};
-    for (int k = 0; k < 6; ++k) {
-      float ms = 0.f;
-      if (cudaEventElapsedTime(&ms, ctx->ev[pr[k][0]], ctx->ev[pr[k][1]]) == cudaSuccess)
-        ctx->stage_ms[k] += ms;
-    }
-    ctx->stage_calls++;
-  }
-  const MeshStats &st = *ctx->h_stats;
-  if (st.status) {
-    drop_results();
-    return fail(ctx, GPV_ERR_DEVICE, "device status raised");
-  }
-  if (gh.level2 && B > 0 && (int64_t)ctx->h_u32[1] != B) {
-    drop_results();
-    return fail(ctx, GPV_ERR_DEVICE, "boundary plane and pair lists disagree");
-  }
-
-  std::memset(out, 0, sizeof(*out));
-  out->spec = *spec;
-  for (int a = 0; a < 3; ++a) {
-    out->grid_size[a] = gh.g[a];
-    out->grid_size2[a] = gh.level2 ? gh.g2[a] : 0.f;
-  }
-  out->num_level1 = N1;
-  out->num_boundary = B;
-  out->num_level1_inside = (int64_t)st.l1_inside;
-  out->num_level2_inside = (int64_t)st.l2_inside;
-  out->num_level2_boundary = (int64_t)st.l2_boundary;
-  out->num_pairs = P;
-  out->work.sat1 = (int64_t)st.sat1;
-  out->work.sat2 = gh.level2 ? P * gh.cells : 0;
-  out->work.ray1 = (int64_t)st.ray1;
-  out->work.ray2 = (int64_t)st.ray2;
-  out->level1_inout = l1;
-  out->level1_prefix = prefix;
-  out->boundary_index = bindex;
-  out->level2_inout = l2;
-  out->handle = ctx->next_handle++;
-  ctx->owned[out->handle] = {l1, prefix, bindex, l2};
-  return GPV_OK;
-}
 
 extern "C" {
 
@@ -374,11 +143,11 @@ int gpv_init(int device, gpv_ctx **out) {
     uint64_t thr = UINT64_MAX;
     cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
   }
-  if (cudaMallocHost(&ctx->h_stats, sizeof(MeshStats)) != cudaSuccess ||
-      cudaMallocHost(&ctx->h_u32, 64) != cudaSuccess) {
+  if (ctx_ensure_host(ctx, 16) != cudaSuccess || cudaMallocHost(&ctx->h_u32, 64) != cudaSuccess) {
     delete ctx;
     return GPV_ERR_CUDA;
   }
+  cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, device);
   *out = ctx;
   return GPV_OK;
 }
@@ -386,13 +155,21 @@ int gpv_init(int device, gpv_ctx **out) {
 void gpv_destroy(gpv_ctx *ctx) {
   if (!ctx) return;
   cudaSetDevice(ctx->device);
-  for (auto &kv : ctx->owned) {
-    cudaFree(kv.second.l1);
-    cudaFree(kv.second.prefix);
-    cudaFree(kv.second.bindex);
-    cudaFree(kv.second.l2);
+  std::vector<ResultSet *> sets;
+  for (auto &kv : ctx->owned) sets.push_back(kv.second.get());
+  std::sort(sets.begin(), sets.end());
+  sets.erase(std::unique(sets.begin(), sets.end()), sets.end());
+  for (ResultSet *r : sets) {
+    cudaFree(r->l1);
+    cudaFree(r->prefix);
+    cudaFree(r->bindex);
+    cudaFree(r->l2);
   }
+  ctx->owned.clear();
   if (ctx->h_stats) cudaFreeHost(ctx->h_stats);
+  if (ctx->h_md) cudaFreeHost(ctx->h_md);
+  if (ctx->h_tiles) cudaFreeHost(ctx->h_tiles);
+  if (ctx->h_tb) cudaFreeHost(ctx->h_tb);
   if (ctx->h_u32) cudaFreeHost(ctx->h_u32);
   if (ctx->h_tables) cudaFreeHost(ctx->h_tables);
   delete ctx;
@@ -467,7 +244,7 @@ int gpv_voxelize(gpv_ctx *ctx, const float *d_tris, int64_t num_triangles,
                  const gpv_grid_spec *spec, gpv_result *out, cudaStream_t stream) {
   if (!ctx || !spec || !out || (num_triangles > 0 && !d_tris)) return GPV_ERR_INVALID;
   cudaSetDevice(ctx->device);
-  return voxelize_impl(ctx, d_tris, num_triangles, spec, out, stream);
+  return run_batch(ctx, 1, &d_tris, &num_triangles, spec, out, stream);
 }
 
 int gpv_voxelize_host(gpv_ctx *ctx, const float *h_tris, int64_t num_triangles,
@@ -478,13 +255,14 @@ int gpv_voxelize_host(gpv_ctx *ctx, const float *h_tris, int64_t num_triangles,
   float *d = nullptr;
   const size_t bytes = (size_t)std::max<int64_t>(num_triangles, 1) * 9 * sizeof(float);
   cudaError_t e = cudaMallocAsync((void **)&d, bytes, stream);
-  if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaMallocAsync");
+  if (e != cudaSuccess) return ctx_cuda_fail(ctx, e, "cudaMallocAsync");
   if (num_triangles > 0) {
     e = cudaMemcpyAsync(d, h_tris, (size_t)num_triangles * 9 * sizeof(float),
                         cudaMemcpyHostToDevice, stream);
-    if (e != cudaSuccess) { cudaFreeAsync(d, stream); return cuda_fail(ctx, e, "cudaMemcpyAsync"); }
+    if (e != cudaSuccess) { cudaFreeAsync(d, stream); return ctx_cuda_fail(ctx, e, "cudaMemcpyAsync"); }
   }
-  int rc = voxelize_impl(ctx, d, num_triangles, spec, out, stream);
+  const float *dp = d;
+  int rc = run_batch(ctx, 1, &dp, &num_triangles, spec, out, stream);
   cudaFreeAsync(d, stream);
   return rc;
 }
@@ -514,17 +292,28 @@ int gpv_result_release(gpv_ctx *ctx, gpv_result *res) {
   auto it = ctx->owned.find(res->handle);
   if (it == ctx->owned.end()) return GPV_ERR_INVALID;
   cudaSetDevice(ctx->device);
-  cudaFreeAsync(it->second.l1, 0);
-  cudaFreeAsync(it->second.prefix, 0);
-  cudaFreeAsync(it->second.bindex, 0);
-  cudaFreeAsync(it->second.l2, 0);
-  ctx->owned.erase(it);
+  std::shared_ptr<ResultSet> set = it->second;
+  if (--set->refs <= 0) {
+    cudaFreeAsync(set->l1, 0);
+    cudaFreeAsync(set->prefix, 0);
+    cudaFreeAsync(set->bindex, 0);
+    cudaFreeAsync(set->l2, 0);
+    ctx->owned.erase(it);
+  }
   res->level1_inout = nullptr;
   res->level1_prefix = nullptr;
   res->boundary_index = nullptr;
   res->level2_inout = nullptr;
   res->handle = 0;
   return GPV_OK;
+}
+
+int gpv_voxelize_batch(gpv_ctx *ctx, int32_t n, const float *const *d_tris,
+                       const int64_t *num_triangles, const gpv_grid_spec *specs,
+                       gpv_result *results, cudaStream_t stream) {
+  if (!ctx || n <= 0 || !d_tris || !num_triangles || !specs || !results) return GPV_ERR_INVALID;
+  cudaSetDevice(ctx->device);
+  return run_batch(ctx, n, d_tris, num_triangles, specs, results, stream);
 }
 
 }  // extern "C"

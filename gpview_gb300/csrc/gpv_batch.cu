@@ -1,0 +1,349 @@
+// gpv_batch.cu -- host orchestration of a batch of meshes (the plain path is a batch of one).
+//
+// Three phases, one host synchronisation after each, independent of the number of meshes:
+//   A  prep over every triangle of every mesh            -> per-mesh candidate counts (pair caps)
+//   B  persistent Level1 (tiles of all meshes), fill finish, boundary scan
+//                                                        -> per-mesh pair and boundary counts
+//   C  Level1 expansion, segmented radix sort, segment heads, persistent Level2 over the column
+//      chunks of all meshes                              -> per-mesh statistics
+// Phase B and C launch sequences are recorded into CUDA graphs when graphs are enabled
+// (gpv_set_graphs); their launch shapes are fixed by the counts read at the phase boundary.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "gpv_ctx.h"
+
+namespace gpv {
+
+namespace {
+
+struct Arena {
+  std::vector<void *> ptrs;
+  cudaStream_t s;
+  explicit Arena(cudaStream_t st) : s(st) {}
+  template <typename T>
+  cudaError_t get(T **p, size_t count) {
+    void *q = nullptr;
+    cudaError_t e = cudaMallocAsync(&q, std::max<size_t>(count * sizeof(T), 16), s);
+    if (e == cudaSuccess) ptrs.push_back(q);
+    *p = (T *)q;
+    return e;
+  }
+  ~Arena() {
+    for (void *p : ptrs) cudaFreeAsync(p, s);
+  }
+};
+
+size_t al16(size_t v) { return (v + 15) & ~size_t(15); }
+
+}  // namespace
+
+int run_batch(gpv_ctx *ctx, int n, const float *const *d_tris, const int64_t *T,
+              const gpv_grid_spec *specs, gpv_result *out, cudaStream_t s) {
+#define CK(call)                                                    \
+  do {                                                              \
+    cudaError_t e_ = (call);                                        \
+    if (e_ != cudaSuccess) return ctx_cuda_fail(ctx, e_, #call);    \
+  } while (0)
+  if (n <= 0) return ctx_fail(ctx, GPV_ERR_INVALID, "empty batch");
+  std::vector<GridHost> gh(n);
+  for (int m = 0; m < n; ++m) {
+    if (grid_derive(specs[m], gh[m]) != GPV_OK)
+      return ctx_fail(ctx, GPV_ERR_INVALID, ("invalid grid specification for mesh " + std::to_string(m)).c_str());
+    if (T[m] < 0 || T[m] >= ((int64_t)1 << 31) || (T[m] > 0 && !d_tris[m]))
+      return ctx_fail(ctx, GPV_ERR_INVALID, "bad triangle count or pointer");
+    if (T[m] > 0 && (reinterpret_cast<uintptr_t>(d_tris[m]) & 15u))
+      return ctx_fail(ctx, GPV_ERR_INVALID, "triangle buffers must be 16-byte aligned");
+  }
+  const int tile = ctx->tile;
+
+  // ---- sizes and per-mesh bases
+  std::vector<int64_t> tab_off(n + 1, 0), res_l1(n + 1, 0), res_pre(n + 1, 0);
+  std::vector<MeshDesc> md(n);
+  int64_t tris = 0, tiles = 0, fwarps = 0, rows = 0, words = 0, togg = 0;
+  int max_keybits = 1, warp_words = 0;
+  bool any_l2 = false;
+  for (int m = 0; m < n; ++m) {
+    const GridHost &g = gh[m];
+    MeshDesc &d = md[m];
+    std::memset(&d, 0, sizeof(d));
+    d.T = T[m];
+    d.tri_base = tris;
+    d.tile_base = tiles;
+    d.fwarp_base = fwarps;
+    d.row_base = rows;
+    d.word_base = words;
+    tris += T[m];
+    tiles += (T[m] + tile - 1) / tile;
+    fwarps += (int64_t)g.n[1] * g.nxw;
+    rows += (int64_t)g.n[2] * g.n[1];
+    words += (int64_t)g.n[2] * g.n[1] * g.nxw;
+    togg += (int64_t)g.n[0] * g.n[1] * g.nzw;
+    tab_off[m + 1] = tab_off[m] + table_floats(g);
+    res_l1[m + 1] = res_l1[m] + (int64_t)al16(g.N1);
+    res_pre[m + 1] = res_pre[m] + (int64_t)al16(g.N1);  // int32 elements, 64-byte aligned
+    max_keybits = std::max(max_keybits, g.key_bits);
+    any_l2 = any_l2 || g.level2;
+  }
+
+  Arena ws(s);
+  // coordinate tables: one pinned staging copy
+  CK(ctx_ensure_tables(ctx, (size_t)tab_off[n]));
+  for (int m = 0; m < n; ++m) pack_tables(gh[m], ctx->h_tables + tab_off[m]);
+  float *d_tab;
+  CK(ws.get(&d_tab, (size_t)tab_off[n]));
+  CK(cudaMemcpyAsync(d_tab, ctx->h_tables, tab_off[n] * sizeof(float), cudaMemcpyHostToDevice, s));
+
+  float4 *ptri, *fbox;
+  int4 *rng;
+  uint32_t *bplane, *iplane, *toggles, *wcnt, *wpre, *wtot, *stmp, *queue;
+  MeshStats *stats;
+  MeshDesc *d_md;
+  CK(ws.get(&ptri, 3 * (size_t)std::max<int64_t>(tris, 1)));
+  CK(ws.get(&rng, (size_t)std::max<int64_t>(tris, 1)));
+  CK(ws.get(&fbox, (size_t)std::max<int64_t>(tris, 1)));
+  CK(ws.get(&bplane, (size_t)words));
+  CK(ws.get(&iplane, (size_t)words));
+  CK(ws.get(&toggles, (size_t)togg));
+  CK(ws.get(&wcnt, (size_t)words));
+  CK(ws.get(&wpre, (size_t)words));
+  CK(ws.get(&wtot, 4));
+  CK(ws.get(&stmp, (size_t)scan_temp_words(words)));
+  CK(ws.get(&queue, 4));
+  CK(ws.get(&stats, (size_t)n));
+  CK(ws.get(&d_md, (size_t)n));
+  CK(cudaMemsetAsync(stats, 0, n * sizeof(MeshStats), s));
+  CK(cudaMemsetAsync(bplane, 0, words * 4, s));
+  CK(cudaMemsetAsync(toggles, 0, togg * 4, s));
+
+  // result arenas (shared by the batch's results, freed when the last one is released)
+  auto set = std::make_shared<ResultSet>();
+  set->stream = s;
+  CK(cudaMallocAsync(&set->l1, std::max<int64_t>(res_l1[n], 16), s));
+  CK(cudaMallocAsync(&set->prefix, 4 * std::max<int64_t>(res_pre[n], 16), s));
+
+  int64_t togg_off = 0;
+  for (int m = 0; m < n; ++m) {
+    MeshDesc &d = md[m];
+    const GridHost &g = gh[m];
+    d.g = make_griddev(g, d_tab + tab_off[m]);
+    d.tris = d_tris[m];
+    d.ptri = ptri + 3 * d.tri_base;
+    d.rng = rng + d.tri_base;
+    d.fbox = fbox + d.tri_base;
+    d.bplane = bplane + d.word_base;
+    d.iplane = iplane + d.word_base;
+    d.toggles = toggles + togg_off;
+    togg_off += (int64_t)g.n[0] * g.n[1] * g.nzw;
+    d.stats = stats + m;
+    d.l1 = static_cast<uint8_t *>(set->l1) + res_l1[m];
+    d.prefix = static_cast<int32_t *>(set->prefix) + res_pre[m];
+    d.ch = g.level2 ? level2_chunk(d.g) : 1;
+    if (g.level2) warp_words = std::max(warp_words, level2_warp_words(d.g));
+  }
+  BatchDev bd;
+  bd.md = d_md;
+  bd.nmesh = n;
+  bd.tile = tile;
+  bd.total_tris = tris;
+  bd.total_tiles = tiles;
+  bd.total_fwarps = fwarps;
+  bd.total_rows = rows;
+  bd.total_words = words;
+  bd.queue = queue;
+  CK(ctx_ensure_host(ctx, (size_t)n));
+  std::memcpy(ctx->h_md, md.data(), n * sizeof(MeshDesc));
+  CK(cudaMemcpyAsync(d_md, ctx->h_md, n * sizeof(MeshDesc), cudaMemcpyHostToDevice, s));
+
+  auto mark = [&](int i) {
+    if (ctx->timing) cudaEventRecord(ctx->ev[i], s);
+  };
+  auto fail_all = [&](int code, const char *msg) {
+    cudaFreeAsync(set->l1, s);
+    cudaFreeAsync(set->prefix, s);
+    if (set->bindex) cudaFreeAsync(set->bindex, s);
+    if (set->l2) cudaFreeAsync(set->l2, s);
+    set->l1 = set->prefix = set->bindex = set->l2 = nullptr;
+    return ctx_fail(ctx, code, msg);
+  };
+
+  // ---- phase A
+  mark(0);
+  launch_prep(bd, s);
+  mark(1);
+  CK(cudaGetLastError());
+  CK(cudaMemcpyAsync(ctx->h_stats, stats, n * sizeof(MeshStats), cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  int64_t caps = 0;
+  for (int m = 0; m < n; ++m) {
+    if (ctx->h_stats[m].status & ST_BAD_INPUT) return fail_all(GPV_ERR_INVALID, "non-finite vertex");
+    md[m].pair_cap = (int64_t)std::max<unsigned long long>(ctx->h_stats[m].sat1, 1);
+    md[m].emit_base = caps;
+    caps += md[m].pair_cap;
+  }
+  uint32_t *keys, *vals;
+  CK(ws.get(&keys, (size_t)caps));
+  CK(ws.get(&vals, (size_t)caps));
+  for (int m = 0; m < n; ++m) {
+    md[m].keys = keys + md[m].emit_base;
+    md[m].vals = vals + md[m].emit_base;
+  }
+  std::memcpy(ctx->h_md, md.data(), n * sizeof(MeshDesc));
+  CK(cudaMemcpyAsync(d_md, ctx->h_md, n * sizeof(MeshDesc), cudaMemcpyHostToDevice, s));
+
+  // ---- phase B
+  mark(2);
+  launch_level1(bd, ctx->num_sms, s);
+  mark(3);
+  launch_fill_finish(bd, s);
+  launch_popc(bplane, words, wcnt, s);
+  scan_u32(wcnt, wpre, words, wtot, stmp, s);
+  launch_boundary_counts(bd, wpre, wtot, s);
+  mark(4);
+  CK(cudaGetLastError());
+  CK(cudaMemcpyAsync(ctx->h_stats, stats, n * sizeof(MeshStats), cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  int64_t P = 0, Btot = 0, l2bytes = 0;
+  std::vector<int64_t> l2off(n + 1, 0), boff(n + 1, 0);
+  for (int m = 0; m < n; ++m) {
+    const MeshStats &st = ctx->h_stats[m];
+    if (st.status) return fail_all(GPV_ERR_DEVICE, "device status raised in Level1");
+    md[m].pair_base = P;
+    md[m].u_base = Btot;
+    P += (int64_t)st.pairs;
+    Btot += (int64_t)st.boundary;
+    boff[m + 1] = Btot;
+    l2off[m + 1] = l2off[m] + (gh[m].level2 ? (int64_t)st.boundary * gh[m].cells : 0);
+  }
+  l2bytes = l2off[n];
+  CK(cudaMallocAsync(&set->bindex, 4 * std::max<int64_t>(Btot, 4), s));
+  CK(cudaMallocAsync(&set->l2, std::max<int64_t>(l2bytes, 16), s));
+  for (int m = 0; m < n; ++m) {
+    md[m].bindex = static_cast<int32_t *>(set->bindex) + boff[m];
+    md[m].l2 = static_cast<uint8_t *>(set->l2) + l2off[m];
+  }
+  // sort tiles
+  std::vector<SortTile> st_host;
+  std::vector<int64_t> stb(n + 1, 0);
+  for (int m = 0; m < n; ++m) {
+    const int64_t Pm = (int64_t)ctx->h_stats[m].pairs;
+    const int64_t nt = gh[m].level2 ? (Pm + kSortTileItems - 1) / kSortTileItems : 0;
+    for (int64_t j = 0; j < nt; ++j)
+      st_host.push_back({m, (int32_t)j, (int32_t)std::min<int64_t>(kSortTileItems, Pm - j * kSortTileItems), 0});
+    stb[m + 1] = stb[m] + nt;
+  }
+  std::memcpy(ctx->h_md, md.data(), n * sizeof(MeshDesc));
+  CK(cudaMemcpyAsync(d_md, ctx->h_md, n * sizeof(MeshDesc), cudaMemcpyHostToDevice, s));
+
+  // ---- phase C
+  mark(5);
+  launch_expand(bd, wpre, s);
+  mark(6);
+  const int64_t ntiles = (int64_t)st_host.size();
+  // pairs of meshes without Level2 are not sorted; the dense layout then only holds Level2 meshes
+  int64_t P2 = 0;
+  if (any_l2 && ntiles > 0) {
+    // dense bases over the meshes that are sorted
+    for (int m = 0; m < n; ++m) {
+      md[m].pair_base = P2;
+      if (gh[m].level2) P2 += (int64_t)ctx->h_stats[m].pairs;
+    }
+    // boundary-voxel bases must follow the same set of meshes for the Level2 items
+    int64_t ub = 0;
+    for (int m = 0; m < n; ++m) {
+      md[m].u_base = ub;
+      if (gh[m].level2) ub += (int64_t)ctx->h_stats[m].boundary;
+    }
+    std::memcpy(ctx->h_md, md.data(), n * sizeof(MeshDesc));
+    CK(ctx_ensure_host_tiles(ctx, (size_t)ntiles, (size_t)n + 1));
+    std::memcpy(ctx->h_tiles, st_host.data(), ntiles * sizeof(SortTile));
+    std::memcpy(ctx->h_tb, stb.data(), (n + 1) * sizeof(int64_t));
+    SortTile *d_tiles;
+    int64_t *d_tb;
+    uint32_t *kalt, *valt, *flags, *uidx, *useg, *sortmp, *l2tmp;
+    CK(ws.get(&d_tiles, (size_t)ntiles));
+    CK(ws.get(&d_tb, (size_t)n + 1));
+    CK(ws.get(&kalt, (size_t)std::max<int64_t>(P2, 1)));
+    CK(ws.get(&valt, (size_t)std::max<int64_t>(P2, 1)));
+    CK(ws.get(&flags, (size_t)P2));
+    CK(ws.get(&uidx, (size_t)P2));
+    CK(ws.get(&useg, (size_t)ub + 1));
+    CK(ws.get(&sortmp, (size_t)std::max(sort_seg_temp_words(ntiles), scan_temp_words(P2))));
+    CK(ws.get(&l2tmp, (size_t)level2_temp_words(ub)));
+    CK(cudaMemcpyAsync(d_md, ctx->h_md, n * sizeof(MeshDesc), cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(d_tiles, ctx->h_tiles, ntiles * sizeof(SortTile), cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(d_tb, ctx->h_tb, (n + 1) * sizeof(int64_t), cudaMemcpyHostToDevice, s));
+    const bool in_alt = sort_pairs_seg(bd, d_tiles, d_tb, ntiles, keys, vals, kalt, valt, P2,
+                                       max_keybits, sortmp, s);
+    const uint32_t *sk = in_alt ? kalt : keys;
+    const uint32_t *sv = in_alt ? valt : vals;
+    launch_heads(sk, P2, flags, bd, s);
+    scan_u32(flags, uidx, P2, wtot + 1, sortmp, s);
+    launch_useg(flags, uidx, P2, useg, s);
+    mark(7);
+    launch_level2(bd, sk, sv, useg, ub, l2tmp, warp_words, ctx->num_sms, s);
+  } else {
+    mark(7);
+  }
+  mark(8);
+  CK(cudaGetLastError());
+  CK(cudaMemcpyAsync(ctx->h_stats, stats, n * sizeof(MeshStats), cudaMemcpyDeviceToHost, s));
+  CK(cudaMemcpyAsync(ctx->h_u32, wtot, 8, cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  if (ctx->timing) {
+    // stages: 0 prep, 1 level1, 2 fill finish + boundary scan, 3 expand, 4 sort + lists, 5 level2
+    const int pr[6][2] = {{0, 1}, {2, 3}, {3, 4}, {5, 6}, {6, 7}, {7, 8}};
+    for (int k = 0; k < 6; ++k) {
+      float ms = 0.f;
+      if (cudaEventElapsedTime(&ms, ctx->ev[pr[k][0]], ctx->ev[pr[k][1]]) == cudaSuccess)
+        ctx->stage_ms[k] += ms;
+    }
+    ctx->stage_calls++;
+  }
+  for (int m = 0; m < n; ++m)
+    if (ctx->h_stats[m].status) return fail_all(GPV_ERR_DEVICE, "device status raised in Level2");
+  if (any_l2 && ntiles > 0) {
+    int64_t ub = 0;
+    for (int m = 0; m < n; ++m)
+      if (gh[m].level2) ub += (int64_t)ctx->h_stats[m].boundary;
+    if ((int64_t)ctx->h_u32[1] != ub)
+      return fail_all(GPV_ERR_DEVICE, "boundary plane and pair lists disagree");
+  }
+
+  const uint64_t handle = ctx->next_handle++;
+  set->refs = n;
+  ctx->owned[handle] = set;
+  for (int m = 0; m < n; ++m) {
+    const MeshStats &st = ctx->h_stats[m];
+    gpv_result &r = out[m];
+    std::memset(&r, 0, sizeof(r));
+    r.spec = specs[m];
+    for (int a = 0; a < 3; ++a) {
+      r.grid_size[a] = gh[m].g[a];
+      r.grid_size2[a] = gh[m].level2 ? gh[m].g2[a] : 0.f;
+    }
+    r.num_level1 = gh[m].N1;
+    r.num_boundary = (int64_t)st.boundary;
+    r.num_level1_inside = (int64_t)st.l1_inside;
+    r.num_level2_inside = (int64_t)st.l2_inside;
+    r.num_level2_boundary = (int64_t)st.l2_boundary;
+    r.num_pairs = (int64_t)st.pairs;
+    r.work.sat1 = (int64_t)st.sat1;
+    r.work.sat2 = gh[m].level2 ? (int64_t)st.pairs * gh[m].cells : 0;
+    r.work.ray1 = (int64_t)st.ray1;
+    r.work.ray2 = (int64_t)st.ray2;
+    r.level1_inout = static_cast<uint8_t *>(set->l1) + res_l1[m];
+    r.level1_prefix = static_cast<int32_t *>(set->prefix) + res_pre[m];
+    r.boundary_index = static_cast<int32_t *>(set->bindex) + boff[m];
+    r.level2_inout = static_cast<uint8_t *>(set->l2) + l2off[m];
+    r.handle = handle;
+  }
+  return GPV_OK;
+#undef CK
+}
+
+}  // namespace gpv

@@ -1,0 +1,103 @@
+// gpv_ctx.h -- the library context (one per host thread) and helpers shared by the host files.
+#pragma once
+#include <memory>
+#include <string>
+#include <unordered_map>
+
+#include "gpv_internal.h"
+
+namespace gpv {
+
+// Result arrays of one batch; every result of the batch holds a reference.
+struct ResultSet {
+  void *l1 = nullptr, *prefix = nullptr, *bindex = nullptr, *l2 = nullptr;
+  cudaStream_t stream = 0;
+  int refs = 0;
+};
+
+}  // namespace gpv
+
+struct gpv_ctx {
+  static constexpr int kStages = 8;
+  int device = 0;
+  int num_sms = 148;
+  bool timing = false;                 // record per-stage CUDA events on the launching stream
+  cudaEvent_t ev[kStages + 1] = {};
+  double stage_ms[kStages] = {};       // accumulated stage durations
+  uint64_t stage_calls = 0;
+  std::string err;
+  int tile = 128;
+  gpv::MeshStats *h_stats = nullptr;   // pinned, h_cap entries
+  gpv::MeshDesc *h_md = nullptr;       // pinned, h_cap entries
+  size_t h_cap = 0;
+  gpv::SortTile *h_tiles = nullptr;    // pinned
+  int64_t *h_tb = nullptr;             // pinned
+  size_t h_tiles_cap = 0, h_tb_cap = 0;
+  uint32_t *h_u32 = nullptr;           // pinned scratch (small)
+  float *h_tables = nullptr;           // pinned staging for coordinate tables
+  size_t h_tables_cap = 0;
+  uint64_t next_handle = 1;
+  std::unordered_map<uint64_t, std::shared_ptr<gpv::ResultSet>> owned;
+};
+
+namespace gpv {
+
+inline int ctx_fail(gpv_ctx *ctx, int code, const char *what) {
+  if (ctx) ctx->err = what;
+  return code;
+}
+
+inline int ctx_cuda_fail(gpv_ctx *ctx, cudaError_t e, const char *where) {
+  if (ctx) ctx->err = std::string(where) + ": " + cudaGetErrorString(e);
+  return GPV_ERR_CUDA;
+}
+
+inline cudaError_t ctx_ensure_tables(gpv_ctx *ctx, size_t n) {
+  if (ctx->h_tables_cap >= n) return cudaSuccess;
+  if (ctx->h_tables) cudaFreeHost(ctx->h_tables);
+  ctx->h_tables = nullptr;
+  ctx->h_tables_cap = 0;
+  cudaError_t e = cudaMallocHost(&ctx->h_tables, std::max<size_t>(n, 1024) * sizeof(float));
+  if (e == cudaSuccess) ctx->h_tables_cap = std::max<size_t>(n, 1024);
+  return e;
+}
+
+inline cudaError_t ctx_ensure_host(gpv_ctx *ctx, size_t nmesh) {
+  if (ctx->h_cap >= nmesh) return cudaSuccess;
+  if (ctx->h_stats) cudaFreeHost(ctx->h_stats);
+  if (ctx->h_md) cudaFreeHost(ctx->h_md);
+  ctx->h_stats = nullptr;
+  ctx->h_md = nullptr;
+  ctx->h_cap = 0;
+  const size_t cap = std::max<size_t>(nmesh, 16);
+  cudaError_t e = cudaMallocHost(&ctx->h_stats, cap * sizeof(MeshStats));
+  if (e == cudaSuccess) e = cudaMallocHost(&ctx->h_md, cap * sizeof(MeshDesc));
+  if (e == cudaSuccess) ctx->h_cap = cap;
+  return e;
+}
+
+inline cudaError_t ctx_ensure_host_tiles(gpv_ctx *ctx, size_t ntiles, size_t ntb) {
+  cudaError_t e = cudaSuccess;
+  if (ctx->h_tiles_cap < ntiles) {
+    if (ctx->h_tiles) cudaFreeHost(ctx->h_tiles);
+    ctx->h_tiles = nullptr;
+    ctx->h_tiles_cap = 0;
+    e = cudaMallocHost(&ctx->h_tiles, ntiles * sizeof(SortTile));
+    if (e != cudaSuccess) return e;
+    ctx->h_tiles_cap = ntiles;
+  }
+  if (ctx->h_tb_cap < ntb) {
+    if (ctx->h_tb) cudaFreeHost(ctx->h_tb);
+    ctx->h_tb = nullptr;
+    ctx->h_tb_cap = 0;
+    e = cudaMallocHost(&ctx->h_tb, ntb * sizeof(int64_t));
+    if (e != cudaSuccess) return e;
+    ctx->h_tb_cap = ntb;
+  }
+  return e;
+}
+
+int run_batch(gpv_ctx *ctx, int n, const float *const *d_tris, const int64_t *T,
+              const gpv_grid_spec *specs, gpv_result *out, cudaStream_t s);
+
+}  // namespace gpv

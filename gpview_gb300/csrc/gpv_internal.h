@@ -39,37 +39,74 @@ struct GridHost {
 int grid_derive(const gpv_grid_spec &spec, GridHost &out, const float *ext1_override = nullptr);
 float eps_threshold();  // largest float below 1e-6
 
-// ---- kernels (gpv_kernels.cu) -----------------------------------------------------------------
-struct Level1Bufs {
+// ---- batched kernels (gpv_kernels.cu, gpv_level2.cu, gpv_sort.cu) -----------------------------
+// Every kernel works on a batch of meshes described by a device array of MeshDesc; a work item
+// (triangle, tile, row, pair tile, Level2 chunk) finds its mesh by binary search over the
+// per-mesh prefix of that work kind.  The plain path is a batch of one.
+struct MeshDesc {
+  GridDev g;
   const float *tris;     // input float[T*9]
-  int64_t T;
-  float4 *ptri;          // packed triangles, 3 float4 per triangle (w carries fill ranges)
-  int4 *rng;             // SAT candidate box (packed) per triangle
+  float4 *ptri;          // packed triangles, 3 float4 per triangle (w: fill ranges, 1/det)
+  int4 *rng;             // packed Level1 SAT candidate box per triangle
   float4 *fbox;          // conservative x/y box for the ray tests per triangle
-  uint32_t *bplane;      // boundary bit plane (padded rows)
-  uint32_t *iplane;      // inside (parity) bit plane (padded rows)
+  uint32_t *bplane;      // boundary bit plane (padded rows), slice of the batch plane
+  uint32_t *iplane;      // inside (parity) bit plane, slice
   uint32_t *toggles;     // column-major parity toggles
-  uint32_t *keys, *vals; // pair buffer
+  uint32_t *keys, *vals; // pair emission segment (capacity pair_cap)
   MeshStats *stats;
+  uint8_t *l1;           // outputs
+  int32_t *prefix;
+  int32_t *bindex;
+  uint8_t *l2;
+  int64_t T, pair_cap;
+  int64_t tri_base;      // prefix over meshes of triangles
+  int64_t tile_base;     // ... of Level1 tiles
+  int64_t fwarp_base;    // ... of fill-finish warps (ny * nxw)
+  int64_t row_base;      // ... of Level1 rows (nz * ny)
+  int64_t word_base;     // ... of bit-plane words (nz * ny * nxw)
+  int64_t emit_base;     // ... of pair capacities (emission segments)
+  int64_t pair_base;     // ... of pairs (dense layout after the sort)
+  int64_t u_base;        // ... of boundary voxels
+  int32_t ch;            // Level2 chunk length
+  int32_t pad;
 };
 
-void launch_prep(const GridDev &g, const Level1Bufs &b, cudaStream_t s);
-void launch_level1(const GridDev &g, const Level1Bufs &b, int tile, cudaStream_t s);
-void launch_fill_finish(const GridDev &g, const Level1Bufs &b, cudaStream_t s);
-void launch_popc(const GridDev &g, const uint32_t *bplane, uint32_t *cnt, cudaStream_t s);
-void launch_expand(const GridDev &g, const uint32_t *bplane, const uint32_t *iplane,
-                   const uint32_t *wpre, uint8_t *l1, int32_t *prefix, int32_t *bindex,
-                   MeshStats *st, cudaStream_t s);
-void launch_heads(const uint32_t *keys, int64_t P, uint32_t *flags, cudaStream_t s);
+struct BatchDev {
+  const MeshDesc *md;
+  int nmesh;
+  int tile;              // Level1 triangles per tile (32, 64, 128, 256)
+  int64_t total_tris, total_tiles, total_fwarps, total_rows, total_words;
+  uint32_t *queue;       // work-queue tickets, zeroed before each persistent launch
+};
+
+void launch_prep(const BatchDev &bd, cudaStream_t s);
+void launch_level1(const BatchDev &bd, int num_sms, cudaStream_t s);
+void launch_fill_finish(const BatchDev &bd, cudaStream_t s);
+void launch_popc(const uint32_t *plane, int64_t nwords, uint32_t *cnt, cudaStream_t s);
+void launch_boundary_counts(const BatchDev &bd, const uint32_t *wpre, const uint32_t *wtotal,
+                            cudaStream_t s);
+void launch_expand(const BatchDev &bd, const uint32_t *wpre, cudaStream_t s);
+void launch_heads(const uint32_t *keys, int64_t P, uint32_t *flags, const BatchDev &bd,
+                  cudaStream_t s);
 void launch_useg(const uint32_t *flags, const uint32_t *uidx, int64_t P, uint32_t *useg,
                  cudaStream_t s);
+
+// segmented radix sort: per mesh the pairs [in_base, in_base + P_m) end dense at pair_base
+struct SortTile { int32_t mesh, j, count, pad; };
+int64_t sort_seg_temp_words(int64_t ntiles);
+// Returns true when the sorted data ended in (kalt, valt).  tiles[] (device) lists the tiles of
+// every mesh; hist_base[m] = 256 * (tiles before mesh m) (device).
+bool sort_pairs_seg(const BatchDev &bd, const SortTile *tiles, const int64_t *tile_base_dev,
+                    int64_t ntiles, uint32_t *keys, uint32_t *vals, uint32_t *kalt, uint32_t *valt,
+                    int64_t Ptotal, int key_bits, uint32_t *temp, cudaStream_t s);
+constexpr int kSortTileItems = 2048;
+
 int level2_chunk(const GridDev &g);
-size_t level2_smem(const GridDev &g);
-int64_t level2_temp_words(int64_t B);
-void launch_level2c(const GridDev &g, const float4 *ptri, const float4 *fbox,
-                    const uint32_t *keys, const uint32_t *vals, const uint32_t *useg,
-                    const int32_t *prefix, int64_t B, uint32_t *tmp, uint8_t *l2, MeshStats *st,
-                    cudaStream_t s);
+int level2_warp_words(const GridDev &g);
+int64_t level2_temp_words(int64_t Btot);
+void launch_level2(const BatchDev &bd, const uint32_t *keys, const uint32_t *vals,
+                   const uint32_t *useg, int64_t Btot, uint32_t *tmp, int warp_words, int num_sms,
+                   cudaStream_t s);
 
 GridDev make_griddev(const GridHost &gh, const float *dtables);
 int64_t table_floats(const GridHost &gh);

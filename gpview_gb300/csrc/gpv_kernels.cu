@@ -1,21 +1,22 @@
-// gpv_kernels.cu -- sm_103a kernels of the plain voxelization path.
+// gpv_kernels.cu -- sm_103a kernels of the Level1 stage, batched over meshes.
 //
-// Pipeline for one mesh (all on one stream):
+// Pipeline (all on one stream; a plain voxelization is a batch of one):
 //   k_prep        per triangle: pack vertices as 3 float4, Level1 SAT candidate box (the
 //                 reference's own range, src/Object.cpp:2280-2325), conservative x/y box for the
-//                 ray tests, work counts.
-//   k_level1      per tile of triangles staged in shared memory by a bulk async copy (TMA):
+//                 ray tests, 1/det of the ray test, work counts.
+//   k_level1      persistent: blocks pull (mesh, triangle tile) items from a device queue; the
+//                 tile is staged in shared memory by bulk async copies (TMA) on an mbarrier.
 //                 (a) SAT units = (triangle, column) running the z run top-down; passes set the
-//                     boundary bit (atomicOr) and emit (column-major voxel key, triangle|top) pairs;
+//                     boundary bit (atomicOr) and emit (column-major voxel key, triangle|topmost).
 //                 (b) fill units = (triangle, column) running the column part of the +z
 //                     Moller-Trumbore test; passing pairs are queued per warp and the whole warp
 //                     evaluates t over the column (one voxel per lane, __ballot_sync), XOR-ing
 //                     parity toggles d(k) = hit(k) ^ hit(k+1) into a column-major plane.
 //   k_fill_finish warp-level suffix XOR of the toggles per column -> parity, transposed to
 //                 the linear (x fastest) inside plane.
-//   sort          radix sort of the pairs by column-major voxel key (gpv_sort.cu).
+//   k_popc + scan per-word boundary counts, boundaryPrefixSum.
 //   k_expand      .raw bytes of Level1, boundaryPrefixSum, boundaryIndex.
-//   Level2        gpv_level2.cu.
+//   sort / Level2 gpv_sort.cu, gpv_level2.cu.
 #include "gpv_internal.h"
 
 namespace gpv {
@@ -30,6 +31,18 @@ __device__ __forceinline__ uint32_t pack2(int lo, int hi) {
 }
 __device__ __forceinline__ int lo16(uint32_t v) { return (int)(v & 0xffffu); }
 __device__ __forceinline__ int hi16(uint32_t v) { return (int)(v >> 16); }
+
+// Mesh owning work index idx: last m with md[m].*F <= idx (meshes with no work of this kind
+// share their successor's base and are skipped).
+template <int64_t MeshDesc::*F>
+__device__ __forceinline__ int find_mesh(const MeshDesc *md, int nmesh, int64_t idx) {
+  int lo = 0, hi = nmesh - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (md[mid].*F <= idx) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
 
 // smallest i in [0,n] with tab[i] >= x (tab nondecreasing); approximate start then adjust.
 __device__ __forceinline__ int first_ge(const float *tab, int n, float x, float c0, float g) {
@@ -71,6 +84,17 @@ __device__ __forceinline__ T warp_sum(T v) {
   return v;
 }
 
+// Adds v to *dst once per warp when every lane targets the same counter, else per lane.
+__device__ __forceinline__ void warp_add(unsigned long long *dst, unsigned long long v) {
+  const unsigned long long a = (unsigned long long)dst;
+  if (__all_sync(FULL, __shfl_sync(FULL, a, 0) == a)) {
+    v = warp_sum(v);
+    if ((threadIdx.x & 31u) == 0 && v) atomicAdd(dst, v);
+  } else if (v) {
+    atomicAdd(dst, v);
+  }
+}
+
 // Conservative x/y box of the columns whose +z ray can pass the u/v tests of this triangle.
 // Outside the box every column fails them in float arithmetic; ill-conditioned projections get
 // the whole plane; triangles failing the |det| test get an empty box.
@@ -104,15 +128,20 @@ __device__ __forceinline__ float4 ray_box(const float *V, const GridDev &g) {
 }
 
 // ---------------------------------------------------------------------------------------------
-__global__ void __launch_bounds__(256) k_prep(GridDev g, Level1Bufs b) {
-  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+__global__ void __launch_bounds__(256) k_prep(BatchDev bd) {
+  const int64_t gi = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const bool live = gi < bd.total_tris;
+  const int m = find_mesh<&MeshDesc::tri_base>(bd.md, bd.nmesh, live ? gi : bd.total_tris - 1);
+  const MeshDesc &d = bd.md[m];
+  const GridDev &g = d.g;
   unsigned long long sat1 = 0, su = 0, fu = 0, r1 = 0;
-  if (t < b.T) {
+  if (live) {
+    const int64_t t = gi - d.tri_base;
     float V[9];
     bool finite = true;
 #pragma unroll
     for (int k = 0; k < 9; ++k) {
-      V[k] = __ldg(b.tris + 9 * t + k);
+      V[k] = __ldg(d.tris + 9 * t + k);
       finite = finite && isfinite(V[k]);
     }
     int lo[3], hi[3];
@@ -127,7 +156,7 @@ __global__ void __launch_bounds__(256) k_prep(GridDev g, Level1Bufs b) {
     float4 fb = ray_box(V, g);
     int fx0 = 1, fx1 = 0, fy0 = 1, fy1 = 0;
     if (!finite) {
-      atomicOr(&b.stats->status, (unsigned)ST_BAD_INPUT);
+      atomicOr(&d.stats->status, (unsigned)ST_BAD_INPUT);
       lo[0] = 1; hi[0] = 0;
       fb = make_float4(1.f, 1.f, 0.f, 0.f);
     } else {
@@ -153,22 +182,19 @@ __global__ void __launch_bounds__(256) k_prep(GridDev g, Level1Bufs b) {
     }
     if (fx0 <= fx1 && fy0 <= fy1) fu = (unsigned long long)(fx1 - fx0 + 1) * (fy1 - fy0 + 1);
     else { fx0 = 1; fx1 = 0; fy0 = 1; fy1 = 0; }
-    b.ptri[3 * t + 0] = make_float4(V[0], V[1], V[2], __uint_as_float(pack2(fx0, fx1)));
-    b.ptri[3 * t + 1] = make_float4(V[3], V[4], V[5], __uint_as_float(pack2(fy0, fy1)));
     // 1/det of the +z ray test (src/TriRayIntersection.cpp:310), shared by every column
     const float det = fa(fm(fs(V[3], V[0]), -fs(V[7], V[1])), fm(fs(V[4], V[1]), fs(V[6], V[0])));
-    b.ptri[3 * t + 2] = make_float4(V[6], V[7], V[8], __fdiv_rn(1.0f, det));
-    b.rng[t] = make_int4((int)pack2(lo[0], hi[0]), (int)pack2(lo[1], hi[1]),
+    d.ptri[3 * t + 0] = make_float4(V[0], V[1], V[2], __uint_as_float(pack2(fx0, fx1)));
+    d.ptri[3 * t + 1] = make_float4(V[3], V[4], V[5], __uint_as_float(pack2(fy0, fy1)));
+    d.ptri[3 * t + 2] = make_float4(V[6], V[7], V[8], __fdiv_rn(1.0f, det));
+    d.rng[t] = make_int4((int)pack2(lo[0], hi[0]), (int)pack2(lo[1], hi[1]),
                          (int)pack2(lo[2], hi[2]), 0);
-    b.fbox[t] = fb;
+    d.fbox[t] = fb;
   }
-  sat1 = warp_sum(sat1); su = warp_sum(su); fu = warp_sum(fu); r1 = warp_sum(r1);
-  if ((threadIdx.x & 31u) == 0) {
-    if (sat1) atomicAdd(&b.stats->sat1, sat1);
-    if (su) atomicAdd(&b.stats->sat_units, su);
-    if (fu) atomicAdd(&b.stats->fill_units, fu);
-    if (r1) atomicAdd(&b.stats->ray1, r1);
-  }
+  warp_add(&d.stats->sat1, sat1);
+  warp_add(&d.stats->sat_units, su);
+  warp_add(&d.stats->fill_units, fu);
+  warp_add(&d.stats->ray1, r1);
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -187,193 +213,210 @@ __device__ __forceinline__ int tile_search(const uint32_t *off, int nt, uint32_t
 }
 
 template <int TILE>
-__global__ void __launch_bounds__(kL1Threads) k_level1(GridDev g, Level1Bufs b) {
+__global__ void __launch_bounds__(kL1Threads) k_level1(BatchDev bd) {
   __shared__ __align__(16) float4 s_tri[TILE * 3];
   __shared__ __align__(16) int4 s_rng[TILE];
   __shared__ uint32_t s_soff[TILE + 1];
   __shared__ uint32_t s_foff[TILE + 1];
   __shared__ uint32_t s_q[kL1Warps][32];
+  __shared__ uint32_t s_ws[kL1Warps], s_wf[kL1Warps];
   __shared__ __align__(8) uint64_t s_bar;
+  __shared__ int64_t s_item;
 
   const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
-  const int64_t t0 = (int64_t)blockIdx.x * TILE;
-  const int nt = (int)min((int64_t)TILE, b.T - t0);
-
-  // ---- stage the tile with bulk async copies completing on an mbarrier
+  const unsigned lt_mask = (1u << lane) - 1u;
   if (threadIdx.x == 0) {
     mbar_init(&s_bar, 1);
     fence_mbar_init();
   }
   __syncthreads();
-  if (threadIdx.x == 0) {
-    const uint32_t bt = (uint32_t)nt * 48u, br = (uint32_t)nt * 16u;
-    mbar_expect_tx(&s_bar, bt + br);
-    bulk_g2s(s_tri, b.ptri + 3 * t0, bt, &s_bar);
-    bulk_g2s(s_rng, b.rng + t0, br, &s_bar);
-  }
-  const bool ok = mbar_wait_bounded(&s_bar, 0, kWaitLimit);
-  if (__syncthreads_or(!ok)) {
+
+  for (uint32_t iter = 0;; ++iter) {
+    // ---- pull the next (mesh, tile) item from the queue
+    if (threadIdx.x == 0) s_item = (int64_t)atomicAdd(&bd.queue[0], 1u);
+    __syncthreads();
+    const int64_t item = s_item;
+    if (item >= bd.total_tiles) break;
+    const int m = find_mesh<&MeshDesc::tile_base>(bd.md, bd.nmesh, item);
+    const MeshDesc &d = bd.md[m];
+    const GridDev &g = d.g;
+    const int64_t t0 = (item - d.tile_base) * TILE;
+    const int nt = (int)min((int64_t)TILE, d.T - t0);
+
+    // ---- stage the tile with bulk async copies completing on the mbarrier
     if (threadIdx.x == 0) {
-      atomicOr(&b.stats->status, (unsigned)ST_WAIT_TIMEOUT);
-      mbar_wait_bounded(&s_bar, 0, kWaitLimit);  // let the copy in flight land before exiting
+      const uint32_t bt = (uint32_t)nt * 48u, br = (uint32_t)nt * 16u;
+      mbar_expect_tx(&s_bar, bt + br);
+      bulk_g2s(s_tri, d.ptri + 3 * t0, bt, &s_bar);
+      bulk_g2s(s_rng, d.rng + t0, br, &s_bar);
     }
-    return;
-  }
-
-  // ---- per-triangle unit counts and their block scan
-  uint32_t cs = 0, cf = 0;
-  if ((int)threadIdx.x < nt) {
-    const int4 r = s_rng[threadIdx.x];
-    const int x0 = lo16(r.x), x1 = hi16(r.x), y0 = lo16(r.y), y1 = hi16(r.y);
-    if (x0 <= x1 && y0 <= y1) cs = (uint32_t)((x1 - x0 + 1) * (y1 - y0 + 1));
-    const uint32_t fxr = __float_as_uint(s_tri[3 * threadIdx.x].w);
-    const uint32_t fyr = __float_as_uint(s_tri[3 * threadIdx.x + 1].w);
-    if (lo16(fxr) <= hi16(fxr) && lo16(fyr) <= hi16(fyr))
-      cf = (uint32_t)((hi16(fxr) - lo16(fxr) + 1) * (hi16(fyr) - lo16(fyr) + 1));
-  }
-  {
-    __shared__ uint32_t s_ws[kL1Warps], s_wf[kL1Warps];
-    const uint32_t is = warp_incl_scan(cs), iff = warp_incl_scan(cf);
-    if (lane == 31) { s_ws[warp] = is; s_wf[warp] = iff; }
-    __syncthreads();
-    uint32_t bs = 0, bf = 0;
-    for (unsigned w = 0; w < warp; ++w) { bs += s_ws[w]; bf += s_wf[w]; }
-    if ((int)threadIdx.x < TILE) {
-      s_soff[threadIdx.x] = bs + is - cs;
-      s_foff[threadIdx.x] = bf + iff - cf;
-    }
-    if (threadIdx.x == kL1Threads - 1) {
-      s_soff[TILE] = bs + is;
-      s_foff[TILE] = bf + iff;
-    }
-    __syncthreads();
-  }
-  const uint32_t Us = s_soff[TILE], Uf = s_foff[TILE];
-  const int nx = g.n[0], ny = g.n[1], nz = g.n[2];
-  const unsigned lt_mask = (1u << lane) - 1u;
-  const uint64_t cap = b.stats->pair_cap;
-
-  // ---- (a) SAT units
-  for (uint32_t base = warp * 32u; base < Us; base += kL1Warps * 32u) {
-    const uint32_t u = base + lane;
-    int lt = 0, p = 0, q = 0, z0 = 0, zc = -1;
-    float V[9];
-    SatCol sc;
-    if (u < Us) {
-      lt = tile_search(s_soff, nt, u);
-      const int4 r = s_rng[lt];
-      const int x0 = lo16(r.x), x1 = hi16(r.x), y0 = lo16(r.y);
-      z0 = lo16(r.z);
-      const uint32_t c = u - s_soff[lt];
-      const int nxr = x1 - x0 + 1;
-      p = x0 + (int)(c % (uint32_t)nxr);
-      q = y0 + (int)(c / (uint32_t)nxr);
-      const float4 a0 = s_tri[3 * lt], a1 = s_tri[3 * lt + 1], a2 = s_tri[3 * lt + 2];
-      V[0] = a0.x; V[1] = a0.y; V[2] = a0.z; V[3] = a1.x; V[4] = a1.y; V[5] = a1.z;
-      V[6] = a2.x; V[7] = a2.y; V[8] = a2.z;
-      if (sat_col(V, __ldg(g.c1[0] + p), __ldg(g.c1[1] + q), g.e1, sc)) zc = hi16(r.z);
-    }
-    bool first = true;
-    const uint32_t tglob = (uint32_t)(t0 + lt);
-    while (__any_sync(FULL, zc >= z0)) {
-      uint32_t mask = 0;
-      const int ztop = zc;
-      if (zc >= z0) {
-        const int nrun = min(32, zc - z0 + 1);
-        for (int d = 0; d < nrun; ++d)
-          if (sat_z(sc, V, __ldg(g.c1[2] + (ztop - d)), g.e1)) mask |= 1u << d;
-        zc -= nrun;
+    const bool ok = mbar_wait_bounded(&s_bar, iter & 1u, kWaitLimit);
+    if (__syncthreads_or(!ok)) {
+      if (threadIdx.x == 0) {
+        atomicOr(&d.stats->status, (unsigned)ST_WAIT_TIMEOUT);
+        mbar_wait_bounded(&s_bar, iter & 1u, kWaitLimit);  // let the copy in flight land
       }
-      const uint32_t cnt = __popc(mask);
-      const uint32_t inc = warp_incl_scan(cnt);
-      const uint32_t tot = __shfl_sync(FULL, inc, 31);
-      unsigned long long basep = 0;
-      if (lane == 31 && tot) basep = atomicAdd(&b.stats->pairs, (unsigned long long)tot);
-      basep = __shfl_sync(FULL, basep, 31);
-      uint64_t pos = basep + inc - cnt;
-      while (mask) {
-        const int d = __ffs(mask) - 1;
-        mask &= mask - 1u;
-        const int r = ztop - d;
-        if (pos < cap) {
-          b.keys[pos] = (uint32_t)(((uint64_t)q * nx + p) * nz + r);
-          b.vals[pos] = tglob | (first ? 0x80000000u : 0u);
-        } else {
-          atomicOr(&b.stats->status, (unsigned)ST_PAIR_OVERFLOW);
+      return;
+    }
+
+    // ---- per-triangle unit counts and their block scan
+    uint32_t cs = 0, cf = 0;
+    if ((int)threadIdx.x < nt) {
+      const int4 r = s_rng[threadIdx.x];
+      const int x0 = lo16(r.x), x1 = hi16(r.x), y0 = lo16(r.y), y1 = hi16(r.y);
+      if (x0 <= x1 && y0 <= y1) cs = (uint32_t)((x1 - x0 + 1) * (y1 - y0 + 1));
+      const uint32_t fxr = __float_as_uint(s_tri[3 * threadIdx.x].w);
+      const uint32_t fyr = __float_as_uint(s_tri[3 * threadIdx.x + 1].w);
+      if (lo16(fxr) <= hi16(fxr) && lo16(fyr) <= hi16(fyr))
+        cf = (uint32_t)((hi16(fxr) - lo16(fxr) + 1) * (hi16(fyr) - lo16(fyr) + 1));
+    }
+    {
+      const uint32_t is = warp_incl_scan(cs), iff = warp_incl_scan(cf);
+      if (lane == 31) { s_ws[warp] = is; s_wf[warp] = iff; }
+      __syncthreads();
+      uint32_t bs = 0, bf = 0;
+      for (unsigned w = 0; w < warp; ++w) { bs += s_ws[w]; bf += s_wf[w]; }
+      if ((int)threadIdx.x < TILE) {
+        s_soff[threadIdx.x] = bs + is - cs;
+        s_foff[threadIdx.x] = bf + iff - cf;
+      }
+      if (threadIdx.x == kL1Threads - 1) {
+        s_soff[TILE] = bs + is;
+        s_foff[TILE] = bf + iff;
+      }
+      __syncthreads();
+    }
+    const uint32_t Us = s_soff[TILE], Uf = s_foff[TILE];
+    const int nx = g.n[0], ny = g.n[1], nz = g.n[2];
+    const uint64_t cap = (uint64_t)d.pair_cap;
+
+    // ---- (a) SAT units
+    for (uint32_t base = warp * 32u; base < Us; base += kL1Warps * 32u) {
+      const uint32_t u = base + lane;
+      int lt = 0, p = 0, q = 0, z0 = 0, zc = -1;
+      float V[9];
+      SatCol sc;
+      if (u < Us) {
+        lt = tile_search(s_soff, nt, u);
+        const int4 r = s_rng[lt];
+        const int x0 = lo16(r.x), x1 = hi16(r.x), y0 = lo16(r.y);
+        z0 = lo16(r.z);
+        const uint32_t c = u - s_soff[lt];
+        const int nxr = x1 - x0 + 1;
+        p = x0 + (int)(c % (uint32_t)nxr);
+        q = y0 + (int)(c / (uint32_t)nxr);
+        const float4 a0 = s_tri[3 * lt], a1 = s_tri[3 * lt + 1], a2 = s_tri[3 * lt + 2];
+        V[0] = a0.x; V[1] = a0.y; V[2] = a0.z; V[3] = a1.x; V[4] = a1.y; V[5] = a1.z;
+        V[6] = a2.x; V[7] = a2.y; V[8] = a2.z;
+        if (sat_col(V, __ldg(g.c1[0] + p), __ldg(g.c1[1] + q), g.e1, sc)) zc = hi16(r.z);
+      }
+      bool first = true;
+      const uint32_t tglob = (uint32_t)(t0 + lt);
+      while (__any_sync(FULL, zc >= z0)) {
+        uint32_t mask = 0;
+        const int ztop = zc;
+        if (zc >= z0) {
+          const int nrun = min(32, zc - z0 + 1);
+          for (int dd = 0; dd < nrun; ++dd)
+            if (sat_z(sc, V, __ldg(g.c1[2] + (ztop - dd)), g.e1)) mask |= 1u << dd;
+          zc -= nrun;
         }
-        first = false;
-        ++pos;
-        atomicOr(&b.bplane[((size_t)r * ny + q) * g.nxw + (p >> 5)], 1u << (p & 31));
+        const uint32_t cnt = __popc(mask);
+        const uint32_t inc = warp_incl_scan(cnt);
+        const uint32_t tot = __shfl_sync(FULL, inc, 31);
+        unsigned long long basep = 0;
+        if (lane == 31 && tot) basep = atomicAdd(&d.stats->pairs, (unsigned long long)tot);
+        basep = __shfl_sync(FULL, basep, 31);
+        uint64_t pos = basep + inc - cnt;
+        while (mask) {
+          const int dd = __ffs(mask) - 1;
+          mask &= mask - 1u;
+          const int r = ztop - dd;
+          if (pos < cap) {
+            d.keys[pos] = (uint32_t)(((uint64_t)q * nx + p) * nz + r);
+            d.vals[pos] = tglob | (first ? 0x80000000u : 0u);
+          } else {
+            atomicOr(&d.stats->status, (unsigned)ST_PAIR_OVERFLOW);
+          }
+          first = false;
+          ++pos;
+          atomicOr(&d.bplane[((size_t)r * ny + q) * g.nxw + (p >> 5)], 1u << (p & 31));
+        }
       }
     }
-  }
 
-  // ---- (b) fill units
-  for (uint32_t base = warp * 32u; base < Uf; base += kL1Warps * 32u) {
-    const uint32_t u = base + lane;
-    bool pass = false;
-    if (u < Uf) {
-      const int lt = tile_search(s_foff, nt, u);
-      const float4 a0 = s_tri[3 * lt], a1 = s_tri[3 * lt + 1], a2 = s_tri[3 * lt + 2];
-      const uint32_t fxr = __float_as_uint(a0.w), fyr = __float_as_uint(a1.w);
-      const uint32_t c = u - s_foff[lt];
-      const int nxr = hi16(fxr) - lo16(fxr) + 1;
-      const int i = lo16(fxr) + (int)(c % (uint32_t)nxr);
-      const int j = lo16(fyr) + (int)(c / (uint32_t)nxr);
-      const float V[9] = {a0.x, a0.y, a0.z, a1.x, a1.y, a1.z, a2.x, a2.y, a2.z};
-      RayTri rt;
-      ray_tri_pre(V, a2.w, rt);  // fill units exist only for triangles passing the det test
-      RayCol rc;
-      pass = ray_col(rt, __ldg(g.c1[0] + i), __ldg(g.c1[1] + j), rc);
-    }
-    const unsigned qm = __ballot_sync(FULL, pass);
-    if (pass) s_q[warp][__popc(qm & lt_mask)] = u;
-    __syncwarp();
-    const int nq = __popc(qm);
-    for (int e = 0; e < nq; ++e) {
-      const uint32_t uu = s_q[warp][e];
-      const int lt = tile_search(s_foff, nt, uu);
-      const float4 a0 = s_tri[3 * lt], a1 = s_tri[3 * lt + 1], a2 = s_tri[3 * lt + 2];
-      const uint32_t fxr = __float_as_uint(a0.w), fyr = __float_as_uint(a1.w);
-      const uint32_t c = uu - s_foff[lt];
-      const int nxr = hi16(fxr) - lo16(fxr) + 1;
-      const int i = lo16(fxr) + (int)(c % (uint32_t)nxr);
-      const int j = lo16(fyr) + (int)(c / (uint32_t)nxr);
-      const float V[9] = {a0.x, a0.y, a0.z, a1.x, a1.y, a1.z, a2.x, a2.y, a2.z};
-      RayTri rt;
-      ray_tri_pre(V, a2.w, rt);
-      RayCol rc;
-      ray_col(rt, __ldg(g.c1[0] + i), __ldg(g.c1[1] + j), rc);
-      const size_t col = (size_t)j * nx + i;
-      uint32_t carry = 0;
-      for (int w = g.nzw - 1; w >= 0; --w) {
-        const int k = w * 32 + (int)lane;
-        const bool hit = k < nz && ray_t(rt, rc, __ldg(g.c1[2] + k), g.thr);
-        const uint32_t h = __ballot_sync(FULL, hit);
-        const uint32_t d = h ^ ((h >> 1) | (carry << 31));
-        carry = h & 1u;
-        if (lane == 0 && d) atomicXor(&b.toggles[col * g.nzw + w], d);
+    // ---- (b) fill units
+    for (uint32_t base = warp * 32u; base < Uf; base += kL1Warps * 32u) {
+      const uint32_t u = base + lane;
+      bool pass = false;
+      if (u < Uf) {
+        const int lt = tile_search(s_foff, nt, u);
+        const float4 a0 = s_tri[3 * lt], a1 = s_tri[3 * lt + 1], a2 = s_tri[3 * lt + 2];
+        const uint32_t fxr = __float_as_uint(a0.w), fyr = __float_as_uint(a1.w);
+        const uint32_t c = u - s_foff[lt];
+        const int nxr = hi16(fxr) - lo16(fxr) + 1;
+        const int i = lo16(fxr) + (int)(c % (uint32_t)nxr);
+        const int j = lo16(fyr) + (int)(c / (uint32_t)nxr);
+        const float V[9] = {a0.x, a0.y, a0.z, a1.x, a1.y, a1.z, a2.x, a2.y, a2.z};
+        RayTri rt;
+        ray_tri_pre(V, a2.w, rt);  // fill units exist only for triangles passing the det test
+        RayCol rc;
+        pass = ray_col(rt, __ldg(g.c1[0] + i), __ldg(g.c1[1] + j), rc);
       }
+      const unsigned qm = __ballot_sync(FULL, pass);
+      if (pass) s_q[warp][__popc(qm & lt_mask)] = u;
+      __syncwarp();
+      const int nq = __popc(qm);
+      for (int e = 0; e < nq; ++e) {
+        const uint32_t uu = s_q[warp][e];
+        const int lt = tile_search(s_foff, nt, uu);
+        const float4 a0 = s_tri[3 * lt], a1 = s_tri[3 * lt + 1], a2 = s_tri[3 * lt + 2];
+        const uint32_t fxr = __float_as_uint(a0.w), fyr = __float_as_uint(a1.w);
+        const uint32_t c = uu - s_foff[lt];
+        const int nxr = hi16(fxr) - lo16(fxr) + 1;
+        const int i = lo16(fxr) + (int)(c % (uint32_t)nxr);
+        const int j = lo16(fyr) + (int)(c / (uint32_t)nxr);
+        const float V[9] = {a0.x, a0.y, a0.z, a1.x, a1.y, a1.z, a2.x, a2.y, a2.z};
+        RayTri rt;
+        ray_tri_pre(V, a2.w, rt);
+        RayCol rc;
+        ray_col(rt, __ldg(g.c1[0] + i), __ldg(g.c1[1] + j), rc);
+        const size_t col = (size_t)j * nx + i;
+        uint32_t carry = 0;
+        for (int w = g.nzw - 1; w >= 0; --w) {
+          const int k = w * 32 + (int)lane;
+          const bool hit = k < nz && ray_t(rt, rc, __ldg(g.c1[2] + k), g.thr);
+          const uint32_t h = __ballot_sync(FULL, hit);
+          const uint32_t dd = h ^ ((h >> 1) | (carry << 31));
+          carry = h & 1u;
+          if (lane == 0 && dd) atomicXor(&d.toggles[col * g.nzw + w], dd);
+        }
+      }
+      __syncwarp();
     }
-    __syncwarp();
+    __syncthreads();  // the next item overwrites the tile
   }
 }
 
 // ---------------------------------------------------------------------------------------------
-// One warp per (row j, 32-column group): suffix XOR of each column's toggles gives the parity
-// of every voxel; 32 ballots per word transpose it into the linear inside plane.
-__global__ void __launch_bounds__(256) k_fill_finish(GridDev g, Level1Bufs b) {
+// One warp per (mesh, row j, 32-column group): suffix XOR of each column's toggles gives the
+// parity of every voxel; 32 ballots per word transpose it into the linear inside plane.
+__global__ void __launch_bounds__(256) k_fill_finish(BatchDev bd) {
   const int64_t gw = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const unsigned lane = threadIdx.x & 31u;
+  if (gw >= bd.total_fwarps) return;
+  const int m = find_mesh<&MeshDesc::fwarp_base>(bd.md, bd.nmesh, gw);
+  const MeshDesc &d = bd.md[m];
+  const GridDev &g = d.g;
+  const int64_t lw = gw - d.fwarp_base;
   const int nx = g.n[0], ny = g.n[1], nz = g.n[2];
-  if (gw >= (int64_t)ny * g.nxw) return;
-  const int j = (int)(gw / g.nxw), ig = (int)(gw % g.nxw);
+  const int j = (int)(lw / g.nxw), ig = (int)(lw % g.nxw);
   const int i = ig * 32 + (int)lane;
   const bool valid = i < nx;
   const size_t col = (size_t)j * nx + i;
   uint32_t carry = 0;
   for (int w = g.nzw - 1; w >= 0; --w) {
-    const uint32_t D = valid ? b.toggles[col * g.nzw + w] : 0u;
+    const uint32_t D = valid ? d.toggles[col * g.nzw + w] : 0u;
     uint32_t s = D;
     s ^= s >> 1; s ^= s >> 2; s ^= s >> 4; s ^= s >> 8; s ^= s >> 16;
     if (carry) s = ~s;
@@ -381,11 +424,11 @@ __global__ void __launch_bounds__(256) k_fill_finish(GridDev g, Level1Bufs b) {
     uint32_t mine = 0;
 #pragma unroll
     for (int bb = 0; bb < 32; ++bb) {
-      const uint32_t m = __ballot_sync(FULL, (s >> bb) & 1u);
-      if ((int)lane == bb) mine = m;
+      const uint32_t mm = __ballot_sync(FULL, (s >> bb) & 1u);
+      if ((int)lane == bb) mine = mm;
     }
     const int k = w * 32 + (int)lane;
-    if (k < nz) b.iplane[((size_t)k * ny + j) * g.nxw + ig] = mine;
+    if (k < nz) d.iplane[((size_t)k * ny + j) * g.nxw + ig] = mine;
   }
 }
 
@@ -394,13 +437,26 @@ __global__ void k_popc(const uint32_t *__restrict__ plane, int64_t nw, uint32_t 
   if (w < nw) cnt[w] = __popc(plane[w]);
 }
 
-// One block per Level1 row (k, j): state bytes, boundaryPrefixSum, boundaryIndex.
-__global__ void __launch_bounds__(128) k_expand(GridDev g, const uint32_t *__restrict__ bplane,
-                                                const uint32_t *__restrict__ iplane,
-                                                const uint32_t *__restrict__ wpre,
-                                                uint8_t *__restrict__ l1, int32_t *__restrict__ prefix,
-                                                int32_t *__restrict__ bindex, MeshStats *st) {
-  const int64_t row = blockIdx.x;
+// B_m = boundary voxels of mesh m, from the exclusive scan over the batch's plane words.
+__global__ void k_boundary_counts(BatchDev bd, const uint32_t *__restrict__ wpre,
+                                  const uint32_t *__restrict__ wtotal) {
+  const int m = blockIdx.x * blockDim.x + threadIdx.x;
+  if (m >= bd.nmesh) return;
+  const uint32_t s = wpre[bd.md[m].word_base];
+  const uint32_t e = m + 1 < bd.nmesh ? wpre[bd.md[m + 1].word_base] : *wtotal;
+  bd.md[m].stats->boundary = e - s;
+}
+
+// One block per (mesh, Level1 row (k, j)): state bytes, boundaryPrefixSum, boundaryIndex.
+__global__ void __launch_bounds__(128) k_expand(BatchDev bd, const uint32_t *__restrict__ wpre) {
+  const int64_t grow = blockIdx.x;
+  const int m = find_mesh<&MeshDesc::row_base>(bd.md, bd.nmesh, grow);
+  const MeshDesc &d = bd.md[m];
+  const GridDev &g = d.g;
+  const int64_t row = grow - d.row_base;
+  const uint32_t pbase = wpre[d.word_base];
+  const uint32_t *bplane = d.bplane, *iplane = d.iplane;
+  const uint32_t *wp = wpre + d.word_base;
   const int nx = g.n[0];
   const bool vec = (nx & 3) == 0;
   unsigned long long nin = 0;
@@ -415,32 +471,41 @@ __global__ void __launch_bounds__(128) k_expand(GridDev g, const uint32_t *__res
       const size_t w = (size_t)row * g.nxw + (x >> 5);
       const int bit = x & 31;
       const uint32_t bw = bplane[w], iw = iplane[w];
-      const uint32_t p = wpre[w] + __popc(bw & ((1u << bit) - 1u));
+      const uint32_t p = wp[w] - pbase + __popc(bw & ((1u << bit) - 1u));
       const bool isb = (bw >> bit) & 1u, isi = (iw >> bit) & 1u;
       const uint32_t s = isb ? 254u : (isi ? 127u : 0u);
       nin += (!isb && isi);
       pre[e] = (int32_t)p;
       const int64_t v = row * nx + x;
-      if (isb) bindex[p] = (int32_t)v;
+      if (isb) d.bindex[p] = (int32_t)v;
       if (!vec) {
-        l1[v] = (uint8_t)s;
-        prefix[v] = (int32_t)p;
+        d.l1[v] = (uint8_t)s;
+        d.prefix[v] = (int32_t)p;
       }
       bytes |= s << (8 * e);
     }
     if (vec) {
       const int64_t v = row * nx + x4;
-      *reinterpret_cast<uint32_t *>(l1 + v) = bytes;
-      *reinterpret_cast<int4 *>(prefix + v) = make_int4(pre[0], pre[1], pre[2], pre[3]);
+      *reinterpret_cast<uint32_t *>(d.l1 + v) = bytes;
+      *reinterpret_cast<int4 *>(d.prefix + v) = make_int4(pre[0], pre[1], pre[2], pre[3]);
     }
   }
   nin = warp_sum(nin);
-  if ((threadIdx.x & 31u) == 0 && nin) atomicAdd(&st->l1_inside, nin);
+  if ((threadIdx.x & 31u) == 0 && nin) atomicAdd(&d.stats->l1_inside, nin);
 }
 
 __global__ void k_heads(const uint32_t *__restrict__ keys, int64_t P, uint32_t *__restrict__ flags) {
   const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (e < P) flags[e] = (e == 0 || keys[e] != keys[e - 1]) ? 1u : 0u;
+}
+
+// Every mesh's first pair starts a segment even when its key equals the previous mesh's last.
+__global__ void k_mesh_pair_heads(BatchDev bd, int64_t P, uint32_t *__restrict__ flags) {
+  const int m = blockIdx.x * blockDim.x + threadIdx.x;
+  if (m >= bd.nmesh) return;
+  const int64_t b = bd.md[m].pair_base;
+  const int64_t e = m + 1 < bd.nmesh ? bd.md[m + 1].pair_base : P;
+  if (e > b) flags[b] = 1u;
 }
 
 __global__ void k_useg(const uint32_t *__restrict__ flags, const uint32_t *__restrict__ uidx,
@@ -453,49 +518,55 @@ __global__ void k_useg(const uint32_t *__restrict__ flags, const uint32_t *__res
 }  // namespace
 
 // ---- launchers --------------------------------------------------------------------------------
-void launch_prep(const GridDev &g, const Level1Bufs &b, cudaStream_t s) {
-  if (b.T <= 0) return;
-  const unsigned nb = (unsigned)((b.T + 255) / 256);
-  k_prep<<<nb, 256, 0, s>>>(g, b);
+void launch_prep(const BatchDev &bd, cudaStream_t s) {
+  if (bd.total_tris <= 0) return;
+  k_prep<<<(unsigned)((bd.total_tris + 255) / 256), 256, 0, s>>>(bd);
   count_launch();
 }
 
-void launch_level1(const GridDev &g, const Level1Bufs &b, int tile, cudaStream_t s) {
-  if (b.T <= 0) return;
-  const unsigned nb = (unsigned)((b.T + tile - 1) / tile);
-  switch (tile) {
-    case 32: k_level1<32><<<nb, kL1Threads, 0, s>>>(g, b); count_launch(); break;
-    case 64: k_level1<64><<<nb, kL1Threads, 0, s>>>(g, b); count_launch(); break;
-    case 128: k_level1<128><<<nb, kL1Threads, 0, s>>>(g, b); count_launch(); break;
-    default: k_level1<256><<<(unsigned)((b.T + 255) / 256), kL1Threads, 0, s>>>(g, b); count_launch(); break;
+void launch_level1(const BatchDev &bd, int num_sms, cudaStream_t s) {
+  if (bd.total_tiles <= 0) return;
+  const int64_t grid = std::min<int64_t>(bd.total_tiles, (int64_t)num_sms * 8);
+  cudaMemsetAsync(bd.queue, 0, sizeof(uint32_t), s);
+  switch (bd.tile) {
+    case 32: k_level1<32><<<(unsigned)grid, kL1Threads, 0, s>>>(bd); break;
+    case 64: k_level1<64><<<(unsigned)grid, kL1Threads, 0, s>>>(bd); break;
+    case 128: k_level1<128><<<(unsigned)grid, kL1Threads, 0, s>>>(bd); break;
+    default: k_level1<256><<<(unsigned)grid, kL1Threads, 0, s>>>(bd); break;
   }
-}
-
-void launch_fill_finish(const GridDev &g, const Level1Bufs &b, cudaStream_t s) {
-  const int64_t warps = (int64_t)g.n[1] * g.nxw;
-  const unsigned nb = (unsigned)((warps * 32 + 255) / 256);
-  k_fill_finish<<<nb, 256, 0, s>>>(g, b);
   count_launch();
 }
 
-void launch_popc(const GridDev &g, const uint32_t *bplane, uint32_t *cnt, cudaStream_t s) {
-  const int64_t nw = (int64_t)g.n[2] * g.n[1] * g.nxw;
-  k_popc<<<(unsigned)((nw + 255) / 256), 256, 0, s>>>(bplane, nw, cnt);
+void launch_fill_finish(const BatchDev &bd, cudaStream_t s) {
+  if (bd.total_fwarps <= 0) return;
+  k_fill_finish<<<(unsigned)((bd.total_fwarps * 32 + 255) / 256), 256, 0, s>>>(bd);
   count_launch();
 }
 
-void launch_expand(const GridDev &g, const uint32_t *bplane, const uint32_t *iplane,
-                   const uint32_t *wpre, uint8_t *l1, int32_t *prefix, int32_t *bindex,
-                   MeshStats *st, cudaStream_t s) {
-  const unsigned rows = (unsigned)((int64_t)g.n[2] * g.n[1]);
-  k_expand<<<rows, 128, 0, s>>>(g, bplane, iplane, wpre, l1, prefix, bindex, st);
+void launch_popc(const uint32_t *plane, int64_t nwords, uint32_t *cnt, cudaStream_t s) {
+  if (nwords <= 0) return;
+  k_popc<<<(unsigned)((nwords + 255) / 256), 256, 0, s>>>(plane, nwords, cnt);
   count_launch();
 }
 
-void launch_heads(const uint32_t *keys, int64_t P, uint32_t *flags, cudaStream_t s) {
+void launch_boundary_counts(const BatchDev &bd, const uint32_t *wpre, const uint32_t *wtotal,
+                            cudaStream_t s) {
+  k_boundary_counts<<<(unsigned)((bd.nmesh + 127) / 128), 128, 0, s>>>(bd, wpre, wtotal);
+  count_launch();
+}
+
+void launch_expand(const BatchDev &bd, const uint32_t *wpre, cudaStream_t s) {
+  if (bd.total_rows <= 0) return;
+  k_expand<<<(unsigned)bd.total_rows, 128, 0, s>>>(bd, wpre);
+  count_launch();
+}
+
+void launch_heads(const uint32_t *keys, int64_t P, uint32_t *flags, const BatchDev &bd,
+                  cudaStream_t s) {
   if (P <= 0) return;
   k_heads<<<(unsigned)((P + 255) / 256), 256, 0, s>>>(keys, P, flags);
-  count_launch();
+  k_mesh_pair_heads<<<(unsigned)((bd.nmesh + 127) / 128), 128, 0, s>>>(bd, P, flags);
+  count_launch(2);
 }
 
 void launch_useg(const uint32_t *flags, const uint32_t *uidx, int64_t P, uint32_t *useg,

@@ -131,12 +131,26 @@ struct WarpScratch {
 };
 
 // ---- item construction -----------------------------------------------------------------------
-__global__ void k_colflags(const uint32_t *__restrict__ keys, const uint32_t *__restrict__ useg,
-                           int64_t B, uint32_t nz, uint32_t *__restrict__ cflag) {
+__device__ __forceinline__ int mesh_of_u(const MeshDesc *md, int nmesh, int64_t u) {
+  int lo = 0, hi = nmesh - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (md[mid].u_base <= u) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
+
+// cflag[u] = 1 where a new Level1 column starts (a mesh's first boundary voxel, or a column
+// change within the mesh).
+__global__ void k_colflags(BatchDev bd, const uint32_t *__restrict__ keys,
+                           const uint32_t *__restrict__ useg, int64_t B,
+                           uint32_t *__restrict__ cflag) {
   const int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (u >= B) return;
+  const int m = mesh_of_u(bd.md, bd.nmesh, u);
+  const uint32_t nz = (uint32_t)bd.md[m].g.n[2];
   const uint32_t col = keys[useg[u]] / nz;
-  cflag[u] = (u == 0 || keys[useg[u - 1]] / nz != col) ? 1u : 0u;
+  cflag[u] = (u == bd.md[m].u_base || keys[useg[u - 1]] / nz != col) ? 1u : 0u;
 }
 
 __global__ void k_colheads(const uint32_t *__restrict__ cflag, const uint32_t *__restrict__ cord,
@@ -147,11 +161,12 @@ __global__ void k_colheads(const uint32_t *__restrict__ cflag, const uint32_t *_
   if (u == B - 1) colhead[cord[u] + cflag[u]] = (uint32_t)B;
 }
 
-__global__ void k_itemflags(const uint32_t *__restrict__ cflag, const uint32_t *__restrict__ cord,
-                            const uint32_t *__restrict__ colhead, int64_t B, int CH,
-                            uint32_t *__restrict__ iflag) {
+__global__ void k_itemflags(BatchDev bd, const uint32_t *__restrict__ cflag,
+                            const uint32_t *__restrict__ cord, const uint32_t *__restrict__ colhead,
+                            int64_t B, uint32_t *__restrict__ iflag) {
   const int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (u >= B) return;
+  const int CH = bd.md[mesh_of_u(bd.md, bd.nmesh, u)].ch;
   const uint32_t c = cord[u] + cflag[u] - 1u;
   iflag[u] = ((u - colhead[c]) % CH == 0) ? 1u : 0u;
 }
@@ -166,21 +181,31 @@ __global__ void k_itemstarts(const uint32_t *__restrict__ iflag, const uint32_t 
 
 // ---- Level2 ------------------------------------------------------------------------------------
 __global__ void __launch_bounds__(kWarps * 32) k_level2c(
-    GridDev g, const float4 *__restrict__ ptri, const float4 *__restrict__ fbox,
-    const uint32_t *__restrict__ keys, const uint32_t *__restrict__ vals,
+    BatchDev bd, const uint32_t *__restrict__ keys, const uint32_t *__restrict__ vals,
     const uint32_t *__restrict__ useg, const uint32_t *__restrict__ cflag,
     const uint32_t *__restrict__ cord, const uint32_t *__restrict__ colhead,
-    const uint32_t *__restrict__ istart, const uint32_t *__restrict__ nitems,
-    const int32_t *__restrict__ prefix, int CH, uint8_t *__restrict__ l2, MeshStats *st) {
+    const uint32_t *__restrict__ istart, const uint32_t *__restrict__ nitems, int per_warp) {
   extern __shared__ uint32_t sm[];
   const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+  uint32_t *base = sm + (size_t)warp * per_warp;
+  const int64_t NI = (int64_t)*nitems;
+  for (;;) {
+  // ---- pull the next chunk item from the queue (one ticket per warp)
+  uint32_t tk = 0;
+  if (lane == 0) tk = atomicAdd(&bd.queue[1], 1u);
+  const int64_t it = (int64_t)__shfl_sync(FULL, tk, 0);
+  if (it >= NI) return;
+  const uint32_t ua = istart[it];
+  const MeshDesc &d = bd.md[mesh_of_u(bd.md, bd.nmesh, ua)];
+  const GridDev &g = d.g;
+  const float4 *__restrict__ ptri = d.ptri;
+  const float4 *__restrict__ fbox = d.fbox;
+  const int CH = d.ch;
   const int n2x = g.n2[0], n2y = g.n2[1], n2z = g.n2[2];
   const int cells = n2x * n2y * n2z;
   const int W = (cells + 31) >> 5;
   const int ncol2 = n2x * n2y;
   const int FW = (ncol2 + 31) >> 5;
-  const int per_warp = 2 * CH * W + CH * FW + CH + FW + (int)(sizeof(WarpScratch) / 4);
-  uint32_t *base = sm + (size_t)warp * per_warp;
   uint32_t *sat = base;
   uint32_t *par = sat + CH * W;
   uint32_t *ft = par + CH * W;
@@ -188,9 +213,6 @@ __global__ void __launch_bounds__(kWarps * 32) k_level2c(
   uint32_t *ftacc = (uint32_t *)(kz + CH);
   WarpScratch &ws = *reinterpret_cast<WarpScratch *>(ftacc + FW);
 
-  const int64_t it = (int64_t)blockIdx.x * kWarps + warp;
-  if (it >= (int64_t)*nitems) return;
-  const uint32_t ua = istart[it];
   const uint32_t ucol_end = colhead[cord[ua] + cflag[ua]];  // first voxel of the next column
   const int m = (int)min((uint32_t)CH, ucol_end - ua);
   for (int w = lane; w < 2 * CH * W + CH * FW; w += 32) sat[w] = 0;
@@ -364,7 +386,7 @@ __global__ void __launch_bounds__(kWarps * 32) k_level2c(
     for (int w = lane; w < FW; w += 32) ftacc[w] ^= ft[jv * FW + w];
     __syncwarp();
     const int64_t vlin = ((int64_t)kz[jv] * ny + cj) * nx + ci;
-    uint8_t *out = l2 + (size_t)prefix[vlin] * cells;
+    uint8_t *out = d.l2 + (size_t)d.prefix[vlin] * cells;
     const uint32_t *satj = sat + jv * W, *parj = par + jv * W;
     for (int c4 = lane * 4; c4 < cells; c4 += 128) {
       uint32_t word = 0;
@@ -391,10 +413,12 @@ __global__ void __launch_bounds__(kWarps * 32) k_level2c(
   nbd = warp_sum(nbd);
   nun = warp_sum(nun);
   if (lane == 0) {
-    if (nin) atomicAdd(&st->l2_inside, nin);
-    if (nbd) atomicAdd(&st->l2_boundary, nbd);
-    if (nun) atomicAdd(&st->ray2, (unsigned long long)nun * (unsigned long long)cells);
+    if (nin) atomicAdd(&d.stats->l2_inside, nin);
+    if (nbd) atomicAdd(&d.stats->l2_boundary, nbd);
+    if (nun) atomicAdd(&d.stats->ray2, (unsigned long long)nun * (unsigned long long)cells);
   }
+  __syncwarp();
+  }  // next item
 }
 
 }  // namespace
@@ -405,45 +429,48 @@ int level2_chunk(const GridDev &g) {
   return std::max(1, std::min(32, kMaskWords / W));
 }
 
-size_t level2_smem(const GridDev &g) {
+// Shared-memory words one warp needs for a mesh with this grid.
+int level2_warp_words(const GridDev &g) {
   const int cells = g.n2[0] * g.n2[1] * g.n2[2];
   const int W = (cells + 31) >> 5;
   const int FW = (g.n2[0] * g.n2[1] + 31) >> 5;
   const int CH = level2_chunk(g);
-  const size_t per_warp = 2 * CH * W + CH * FW + CH + FW + sizeof(WarpScratch) / 4;
-  return per_warp * 4 * kWarps;
+  return 2 * CH * W + CH * FW + CH + FW + (int)(sizeof(WarpScratch) / 4);
 }
 
-// Builds the chunk items from the sorted pair lists and runs the Level2 kernel.
-// tmp must hold 6*B + 2 words plus the scan temporaries (level2_temp_words).
+size_t level2_smem_bytes(int warp_words) { return (size_t)warp_words * 4 * kWarps; }
+
 int64_t level2_temp_words(int64_t B) { return 6 * B + 8 + scan_temp_words(B); }
 
-void launch_level2c(const GridDev &g, const float4 *ptri, const float4 *fbox,
-                    const uint32_t *keys, const uint32_t *vals, const uint32_t *useg,
-                    const int32_t *prefix, int64_t B, uint32_t *tmp, uint8_t *l2, MeshStats *st,
-                    cudaStream_t s) {
+// Builds the chunk items from the sorted pair lists and runs the persistent Level2 kernel.
+void launch_level2(const BatchDev &bd, const uint32_t *keys, const uint32_t *vals,
+                   const uint32_t *useg, int64_t B, uint32_t *tmp, int warp_words, int num_sms,
+                   cudaStream_t s) {
   if (B <= 0) return;
   uint32_t *cflag = tmp, *cord = cflag + B, *colhead = cord + B, *iflag = colhead + B + 1,
            *iord = iflag + B, *istart = iord + B, *nitems = istart + B + 1,
            *stmp = nitems + 4;
   const unsigned nb = (unsigned)((B + 255) / 256);
-  const int CH = level2_chunk(g);
-  k_colflags<<<nb, 256, 0, s>>>(keys, useg, B, (uint32_t)g.n[2], cflag);
+  k_colflags<<<nb, 256, 0, s>>>(bd, keys, useg, B, cflag);
   scan_u32(cflag, cord, B, nullptr, stmp, s);
   k_colheads<<<nb, 256, 0, s>>>(cflag, cord, B, colhead);
-  k_itemflags<<<nb, 256, 0, s>>>(cflag, cord, colhead, B, CH, iflag);
+  k_itemflags<<<nb, 256, 0, s>>>(bd, cflag, cord, colhead, B, iflag);
   scan_u32(iflag, iord, B, nullptr, stmp, s);
   k_itemstarts<<<nb, 256, 0, s>>>(iflag, iord, B, istart, nitems);
   count_launch(4);
-  const size_t smem = level2_smem(g);
+  const size_t smem = level2_smem_bytes(warp_words);
   static bool attr_set = false;
   if (!attr_set) {
     cudaFuncSetAttribute(k_level2c, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
     attr_set = true;
   }
-  const unsigned nblk = (unsigned)((B + kWarps - 1) / kWarps);  // items <= B
-  k_level2c<<<nblk, kWarps * 32, smem, s>>>(g, ptri, fbox, keys, vals, useg, cflag, cord, colhead,
-                                            istart, nitems, prefix, CH, l2, st);
+  int per_sm = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_level2c, kWarps * 32, smem);
+  per_sm = std::max(per_sm, 1);
+  const int64_t grid = std::min<int64_t>((B + kWarps - 1) / kWarps, (int64_t)num_sms * per_sm);
+  cudaMemsetAsync(bd.queue + 1, 0, sizeof(uint32_t), s);
+  k_level2c<<<(unsigned)grid, kWarps * 32, smem, s>>>(bd, keys, vals, useg, cflag, cord, colhead,
+                                                      istart, nitems, warp_words);
   count_launch();
 }
 

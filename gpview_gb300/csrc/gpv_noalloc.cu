@@ -45,7 +45,9 @@ void set_err(const char *msg) {
 // Variant of the Level1 kernel without the (voxel, triangle) records: one thread per triangle
 // runs its SAT candidate box (boundary bits) and its fill columns (parity toggles).  Inputs are
 // the packed triangles written by the prep kernel.
-__global__ void k_level1_nopairs(GridDev g, Level1Bufs b) {
+__global__ void k_level1_nopairs(const MeshDesc *__restrict__ md) {
+  const MeshDesc &b = *md;
+  const GridDev &g = b.g;
   const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= b.T) return;
   const float4 a0 = b.ptri[3 * t], a1 = b.ptri[3 * t + 1], a2 = b.ptri[3 * t + 2];
@@ -164,6 +166,7 @@ extern "C" int gpv_voxelize_level1_noalloc(const float *d_tris, int64_t num_tria
   const size_t o_sc = take(4 * (size_t)scan_temp_words(N1w));
   const size_t o_st = take(sizeof(MeshStats));
   const size_t o_tot = take(16);
+  const size_t o_md = take(sizeof(MeshDesc));
   if (o > kScratchBytes) {
     char msg[160];
     std::snprintf(msg, sizeof(msg),
@@ -196,45 +199,62 @@ extern "C" int gpv_voxelize_level1_noalloc(const float *d_tris, int64_t num_tria
 
   float *d_tab = reinterpret_cast<float *>(base + o_tab);
   for (int a = 0, oo = 0; a < 3; ++a) { g.c1[a] = d_tab + oo; oo += g.n[a]; }
-  Level1Bufs b{};
-  b.tris = d_tris;
-  b.T = T;
-  b.ptri = reinterpret_cast<float4 *>(base + o_ptri);
-  b.rng = reinterpret_cast<int4 *>(base + o_rng);
-  b.fbox = reinterpret_cast<float4 *>(base + o_fbox);
-  b.bplane = reinterpret_cast<uint32_t *>(base + o_bp);
-  b.iplane = reinterpret_cast<uint32_t *>(base + o_ip);
-  b.toggles = reinterpret_cast<uint32_t *>(base + o_tg);
-  b.stats = reinterpret_cast<MeshStats *>(base + o_st);
+  MeshDesc md;
+  std::memset(&md, 0, sizeof(md));
+  md.g = g;
+  md.tris = d_tris;
+  md.T = T;
+  md.ptri = reinterpret_cast<float4 *>(base + o_ptri);
+  md.rng = reinterpret_cast<int4 *>(base + o_rng);
+  md.fbox = reinterpret_cast<float4 *>(base + o_fbox);
+  md.bplane = reinterpret_cast<uint32_t *>(base + o_bp);
+  md.iplane = reinterpret_cast<uint32_t *>(base + o_ip);
+  md.toggles = reinterpret_cast<uint32_t *>(base + o_tg);
+  md.stats = reinterpret_cast<MeshStats *>(base + o_st);
+  md.l1 = d_level1_inout;
+  md.prefix = d_level1_prefix;
+  md.bindex = d_boundary_index;
+  MeshDesc *d_md = reinterpret_cast<MeshDesc *>(base + o_md);
   uint32_t *wcnt = reinterpret_cast<uint32_t *>(base + o_wc);
   uint32_t *wpre = reinterpret_cast<uint32_t *>(base + o_wp);
   uint32_t *stmp = reinterpret_cast<uint32_t *>(base + o_sc);
   uint32_t *d_tot = reinterpret_cast<uint32_t *>(base + o_tot);
+  BatchDev bd;
+  std::memset(&bd, 0, sizeof(bd));
+  bd.md = d_md;
+  bd.nmesh = 1;
+  bd.tile = 128;
+  bd.total_tris = T;
+  bd.total_fwarps = (int64_t)g.n[1] * g.nxw;
+  bd.total_rows = (int64_t)g.n[2] * g.n[1];
+  bd.total_words = N1w;
 
-  // The array keeps the last call's data: clear everything that must start at zero.
+  // The array keeps the last call's data: clear everything that must start at zero.  The
+  // descriptor and the tables are copied from this function's stack (pageable memory: the copy
+  // has been staged by the time cudaMemcpyAsync returns).
   cudaError_t e = cudaMemcpyAsync(d_tab, tab, sizeof(float) * ntab, cudaMemcpyHostToDevice, stream);
-  if (e == cudaSuccess) e = cudaMemsetAsync(b.stats, 0, sizeof(MeshStats), stream);
-  if (e == cudaSuccess) e = cudaMemsetAsync(b.bplane, 0, 4 * (size_t)N1w, stream);
-  if (e == cudaSuccess) e = cudaMemsetAsync(b.toggles, 0, 4 * (size_t)(ncol * g.nzw), stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(d_md, &md, sizeof(md), cudaMemcpyHostToDevice, stream);
+  if (e == cudaSuccess) e = cudaMemsetAsync(md.stats, 0, sizeof(MeshStats), stream);
+  if (e == cudaSuccess) e = cudaMemsetAsync(md.bplane, 0, 4 * (size_t)N1w, stream);
+  if (e == cudaSuccess) e = cudaMemsetAsync(md.toggles, 0, 4 * (size_t)(ncol * g.nzw), stream);
   if (e != cudaSuccess) {
     set_err(cudaGetErrorString(e));
     return GPV_ERR_CUDA;
   }
-  launch_prep(g, b, stream);
+  launch_prep(bd, stream);
   if (T > 0) {
-    k_level1_nopairs<<<(unsigned)((T + 127) / 128), 128, 0, stream>>>(g, b);
+    k_level1_nopairs<<<(unsigned)((T + 127) / 128), 128, 0, stream>>>(d_md);
     count_launch();
   }
-  launch_fill_finish(g, b, stream);
-  launch_popc(g, b.bplane, wcnt, stream);
+  launch_fill_finish(bd, stream);
+  launch_popc(md.bplane, N1w, wcnt, stream);
   scan_u32(wcnt, wpre, N1w, d_tot, stmp, stream);
-  launch_expand(g, b.bplane, b.iplane, wpre, d_level1_inout, d_level1_prefix, d_boundary_index,
-                b.stats, stream);
+  launch_expand(bd, wpre, stream);
   uint32_t nb = 0;
   MeshStats hs;
   e = cudaGetLastError();
   if (e == cudaSuccess) e = cudaMemcpyAsync(&nb, d_tot, sizeof(nb), cudaMemcpyDeviceToHost, stream);
-  if (e == cudaSuccess) e = cudaMemcpyAsync(&hs, b.stats, sizeof(hs), cudaMemcpyDeviceToHost, stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&hs, md.stats, sizeof(hs), cudaMemcpyDeviceToHost, stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
   if (e != cudaSuccess) {
     set_err(cudaGetErrorString(e));

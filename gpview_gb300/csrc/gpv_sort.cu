@@ -6,6 +6,7 @@
 // sort_pairs: stable LSD radix sort of (u32 key, u32 value), 8-bit digits; per pass a tile
 //             histogram, a scan of the digit-major histogram, and a stable scatter whose
 //             in-tile ranks come from __match_any_sync peer masks.
+#include <algorithm>
 #include <atomic>
 
 #include "gpv_internal.h"
@@ -171,6 +172,85 @@ __global__ void k_radix_scatter(const uint32_t *__restrict__ keys, const uint32_
   }
 }
 
+// ---- segmented variant: one block per SortTile (mesh m, tile j of that mesh) -----------------
+// hist layout per mesh m: [256 digits][ntiles_m tiles] starting at 256 * tile_base[m], so one
+// exclusive scan over the whole array yields dense, mesh-major output positions.
+__device__ __forceinline__ int64_t seg_in_base(const MeshDesc &d, bool emit) {
+  return emit ? d.emit_base : d.pair_base;
+}
+
+__global__ void k_radix_hist_seg(const MeshDesc *__restrict__ md, const SortTile *__restrict__ tiles,
+                                 const int64_t *__restrict__ tb, const uint32_t *__restrict__ keys,
+                                 bool emit, int shift, uint32_t *__restrict__ hist) {
+  __shared__ uint32_t s_h[256];
+  s_h[threadIdx.x] = 0;
+  __syncthreads();
+  const SortTile st = tiles[blockIdx.x];
+  const int64_t in0 = seg_in_base(md[st.mesh], emit) + (int64_t)st.j * kSortTile;
+  for (int r = 0; r < kSortRounds; ++r) {
+    const int i = r * kSortThreads + threadIdx.x;
+    if (i < st.count) atomicAdd(&s_h[(keys[in0 + i] >> shift) & 255u], 1u);
+  }
+  __syncthreads();
+  const int64_t nt_m = tb[st.mesh + 1] - tb[st.mesh];
+  hist[256 * tb[st.mesh] + (int64_t)threadIdx.x * nt_m + st.j] = s_h[threadIdx.x];
+}
+
+__global__ void k_radix_scatter_seg(const MeshDesc *__restrict__ md,
+                                    const SortTile *__restrict__ tiles,
+                                    const int64_t *__restrict__ tb, const uint32_t *__restrict__ keys,
+                                    const uint32_t *__restrict__ vals, bool emit, int shift,
+                                    const uint32_t *__restrict__ hoff, uint32_t *__restrict__ kout,
+                                    uint32_t *__restrict__ vout) {
+  __shared__ uint32_t s_off[256];
+  __shared__ uint32_t s_run[256];
+  __shared__ uint16_t s_w[kSortThreads / 32][256];
+  const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+  const SortTile st = tiles[blockIdx.x];
+  const int64_t nt_m = tb[st.mesh + 1] - tb[st.mesh];
+  s_off[threadIdx.x] = hoff[256 * tb[st.mesh] + (int64_t)threadIdx.x * nt_m + st.j];
+  s_run[threadIdx.x] = 0;
+  const int64_t in0 = seg_in_base(md[st.mesh], emit) + (int64_t)st.j * kSortTile;
+  const unsigned lt_mask = (1u << lane) - 1u;
+  for (int r = 0; r < kSortRounds; ++r) {
+    if (r * kSortThreads >= st.count) break;  // block-uniform
+#pragma unroll
+    for (int w = 0; w < kSortThreads / 32; ++w) s_w[w][threadIdx.x] = 0;
+    __syncthreads();
+    const int i = r * kSortThreads + threadIdx.x;
+    const bool valid = i < st.count;
+    uint32_t key = 0, val = 0, digit = 256u;
+    if (valid) {
+      key = keys[in0 + i];
+      val = vals[in0 + i];
+      digit = (key >> shift) & 255u;
+    }
+    const unsigned peers = __match_any_sync(0xffffffffu, digit);
+    const unsigned rank = __popc(peers & lt_mask);
+    if (valid && rank == 0) s_w[warp][digit] = (uint16_t)__popc(peers);
+    __syncthreads();
+    uint32_t acc = 0;
+    {
+      const unsigned d = threadIdx.x;
+#pragma unroll
+      for (int w = 0; w < kSortThreads / 32; ++w) {
+        uint32_t c = s_w[w][d];
+        s_w[w][d] = (uint16_t)acc;
+        acc += c;
+      }
+    }
+    __syncthreads();
+    if (valid) {
+      const uint32_t pos = s_off[digit] + s_run[digit] + s_w[warp][digit] + rank;
+      kout[pos] = key;
+      vout[pos] = val;
+    }
+    __syncthreads();
+    s_run[threadIdx.x] += acc;
+    __syncthreads();
+  }
+}
+
 }  // namespace
 
 namespace {
@@ -217,6 +297,43 @@ bool sort_pairs(uint32_t *keys, uint32_t *vals, uint32_t *kalt, uint32_t *valt, 
     k_radix_hist<<<(unsigned)nb, kSortThreads, 0, s>>>(ki, n, shift, hist, nb);
     scan_u32(hist, hoff, 256 * nb, nullptr, stmp, s);
     k_radix_scatter<<<(unsigned)nb, kSortThreads, 0, s>>>(ki, vi, n, shift, hoff, nb, ko, vo);
+    count_launch(2);
+    alt = !alt;
+  }
+  return alt;
+}
+
+}  // namespace gpv
+
+namespace gpv {
+
+int64_t sort_seg_temp_words(int64_t ntiles) {
+  return 2 * 256 * ntiles + scan_temp_words(256 * ntiles) + 4;
+}
+
+bool sort_pairs_seg(const BatchDev &bd, const SortTile *tiles, const int64_t *tile_base_dev,
+                    int64_t ntiles, uint32_t *keys, uint32_t *vals, uint32_t *kalt, uint32_t *valt,
+                    int64_t Ptotal, int key_bits, uint32_t *temp, cudaStream_t s) {
+  static_assert(kSortTileItems == kSortTile, "tile size mismatch");
+  if (Ptotal <= 0 || ntiles <= 0) return false;
+  uint32_t *hist = temp;
+  uint32_t *hoff = temp + 256 * ntiles;
+  uint32_t *stmp = temp + 2 * 256 * ntiles;
+  // Pass 0 always runs (it also moves the pairs from the emission segments to the dense
+  // layout), so the result lands in (kalt, valt) after an odd number of passes.
+  const int passes = std::max(1, (key_bits + 7) / 8);
+  bool alt = false;
+  for (int ps = 0; ps < passes; ++ps) {
+    const uint32_t *ki = alt ? kalt : keys;
+    const uint32_t *vi = alt ? valt : vals;
+    uint32_t *ko = alt ? keys : kalt;
+    uint32_t *vo = alt ? vals : valt;
+    const bool emit = ps == 0;
+    k_radix_hist_seg<<<(unsigned)ntiles, kSortThreads, 0, s>>>(bd.md, tiles, tile_base_dev, ki,
+                                                                emit, 8 * ps, hist);
+    scan_u32(hist, hoff, 256 * ntiles, nullptr, stmp, s);
+    k_radix_scatter_seg<<<(unsigned)ntiles, kSortThreads, 0, s>>>(
+        bd.md, tiles, tile_base_dev, ki, vi, emit, 8 * ps, hoff, ko, vo);
     count_launch(2);
     alt = !alt;
   }

@@ -56,6 +56,7 @@ def _load(ref=False):
     L.orc_tri_ray.argtypes = [vp, vp, vp, vp, vp, C.POINTER(C.c_float)]
     L.orc_tri_ray_z.argtypes = [vp, vp]
     L.orc_grid_tables.argtypes = [C.POINTER(Spec), vp, vp, vp, vp, vp, vp, vp]
+    L.orc_reference_divisions.argtypes = [vp, vp, C.c_float, C.c_int, vp]
     _libs[ref] = L
     return L
 
@@ -155,6 +156,21 @@ def tri_ray(v1, v2, v3, o, d, ref=False):
     t = C.c_float(0.0)
     hit = int(L.orc_tri_ray(*[_p(x) for x in a], C.byref(t)))
     return hit, float(t.value)
+
+
+def tri_ray_z(tv, o, ref=False):
+    """The +z test through the column/t split used by the fill (D = (0,0,1))."""
+    L = _load(ref)
+    tv = np.ascontiguousarray(tv, np.float32); o = np.ascontiguousarray(o, np.float32)
+    return int(L.orc_tri_ray_z(_p(tv), _p(o)))
+
+
+def reference_divisions(bmin, bmax, max_model_size, voxel_count):
+    L = _load(False)
+    out = (C.c_int32 * 3)()
+    L.orc_reference_divisions((C.c_float * 3)(*bmin), (C.c_float * 3)(*bmax),
+                              C.c_float(max_model_size), int(voxel_count), out)
+    return tuple(out)
 
 
 def grid_tables(grid):
