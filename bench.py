@@ -41,6 +41,8 @@ def parse():
     p.add_argument("--tile", type=int, default=0)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--cpu-seconds", type=float, default=15.0)
+    p.add_argument("--batch", type=int, default=4096, help="meshes of the batched workload (0: skip)")
+    p.add_argument("--batch-reps", type=int, default=3)
     return p.parse_args()
 
 
@@ -141,6 +143,65 @@ def cpu_baseline(tris, spec, work_total, seconds, threads):
             "sample": f"Level1 in full + Level2 on {done}/{B} boundary voxels, extrapolated "
                       f"({t_l1 + t_l2:.1f} s of CPU work, est. {t_full:.2f} s per mesh)",
             "sec_per_mesh": t_full}
+
+
+def batch_bench(gpv, ctx, torch, stream, local, args):
+    """The 4096-mesh mixed workload: plain one-mesh-per-launch path vs the batched path."""
+    import numpy as np
+
+    import workloads as W
+
+    t0 = time.perf_counter()
+    meshes = W.batch4096(args.batch)
+    gen_s = time.perf_counter() - t0
+    counts = [t.size // 9 for t, _ in meshes]
+    specs = [s for _, s in meshes]
+    offs, o = [], 0
+    for c in counts:
+        offs.append(o)
+        o += (c * 9 + 3) // 4 * 4  # keep every mesh 16-byte aligned
+    host = np.zeros(max(o, 4), np.float32)
+    for (t, _), off in zip(meshes, offs):
+        host[off:off + t.size] = t
+    dev = torch.from_numpy(host).to(f"cuda:{local}")
+    ptrs = [dev.data_ptr() + 4 * off for off in offs]
+    sp = stream.cuda_stream
+    with torch.cuda.stream(stream):
+        # autotuner on a sample of the batch
+        ns = min(256, len(ptrs))
+        tile, chunk, tune_ms = ctx.autotune(ptrs[:ns], counts[:ns], specs[:ns], sp)
+        # plain path: one voxelization (full launch sequence, host syncs) per mesh
+        torch.cuda.synchronize()
+        tp = time.perf_counter()
+        work = 0
+        for p_, c, s_ in zip(ptrs, counts, specs):
+            r = ctx.voxelize_device(p_, c, s_, sp)
+            work += r.work.total()
+            ctx.release(r)
+        torch.cuda.synchronize()
+        plain_s = time.perf_counter() - tp
+        # batched path
+        times = []
+        for k in range(args.batch_reps + 1):
+            torch.cuda.synchronize()
+            tb = time.perf_counter()
+            res = ctx.voxelize_batch(ptrs, counts, specs, sp)
+            torch.cuda.synchronize()
+            dt = time.perf_counter() - tb
+            bwork = sum(r.work.total() for r in res)
+            for r in res:
+                ctx.release(r)
+            if k > 0:
+                times.append(dt)
+    batch_s = sum(times) / len(times)
+    assert bwork == work, (bwork, work)
+    n = len(meshes)
+    return {"workload": "batch4096", "meshes": n, "triangles": int(sum(counts)),
+            "desc": "sphere/noisy torus/superellipsoid, T log-uniform 500-200000, Level1 {32..128}^3, Level2 {2,4,8}^3",
+            "tile": tile, "level2_chunk": chunk, "autotune_sample_ms": tune_ms,
+            "plain_meshes_per_s": n / plain_s, "batched_meshes_per_s": n / batch_s,
+            "batched_vs_plain": plain_s / batch_s, "batched_tests_per_s": work / batch_s,
+            "plain_s": plain_s, "batched_s": batch_s, "generate_s": gen_s}
 
 
 def run_reference(args):
@@ -335,6 +396,8 @@ def main():
             "e2e": {"value": e2e_value, "unit": "tests/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h, "ms_per_step": e2e_t * 1e3 / args.steps},
             "gpu_launches": launches, "roofline": roof, "clocks": clk}
+    if args.batch > 0:
+        line["batched"] = batch_bench(gpv, ctx, torch, stream, local, args)
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(tris, spec, tests_per_step, args.cpu_seconds,
                                             os.cpu_count() or 1)

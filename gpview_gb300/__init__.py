@@ -107,6 +107,10 @@ def lib():
                                               C.c_void_p, C.c_void_p, C.c_void_p,
                                               C.POINTER(C.c_int64), C.c_void_p]
     L.gpv_noalloc_last_error.restype = C.c_char_p
+    L.gpv_set_level2_chunk.argtypes = [C.c_void_p, C.c_int]
+    L.gpv_autotune.argtypes = [C.c_void_p, C.c_int32, C.POINTER(C.c_void_p), C.POINTER(C.c_int64),
+                               C.POINTER(GridSpec), C.c_void_p, C.POINTER(C.c_int32),
+                               C.POINTER(C.c_int32), C.POINTER(C.c_float)]
     if hasattr(L, "gpv_voxelize_batch"):
         L.gpv_voxelize_batch.argtypes = [C.c_void_p, C.c_int32, C.POINTER(C.c_void_p),
                                          C.POINTER(C.c_int64), C.POINTER(GridSpec),
@@ -258,6 +262,17 @@ class Context:
         self._check(lib().gpv_voxelize_batch(self._h, n, ptrs, cnts, sp, res, C.c_void_p(stream)),
                     "gpv_voxelize_batch")
         return list(res)
+
+    def autotune(self, d_ptrs, counts, specs, stream=0):
+        """Picks the (Level1 tile, Level2 chunk) pair that runs this sample batch fastest."""
+        n = len(d_ptrs)
+        ptrs = (C.c_void_p * n)(*[C.c_void_p(p) for p in d_ptrs])
+        cnts = (C.c_int64 * n)(*[int(c) for c in counts])
+        sp = (GridSpec * n)(*specs)
+        t, ch, ms = C.c_int32(), C.c_int32(), C.c_float()
+        self._check(lib().gpv_autotune(self._h, n, ptrs, cnts, sp, C.c_void_p(stream), C.byref(t),
+                                       C.byref(ch), C.byref(ms)), "gpv_autotune")
+        return t.value, ch.value, ms.value
 
     def fetch(self, res, stream=0):
         """Copies a result to host numpy arrays: (level1 u8, prefix i32, boundary i32, level2 u8)."""

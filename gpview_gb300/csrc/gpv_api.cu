@@ -197,6 +197,24 @@ int gpv_stage_times(gpv_ctx *ctx, double *ms, int n) {
 
 uint64_t gpv_kernel_launches(void) { return gpv::launch_count(); }
 
+int gpv_set_level2_chunk(gpv_ctx *ctx, int cap) {
+  if (!ctx || cap < 1 || cap > 32) return GPV_ERR_INVALID;
+  ctx->l2_chunk_cap = cap;
+  return GPV_OK;
+}
+
+int gpv_autotune(gpv_ctx *ctx, int32_t n, const float *const *d_tris, const int64_t *num_triangles,
+                 const gpv_grid_spec *specs, cudaStream_t stream, int32_t *tile,
+                 int32_t *level2_chunk, float *ms_per_batch) {
+  if (!ctx || n <= 0 || !d_tris || !num_triangles || !specs) return GPV_ERR_INVALID;
+  cudaSetDevice(ctx->device);
+  int t = 0, c = 0;
+  const int rc = autotune(ctx, n, d_tris, num_triangles, specs, stream, 2, &t, &c, ms_per_batch);
+  if (tile) *tile = t;
+  if (level2_chunk) *level2_chunk = c;
+  return rc;
+}
+
 int gpv_set_tile(gpv_ctx *ctx, int t) {
   if (!ctx || (t != 32 && t != 64 && t != 128 && t != 256)) return GPV_ERR_INVALID;
   ctx->tile = t;

@@ -142,8 +142,8 @@ int run_batch(gpv_ctx *ctx, int n, const float *const *d_tris, const int64_t *T,
     d.stats = stats + m;
     d.l1 = static_cast<uint8_t *>(set->l1) + res_l1[m];
     d.prefix = static_cast<int32_t *>(set->prefix) + res_pre[m];
-    d.ch = g.level2 ? level2_chunk(d.g) : 1;
-    if (g.level2) warp_words = std::max(warp_words, level2_warp_words(d.g));
+    d.ch = g.level2 ? level2_chunk(d.g, ctx->l2_chunk_cap) : 1;
+    if (g.level2) warp_words = std::max(warp_words, level2_warp_words(d.g, ctx->l2_chunk_cap));
   }
   BatchDev bd;
   bd.md = d_md;
@@ -207,14 +207,18 @@ int run_batch(gpv_ctx *ctx, int n, const float *const *d_tris, const int64_t *T,
   CK(cudaGetLastError());
   CK(cudaMemcpyAsync(ctx->h_stats, stats, n * sizeof(MeshStats), cudaMemcpyDeviceToHost, s));
   CK(cudaStreamSynchronize(s));
-  int64_t P = 0, Btot = 0, l2bytes = 0;
+  int64_t Btot = 0, l2bytes = 0, P2 = 0, ub = 0;
   std::vector<int64_t> l2off(n + 1, 0), boff(n + 1, 0);
   for (int m = 0; m < n; ++m) {
     const MeshStats &st = ctx->h_stats[m];
     if (st.status) return fail_all(GPV_ERR_DEVICE, "device status raised in Level1");
-    md[m].pair_base = P;
-    md[m].u_base = Btot;
-    P += (int64_t)st.pairs;
+    // dense pair / boundary-voxel bases over the meshes with a Level2 stage (only they are sorted)
+    md[m].pair_base = P2;
+    md[m].u_base = ub;
+    if (gh[m].level2) {
+      P2 += (int64_t)st.pairs;
+      ub += (int64_t)st.boundary;
+    }
     Btot += (int64_t)st.boundary;
     boff[m + 1] = Btot;
     l2off[m + 1] = l2off[m] + (gh[m].level2 ? (int64_t)st.boundary * gh[m].cells : 0);
@@ -244,21 +248,7 @@ int run_batch(gpv_ctx *ctx, int n, const float *const *d_tris, const int64_t *T,
   launch_expand(bd, wpre, s);
   mark(6);
   const int64_t ntiles = (int64_t)st_host.size();
-  // pairs of meshes without Level2 are not sorted; the dense layout then only holds Level2 meshes
-  int64_t P2 = 0;
   if (any_l2 && ntiles > 0) {
-    // dense bases over the meshes that are sorted
-    for (int m = 0; m < n; ++m) {
-      md[m].pair_base = P2;
-      if (gh[m].level2) P2 += (int64_t)ctx->h_stats[m].pairs;
-    }
-    // boundary-voxel bases must follow the same set of meshes for the Level2 items
-    int64_t ub = 0;
-    for (int m = 0; m < n; ++m) {
-      md[m].u_base = ub;
-      if (gh[m].level2) ub += (int64_t)ctx->h_stats[m].boundary;
-    }
-    std::memcpy(ctx->h_md, md.data(), n * sizeof(MeshDesc));
     CK(ctx_ensure_host_tiles(ctx, (size_t)ntiles, (size_t)n + 1));
     std::memcpy(ctx->h_tiles, st_host.data(), ntiles * sizeof(SortTile));
     std::memcpy(ctx->h_tb, stb.data(), (n + 1) * sizeof(int64_t));
@@ -274,7 +264,6 @@ int run_batch(gpv_ctx *ctx, int n, const float *const *d_tris, const int64_t *T,
     CK(ws.get(&useg, (size_t)ub + 1));
     CK(ws.get(&sortmp, (size_t)std::max(sort_seg_temp_words(ntiles), scan_temp_words(P2))));
     CK(ws.get(&l2tmp, (size_t)level2_temp_words(ub)));
-    CK(cudaMemcpyAsync(d_md, ctx->h_md, n * sizeof(MeshDesc), cudaMemcpyHostToDevice, s));
     CK(cudaMemcpyAsync(d_tiles, ctx->h_tiles, ntiles * sizeof(SortTile), cudaMemcpyHostToDevice, s));
     CK(cudaMemcpyAsync(d_tb, ctx->h_tb, (n + 1) * sizeof(int64_t), cudaMemcpyHostToDevice, s));
     const bool in_alt = sort_pairs_seg(bd, d_tiles, d_tb, ntiles, keys, vals, kalt, valt, P2,
@@ -307,9 +296,6 @@ int run_batch(gpv_ctx *ctx, int n, const float *const *d_tris, const int64_t *T,
   for (int m = 0; m < n; ++m)
     if (ctx->h_stats[m].status) return fail_all(GPV_ERR_DEVICE, "device status raised in Level2");
   if (any_l2 && ntiles > 0) {
-    int64_t ub = 0;
-    for (int m = 0; m < n; ++m)
-      if (gh[m].level2) ub += (int64_t)ctx->h_stats[m].boundary;
     if ((int64_t)ctx->h_u32[1] != ub)
       return fail_all(GPV_ERR_DEVICE, "boundary plane and pair lists disagree");
   }
@@ -344,6 +330,57 @@ int run_batch(gpv_ctx *ctx, int n, const float *const *d_tris, const int64_t *T,
   }
   return GPV_OK;
 #undef CK
+}
+
+}  // namespace gpv
+
+namespace gpv {
+
+// Grid search over (Level1 tile, Level2 chunk cap) on a sample batch; each candidate runs once
+// to warm up and `reps` times timed with CUDA events on the stream.  The fastest pair is kept.
+int autotune(gpv_ctx *ctx, int n, const float *const *d_tris, const int64_t *T,
+             const gpv_grid_spec *specs, cudaStream_t s, int reps, int *best_tile,
+             int *best_chunk, float *best_ms) {
+  static const int tiles[] = {32, 64, 128, 256};
+  static const int chunks[] = {4, 8, 16, 32};
+  std::vector<gpv_result> res(n);
+  cudaEvent_t e0, e1;
+  if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess)
+    return ctx_fail(ctx, GPV_ERR_CUDA, "event creation failed");
+  float best = 1e30f;
+  int bt = ctx->tile, bc = ctx->l2_chunk_cap;
+  int rc = GPV_OK;
+  for (int ti : tiles)
+    for (int ch : chunks) {
+      ctx->tile = ti;
+      ctx->l2_chunk_cap = ch;
+      float total = 0.f;
+      for (int r = 0; r <= reps && rc == GPV_OK; ++r) {
+        cudaEventRecord(e0, s);
+        rc = run_batch(ctx, n, d_tris, T, specs, res.data(), s);
+        cudaEventRecord(e1, s);
+        if (rc != GPV_OK) break;
+        cudaEventSynchronize(e1);
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (r > 0) total += ms;
+        for (int m = 0; m < n; ++m) gpv_result_release(ctx, &res[m]);
+      }
+      if (rc != GPV_OK) break;
+      if (total < best) {
+        best = total;
+        bt = ti;
+        bc = ch;
+      }
+    }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  ctx->tile = bt;
+  ctx->l2_chunk_cap = bc;
+  if (best_tile) *best_tile = bt;
+  if (best_chunk) *best_chunk = bc;
+  if (best_ms) *best_ms = best / std::max(reps, 1);
+  return rc;
 }
 
 }  // namespace gpv

@@ -26,7 +26,8 @@ struct gpv_ctx {
   double stage_ms[kStages] = {};       // accumulated stage durations
   uint64_t stage_calls = 0;
   std::string err;
-  int tile = 128;
+  int tile = 128;                      // Level1 triangles per tile (autotuned)
+  int l2_chunk_cap = 32;               // Level2 boundary voxels per chunk, upper bound (autotuned)
   gpv::MeshStats *h_stats = nullptr;   // pinned, h_cap entries
   gpv::MeshDesc *h_md = nullptr;       // pinned, h_cap entries
   size_t h_cap = 0;
@@ -99,5 +100,8 @@ inline cudaError_t ctx_ensure_host_tiles(gpv_ctx *ctx, size_t ntiles, size_t ntb
 
 int run_batch(gpv_ctx *ctx, int n, const float *const *d_tris, const int64_t *T,
               const gpv_grid_spec *specs, gpv_result *out, cudaStream_t s);
+int autotune(gpv_ctx *ctx, int n, const float *const *d_tris, const int64_t *T,
+             const gpv_grid_spec *specs, cudaStream_t s, int reps, int *best_tile,
+             int *best_chunk, float *best_ms);
 
 }  // namespace gpv

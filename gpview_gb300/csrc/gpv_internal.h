@@ -101,8 +101,8 @@ bool sort_pairs_seg(const BatchDev &bd, const SortTile *tiles, const int64_t *ti
                     int64_t Ptotal, int key_bits, uint32_t *temp, cudaStream_t s);
 constexpr int kSortTileItems = 2048;
 
-int level2_chunk(const GridDev &g);
-int level2_warp_words(const GridDev &g);
+int level2_chunk(const GridDev &g, int cap = 32);
+int level2_warp_words(const GridDev &g, int cap = 32);
 int64_t level2_temp_words(int64_t Btot);
 void launch_level2(const BatchDev &bd, const uint32_t *keys, const uint32_t *vals,
                    const uint32_t *useg, int64_t Btot, uint32_t *tmp, int warp_words, int num_sms,

@@ -423,18 +423,18 @@ __global__ void __launch_bounds__(kWarps * 32) k_level2c(
 
 }  // namespace
 
-int level2_chunk(const GridDev &g) {
+int level2_chunk(const GridDev &g, int cap) {
   const int cells = g.n2[0] * g.n2[1] * g.n2[2];
   const int W = (cells + 31) >> 5;
-  return std::max(1, std::min(32, kMaskWords / W));
+  return std::max(1, std::min(std::min(32, std::max(cap, 1)), kMaskWords / W));
 }
 
 // Shared-memory words one warp needs for a mesh with this grid.
-int level2_warp_words(const GridDev &g) {
+int level2_warp_words(const GridDev &g, int cap) {
   const int cells = g.n2[0] * g.n2[1] * g.n2[2];
   const int W = (cells + 31) >> 5;
   const int FW = (g.n2[0] * g.n2[1] + 31) >> 5;
-  const int CH = level2_chunk(g);
+  const int CH = level2_chunk(g, cap);
   return 2 * CH * W + CH * FW + CH + FW + (int)(sizeof(WarpScratch) / 4);
 }
 

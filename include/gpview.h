@@ -101,8 +101,15 @@ typedef struct {
 int gpv_init(int device, gpv_ctx **out);
 void gpv_destroy(gpv_ctx *ctx);
 const char *gpv_last_error(gpv_ctx *ctx);
-/* Tunables (autotuner output): triangles per Level1 tile (32..256, power of two). */
+/* Tunables (autotuner output): triangles per Level1 tile (32..256, power of two) and the largest
+ * number of boundary voxels of one Level1 column that one Level2 work item takes (1..32). */
 int gpv_set_tile(gpv_ctx *ctx, int tris_per_tile);
+int gpv_set_level2_chunk(gpv_ctx *ctx, int max_voxels);
+/* Autotuner: times every (tile, Level2 chunk) pair of {32,64,128,256} x {4,8,16,32} on the given
+ * sample batch (CUDA events on `stream`), keeps the fastest in the context and reports it. */
+int gpv_autotune(gpv_ctx *ctx, int32_t n, const float *const *d_tris, const int64_t *num_triangles,
+                 const gpv_grid_spec *specs, cudaStream_t stream, int32_t *tile,
+                 int32_t *level2_chunk, float *ms_per_batch);
 /* Per-stage CUDA-event timing on the launching stream (off by default).  Stages:
  * 0 prep, 1 Level1 SAT+fill, 2 fill finish + boundary scan, 3 Level1 expansion,
  * 4 pair sort + lists, 5 Level2.  gpv_stage_times returns the number of timed calls and the

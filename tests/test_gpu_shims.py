@@ -114,11 +114,14 @@ def test_shims_follow_reference(built):
         xcnt[c] = len(lst)
         xflat += lst
     l2b = torch.zeros(B * cells, dtype=torch.float32, device="cuda")
+    # keep every device buffer referenced until the kernel has run
+    txc = torch.from_numpy(xcnt).cuda()
+    txi = torch.from_numpy(xidx).cuda()
+    txf = torch.from_numpy(np.array(xflat or [0], np.int32)).cuda()
     rc = L.CUDAClassifyInOutLevel2(d_tris.data_ptr(), l2b.data_ptr(), tmid.data_ptr(), tl2i.data_ptr(),
-                                   torch.from_numpy(xcnt).cuda().data_ptr(),
-                                   torch.from_numpy(xidx).cuda().data_ptr(),
-                                   torch.from_numpy(np.array(xflat or [0], np.int32)).cuda().data_ptr(),
+                                   txc.data_ptr(), txi.data_ptr(), txf.data_ptr(),
                                    B, I3(*nd), I3(*n2), e1, e2)
+    torch.cuda.synchronize()
     assert rc == 1
     got = l2b.cpu().numpy()
     f32 = np.float32

@@ -33,3 +33,64 @@ def make(cfg, seed=None):
     mn, mx = gpv.mesh_bounds(tris)
     spec = gpv.grid_padded(mn, mx, cfg["level1"], cfg["level2"])
     return tris, spec
+
+
+def batch4096(count=4096, seed=4096, threads=None):
+    """The batched configuration: `count` closed meshes drawn uniformly from {UV-sphere, noisy
+    torus, superellipsoid (e1, e2 ~ U(0.3, 2.0), semi-axes ~ U(0.2, 0.45))}, triangle counts
+    log-uniform in [500, 200000], random rotation and placement inside the unit cube; Level1
+    uniform over {32, 48, 64, 96, 128}^3 and Level2 uniform over {2, 4, 8}^3 (grid = mesh box
+    padded by one cell).  Parameters are drawn in order from one seed; meshes are generated in
+    parallel threads (the generators are C++ and release the GIL)."""
+    import os
+    from concurrent.futures import ThreadPoolExecutor
+
+    rng = np.random.default_rng(seed)
+    params = []
+    for i in range(count):
+        fam = int(rng.integers(0, 3))
+        T = float(np.exp(rng.uniform(np.log(500), np.log(200000))))
+        q, _ = np.linalg.qr(rng.normal(size=(3, 3)))
+        p = dict(i=i, fam=fam, q=q.astype(np.float32), gseed=seed * 7919 + i)
+        if fam == 0:
+            p["nlat"] = max(3, int(round(np.sqrt(T / 4.0))) + 1)
+            p["r"] = float(rng.uniform(0.2, 0.45))
+            p["c"] = rng.uniform(p["r"], 1.0 - p["r"], 3)
+        elif fam == 1:
+            p["nv"] = max(3, int(round(np.sqrt(T / 4.0))))
+            p["R"] = float(rng.uniform(0.2, 0.33))
+            p["rr"] = float(rng.uniform(0.05, min(0.12, p["R"] - 0.02)))
+        else:
+            p["nlat"] = max(3, int(round(np.sqrt(T / 4.0))) + 1)
+            p["semi"] = rng.uniform(0.2, 0.45, 3)
+            p["e"] = rng.uniform(0.3, 2.0, 2)
+        p["place"] = rng.uniform(0, 1, 3)
+        p["n1"] = int(rng.choice([32, 48, 64, 96, 128]))
+        p["n2"] = int(rng.choice([2, 4, 8]))
+        params.append(p)
+
+    def make_one(p):
+        if p["fam"] == 0:
+            t = gpv.gen_uvsphere(p["gseed"], 2 * (p["nlat"] - 1), p["nlat"], p["c"], p["r"], 0.002)
+        elif p["fam"] == 1:
+            t = gpv.gen_torus(p["gseed"], 2 * p["nv"], p["nv"], (0.0, 0.0, 0.0), p["R"], p["rr"], 0.01)
+            t = _place(p["place"], t.reshape(-1, 3) @ p["q"].T)
+        else:
+            t = gpv.gen_superellipsoid(p["gseed"], 2 * (p["nlat"] - 1), p["nlat"], (0.0, 0.0, 0.0),
+                                       p["semi"], p["e"][0], p["e"][1], p["q"])
+            t = _place(p["place"], t.reshape(-1, 3))
+        t = np.ascontiguousarray(t, np.float32).reshape(-1)
+        return t, gpv.grid_padded(*gpv.mesh_bounds(t), p["n1"], p["n2"])
+
+    with ThreadPoolExecutor(max_workers=threads or os.cpu_count() or 4) as ex:
+        return list(ex.map(make_one, params))
+
+
+def _place(u, pts):
+    """Translates points so their box sits at position u (in [0,1]^3 of the free room) inside the
+    unit cube (centred when the box is larger than the cube)."""
+    pts = np.asarray(pts, np.float32)
+    mn, mx = pts.min(0), pts.max(0)
+    size = mx - mn
+    lo = np.where(size < 1.0, np.asarray(u) * np.maximum(1.0 - size, 0), 0.5 - size / 2)
+    return (pts - mn + lo).astype(np.float32)
