@@ -43,6 +43,9 @@ def parse():
     p.add_argument("--cpu-seconds", type=float, default=15.0)
     p.add_argument("--batch", type=int, default=4096, help="meshes of the batched workload (0: skip)")
     p.add_argument("--batch-reps", type=int, default=3)
+    p.add_argument("--serve-seconds", type=float, default=60.0, help="served stream length (0: skip)")
+    p.add_argument("--serve-pool", type=int, default=256)
+    p.add_argument("--serve-rate", type=float, nargs=2, default=(100.0, 5000.0))
     return p.parse_args()
 
 
@@ -202,6 +205,93 @@ def batch_bench(gpv, ctx, torch, stream, local, args):
             "plain_meshes_per_s": n / plain_s, "batched_meshes_per_s": n / batch_s,
             "batched_vs_plain": plain_s / batch_s, "batched_tests_per_s": work / batch_s,
             "plain_s": plain_s, "batched_s": batch_s, "generate_s": gen_s}
+
+
+def served_bench(gpv, torch, local, args, tuned):
+    """Open-loop Poisson stream (rate ramped linearly over the run) against the continuous-
+    batching server with a 150 GB HBM budget; latency = submit to results on the device."""
+    import threading
+    from collections import deque
+
+    import numpy as np
+
+    import workloads as W
+
+    pool = W.served_pool(args.serve_pool)
+    pinned = [torch.from_numpy(t).pin_memory() for t, _ in pool]
+    specs = [s for _, s in pool]
+    D = args.serve_seconds
+    r0, r1 = args.serve_rate
+    rng = np.random.default_rng(77)
+    sched, t = [], 0.0
+    while True:  # thinning of a Poisson process with rate r(t) = r0 + (r1 - r0) t / D
+        t += rng.exponential(1.0 / r1)
+        if t >= D:
+            break
+        if rng.random() < (r0 + (r1 - r0) * t / D) / r1:
+            sched.append(t)
+    picks = rng.integers(0, len(pool), len(sched))
+    srv = gpv.Server(local, budget_bytes=150 << 30, workers=2, max_batch=256)
+    srv.set_tunables(*tuned)
+    for i in range(8):  # warm-up
+        tk = srv.submit(pinned[i % len(pool)], specs[i % len(pool)])
+        srv.poll(tk, -1)
+        srv.release(tk)
+    shed_limit = 2000
+    q = deque()
+    done = []
+    shed = [0]
+    finished = threading.Event()
+
+    def collector():
+        while True:
+            if not q:
+                if finished.is_set():
+                    return
+                time.sleep(0.0005)
+                continue
+            tk, ts = q.popleft()
+            rc, _, lat, qms = srv.poll(tk, -1)
+            done.append((ts, lat, qms, rc))
+            srv.release(tk)
+
+    col = threading.Thread(target=collector)
+    col.start()
+    start = time.perf_counter()
+    for ts, k in zip(sched, picks):
+        now = time.perf_counter() - start
+        if ts > now:
+            time.sleep(ts - now)
+        if srv.stats()["pending"] > shed_limit:
+            shed[0] += 1
+            continue
+        q.append((srv.submit(pinned[k], specs[k]), ts))
+    finished.set()
+    col.join()
+    wall = time.perf_counter() - start
+    st = srv.stats()
+    srv.close()
+    lat = np.array([d[1] for d in done if d[3] == 0])
+    ts = np.array([d[0] for d in done if d[3] == 0])
+    bins = []
+    for b in range(6):
+        lo, hi = b * D / 6, (b + 1) * D / 6
+        m = (ts >= lo) & (ts < hi)
+        if m.any():
+            bins.append({"rate_req_s": round(r0 + (r1 - r0) * (lo + hi) / 2 / D),
+                         "completed": int(m.sum()), "p50_ms": float(np.percentile(lat[m], 50)),
+                         "p99_ms": float(np.percentile(lat[m], 99))})
+    return {"workload": "served", "duration_s": D, "rate_req_s": [r0, r1],
+            "desc": "Poisson stream, rate ramped linearly; pool of %d meshes (3 families, T log-uniform "
+                    "1e3-1e6, Level1 {64,128,256}^3, Level2 {4,8}^3); 150 GB budget; 2 workers" % len(pool),
+            "offered": len(sched), "shed": shed[0], "completed": int(len(lat)),
+            "failed": int(sum(1 for d in done if d[3] != 0)),
+            "meshes_per_s": len(lat) / wall, "batches": st["batches"],
+            "p50_ms": float(np.percentile(lat, 50)) if len(lat) else None,
+            "p95_ms": float(np.percentile(lat, 95)) if len(lat) else None,
+            "p99_ms": float(np.percentile(lat, 99)) if len(lat) else None,
+            "queue_p50_ms": float(np.percentile([d[2] for d in done], 50)) if done else None,
+            "by_rate": bins}
 
 
 def run_reference(args):
@@ -396,8 +486,12 @@ def main():
             "e2e": {"value": e2e_value, "unit": "tests/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h, "ms_per_step": e2e_t * 1e3 / args.steps},
             "gpu_launches": launches, "roofline": roof, "clocks": clk}
+    tuned = (128, 16)
     if args.batch > 0:
         line["batched"] = batch_bench(gpv, ctx, torch, stream, local, args)
+        tuned = (line["batched"]["tile"], line["batched"]["level2_chunk"])
+    if args.serve_seconds > 0:
+        line["served"] = served_bench(gpv, torch, local, args, tuned)
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(tris, spec, tests_per_step, args.cpu_seconds,
                                             os.cpu_count() or 1)

@@ -111,6 +111,16 @@ def lib():
     L.gpv_autotune.argtypes = [C.c_void_p, C.c_int32, C.POINTER(C.c_void_p), C.POINTER(C.c_int64),
                                C.POINTER(GridSpec), C.c_void_p, C.POINTER(C.c_int32),
                                C.POINTER(C.c_int32), C.POINTER(C.c_float)]
+    L.gpv_server_create.argtypes = [C.c_int, C.c_int64, C.c_int32, C.c_int32, C.POINTER(C.c_void_p)]
+    L.gpv_server_set_tunables.argtypes = [C.c_void_p, C.c_int32, C.c_int32]
+    L.gpv_server_submit.argtypes = [C.c_void_p, C.c_void_p, C.c_int64, C.POINTER(GridSpec),
+                                    C.POINTER(C.c_uint64)]
+    L.gpv_server_poll.argtypes = [C.c_void_p, C.c_uint64, C.c_int32, C.POINTER(Result),
+                                  C.POINTER(C.c_double), C.POINTER(C.c_double)]
+    L.gpv_server_release.argtypes = [C.c_void_p, C.c_uint64]
+    L.gpv_server_stats.argtypes = [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int64),
+                                   C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]
+    L.gpv_server_destroy.argtypes = [C.c_void_p]
     if hasattr(L, "gpv_voxelize_batch"):
         L.gpv_voxelize_batch.argtypes = [C.c_void_p, C.c_int32, C.POINTER(C.c_void_p),
                                          C.POINTER(C.c_int64), C.POINTER(GridSpec),
@@ -389,3 +399,61 @@ class Object:
                                  vd.level2InOut.ctypes.data_as(C.c_void_p))
         if rc:
             raise GpvError(rc, "SaveVoxelization")
+
+
+class Server:
+    """Continuous-batching voxelization server (gpv_server_* in include/gpview.h)."""
+
+    def __init__(self, device=0, budget_bytes=150 << 30, workers=2, max_batch=256):
+        self._h = C.c_void_p()
+        rc = lib().gpv_server_create(int(device), int(budget_bytes), int(workers), int(max_batch),
+                                     C.byref(self._h))
+        if rc:
+            raise GpvError(rc, "gpv_server_create")
+        self._keep = {}
+
+    def set_tunables(self, tile, level2_chunk):
+        rc = lib().gpv_server_set_tunables(self._h, int(tile), int(level2_chunk))
+        if rc:
+            raise GpvError(rc, "set_tunables")
+
+    def submit(self, tris, spec):
+        """tris: float32 array (pinned torch tensor or numpy), kept alive until release."""
+        ptr = tris.data_ptr() if hasattr(tris, "data_ptr") else tris.ctypes.data
+        n = (tris.numel() if hasattr(tris, "numel") else tris.size) // 9
+        t = C.c_uint64()
+        rc = lib().gpv_server_submit(self._h, C.c_void_p(ptr), int(n), C.byref(spec), C.byref(t))
+        if rc:
+            raise GpvError(rc, "submit")
+        self._keep[t.value] = tris
+        return t.value
+
+    def poll(self, ticket, timeout_ms=0):
+        """(status, result, latency_ms, queue_ms); status GPV_ERR_PENDING (-8) while running."""
+        res = Result()
+        lat, q = C.c_double(), C.c_double()
+        rc = lib().gpv_server_poll(self._h, C.c_uint64(ticket), int(timeout_ms), C.byref(res),
+                                   C.byref(lat), C.byref(q))
+        return rc, res, lat.value, q.value
+
+    def release(self, ticket):
+        rc = lib().gpv_server_release(self._h, C.c_uint64(ticket))
+        self._keep.pop(ticket, None)
+        return rc
+
+    def stats(self):
+        a, b, c, d = C.c_int64(), C.c_int64(), C.c_uint64(), C.c_uint64()
+        lib().gpv_server_stats(self._h, C.byref(a), C.byref(b), C.byref(c), C.byref(d))
+        return dict(in_use_bytes=a.value, pending=b.value, batches=c.value, served=d.value)
+
+    def close(self):
+        if self._h:
+            lib().gpv_server_destroy(self._h)
+            self._h = C.c_void_p()
+            self._keep.clear()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -307,16 +307,21 @@ int gpv_result_copy_to_host(gpv_ctx *ctx, const gpv_result *res, uint8_t *l1, in
 
 int gpv_result_release(gpv_ctx *ctx, gpv_result *res) {
   if (!ctx || !res) return GPV_ERR_INVALID;
-  auto it = ctx->owned.find(res->handle);
-  if (it == ctx->owned.end()) return GPV_ERR_INVALID;
+  std::shared_ptr<ResultSet> set;
+  {
+    std::lock_guard<std::mutex> lk(ctx->owned_mu);
+    auto it = ctx->owned.find(res->handle);
+    if (it == ctx->owned.end()) return GPV_ERR_INVALID;
+    set = it->second;
+    if (--set->refs <= 0) ctx->owned.erase(it);
+    else set.reset();
+  }
   cudaSetDevice(ctx->device);
-  std::shared_ptr<ResultSet> set = it->second;
-  if (--set->refs <= 0) {
+  if (set) {
     cudaFreeAsync(set->l1, 0);
     cudaFreeAsync(set->prefix, 0);
     cudaFreeAsync(set->bindex, 0);
     cudaFreeAsync(set->l2, 0);
-    ctx->owned.erase(it);
   }
   res->level1_inout = nullptr;
   res->level1_prefix = nullptr;

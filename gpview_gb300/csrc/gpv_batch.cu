@@ -300,9 +300,13 @@ int run_batch(gpv_ctx *ctx, int n, const float *const *d_tris, const int64_t *T,
       return fail_all(GPV_ERR_DEVICE, "boundary plane and pair lists disagree");
   }
 
-  const uint64_t handle = ctx->next_handle++;
-  set->refs = n;
-  ctx->owned[handle] = set;
+  uint64_t handle;
+  {
+    std::lock_guard<std::mutex> lk(ctx->owned_mu);
+    handle = ctx->next_handle++;
+    set->refs = n;
+    ctx->owned[handle] = set;
+  }
   for (int m = 0; m < n; ++m) {
     const MeshStats &st = ctx->h_stats[m];
     gpv_result &r = out[m];

@@ -1,6 +1,7 @@
 // gpv_ctx.h -- the library context (one per host thread) and helpers shared by the host files.
 #pragma once
 #include <memory>
+#include <mutex>
 #include <string>
 #include <unordered_map>
 
@@ -38,6 +39,7 @@ struct gpv_ctx {
   float *h_tables = nullptr;           // pinned staging for coordinate tables
   size_t h_tables_cap = 0;
   uint64_t next_handle = 1;
+  std::mutex owned_mu;                 // results may be released from another host thread
   std::unordered_map<uint64_t, std::shared_ptr<gpv::ResultSet>> owned;
 };
 

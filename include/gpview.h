@@ -164,6 +164,29 @@ int gpv_voxelize_level1_noalloc(const float *d_tris, int64_t num_triangles,
                                 int64_t *num_boundary, cudaStream_t stream);
 const char *gpv_noalloc_last_error(void);
 
+/* ---- serving: continuous batching (no counterpart in the reference) -------------------------
+ * Requests carry host triangles (caller memory, valid until the request completes; pinned memory
+ * gives the fastest copies) and a grid.  `workers` threads, each with its own context and stream,
+ * admit every waiting request that fits `budget_bytes` of device memory by a predicted footprint
+ * (FIFO), and voxelize each admitted set with one batched launch sequence; requests arriving
+ * meanwhile join the next set.  Results stay on the device (and count against the budget) until
+ * gpv_server_release.  Submit returns GPV_ERR_BUDGET for a request that can never fit. */
+typedef struct gpv_server gpv_server;
+int gpv_server_create(int device, int64_t budget_bytes, int32_t workers, int32_t max_batch,
+                      gpv_server **out);
+int gpv_server_set_tunables(gpv_server *srv, int32_t tile, int32_t level2_chunk);
+int gpv_server_submit(gpv_server *srv, const float *h_tris, int64_t num_triangles,
+                      const gpv_grid_spec *spec, uint64_t *ticket);
+/* Waits up to timeout_ms (0: no wait, <0: forever).  GPV_ERR_PENDING while running; on
+ * completion the result's status, its device arrays, the submit-to-done latency and the time the
+ * request waited before its batch started. */
+int gpv_server_poll(gpv_server *srv, uint64_t ticket, int32_t timeout_ms, gpv_result *out,
+                    double *latency_ms, double *queue_ms);
+int gpv_server_release(gpv_server *srv, uint64_t ticket);
+int gpv_server_stats(gpv_server *srv, int64_t *in_use_bytes, int64_t *pending, uint64_t *batches,
+                     uint64_t *served);
+void gpv_server_destroy(gpv_server *srv);
+
 /* ---- meshes and files (host) ---------------------------------------------------------------- */
 int gpv_load_obj(const char *path, gpv_mesh *out); /* Object::ReadObject (src/Object.cpp:395) */
 int gpv_load_off(const char *path, gpv_mesh *out); /* Object::ReadOFFObject (src/Object.cpp:171) */

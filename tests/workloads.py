@@ -94,3 +94,43 @@ def _place(u, pts):
     size = mx - mn
     lo = np.where(size < 1.0, np.asarray(u) * np.maximum(1.0 - size, 0), 0.5 - size / 2)
     return (pts - mn + lo).astype(np.float32)
+
+
+def served_pool(count=256, seed=5000, threads=None):
+    """Mesh pool of the served configuration: the three families, triangle counts log-uniform
+    in [1000, 1000000], Level1 uniform over {64, 128, 256}^3, Level2 uniform over {4, 8}^3."""
+    import os
+    from concurrent.futures import ThreadPoolExecutor
+
+    rng = np.random.default_rng(seed)
+    params = []
+    for i in range(count):
+        fam = int(rng.integers(0, 3))
+        T = float(np.exp(rng.uniform(np.log(1000), np.log(1000000))))
+        q, _ = np.linalg.qr(rng.normal(size=(3, 3)))
+        params.append(dict(fam=fam, T=T, q=q.astype(np.float32), gseed=seed * 7919 + i,
+                           semi=rng.uniform(0.2, 0.45, 3), e=rng.uniform(0.3, 2.0, 2),
+                           place=rng.uniform(0, 1, 3), r=float(rng.uniform(0.2, 0.45)),
+                           R=float(rng.uniform(0.2, 0.33)), rr=float(rng.uniform(0.05, 0.12)),
+                           n1=int(rng.choice([64, 128, 256])), n2=int(rng.choice([4, 8]))))
+
+    def make_one(p):
+        T = p["T"]
+        if p["fam"] == 0:
+            nlat = max(3, int(round(np.sqrt(T / 4.0))) + 1)
+            t = gpv.gen_uvsphere(p["gseed"], 2 * (nlat - 1), nlat, (0.5, 0.5, 0.5), p["r"], 0.002)
+        elif p["fam"] == 1:
+            nv = max(3, int(round(np.sqrt(T / 4.0))))
+            rr = min(p["rr"], p["R"] - 0.02)
+            t = gpv.gen_torus(p["gseed"], 2 * nv, nv, (0.0, 0.0, 0.0), p["R"], rr, 0.01)
+            t = _place(p["place"], t.reshape(-1, 3) @ p["q"].T)
+        else:
+            nlat = max(3, int(round(np.sqrt(T / 4.0))) + 1)
+            t = gpv.gen_superellipsoid(p["gseed"], 2 * (nlat - 1), nlat, (0.0, 0.0, 0.0), p["semi"],
+                                       p["e"][0], p["e"][1], p["q"])
+            t = _place(p["place"], t.reshape(-1, 3))
+        t = np.ascontiguousarray(t, np.float32).reshape(-1)
+        return t, gpv.grid_padded(*gpv.mesh_bounds(t), p["n1"], p["n2"])
+
+    with ThreadPoolExecutor(max_workers=threads or os.cpu_count() or 4) as ex:
+        return list(ex.map(make_one, params))
