@@ -44,19 +44,21 @@ __device__ __forceinline__ T warp_sum(T v) {
   return v;
 }
 
-// Sub-cells along one axis whose box can meet [tmin, tmax]: every cell outside the returned
-// range is rejected by the SAT's own box-axis test (the range is widened by several ulps and
-// one cell on each side).
+// Sub-cells along one axis whose box can meet [tmin, tmax].  Cell p spans
+// [c2s[p] - h, c2s[p] + h] ~ [vmin + p g2, vmin + (p+1) g2]; a cell whose box misses
+// [tmin - delta, tmax + delta] is rejected by the SAT's own box-axis test (delta covers the
+// rounding of the coordinates and of this computation, the 1e-3 cell margin that of the
+// quotient).
 __device__ __forceinline__ void l2_range(float tmin, float tmax, float c0, float h, float g2,
                                          int n2, int &lo, int &hi) {
   const float vmin = c0 - h;
-  const float delta = 8.f * EPS24 * (fabsf(tmin) + fabsf(tmax) + fabsf(vmin) + h);
-  float f0 = (tmin - delta - vmin) / g2;
-  float f1 = (tmax + delta - vmin) / g2;
+  const float delta = 8.f * EPS24 * (fabsf(tmin) + fabsf(tmax) + fabsf(vmin) + h) + 1e-30f;
+  float f0 = (tmin - delta - vmin) / g2 - 1e-3f;  // first p with vmin + (p+1) g2 >= tmin - delta
+  float f1 = (tmax + delta - vmin) / g2 + 1e-3f;  // last p with vmin + p g2 <= tmax + delta
   f0 = fminf(fmaxf(f0, -4.f), (float)n2 + 4.f);
   f1 = fminf(fmaxf(f1, -4.f), (float)n2 + 4.f);
-  lo = max((int)floorf(f0) - 1, 0);
-  hi = min((int)floorf(f1) + 1, n2 - 1);
+  lo = max((int)floorf(f0), 0);
+  hi = min((int)floorf(f1), n2 - 1);
 }
 
 // Slab of cell centres the triangle's plane test can accept.  For a cell centre c the SAT's
@@ -274,6 +276,12 @@ __global__ void __launch_bounds__(kWarps * 32) k_level2c(
         float V[9];
 #pragma unroll
         for (int qq = 0; qq < 9; ++qq) V[qq] = ws.v[tl][qq];
+        // cells of this column already marked by another triangle need no test (OR only)
+        const int off = (q * n2x + p) * n2z, sh = off & 31;
+        uint32_t done = satj[off >> 5] >> sh;
+        if (sh + n2z > 32) done |= satj[(off >> 5) + 1] << (32 - sh);
+        const uint32_t rmask = ((r1 - r0 + 1) >= 32 ? 0xffffffffu : ((1u << (r1 - r0 + 1)) - 1u)) << r0;
+        if ((~done & rmask) == 0) continue;
         const float cx = __ldg(sx + p), cy = __ldg(sy + q);
         SatCol s;
         if (!sat_col(V, cx, cy, g.e2, s)) continue;
@@ -281,6 +289,7 @@ __global__ void __launch_bounds__(kWarps * 32) k_level2c(
         const float sxy = fa(fm(nxs, fs(V[0], cx)), fm(nys, fs(V[1], cy)));
         uint32_t bits = 0;
         for (int r = r0; r <= r1; ++r) {
+          if ((done >> r) & 1u) continue;
           const float cz = __ldg(sz + r);
           if (fabsf(fa(sxy, fm(nzs, fs(V[2], cz)))) > H) continue;  // plane misses the cell
           if (sat_z(s, V, cz, g.e2)) bits |= 1u << r;
