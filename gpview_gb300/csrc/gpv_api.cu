@@ -116,6 +116,7 @@ GridDev make_griddev(const GridHost &gh, const float *dt) {
   g.key_bits = gh.key_bits;
   g.thr = gh.thr;
   g.oz_monotone = gh.oz_monotone ? 1 : 0;
+  for (int a = 0; a < 3; ++a) g.inv_g2[a] = gh.g2[a] > 0.f ? 1.0f / gh.g2[a] : 0.f;
   return g;
 }
 

@@ -50,6 +50,7 @@ struct GridDev {
   int key_bits;         // bits of the column-major voxel key
   float thr;            // largest float below 1e-6
   int oz_monotone;      // Level2 ray-origin heights strictly increase along every column
+  float inv_g2[3];      // 1 / gridSize2 (range arithmetic only, never inside a predicate)
 };
 
 __device__ __forceinline__ float fm(float a, float b) { return __fmul_rn(a, b); }

@@ -49,12 +49,14 @@ __device__ __forceinline__ T warp_sum(T v) {
 // [tmin - delta, tmax + delta] is rejected by the SAT's own box-axis test (delta covers the
 // rounding of the coordinates and of this computation, the 1e-3 cell margin that of the
 // quotient).
-__device__ __forceinline__ void l2_range(float tmin, float tmax, float c0, float h, float g2,
+__device__ __forceinline__ void l2_range(float tmin, float tmax, float c0, float h, float inv_g2,
                                          int n2, int &lo, int &hi) {
   const float vmin = c0 - h;
   const float delta = 8.f * EPS24 * (fabsf(tmin) + fabsf(tmax) + fabsf(vmin) + h) + 1e-30f;
-  float f0 = (tmin - delta - vmin) / g2 - 1e-3f;  // first p with vmin + (p+1) g2 >= tmin - delta
-  float f1 = (tmax + delta - vmin) / g2 + 1e-3f;  // last p with vmin + p g2 <= tmax + delta
+  // first p with vmin + (p+1) g2 >= tmin - delta, last p with vmin + p g2 <= tmax + delta
+  // (the reciprocal's rounding moves the quotients by far less than the 1e-3 cell margin)
+  float f0 = (tmin - delta - vmin) * inv_g2 - 1e-3f;
+  float f1 = (tmax + delta - vmin) * inv_g2 + 1e-3f;
   f0 = fminf(fmaxf(f0, -4.f), (float)n2 + 4.f);
   f1 = fminf(fmaxf(f1, -4.f), (float)n2 + 4.f);
   lo = max((int)floorf(f0), 0);
@@ -182,7 +184,7 @@ __global__ void k_itemstarts(const uint32_t *__restrict__ iflag, const uint32_t 
 }
 
 // ---- Level2 ------------------------------------------------------------------------------------
-__global__ void __launch_bounds__(kWarps * 32) k_level2c(
+__global__ void __launch_bounds__(kWarps * 32, 5) k_level2c(
     BatchDev bd, const uint32_t *__restrict__ keys, const uint32_t *__restrict__ vals,
     const uint32_t *__restrict__ useg, const uint32_t *__restrict__ cflag,
     const uint32_t *__restrict__ cord, const uint32_t *__restrict__ colhead,
@@ -245,11 +247,11 @@ __global__ void __launch_bounds__(kWarps * 32) k_level2c(
         const float V[9] = {a0.x, a0.y, a0.z, a1.x, a1.y, a1.z, a2.x, a2.y, a2.z};
         int p0, p1, q0, q1, r0, r1;
         l2_range(fminf(V[0], fminf(V[3], V[6])), fmaxf(V[0], fmaxf(V[3], V[6])), sx0, g.e2[0],
-                 g.g2[0], n2x, p0, p1);
+                 g.inv_g2[0], n2x, p0, p1);
         l2_range(fminf(V[1], fminf(V[4], V[7])), fmaxf(V[1], fmaxf(V[4], V[7])), sy0, g.e2[1],
-                 g.g2[1], n2y, q0, q1);
+                 g.inv_g2[1], n2y, q0, q1);
         l2_range(fminf(V[2], fminf(V[5], V[8])), fmaxf(V[2], fmaxf(V[5], V[8])), sz0, g.e2[2],
-                 g.g2[2], n2z, r0, r1);
+                 g.inv_g2[2], n2z, r0, r1);
         if (p0 <= p1 && q0 <= q1 && r0 <= r1) {
           const PlaneSlab ps = plane_slab(V, sx0, sx1, sy0, sy1, sz0, sz1, g.e2);
 #pragma unroll
@@ -270,8 +272,11 @@ __global__ void __launch_bounds__(kWarps * 32) k_level2c(
         const uint32_t loc = w - ws.pre[tl];
         const uint32_t rg = ws.rng[tl];
         const int np = (int)((rg >> 6) & 63u);
-        const int p = (int)(rg & 63u) + (int)(loc % (uint32_t)np);
-        const int q = (int)((rg >> 12) & 63u) + (int)(loc / (uint32_t)np);
+        // loc / np by a float reciprocal: exact here (loc < 1024, np <= 32, so the quotient of
+        // loc + 1/2 stays at least 1/64 away from an integer, far above the rounding)
+        const int qq = __float2int_rz(((float)loc + 0.5f) * __frcp_rn((float)np));
+        const int p = (int)(rg & 63u) + (int)loc - qq * np;
+        const int q = (int)((rg >> 12) & 63u) + qq;
         const int r0 = (int)((rg >> 18) & 63u), r1 = (int)((rg >> 24) & 63u);
         float V[9];
 #pragma unroll
@@ -287,8 +292,22 @@ __global__ void __launch_bounds__(kWarps * 32) k_level2c(
         if (!sat_col(V, cx, cy, g.e2, s)) continue;
         const float nxs = ws.x[tl][0], nys = ws.x[tl][1], nzs = ws.x[tl][2], H = ws.x[tl][3];
         const float sxy = fa(fm(nxs, fs(V[0], cx)), fm(nys, fs(V[1], cy)));
+        // The per-cell slab test |sxy + nz (V0z - cz)| <= H can only pass for cz within
+        // H/|nz| of V0z + sxy/nz; the interval is widened by the float error of that test (a few
+        // ulps of its terms, over |nz|) and one cell, and the exact per-cell test still runs.
+        int ra = r0, rb = r1;
+        if (fabsf(nzs) > 0.f) {
+          const float rnz = __frcp_rn(nzs);
+          const float zc = V[2] + sxy * rnz;
+          const float ext = (H + 8.f * EPS24 * (fabsf(sxy) + fabsf(nzs) * (fabsf(V[2]) + fabsf(sz0) +
+                                                                           fabsf(sz1)))) * fabsf(rnz);
+          const float igz = g.inv_g2[2];
+          const float fa0 = (zc - ext - sz0) * igz - 1.f, fb0 = (zc + ext - sz0) * igz + 1.f;
+          if (fa0 > -2.f) ra = max(ra, (int)floorf(fminf(fa0, (float)n2z + 2.f)));
+          if (fb0 < (float)n2z + 2.f) rb = min(rb, (int)ceilf(fmaxf(fb0, -2.f)));
+        }
         uint32_t bits = 0;
-        for (int r = r0; r <= r1; ++r) {
+        for (int r = ra; r <= rb; ++r) {
           if ((done >> r) & 1u) continue;
           const float cz = __ldg(sz + r);
           if (fabsf(fa(sxy, fm(nzs, fs(V[2], cz)))) > H) continue;  // plane misses the cell
@@ -348,8 +367,9 @@ __global__ void __launch_bounds__(kWarps * 32) k_level2c(
       const uint32_t loc = w - ws.pre[tl];
       const uint32_t rg = ws.rng[tl];
       const int np = (int)((rg >> 6) & 63u);
-      const int p = (int)(rg & 63u) + (int)(loc % (uint32_t)np);
-      const int q = (int)((rg >> 12) & 63u) + (int)(loc / (uint32_t)np);
+      const int qq = __float2int_rz(((float)loc + 0.5f) * __frcp_rn((float)np));
+      const int p = (int)(rg & 63u) + (int)loc - qq * np;
+      const int q = (int)((rg >> 12) & 63u) + qq;
       float V[9];
 #pragma unroll
       for (int qq = 0; qq < 9; ++qq) V[qq] = ws.v[tl][qq];
@@ -391,6 +411,8 @@ __global__ void __launch_bounds__(kWarps * 32) k_level2c(
   __syncwarp();
   unsigned long long nin = 0, nbd = 0;
   const bool vec = (cells & 3) == 0;
+  const bool pow2 = ((n2x & (n2x - 1)) == 0) && ((n2y & (n2y - 1)) == 0);
+  const int lx = __ffs(n2x) - 1, ly = __ffs(n2y) - 1;
   for (int jv = m - 1; jv >= 0; --jv) {
     for (int w = lane; w < FW; w += 32) ftacc[w] ^= ft[jv * FW + w];
     __syncwarp();
@@ -403,7 +425,16 @@ __global__ void __launch_bounds__(kWarps * 32) k_level2c(
       for (int d = 0; d < 4; ++d) {
         const int c = c4 + d;
         if (c >= cells) break;
-        const int p = c % n2x, q = (c / n2x) % n2y, r = c / ncol2;
+        int p, q, r;
+        if (pow2) {
+          p = c & (n2x - 1);
+          q = (c >> lx) & (n2y - 1);
+          r = c >> (lx + ly);
+        } else {
+          p = c % n2x;
+          q = (c / n2x) % n2y;
+          r = c / ncol2;
+        }
         const int pq = q * n2x + p;
         const int bi = pq * n2z + r;
         const uint32_t sb = (satj[bi >> 5] >> (bi & 31)) & 1u;
