@@ -39,6 +39,7 @@ def parse():
     p.add_argument("--impl", default="gpv", choices=["gpv", "reference"])
     p.add_argument("--workload", default="torus262k", choices=["sphere16k", "torus262k", "star1310k"])
     p.add_argument("--tile", type=int, default=0)
+    p.add_argument("--no-graphs", action="store_true")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--cpu-seconds", type=float, default=15.0)
     p.add_argument("--batch", type=int, default=4096, help="meshes of the batched workload (0: skip)")
@@ -357,6 +358,7 @@ def main():
     ctx = gpv.Context(local)
     if args.tile:
         ctx.set_tile(args.tile)
+    ctx.set_graphs(not args.no_graphs)
     stream = torch.cuda.Stream(device=local)
     sp = stream.cuda_stream
     d_tris = torch.from_numpy(tris).to(f"cuda:{local}")

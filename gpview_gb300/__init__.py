@@ -108,6 +108,7 @@ def lib():
                                               C.POINTER(C.c_int64), C.c_void_p]
     L.gpv_noalloc_last_error.restype = C.c_char_p
     L.gpv_set_level2_chunk.argtypes = [C.c_void_p, C.c_int]
+    L.gpv_set_graphs.argtypes = [C.c_void_p, C.c_int]
     L.gpv_autotune.argtypes = [C.c_void_p, C.c_int32, C.POINTER(C.c_void_p), C.POINTER(C.c_int64),
                                C.POINTER(GridSpec), C.c_void_p, C.POINTER(C.c_int32),
                                C.POINTER(C.c_int32), C.POINTER(C.c_float)]
@@ -237,6 +238,9 @@ class Context:
         ms = (C.c_double * 8)()
         calls = lib().gpv_stage_times(self._h, ms, 8)
         return calls, {k: ms[i] for i, k in enumerate(self.STAGES)}
+
+    def set_graphs(self, on=True):
+        self._check(lib().gpv_set_graphs(self._h, int(bool(on))), "set_graphs")
 
     def set_tile(self, t):
         rc = lib().gpv_set_tile(self._h, int(t))

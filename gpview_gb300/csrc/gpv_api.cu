@@ -167,6 +167,8 @@ void gpv_destroy(gpv_ctx *ctx) {
     cudaFree(r->l2);
   }
   ctx->owned.clear();
+  for (cudaGraphExec_t &ge : ctx->gexec)
+    if (ge) cudaGraphExecDestroy(ge);
   if (ctx->h_stats) cudaFreeHost(ctx->h_stats);
   if (ctx->h_md) cudaFreeHost(ctx->h_md);
   if (ctx->h_tiles) cudaFreeHost(ctx->h_tiles);
@@ -197,6 +199,12 @@ int gpv_stage_times(gpv_ctx *ctx, double *ms, int n) {
 }
 
 uint64_t gpv_kernel_launches(void) { return gpv::launch_count(); }
+
+int gpv_set_graphs(gpv_ctx *ctx, int on) {
+  if (!ctx) return GPV_ERR_INVALID;
+  ctx->graphs = on != 0;
+  return GPV_OK;
+}
 
 int gpv_set_level2_chunk(gpv_ctx *ctx, int cap) {
   if (!ctx || cap < 1 || cap > 32) return GPV_ERR_INVALID;

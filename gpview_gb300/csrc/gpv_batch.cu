@@ -40,6 +40,58 @@ struct Arena {
 
 size_t al16(size_t v) { return (v + 15) & ~size_t(15); }
 
+// Runs `launches` on stream s, recorded as a CUDA graph when the context asks for graphs.  The
+// executable graph of each phase is cached in the context and updated in place when the new
+// recording has the same topology; otherwise it is re-instantiated.  If recording fails the
+// launches run directly.
+template <typename F>
+cudaError_t run_phase(gpv_ctx *ctx, int phase, cudaStream_t s, bool &capturing, F &&launches) {
+  if (!ctx->graphs) {
+    launches();
+    return cudaGetLastError();
+  }
+  if (cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+    cudaGetLastError();
+    launches();
+    return cudaGetLastError();
+  }
+  capturing = true;
+  launches();
+  capturing = false;
+  cudaGraph_t graph = nullptr;
+  cudaError_t e = cudaStreamEndCapture(s, &graph);
+  if (e != cudaSuccess || !graph) {
+    cudaGetLastError();
+    if (graph) cudaGraphDestroy(graph);
+    launches();
+    return cudaGetLastError();
+  }
+  cudaGraphExec_t &ge = ctx->gexec[phase];
+  bool ok = false;
+  if (ge) {
+    cudaGraphExecUpdateResultInfo info;
+    ok = cudaGraphExecUpdate(ge, graph, &info) == cudaSuccess;
+    if (!ok) {
+      cudaGetLastError();
+      cudaGraphExecDestroy(ge);
+      ge = nullptr;
+    }
+  }
+  if (!ok) {
+    e = cudaGraphInstantiate(&ge, graph, 0);
+    ctx->graph_instantiations++;
+    if (e != cudaSuccess) {
+      cudaGraphDestroy(graph);
+      ge = nullptr;
+      return e;
+    }
+  }
+  e = cudaGraphLaunch(ge, s);
+  ctx->graph_launches++;
+  cudaGraphDestroy(graph);
+  return e;
+}
+
 }  // namespace
 
 int run_batch(gpv_ctx *ctx, int n, const float *const *d_tris, const int64_t *T,
@@ -159,8 +211,11 @@ int run_batch(gpv_ctx *ctx, int n, const float *const *d_tris, const int64_t *T,
   std::memcpy(ctx->h_md, md.data(), n * sizeof(MeshDesc));
   CK(cudaMemcpyAsync(d_md, ctx->h_md, n * sizeof(MeshDesc), cudaMemcpyHostToDevice, s));
 
+  bool capturing = false;
   auto mark = [&](int i) {
-    if (ctx->timing) cudaEventRecord(ctx->ev[i], s);
+    if (!ctx->timing) return;
+    if (capturing) cudaEventRecordWithFlags(ctx->ev[i], s, cudaEventRecordExternal);
+    else cudaEventRecord(ctx->ev[i], s);
   };
   auto fail_all = [&](int code, const char *msg) {
     cudaFreeAsync(set->l1, s);
@@ -196,15 +251,16 @@ int run_batch(gpv_ctx *ctx, int n, const float *const *d_tris, const int64_t *T,
   CK(cudaMemcpyAsync(d_md, ctx->h_md, n * sizeof(MeshDesc), cudaMemcpyHostToDevice, s));
 
   // ---- phase B
-  mark(2);
-  launch_level1(bd, ctx->num_sms, s);
-  mark(3);
-  launch_fill_finish(bd, s);
-  launch_popc(bplane, words, wcnt, s);
-  scan_u32(wcnt, wpre, words, wtot, stmp, s);
-  launch_boundary_counts(bd, wpre, wtot, s);
-  mark(4);
-  CK(cudaGetLastError());
+  CK(run_phase(ctx, 0, s, capturing, [&] {
+    mark(2);
+    launch_level1(bd, ctx->num_sms, s);
+    mark(3);
+    launch_fill_finish(bd, s);
+    launch_popc(bplane, words, wcnt, s);
+    scan_u32(wcnt, wpre, words, wtot, stmp, s);
+    launch_boundary_counts(bd, wpre, wtot, s);
+    mark(4);
+  }));
   CK(cudaMemcpyAsync(ctx->h_stats, stats, n * sizeof(MeshStats), cudaMemcpyDeviceToHost, s));
   CK(cudaStreamSynchronize(s));
   int64_t Btot = 0, l2bytes = 0, P2 = 0, ub = 0;
@@ -243,18 +299,17 @@ int run_batch(gpv_ctx *ctx, int n, const float *const *d_tris, const int64_t *T,
   std::memcpy(ctx->h_md, md.data(), n * sizeof(MeshDesc));
   CK(cudaMemcpyAsync(d_md, ctx->h_md, n * sizeof(MeshDesc), cudaMemcpyHostToDevice, s));
 
-  // ---- phase C
-  mark(5);
-  launch_expand(bd, wpre, s);
-  mark(6);
+  // ---- phase C: allocations and uploads first, then the recorded launch sequence
   const int64_t ntiles = (int64_t)st_host.size();
-  if (any_l2 && ntiles > 0) {
+  const bool do_l2 = any_l2 && ntiles > 0;
+  SortTile *d_tiles = nullptr;
+  int64_t *d_tb = nullptr;
+  uint32_t *kalt = nullptr, *valt = nullptr, *flags = nullptr, *uidx = nullptr, *useg = nullptr,
+           *sortmp = nullptr, *l2tmp = nullptr;
+  if (do_l2) {
     CK(ctx_ensure_host_tiles(ctx, (size_t)ntiles, (size_t)n + 1));
     std::memcpy(ctx->h_tiles, st_host.data(), ntiles * sizeof(SortTile));
     std::memcpy(ctx->h_tb, stb.data(), (n + 1) * sizeof(int64_t));
-    SortTile *d_tiles;
-    int64_t *d_tb;
-    uint32_t *kalt, *valt, *flags, *uidx, *useg, *sortmp, *l2tmp;
     CK(ws.get(&d_tiles, (size_t)ntiles));
     CK(ws.get(&d_tb, (size_t)n + 1));
     CK(ws.get(&kalt, (size_t)std::max<int64_t>(P2, 1)));
@@ -266,20 +321,26 @@ int run_batch(gpv_ctx *ctx, int n, const float *const *d_tris, const int64_t *T,
     CK(ws.get(&l2tmp, (size_t)level2_temp_words(ub)));
     CK(cudaMemcpyAsync(d_tiles, ctx->h_tiles, ntiles * sizeof(SortTile), cudaMemcpyHostToDevice, s));
     CK(cudaMemcpyAsync(d_tb, ctx->h_tb, (n + 1) * sizeof(int64_t), cudaMemcpyHostToDevice, s));
-    const bool in_alt = sort_pairs_seg(bd, d_tiles, d_tb, ntiles, keys, vals, kalt, valt, P2,
-                                       max_keybits, sortmp, s);
-    const uint32_t *sk = in_alt ? kalt : keys;
-    const uint32_t *sv = in_alt ? valt : vals;
-    launch_heads(sk, P2, flags, bd, s);
-    scan_u32(flags, uidx, P2, wtot + 1, sortmp, s);
-    launch_useg(flags, uidx, P2, useg, s);
-    mark(7);
-    launch_level2(bd, sk, sv, useg, ub, l2tmp, warp_words, ctx->num_sms, s);
-  } else {
-    mark(7);
   }
-  mark(8);
-  CK(cudaGetLastError());
+  CK(run_phase(ctx, 1, s, capturing, [&] {
+    mark(5);
+    launch_expand(bd, wpre, s);
+    mark(6);
+    if (do_l2) {
+      const bool in_alt = sort_pairs_seg(bd, d_tiles, d_tb, ntiles, keys, vals, kalt, valt, P2,
+                                         max_keybits, sortmp, s);
+      const uint32_t *sk = in_alt ? kalt : keys;
+      const uint32_t *sv = in_alt ? valt : vals;
+      launch_heads(sk, P2, flags, bd, s);
+      scan_u32(flags, uidx, P2, wtot + 1, sortmp, s);
+      launch_useg(flags, uidx, P2, useg, s);
+      mark(7);
+      launch_level2(bd, sk, sv, useg, ub, l2tmp, warp_words, ctx->num_sms, s);
+    } else {
+      mark(7);
+    }
+    mark(8);
+  }));
   CK(cudaMemcpyAsync(ctx->h_stats, stats, n * sizeof(MeshStats), cudaMemcpyDeviceToHost, s));
   CK(cudaMemcpyAsync(ctx->h_u32, wtot, 8, cudaMemcpyDeviceToHost, s));
   CK(cudaStreamSynchronize(s));
@@ -295,7 +356,7 @@ int run_batch(gpv_ctx *ctx, int n, const float *const *d_tris, const int64_t *T,
   }
   for (int m = 0; m < n; ++m)
     if (ctx->h_stats[m].status) return fail_all(GPV_ERR_DEVICE, "device status raised in Level2");
-  if (any_l2 && ntiles > 0) {
+  if (do_l2) {
     if ((int64_t)ctx->h_u32[1] != ub)
       return fail_all(GPV_ERR_DEVICE, "boundary plane and pair lists disagree");
   }

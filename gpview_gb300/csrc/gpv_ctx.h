@@ -29,6 +29,9 @@ struct gpv_ctx {
   std::string err;
   int tile = 128;                      // Level1 triangles per tile (autotuned)
   int l2_chunk_cap = 32;               // Level2 boundary voxels per chunk, upper bound (autotuned)
+  bool graphs = true;                  // record phases B and C as CUDA graphs
+  cudaGraphExec_t gexec[2] = {};       // cached executable graphs of phases B and C
+  uint64_t graph_launches = 0, graph_instantiations = 0;
   gpv::MeshStats *h_stats = nullptr;   // pinned, h_cap entries
   gpv::MeshDesc *h_md = nullptr;       // pinned, h_cap entries
   size_t h_cap = 0;

@@ -105,6 +105,9 @@ const char *gpv_last_error(gpv_ctx *ctx);
  * number of boundary voxels of one Level1 column that one Level2 work item takes (1..32). */
 int gpv_set_tile(gpv_ctx *ctx, int tris_per_tile);
 int gpv_set_level2_chunk(gpv_ctx *ctx, int max_voxels);
+/* Record the Level1 and Level2 launch sequences of each voxelization as CUDA graphs (default on;
+ * the executable graphs are cached in the context and updated in place). */
+int gpv_set_graphs(gpv_ctx *ctx, int on);
 /* Autotuner: times every (tile, Level2 chunk) pair of {32,64,128,256} x {4,8,16,32} on the given
  * sample batch (CUDA events on `stream`), keeps the fastest in the context and reports it. */
 int gpv_autotune(gpv_ctx *ctx, int32_t n, const float *const *d_tris, const int64_t *num_triangles,
