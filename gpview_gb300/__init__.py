@@ -228,15 +228,15 @@ class Context:
     def error(self):
         return lib().gpv_last_error(self._h).decode()
 
-    STAGES = ("prep", "level1", "fill_finish", "expand", "sort_lists", "level2")
+    STAGES = ("prep", "level1", "fill_finish", "expand", "sort_lists", "level2", "level2_kernel")
 
     def set_timing(self, on=True):
         self._check(lib().gpv_set_timing(self._h, int(bool(on))), "set_timing")
 
     def stage_times(self):
         """(calls, {stage: accumulated ms}) from the per-stage CUDA events."""
-        ms = (C.c_double * 8)()
-        calls = lib().gpv_stage_times(self._h, ms, 8)
+        ms = (C.c_double * 9)()
+        calls = lib().gpv_stage_times(self._h, ms, 9)
         return calls, {k: ms[i] for i, k in enumerate(self.STAGES)}
 
     def set_graphs(self, on=True):

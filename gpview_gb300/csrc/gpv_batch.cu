@@ -335,9 +335,10 @@ int run_batch(gpv_ctx *ctx, int n, const float *const *d_tris, const int64_t *T,
       scan_u32(flags, uidx, P2, wtot + 1, sortmp, s);
       launch_useg(flags, uidx, P2, useg, s);
       mark(7);
-      launch_level2(bd, sk, sv, useg, ub, l2tmp, warp_words, ctx->num_sms, s);
+      launch_level2(bd, sk, sv, useg, ub, l2tmp, warp_words, ctx->num_sms, s, [&] { mark(9); });
     } else {
       mark(7);
+      mark(9);
     }
     mark(8);
   }));
@@ -345,9 +346,10 @@ int run_batch(gpv_ctx *ctx, int n, const float *const *d_tris, const int64_t *T,
   CK(cudaMemcpyAsync(ctx->h_u32, wtot, 8, cudaMemcpyDeviceToHost, s));
   CK(cudaStreamSynchronize(s));
   if (ctx->timing) {
-    // stages: 0 prep, 1 level1, 2 fill finish + boundary scan, 3 expand, 4 sort + lists, 5 level2
-    const int pr[6][2] = {{0, 1}, {2, 3}, {3, 4}, {5, 6}, {6, 7}, {7, 8}};
-    for (int k = 0; k < 6; ++k) {
+    // stages: 0 prep, 1 level1, 2 fill finish + boundary scan, 3 expand, 4 sort + lists,
+    // 5 level2 (work items + kernel), 6 the Level2 kernel alone
+    const int pr[7][2] = {{0, 1}, {2, 3}, {3, 4}, {5, 6}, {6, 7}, {7, 8}, {9, 8}};
+    for (int k = 0; k < 7; ++k) {
       float ms = 0.f;
       if (cudaEventElapsedTime(&ms, ctx->ev[pr[k][0]], ctx->ev[pr[k][1]]) == cudaSuccess)
         ctx->stage_ms[k] += ms;

@@ -19,7 +19,7 @@ struct ResultSet {
 }  // namespace gpv
 
 struct gpv_ctx {
-  static constexpr int kStages = 8;
+  static constexpr int kStages = 9;
   int device = 0;
   int num_sms = 148;
   bool timing = false;                 // record per-stage CUDA events on the launching stream

@@ -1,6 +1,7 @@
 // gpv_internal.h -- declarations shared by the library's translation units (not installed).
 #pragma once
 #include <cstdint>
+#include <functional>
 #include <string>
 #include <vector>
 #include <cuda_runtime.h>
@@ -104,9 +105,11 @@ constexpr int kSortTileItems = 2048;
 int level2_chunk(const GridDev &g, int cap = 32);
 int level2_warp_words(const GridDev &g, int cap = 32);
 int64_t level2_temp_words(int64_t Btot);
+// before_kernel (optional) runs on the host between the work-item launches and the Level2
+// kernel's launch, e.g. to record an event that times the kernel alone.
 void launch_level2(const BatchDev &bd, const uint32_t *keys, const uint32_t *vals,
                    const uint32_t *useg, int64_t Btot, uint32_t *tmp, int warp_words, int num_sms,
-                   cudaStream_t s);
+                   cudaStream_t s, const std::function<void()> &before_kernel = {});
 
 GridDev make_griddev(const GridHost &gh, const float *dtables);
 int64_t table_floats(const GridHost &gh);

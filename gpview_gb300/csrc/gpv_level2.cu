@@ -485,7 +485,7 @@ int64_t level2_temp_words(int64_t B) { return 6 * B + 8 + scan_temp_words(B); }
 // Builds the chunk items from the sorted pair lists and runs the persistent Level2 kernel.
 void launch_level2(const BatchDev &bd, const uint32_t *keys, const uint32_t *vals,
                    const uint32_t *useg, int64_t B, uint32_t *tmp, int warp_words, int num_sms,
-                   cudaStream_t s) {
+                   cudaStream_t s, const std::function<void()> &before_kernel) {
   if (B <= 0) return;
   uint32_t *cflag = tmp, *cord = cflag + B, *colhead = cord + B, *iflag = colhead + B + 1,
            *iord = iflag + B, *istart = iord + B, *nitems = istart + B + 1,
@@ -509,6 +509,7 @@ void launch_level2(const BatchDev &bd, const uint32_t *keys, const uint32_t *val
   per_sm = std::max(per_sm, 1);
   const int64_t grid = std::min<int64_t>((B + kWarps - 1) / kWarps, (int64_t)num_sms * per_sm);
   cudaMemsetAsync(bd.queue + 1, 0, sizeof(uint32_t), s);
+  if (before_kernel) before_kernel();
   k_level2c<<<(unsigned)grid, kWarps * 32, smem, s>>>(bd, keys, vals, useg, cflag, cord, colhead,
                                                       istart, nitems, warp_words);
   count_launch();

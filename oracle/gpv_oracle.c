@@ -56,7 +56,7 @@ int ref_tri_ray(const float *V1, const float *V2, const float *V3, const float *
 /* ------------------------------------------------------------------------------------------ */
 
 /* Plane/box part of the SAT (src/TriBoxIntersection.cpp:64-86). */
-static int orc_plane_box(const float nrm[3], const float vert[3], const float maxbox[3])
+static int orc_plane_box(const float nrm[3], const float vert[3], const float maxbox[3], int *full)
 {
     float vmin[3], vmax[3];
     for (int q = 0; q < 3; ++q) {
@@ -71,6 +71,7 @@ static int orc_plane_box(const float nrm[3], const float vert[3], const float ma
     }
     float dmin = nrm[0] * vmin[0] + nrm[1] * vmin[1] + nrm[2] * vmin[2];
     if (dmin > 0.0f) return 0;
+    *full = 1;
     float dmax = nrm[0] * vmax[0] + nrm[1] * vmax[1] + nrm[2] * vmax[2];
     if (dmax >= 0.0f) return 1;
     return 0;
@@ -87,17 +88,32 @@ static inline int orc_axis_sep(float pa, float pb, float rad)
 
 /* Akenine-Moller triangle/box overlap in the reference's order and roundings
  * (src/TriBoxIntersection.cpp:135-210). tv = 9 floats, vertex-major. */
-static int orc_tri_box_own(const float c[3], const float h[3], const float *tv);
+/* Executed FP32 operation counts of the reference predicates by exit point (add, sub, mul, and
+ * the one divide of the ray test; fabs, negation and compares excluded).  SAT
+ * (src/TriBoxIntersection.cpp:135-210, :64-86): 18 subtractions for the translated vertices and
+ * edges, 9 per edge-cross axis (two 2-product differences and the radius), nothing for the box
+ * axes, then the normal (9), vmin/vmax (6) and one dot product (5) before the first plane exit and
+ * a second dot product (5) before the last.  Ray (src/TriRayIntersection.cpp:78-131): edges (6),
+ * P (9) and det (5); 1/det, T (3) and u (6); Q (9), v (6) and u+v (1); t (6). */
+enum {
+    ORC_OPS_SAT_SETUP = 18, ORC_OPS_SAT_AXIS = 9, ORC_OPS_SAT_BOX = 99, ORC_OPS_SAT_PLANE = 119,
+    ORC_OPS_SAT_FULL = 124
+};
+enum { ORC_OPS_RAY_DET = 20, ORC_OPS_RAY_U = 30, ORC_OPS_RAY_V = 46, ORC_OPS_RAY_FULL = 52 };
+
+static int orc_tri_box_own(const float c[3], const float h[3], const float *tv, int *ops);
 int orc_tri_box(const float c[3], const float h[3], const float *tv)
 {
 #ifdef ORC_REF_PREDICATES
     return ref_tri_box(c, h, tv);
 #else
-    return orc_tri_box_own(c, h, tv);
+    int ops;
+    return orc_tri_box_own(c, h, tv, &ops);
 #endif
 }
 
-static int orc_tri_box_own(const float c[3], const float h[3], const float *tv)
+/* The nine edge-cross axes in the reference's order: (edge, vertex pair, axis). */
+static int orc_tri_box_own(const float c[3], const float h[3], const float *tv, int *ops)
 {
     float v0[3], v1[3], v2[3], e0[3], e1[3], e2[3];
     for (int a = 0; a < 3; ++a) {
@@ -111,31 +127,35 @@ static int orc_tri_box_own(const float c[3], const float h[3], const float *tv)
         e2[a] = v0[a] - v2[a];
     }
     float fx, fy, fz, a_, b_;
+#define ORC_SEP(k, pa, pb, rad) \
+    if (orc_axis_sep((pa), (pb), (rad))) { *ops = ORC_OPS_SAT_SETUP + ORC_OPS_SAT_AXIS * (k); return 0; }
     /* edge 0 */
     fx = fabsf(e0[0]); fy = fabsf(e0[1]); fz = fabsf(e0[2]);
     a_ = e0[2]; b_ = e0[1]; /* X01 */
-    if (orc_axis_sep(a_ * v0[1] - b_ * v0[2], a_ * v2[1] - b_ * v2[2], fz * h[1] + fy * h[2])) return 0;
+    ORC_SEP(1, a_ * v0[1] - b_ * v0[2], a_ * v2[1] - b_ * v2[2], fz * h[1] + fy * h[2])
     a_ = e0[2]; b_ = e0[0]; /* Y02 */
-    if (orc_axis_sep(-a_ * v0[0] + b_ * v0[2], -a_ * v2[0] + b_ * v2[2], fz * h[0] + fx * h[2])) return 0;
+    ORC_SEP(2, -a_ * v0[0] + b_ * v0[2], -a_ * v2[0] + b_ * v2[2], fz * h[0] + fx * h[2])
     a_ = e0[1]; b_ = e0[0]; /* Z12 */
-    if (orc_axis_sep(a_ * v1[0] - b_ * v1[1], a_ * v2[0] - b_ * v2[1], fy * h[0] + fx * h[1])) return 0;
+    ORC_SEP(3, a_ * v1[0] - b_ * v1[1], a_ * v2[0] - b_ * v2[1], fy * h[0] + fx * h[1])
     /* edge 1 */
     fx = fabsf(e1[0]); fy = fabsf(e1[1]); fz = fabsf(e1[2]);
     a_ = e1[2]; b_ = e1[1]; /* X01 */
-    if (orc_axis_sep(a_ * v0[1] - b_ * v0[2], a_ * v2[1] - b_ * v2[2], fz * h[1] + fy * h[2])) return 0;
+    ORC_SEP(4, a_ * v0[1] - b_ * v0[2], a_ * v2[1] - b_ * v2[2], fz * h[1] + fy * h[2])
     a_ = e1[2]; b_ = e1[0]; /* Y02 */
-    if (orc_axis_sep(-a_ * v0[0] + b_ * v0[2], -a_ * v2[0] + b_ * v2[2], fz * h[0] + fx * h[2])) return 0;
+    ORC_SEP(5, -a_ * v0[0] + b_ * v0[2], -a_ * v2[0] + b_ * v2[2], fz * h[0] + fx * h[2])
     a_ = e1[1]; b_ = e1[0]; /* Z0 */
-    if (orc_axis_sep(a_ * v0[0] - b_ * v0[1], a_ * v1[0] - b_ * v1[1], fy * h[0] + fx * h[1])) return 0;
+    ORC_SEP(6, a_ * v0[0] - b_ * v0[1], a_ * v1[0] - b_ * v1[1], fy * h[0] + fx * h[1])
     /* edge 2 */
     fx = fabsf(e2[0]); fy = fabsf(e2[1]); fz = fabsf(e2[2]);
     a_ = e2[2]; b_ = e2[1]; /* X2 */
-    if (orc_axis_sep(a_ * v0[1] - b_ * v0[2], a_ * v1[1] - b_ * v1[2], fz * h[1] + fy * h[2])) return 0;
+    ORC_SEP(7, a_ * v0[1] - b_ * v0[2], a_ * v1[1] - b_ * v1[2], fz * h[1] + fy * h[2])
     a_ = e2[2]; b_ = e2[0]; /* Y1 */
-    if (orc_axis_sep(-a_ * v0[0] + b_ * v0[2], -a_ * v1[0] + b_ * v1[2], fz * h[0] + fx * h[2])) return 0;
+    ORC_SEP(8, -a_ * v0[0] + b_ * v0[2], -a_ * v1[0] + b_ * v1[2], fz * h[0] + fx * h[2])
     a_ = e2[1]; b_ = e2[0]; /* Z12 */
-    if (orc_axis_sep(a_ * v1[0] - b_ * v1[1], a_ * v2[0] - b_ * v2[1], fy * h[0] + fx * h[1])) return 0;
+    ORC_SEP(9, a_ * v1[0] - b_ * v1[1], a_ * v2[0] - b_ * v2[1], fy * h[0] + fx * h[1])
+#undef ORC_SEP
     /* box axes: min/max of the translated vertices */
+    *ops = ORC_OPS_SAT_BOX;
     for (int a = 0; a < 3; ++a) {
         float mn = v0[a], mx = v0[a];
         if (v1[a] < mn) mn = v1[a];
@@ -149,7 +169,10 @@ static int orc_tri_box_own(const float c[3], const float h[3], const float *tv)
     nrm[0] = e0[1] * e1[2] - e0[2] * e1[1];
     nrm[1] = e0[2] * e1[0] - e0[0] * e1[2];
     nrm[2] = e0[0] * e1[1] - e0[1] * e1[0];
-    return orc_plane_box(nrm, v0, h);
+    int full = 0;
+    const int hit = orc_plane_box(nrm, v0, h, &full);
+    *ops = full ? ORC_OPS_SAT_FULL : ORC_OPS_SAT_PLANE;
+    return hit;
 }
 
 /* Moller-Trumbore ray/triangle test with a general direction, as src/TriRayIntersection.cpp:
@@ -195,26 +218,40 @@ typedef struct {
     float ox, oy;
 } orc_colhit;
 
+/* *ops receives the reference's executed operation count for one origin of this column: the
+ * det/u/v exits depend on the column only (D = +z), so every origin of the column takes the
+ * same exit, and origins that reach the t test run the whole test. */
+static int orc_ray_column_own(const float *tv, float ox, float oy, orc_colhit *st, int *ops)
+{
+    float e1x = tv[3] - tv[0], e1y = tv[4] - tv[1], e1z = tv[5] - tv[2];
+    float e2x = tv[6] - tv[0], e2y = tv[7] - tv[1], e2z = tv[8] - tv[2];
+    float det = e1x * (-e2y) + e1y * e2x;
+    *ops = ORC_OPS_RAY_DET;
+    if ((double)det > -0.000001 && (double)det < 0.000001) return 0;
+    float inv_det = 1.f / det;
+    float Tx = ox - tv[0], Ty = oy - tv[1];
+    float u = (Tx * (-e2y) + Ty * e2x) * inv_det;
+    *ops = ORC_OPS_RAY_U;
+    if (u < 0.f || u > 1.f) return 0;
+    float v = (Tx * e1y - Ty * e1x) * inv_det;
+    *ops = ORC_OPS_RAY_V;
+    if (v < 0.f || u + v > 1.f) return 0;
+    *ops = ORC_OPS_RAY_FULL;
+    st->e1[0] = e1x; st->e1[1] = e1y; st->e1[2] = e1z;
+    st->e2[0] = e2x; st->e2[1] = e2y; st->e2[2] = e2z;
+    st->inv_det = inv_det; st->Tx = Tx; st->Ty = Ty; st->v1z = tv[2];
+    return 1;
+}
+
 static int orc_ray_column(const float *tv, float ox, float oy, orc_colhit *st)
 {
 #ifdef ORC_REF_PREDICATES
     st->tv = tv; st->ox = ox; st->oy = oy;
     return 1;
+#else
+    int ops;
+    return orc_ray_column_own(tv, ox, oy, st, &ops);
 #endif
-    float e1x = tv[3] - tv[0], e1y = tv[4] - tv[1], e1z = tv[5] - tv[2];
-    float e2x = tv[6] - tv[0], e2y = tv[7] - tv[1], e2z = tv[8] - tv[2];
-    float det = e1x * (-e2y) + e1y * e2x;
-    if ((double)det > -0.000001 && (double)det < 0.000001) return 0;
-    float inv_det = 1.f / det;
-    float Tx = ox - tv[0], Ty = oy - tv[1];
-    float u = (Tx * (-e2y) + Ty * e2x) * inv_det;
-    if (u < 0.f || u > 1.f) return 0;
-    float v = (Tx * e1y - Ty * e1x) * inv_det;
-    if (v < 0.f || u + v > 1.f) return 0;
-    st->e1[0] = e1x; st->e1[1] = e1y; st->e1[2] = e1z;
-    st->e2[0] = e2x; st->e2[1] = e2y; st->e2[2] = e2z;
-    st->inv_det = inv_det; st->Tx = Tx; st->Ty = Ty; st->v1z = tv[2];
-    return 1;
 }
 
 /* t part of the +z test for one origin height. */
@@ -732,4 +769,107 @@ void orc_level2(const orc_run *r, int64_t b0, int64_t b1, uint8_t *out, int nthr
     }
     if (sat2_tests) *sat2_tests = s2;
     if (ray2_tests) *ray2_tests = r2;
+}
+
+/* Algorithmic FP32 work of the reference predicates over the tests the work counts define,
+ * early exits included (operation counts per exit above).  Level1 over the whole mesh, Level2
+ * over boundary voxels [b0, b1):
+ *   out[0] sat1 ops  (every candidate-box test of every triangle)
+ *   out[1] ray1 ops  (every column centre in a triangle's exact x/y box, times nz origins)
+ *   out[2] sat2 ops  (every triangle of a boundary voxel against its n2^3 sub-cells)
+ *   out[3] ray2 ops  (every triangle of the column union against the n2^3 Level2 origins) */
+void orc_count_ops(const orc_run *r, int64_t b0, int64_t b1, int nthreads, int64_t out[4])
+{
+    int nth = orc_threads(nthreads);
+    const int nx = r->s.n[0], ny = r->s.n[1], nz = r->s.n[2];
+    const int64_t T = r->T;
+    int64_t s1 = 0, r1 = 0, s2 = 0, r2 = 0;
+#pragma omp parallel for schedule(dynamic, 256) reduction(+ : s1, r1) num_threads(nth)
+    for (int64_t t = 0; t < T; ++t) {
+        const float *tv = r->tris + 9 * t;
+        int lo[3], hi[3], ops;
+        orc_tri_range(r, tv, lo, hi);
+        for (int p = lo[0]; p <= hi[0]; ++p)
+            for (int q = lo[1]; q <= hi[1]; ++q)
+                for (int k = lo[2]; k <= hi[2]; ++k) {
+                    float c3[3] = {r->t.c1[0][p], r->t.c1[1][q], r->t.c1[2][k]};
+                    orc_tri_box_own(c3, r->t.e1, tv, &ops);
+                    s1 += ops;
+                }
+        int clo[2], chi[2];
+        for (int a = 0; a < 2; ++a) {
+            float mn = tv[a], mx = tv[a];
+            for (int w = 1; w < 3; ++w) {
+                if (tv[3 * w + a] < mn) mn = tv[3 * w + a];
+                if (tv[3 * w + a] > mx) mx = tv[3 * w + a];
+            }
+            int n = a == 0 ? nx : ny;
+            clo[a] = orc_first_ge(r->t.c1[a], n, mn);
+            chi[a] = orc_last_le(r->t.c1[a], n, mx);
+        }
+        for (int j = clo[1]; j <= chi[1]; ++j)
+            for (int i = clo[0]; i <= chi[0]; ++i) {
+                orc_colhit st;
+                orc_ray_column_own(tv, r->t.c1[0][i], r->t.c1[1][j], &st, &ops);
+                r1 += (int64_t)ops * nz;
+            }
+    }
+    if (b1 > r->B) b1 = r->B;
+    const int n2x = r->s.n2[0], n2y = r->s.n2[1], n2z = r->s.n2[2];
+    if (n2x > 0 && b0 < b1) {
+#pragma omp parallel num_threads(nth) reduction(+ : s2, r2)
+        {
+            int32_t *uni = NULL;
+            int64_t ucap = 0;
+            uint8_t *mark = (uint8_t *)calloc((size_t)r->T + 1, 1);
+#pragma omp for schedule(dynamic, 16)
+            for (int64_t b = b0; b < b1; ++b) {
+                int64_t v = r->bindex[b];
+                int k = (int)(v / ((int64_t)nx * ny));
+                int64_t ij = v - (int64_t)k * nx * ny;
+                int j = (int)(ij / nx), i = (int)(ij % nx);
+                int64_t nu = 0;
+                for (int z = k; z < nz; ++z) {
+                    int64_t w = (int64_t)z * nx * ny + ij;
+                    for (int64_t e = r->vstart[w]; e < r->vstart[w + 1]; ++e) {
+                        int32_t t = r->vtris[e];
+                        if (mark[t]) continue;
+                        mark[t] = 1;
+                        if (nu == ucap) {
+                            ucap = ucap ? 2 * ucap : 256;
+                            uni = (int32_t *)realloc(uni, sizeof(int32_t) * (size_t)ucap);
+                        }
+                        uni[nu++] = t;
+                    }
+                }
+                for (int64_t e = 0; e < nu; ++e) mark[uni[e]] = 0;
+                const float *ox = r->t.o2[0] + (size_t)i * n2x;
+                const float *oy = r->t.o2[1] + (size_t)j * n2y;
+                for (int q = 0; q < n2y; ++q)
+                    for (int p = 0; p < n2x; ++p)
+                        for (int64_t e = 0; e < nu; ++e) {
+                            orc_colhit st;
+                            int ops;
+                            orc_ray_column_own(r->tris + 9 * (int64_t)uni[e], ox[p], oy[q], &st, &ops);
+                            r2 += (int64_t)ops * n2z;
+                        }
+                const float *sx = r->t.c2s[0] + (size_t)i * n2x;
+                const float *sy = r->t.c2s[1] + (size_t)j * n2y;
+                const float *sz = r->t.c2s[2] + (size_t)k * n2z;
+                for (int64_t e = r->vstart[v]; e < r->vstart[v + 1]; ++e) {
+                    const float *tv = r->tris + 9 * (int64_t)r->vtris[e];
+                    for (int p = 0; p < n2x; ++p)
+                        for (int q = 0; q < n2y; ++q)
+                            for (int rr = 0; rr < n2z; ++rr) {
+                                float c3[3] = {sx[p], sy[q], sz[rr]};
+                                int ops;
+                                orc_tri_box_own(c3, r->t.e2, tv, &ops);
+                                s2 += ops;
+                            }
+                }
+            }
+            free(uni); free(mark);
+        }
+    }
+    out[0] = s1; out[1] = r1; out[2] = s2; out[3] = r2;
 }

@@ -52,6 +52,7 @@ def _load(ref=False):
     L.orc_voxel_tris.argtypes = [vp, i64, vp, i64]
     L.orc_voxel_tris.restype = i64
     L.orc_level2.argtypes = [vp, i64, i64, vp, C.c_int, C.POINTER(i64), C.POINTER(i64)]
+    L.orc_count_ops.argtypes = [vp, i64, i64, C.c_int, vp]
     L.orc_tri_box.argtypes = [vp, vp, vp]
     L.orc_tri_ray.argtypes = [vp, vp, vp, vp, vp, C.POINTER(C.c_float)]
     L.orc_tri_ray_z.argtypes = [vp, vp]
@@ -138,6 +139,14 @@ class Run:
         if b1 > b0:
             self.L.orc_level2(self.h, int(b0), int(b1), _p(out), int(threads), C.byref(s2), C.byref(r2))
         return out, int(s2.value), int(r2.value)
+
+    def count_ops(self, b0=0, b1=None, threads=0):
+        """Executed FP32 operations of the reference predicates over the algorithmic tests
+        (early exits included): sat1/ray1 over the mesh, sat2/ray2 over boundary voxels [b0,b1)."""
+        b1 = self.B if b1 is None else b1
+        out = np.zeros(4, np.int64)
+        self.L.orc_count_ops(self.h, int(b0), int(b1), int(threads), _p(out))
+        return dict(zip(("sat1", "ray1", "sat2", "ray2"), (int(x) for x in out)))
 
     def level2_bytes(self, b0=0, b1=None, threads=0):
         st, _, _ = self.level2_state(b0, b1, threads)

@@ -75,3 +75,25 @@ def test_reference_sizing_formula():
     # maxModelSize/voxelCount and GetNextDiv4 (src/Object.cpp:3094-3107)
     assert orc.reference_divisions((0, 0, 0), (1.0, 0.5, 0.26), 1.0, 8) == (8, 4, 4)
     assert orc.reference_divisions((0, 0, 0), (1.0, 0.01, 0.3), 1.0, 10) == (12, 4, 4)
+
+
+def test_op_counts_fixture_sphere16k():
+    """The committed algorithmic-work fixture matches a fresh count, and every class's average
+    lies between its cheapest and dearest exit (SAT 27..124, ray 20..52 operations)."""
+    import json
+
+    import workloads as W
+
+    with open(os.path.join(GOLD, "op_counts.json")) as f:
+        fix = json.load(f)
+    tris, spec = W.make(W.C1)
+    run = orc.Run(tris, spec)
+    _, s2, r2 = run.level2_state(0, run.B)
+    ops = run.count_ops()
+    tests = {"sat1": run.sat1_tests(), "ray1": run.ray1_candidates(), "sat2": s2, "ray2": r2}
+    for k in tests:
+        assert fix["sphere16k"][k] == {"tests": tests[k], "ops": ops[k]}
+    for name in ("sphere16k", "torus262k", "star1310k"):
+        for k, (lo, hi) in {"sat1": (27, 124), "sat2": (27, 124), "ray1": (20, 52), "ray2": (20, 52)}.items():
+            e = fix[name][k]
+            assert lo * e["tests"] <= e["ops"] <= hi * e["tests"], (name, k)
