@@ -336,6 +336,22 @@ def run_reference(args):
 LEVEL2_INST_PER_LAUNCH = {"torus262k": 575574987}
 
 
+def max_over_ranks(seconds, dist, device):
+    """Replicas: every rank voxelizes its own copy; the job's time is the slowest rank's."""
+    if not dist:
+        return seconds
+    import torch
+
+    t = torch.tensor([seconds], device=device, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_value(tests_per_step, steps, world, seconds):
+    """Whole-job throughput: the tests all ranks processed over the slowest rank's time."""
+    return tests_per_step * steps * world / seconds
+
+
 def roofline(name, per_call, work, stats, spec, T, peaks, peak_kind, clk):
     """Roofline of the dominant kernel, k_level2c.
 
@@ -464,12 +480,9 @@ def main():
         dist.barrier()
     step_ms = [a.elapsed_time(b) for a, b in ev]
     t_total = sum(step_ms) / 1e3
-    if dist:
-        tt = torch.tensor([t_total], device=f"cuda:{local}", dtype=torch.float64)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t_total = float(tt.item())
+    t_total = max_over_ranks(t_total, dist, f"cuda:{local}")
     tests_per_step = sum(work)
-    value = tests_per_step * args.steps * world / t_total
+    value = job_value(tests_per_step, args.steps, world, t_total)
 
     # e2e through the host API: pinned H2D, voxelize, D2H of all outputs
     cells = spec.ndiv2[0] * spec.ndiv2[1] * spec.ndiv2[2]
@@ -501,16 +514,14 @@ def main():
         if k >= args.warmup:
             e2e_times.append(t1 - t0)
     e2e_t = sum(e2e_times)
-    if dist:
-        tt = torch.tensor([e2e_t], device=f"cuda:{local}", dtype=torch.float64)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        e2e_t = float(tt.item())
-    e2e_value = tests_per_step * args.steps * world / e2e_t
+    e2e_t = max_over_ranks(e2e_t, dist, f"cuda:{local}")
+    e2e_value = job_value(tests_per_step, args.steps, world, e2e_t)
     h2d = T * 36
     d2h = stats["level1"] * 5 + stats["boundary"] * (4 + cells)
 
     # roofline of the dominant kernel (the Level2 kernel: instruction-issue-bound integer/FP32 work)
     per_call = {k: v / max(calls, 1) for k, v in stage_ms.items()}
+    N1, B = stats["level1"], stats["boundary"]
     roof = roofline(cfg["name"], per_call, work, stats, spec, T, peaks, peak_kind, clk)
 
     line = {"metric": "tri-voxel tests/s", "value": value, "unit": "tests/s", "n_gpus": world,
@@ -527,7 +538,7 @@ def main():
             "e2e": {"value": e2e_value, "unit": "tests/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h, "ms_per_step": e2e_t * 1e3 / args.steps},
             "gpu_launches": launches, "roofline": roof, "clocks": clk}
-    tuned = (128, 16)
+    tuned = (128, 8)
     if args.batch > 0:
         line["batched"] = batch_bench(gpv, ctx, torch, stream, local, args)
         tuned = (line["batched"]["tile"], line["batched"]["level2_chunk"])

@@ -53,7 +53,12 @@ class Result(C.Structure):
                 ("num_level2_boundary", C.c_int64), ("num_pairs", C.c_int64), ("work", Work),
                 ("level1_inout", C.c_void_p), ("level1_prefix", C.c_void_p),
                 ("boundary_index", C.c_void_p), ("level2_inout", C.c_void_p),
-                ("handle", C.c_uint64)]
+                ("handle", C.c_uint64), ("level1_normal", C.c_void_p),
+                ("level2_normal", C.c_void_p), ("normal_mode", C.c_int32),
+                ("reserved", C.c_int32)]
+
+
+NORMALS_OFF, NORMALS_BYTES, NORMALS_FLOAT = 0, 1, 2
 
 
 class MeshC(C.Structure):
@@ -95,6 +100,10 @@ def lib():
     L.gpv_load_off.argtypes = [C.c_char_p, C.POINTER(MeshC)]
     L.gpv_mesh_free.argtypes = [C.POINTER(MeshC)]
     L.gpv_write_raw.argtypes = [C.c_char_p, C.POINTER(Result), C.c_void_p, C.c_void_p, C.c_void_p]
+    L.gpv_write_raw_normals.argtypes = [C.c_char_p, C.POINTER(Result), C.c_void_p, C.c_void_p]
+    L.gpv_set_normals.argtypes = [C.c_void_p, C.c_int]
+    L.gpv_result_copy_normals_to_host.argtypes = [C.c_void_p, C.POINTER(Result), C.c_void_p,
+                                                  C.c_void_p, C.c_void_p]
     for name, extra in (("gpv_gen_uvsphere", [C.c_int32, C.c_int32, f3, C.c_float, C.c_float]),
                         ("gpv_gen_torus", [C.c_int32, C.c_int32, f3, C.c_float, C.c_float, C.c_float]),
                         ("gpv_gen_star", [C.c_int32, f3, C.c_float, C.c_float, f3]),
@@ -301,6 +310,22 @@ class Context:
             "copy_to_host")
         return l1, pre, bi, l2
 
+    def set_normals(self, mode):
+        """NORMALS_OFF, NORMALS_BYTES (the .raw encoding) or NORMALS_FLOAT for the next calls."""
+        self._check(lib().gpv_set_normals(self._h, int(mode)), "set_normals")
+
+    def fetch_normals(self, res, stream=0):
+        """Copies a result's normals to host: (level1 [N1, 3], level2 [B*cells, 3]), uint8 or
+        float32 per the result's normal mode."""
+        cells = res.spec.ndiv2[0] * res.spec.ndiv2[1] * res.spec.ndiv2[2]
+        dt = np.float32 if res.normal_mode == NORMALS_FLOAT else np.uint8
+        l1 = np.empty((res.num_level1, 3), dt)
+        l2 = np.empty((res.num_boundary * cells, 3), dt)
+        self._check(lib().gpv_result_copy_normals_to_host(
+            self._h, C.byref(res), l1.ctypes.data_as(C.c_void_p), l2.ctypes.data_as(C.c_void_p),
+            C.c_void_p(stream)), "copy_normals_to_host")
+        return l1, l2
+
     def release(self, res):
         self._check(lib().gpv_result_release(self._h, C.byref(res)), "release")
 
@@ -333,6 +358,8 @@ class VoxelData:
         self.numLevel1BoundaryVoxels = int(res.num_boundary)
         self.numLevel2InsideVoxels = int(res.num_level2_inside)
         self.numLevel2BoundaryVoxels = int(res.num_level2_boundary)
+        self.level1Normal = None         # float32 [N1, 3] when computed
+        self.level2Normal = None         # float32 [B * n2^3, 3] when computed
 
 
 class Object:
@@ -373,8 +400,10 @@ class Object:
         self.flatCPUTriangleData = self._tris
         self.totalNumTriangles = self._tris.size // 9
 
-    def PerformVoxelization(self, glParam, bufferSize=-1, spec=None):
-        """Voxelizes on the GPU.  `spec` overrides the reference sizing (explicit grids)."""
+    def PerformVoxelization(self, glParam, bufferSize=-1, spec=None, normals=True):
+        """Voxelizes on the GPU.  `spec` overrides the reference sizing (explicit grids).  Normals
+        are computed as the reference does (float, src/Object.cpp:3219-3253, :2402-2424) unless
+        `normals` is False."""
         del bufferSize  # the device path has no fixed per-voxel buffer
         if self.flatCPUTriangleData is None:
             self.CreateFlatTriangleData()
@@ -383,12 +412,18 @@ class Object:
         if spec is None:
             spec = grid_reference(self.bBoxMin, self.bBoxMax, self.maxModelSize,
                                   glParam.voxelCount, glParam.voxelCount2 if glParam.level2Voxels else 0)
-        res = self.ctx.voxelize_host(self.flatCPUTriangleData, spec)
+        self.ctx.set_normals(NORMALS_FLOAT if normals else NORMALS_OFF)
+        try:
+            res = self.ctx.voxelize_host(self.flatCPUTriangleData, spec)
+        finally:
+            self.ctx.set_normals(NORMALS_OFF)
         try:
             l1, pre, bi, l2 = self.ctx.fetch(res)
+            nrm = self.ctx.fetch_normals(res) if normals else (None, None)
         finally:
             self._result = res
         self.voxelData = VoxelData(res, l1, pre, bi, l2)
+        self.voxelData.level1Normal, self.voxelData.level2Normal = nrm
         if glParam.saveVoxels:
             self.SaveVoxelization(glParam)
         self.ctx.release(res)
@@ -403,6 +438,20 @@ class Object:
                                  vd.level2InOut.ctypes.data_as(C.c_void_p))
         if rc:
             raise GpvError(rc, "SaveVoxelization")
+        if vd.level1Normal is not None:
+            n1 = normal_bytes(vd.level1Normal)
+            n2 = normal_bytes(vd.level2Normal)
+            rc = lib().gpv_write_raw_normals(prefix.encode(), C.byref(self._result),
+                                             n1.ctypes.data_as(C.c_void_p), n2.ctypes.data_as(C.c_void_p))
+            if rc:
+                raise GpvError(rc, "SaveVoxelization (normals)")
+
+
+def normal_bytes(n):
+    """The .raw encoding of normals, uint8(n * float(256/3) + 127) in float arithmetic
+    (src/Object.cpp:2940-2941, :3033-3035); the device's GPV_NORMALS_BYTES mode writes the same."""
+    n = np.ascontiguousarray(n, np.float32)
+    return (n * np.float32(256.0 / 3.0) + np.float32(127.0)).astype(np.int32).astype(np.uint8)
 
 
 class Server:

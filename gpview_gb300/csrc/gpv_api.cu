@@ -165,6 +165,8 @@ void gpv_destroy(gpv_ctx *ctx) {
     cudaFree(r->prefix);
     cudaFree(r->bindex);
     cudaFree(r->l2);
+    if (r->l1n) cudaFree(r->l1n);
+    if (r->l2n) cudaFree(r->l2n);
   }
   ctx->owned.clear();
   for (cudaGraphExec_t &ge : ctx->gexec)
@@ -203,6 +205,12 @@ uint64_t gpv_kernel_launches(void) { return gpv::launch_count(); }
 int gpv_set_graphs(gpv_ctx *ctx, int on) {
   if (!ctx) return GPV_ERR_INVALID;
   ctx->graphs = on != 0;
+  return GPV_OK;
+}
+
+int gpv_set_normals(gpv_ctx *ctx, int mode) {
+  if (!ctx || mode < GPV_NORMALS_OFF || mode > GPV_NORMALS_FLOAT) return GPV_ERR_INVALID;
+  ctx->normals = mode;
   return GPV_OK;
 }
 
@@ -314,6 +322,23 @@ int gpv_result_copy_to_host(gpv_ctx *ctx, const gpv_result *res, uint8_t *l1, in
   return GPV_OK;
 }
 
+int gpv_result_copy_normals_to_host(gpv_ctx *ctx, const gpv_result *res, void *l1n, void *l2n,
+                                    cudaStream_t s) {
+  if (!ctx || !res) return GPV_ERR_INVALID;
+  if (res->normal_mode == GPV_NORMALS_OFF || !res->level1_normal)
+    return ctx_fail(ctx, GPV_ERR_INVALID, "the result has no normals (gpv_set_normals)");
+  cudaSetDevice(ctx->device);
+  const int64_t cells = (int64_t)res->spec.ndiv2[0] * res->spec.ndiv2[1] * res->spec.ndiv2[2];
+  const int64_t vb = res->normal_mode == GPV_NORMALS_FLOAT ? 12 : 3;  // bytes per voxel / cell
+  if (l1n && res->num_level1)
+    GPV_CUDA(cudaMemcpyAsync(l1n, res->level1_normal, vb * res->num_level1, cudaMemcpyDeviceToHost, s));
+  if (l2n && res->num_boundary && cells)
+    GPV_CUDA(cudaMemcpyAsync(l2n, res->level2_normal, vb * res->num_boundary * cells,
+                             cudaMemcpyDeviceToHost, s));
+  GPV_CUDA(cudaStreamSynchronize(s));
+  return GPV_OK;
+}
+
 int gpv_result_release(gpv_ctx *ctx, gpv_result *res) {
   if (!ctx || !res) return GPV_ERR_INVALID;
   std::shared_ptr<ResultSet> set;
@@ -331,11 +356,15 @@ int gpv_result_release(gpv_ctx *ctx, gpv_result *res) {
     cudaFreeAsync(set->prefix, 0);
     cudaFreeAsync(set->bindex, 0);
     cudaFreeAsync(set->l2, 0);
+    if (set->l1n) cudaFreeAsync(set->l1n, 0);
+    if (set->l2n) cudaFreeAsync(set->l2n, 0);
   }
   res->level1_inout = nullptr;
   res->level1_prefix = nullptr;
   res->boundary_index = nullptr;
   res->level2_inout = nullptr;
+  res->level1_normal = nullptr;
+  res->level2_normal = nullptr;
   res->handle = 0;
   return GPV_OK;
 }

@@ -112,12 +112,15 @@ int run_batch(gpv_ctx *ctx, int n, const float *const *d_tris, const int64_t *T,
       return ctx_fail(ctx, GPV_ERR_INVALID, "triangle buffers must be 16-byte aligned");
   }
   const int tile = ctx->tile;
+  const int nmode = ctx->normals;
+  const size_t nsz = nmode == GPV_NORMALS_FLOAT ? sizeof(float) : 1;  // bytes per normal value
 
   // ---- sizes and per-mesh bases
-  std::vector<int64_t> tab_off(n + 1, 0), res_l1(n + 1, 0), res_pre(n + 1, 0);
+  std::vector<int64_t> tab_off(n + 1, 0), res_l1(n + 1, 0), res_pre(n + 1, 0), res_l1n(n + 1, 0);
   std::vector<MeshDesc> md(n);
   int64_t tris = 0, tiles = 0, fwarps = 0, rows = 0, words = 0, togg = 0;
   int max_keybits = 1, warp_words = 0;
+  int64_t max_T = 1;
   bool any_l2 = false;
   for (int m = 0; m < n; ++m) {
     const GridHost &g = gh[m];
@@ -138,9 +141,14 @@ int run_batch(gpv_ctx *ctx, int n, const float *const *d_tris, const int64_t *T,
     tab_off[m + 1] = tab_off[m] + table_floats(g);
     res_l1[m + 1] = res_l1[m] + (int64_t)al16(g.N1);
     res_pre[m + 1] = res_pre[m] + (int64_t)al16(g.N1);  // int32 elements, 64-byte aligned
+    res_l1n[m + 1] = res_l1n[m] + (int64_t)al16(3 * g.N1 * nsz);  // bytes
     max_keybits = std::max(max_keybits, g.key_bits);
+    max_T = std::max(max_T, T[m]);
     any_l2 = any_l2 || g.level2;
   }
+
+  int val_bits = 1;  // bits of the largest triangle id (normals: the sort's value digits)
+  while (val_bits < 31 && ((int64_t)1 << val_bits) < max_T) ++val_bits;
 
   Arena ws(s);
   // coordinate tables: one pinned staging copy
@@ -171,12 +179,19 @@ int run_batch(gpv_ctx *ctx, int n, const float *const *d_tris, const int64_t *T,
   CK(cudaMemsetAsync(stats, 0, n * sizeof(MeshStats), s));
   CK(cudaMemsetAsync(bplane, 0, words * 4, s));
   CK(cudaMemsetAsync(toggles, 0, togg * 4, s));
+  float4 *fnorm = nullptr;
+  if (nmode) CK(ws.get(&fnorm, (size_t)std::max<int64_t>(tris, 1)));
 
   // result arenas (shared by the batch's results, freed when the last one is released)
   auto set = std::make_shared<ResultSet>();
   set->stream = s;
   CK(cudaMallocAsync(&set->l1, std::max<int64_t>(res_l1[n], 16), s));
   CK(cudaMallocAsync(&set->prefix, 4 * std::max<int64_t>(res_pre[n], 16), s));
+  if (nmode) {
+    // voxels without recorded triangles keep the zero normal: 0.0f, or byte 127 (0 * scale + 127)
+    CK(cudaMallocAsync(&set->l1n, std::max<int64_t>(res_l1n[n], 16), s));
+    CK(cudaMemsetAsync(set->l1n, nmode == GPV_NORMALS_FLOAT ? 0 : 127, res_l1n[n], s));
+  }
 
   int64_t togg_off = 0;
   for (int m = 0; m < n; ++m) {
@@ -195,6 +210,9 @@ int run_batch(gpv_ctx *ctx, int n, const float *const *d_tris, const int64_t *T,
     d.l1 = static_cast<uint8_t *>(set->l1) + res_l1[m];
     d.prefix = static_cast<int32_t *>(set->prefix) + res_pre[m];
     d.ch = g.level2 ? level2_chunk(d.g, ctx->l2_chunk_cap) : 1;
+    d.has_l2 = g.level2 ? 1 : 0;
+    d.fnorm = fnorm ? fnorm + d.tri_base : nullptr;
+    d.l1n = nmode ? static_cast<uint8_t *>(set->l1n) + res_l1n[m] : nullptr;
     if (g.level2) warp_words = std::max(warp_words, level2_warp_words(d.g, ctx->l2_chunk_cap));
   }
   BatchDev bd;
@@ -207,6 +225,7 @@ int run_batch(gpv_ctx *ctx, int n, const float *const *d_tris, const int64_t *T,
   bd.total_rows = rows;
   bd.total_words = words;
   bd.queue = queue;
+  bd.normals = nmode;
   CK(ctx_ensure_host(ctx, (size_t)n));
   std::memcpy(ctx->h_md, md.data(), n * sizeof(MeshDesc));
   CK(cudaMemcpyAsync(d_md, ctx->h_md, n * sizeof(MeshDesc), cudaMemcpyHostToDevice, s));
@@ -222,7 +241,9 @@ int run_batch(gpv_ctx *ctx, int n, const float *const *d_tris, const int64_t *T,
     cudaFreeAsync(set->prefix, s);
     if (set->bindex) cudaFreeAsync(set->bindex, s);
     if (set->l2) cudaFreeAsync(set->l2, s);
-    set->l1 = set->prefix = set->bindex = set->l2 = nullptr;
+    if (set->l1n) cudaFreeAsync(set->l1n, s);
+    if (set->l2n) cudaFreeAsync(set->l2n, s);
+    set->l1 = set->prefix = set->bindex = set->l2 = set->l1n = set->l2n = nullptr;
     return ctx_fail(ctx, code, msg);
   };
 
@@ -268,10 +289,11 @@ int run_batch(gpv_ctx *ctx, int n, const float *const *d_tris, const int64_t *T,
   for (int m = 0; m < n; ++m) {
     const MeshStats &st = ctx->h_stats[m];
     if (st.status) return fail_all(GPV_ERR_DEVICE, "device status raised in Level1");
-    // dense pair / boundary-voxel bases over the meshes with a Level2 stage (only they are sorted)
+    // dense pair / boundary-voxel bases over the sorted meshes: those with a Level2 stage, and
+    // every mesh when normals are on
     md[m].pair_base = P2;
     md[m].u_base = ub;
-    if (gh[m].level2) {
+    if (gh[m].level2 || nmode) {
       P2 += (int64_t)st.pairs;
       ub += (int64_t)st.boundary;
     }
@@ -282,6 +304,10 @@ int run_batch(gpv_ctx *ctx, int n, const float *const *d_tris, const int64_t *T,
   l2bytes = l2off[n];
   CK(cudaMallocAsync(&set->bindex, 4 * std::max<int64_t>(Btot, 4), s));
   CK(cudaMallocAsync(&set->l2, std::max<int64_t>(l2bytes, 16), s));
+  if (nmode) {
+    CK(cudaMallocAsync(&set->l2n, std::max<int64_t>(3 * l2bytes * (int64_t)nsz, 16), s));
+    for (int m = 0; m < n; ++m) md[m].l2n = static_cast<uint8_t *>(set->l2n) + 3 * l2off[m] * nsz;
+  }
   for (int m = 0; m < n; ++m) {
     md[m].bindex = static_cast<int32_t *>(set->bindex) + boff[m];
     md[m].l2 = static_cast<uint8_t *>(set->l2) + l2off[m];
@@ -291,7 +317,7 @@ int run_batch(gpv_ctx *ctx, int n, const float *const *d_tris, const int64_t *T,
   std::vector<int64_t> stb(n + 1, 0);
   for (int m = 0; m < n; ++m) {
     const int64_t Pm = (int64_t)ctx->h_stats[m].pairs;
-    const int64_t nt = gh[m].level2 ? (Pm + kSortTileItems - 1) / kSortTileItems : 0;
+    const int64_t nt = (gh[m].level2 || nmode) ? (Pm + kSortTileItems - 1) / kSortTileItems : 0;
     for (int64_t j = 0; j < nt; ++j)
       st_host.push_back({m, (int32_t)j, (int32_t)std::min<int64_t>(kSortTileItems, Pm - j * kSortTileItems), 0});
     stb[m + 1] = stb[m] + nt;
@@ -301,7 +327,7 @@ int run_batch(gpv_ctx *ctx, int n, const float *const *d_tris, const int64_t *T,
 
   // ---- phase C: allocations and uploads first, then the recorded launch sequence
   const int64_t ntiles = (int64_t)st_host.size();
-  const bool do_l2 = any_l2 && ntiles > 0;
+  const bool do_l2 = (any_l2 || nmode) && ntiles > 0;  // sort + lists (+ Level2, normals)
   SortTile *d_tiles = nullptr;
   int64_t *d_tb = nullptr;
   uint32_t *kalt = nullptr, *valt = nullptr, *flags = nullptr, *uidx = nullptr, *useg = nullptr,
@@ -328,14 +354,21 @@ int run_batch(gpv_ctx *ctx, int n, const float *const *d_tris, const int64_t *T,
     mark(6);
     if (do_l2) {
       const bool in_alt = sort_pairs_seg(bd, d_tiles, d_tb, ntiles, keys, vals, kalt, valt, P2,
-                                         max_keybits, sortmp, s);
+                                         max_keybits, nmode ? val_bits : 0, sortmp, s);
       const uint32_t *sk = in_alt ? kalt : keys;
       const uint32_t *sv = in_alt ? valt : vals;
       launch_heads(sk, P2, flags, bd, s);
       scan_u32(flags, uidx, P2, wtot + 1, sortmp, s);
       launch_useg(flags, uidx, P2, useg, s);
       mark(7);
-      launch_level2(bd, sk, sv, useg, ub, l2tmp, warp_words, ctx->num_sms, s, [&] { mark(9); });
+      if (any_l2)
+        launch_level2(bd, sk, sv, useg, ub, l2tmp, warp_words, ctx->num_sms, s, [&] { mark(9); });
+      else
+        mark(9);
+      if (nmode) {
+        launch_face_normals(bd, s);
+        launch_normals(bd, sk, sv, useg, ub, any_l2, ctx->num_sms, s);
+      }
     } else {
       mark(7);
       mark(9);
@@ -394,6 +427,11 @@ int run_batch(gpv_ctx *ctx, int n, const float *const *d_tris, const int64_t *T,
     r.boundary_index = static_cast<int32_t *>(set->bindex) + boff[m];
     r.level2_inout = static_cast<uint8_t *>(set->l2) + l2off[m];
     r.handle = handle;
+    r.normal_mode = nmode;
+    if (nmode) {
+      r.level1_normal = static_cast<uint8_t *>(set->l1n) + res_l1n[m];
+      r.level2_normal = static_cast<uint8_t *>(set->l2n) + 3 * l2off[m] * nsz;
+    }
   }
   return GPV_OK;
 #undef CK

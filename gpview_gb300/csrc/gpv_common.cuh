@@ -83,14 +83,20 @@ struct SatCol {
   float e0x, e0y, e1x, e1y, e2x, e2y;
 };
 
-// z-invariant part: the three Z-axis edge tests and the x/y box axes.  False = separated.
-__device__ __forceinline__ bool sat_col(const float *V, float cx, float cy, const float h[3],
-                                        SatCol &s) {
+// The translated x/y vertex coordinates and edges of sat_col, without its tests (for a column
+// already known to pass them).
+__device__ __forceinline__ void sat_col_values(const float *V, float cx, float cy, SatCol &s) {
   s.v0x = fs(V[0], cx); s.v1x = fs(V[3], cx); s.v2x = fs(V[6], cx);
   s.v0y = fs(V[1], cy); s.v1y = fs(V[4], cy); s.v2y = fs(V[7], cy);
   s.e0x = fs(s.v1x, s.v0x); s.e0y = fs(s.v1y, s.v0y);
   s.e1x = fs(s.v2x, s.v1x); s.e1y = fs(s.v2y, s.v1y);
   s.e2x = fs(s.v0x, s.v2x); s.e2y = fs(s.v0y, s.v2y);
+}
+
+// z-invariant part: the three Z-axis edge tests and the x/y box axes.  False = separated.
+__device__ __forceinline__ bool sat_col(const float *V, float cx, float cy, const float h[3],
+                                        SatCol &s) {
+  sat_col_values(V, cx, cy, s);
   float fx, fy;
   // edge 0, Z12: a = e0y, b = e0x on v1, v2
   fx = fabsf(s.e0x); fy = fabsf(s.e0y);
@@ -164,6 +170,25 @@ __device__ __forceinline__ bool sat_z(const SatCol &s, const float *V, float cz,
   else           { lo2 = fs(h[2], v0z);    hi2 = fs(-h[2], v0z); }
   if (fa(fa(fm(nx, lo0), fm(ny, lo1)), fm(nz, lo2)) > 0.0f) return false;
   return fa(fa(fm(nx, hi0), fm(ny, hi1)), fm(nz, hi2)) >= 0.0f;
+}
+
+// Sub-cells along one axis whose box can meet [tmin, tmax].  Cell p spans
+// [c2s[p] - h, c2s[p] + h] ~ [vmin + p g2, vmin + (p+1) g2]; a cell whose box misses
+// [tmin - delta, tmax + delta] is rejected by the SAT's own box-axis test (delta covers the
+// rounding of the coordinates and of this computation, the 1e-3 cell margin that of the
+// quotient).
+__device__ __forceinline__ void l2_cell_range(float tmin, float tmax, float c0, float h,
+                                              float inv_g2, int n2, int &lo, int &hi) {
+  const float vmin = c0 - h;
+  const float delta = 8.f * 5.9604644775390625e-08f * (fabsf(tmin) + fabsf(tmax) + fabsf(vmin) + h) + 1e-30f;
+  // first p with vmin + (p+1) g2 >= tmin - delta, last p with vmin + p g2 <= tmax + delta
+  // (the reciprocal's rounding moves the quotients by far less than the 1e-3 cell margin)
+  float f0 = (tmin - delta - vmin) * inv_g2 - 1e-3f;
+  float f1 = (tmax + delta - vmin) * inv_g2 + 1e-3f;
+  f0 = fminf(fmaxf(f0, -4.f), (float)n2 + 4.f);
+  f1 = fminf(fmaxf(f1, -4.f), (float)n2 + 4.f);
+  lo = max((int)floorf(f0), 0);
+  hi = min((int)floorf(f1), n2 - 1);
 }
 
 __device__ __forceinline__ bool tri_box(const float *V, const float c[3], const float h[3]) {

@@ -12,6 +12,7 @@ namespace gpv {
 // Result arrays of one batch; every result of the batch holds a reference.
 struct ResultSet {
   void *l1 = nullptr, *prefix = nullptr, *bindex = nullptr, *l2 = nullptr;
+  void *l1n = nullptr, *l2n = nullptr;  // normals (optional)
   cudaStream_t stream = 0;
   int refs = 0;
 };
@@ -28,8 +29,9 @@ struct gpv_ctx {
   uint64_t stage_calls = 0;
   std::string err;
   int tile = 128;                      // Level1 triangles per tile (autotuned)
-  int l2_chunk_cap = 32;               // Level2 boundary voxels per chunk, upper bound (autotuned)
+  int l2_chunk_cap = 8;                // Level2 boundary voxels per chunk, upper bound (autotuned)
   bool graphs = true;                  // record phases B and C as CUDA graphs
+  int normals = 0;                     // GPV_NORMALS_* for the next voxelizations
   cudaGraphExec_t gexec[2] = {};       // cached executable graphs of phases B and C
   uint64_t graph_launches = 0, graph_instantiations = 0;
   gpv::MeshStats *h_stats = nullptr;   // pinned, h_cap entries

@@ -69,7 +69,9 @@ struct MeshDesc {
   int64_t pair_base;     // ... of pairs (dense layout after the sort)
   int64_t u_base;        // ... of boundary voxels
   int32_t ch;            // Level2 chunk length
-  int32_t pad;
+  int32_t has_l2;        // the mesh has a Level2 grid
+  float4 *fnorm;         // normals on: normalised face normal per triangle
+  void *l1n, *l2n;       // normals on: Level1 / Level2 normal outputs (bytes or floats)
 };
 
 struct BatchDev {
@@ -78,6 +80,7 @@ struct BatchDev {
   int tile;              // Level1 triangles per tile (32, 64, 128, 256)
   int64_t total_tris, total_tiles, total_fwarps, total_rows, total_words;
   uint32_t *queue;       // work-queue tickets, zeroed before each persistent launch
+  int normals;           // GPV_NORMALS_* of this batch
 };
 
 void launch_prep(const BatchDev &bd, cudaStream_t s);
@@ -99,7 +102,7 @@ int64_t sort_seg_temp_words(int64_t ntiles);
 // every mesh; hist_base[m] = 256 * (tiles before mesh m) (device).
 bool sort_pairs_seg(const BatchDev &bd, const SortTile *tiles, const int64_t *tile_base_dev,
                     int64_t ntiles, uint32_t *keys, uint32_t *vals, uint32_t *kalt, uint32_t *valt,
-                    int64_t Ptotal, int key_bits, uint32_t *temp, cudaStream_t s);
+                    int64_t Ptotal, int key_bits, int val_bits, uint32_t *temp, cudaStream_t s);
 constexpr int kSortTileItems = 2048;
 
 int level2_chunk(const GridDev &g, int cap = 32);
@@ -110,6 +113,12 @@ int64_t level2_temp_words(int64_t Btot);
 void launch_level2(const BatchDev &bd, const uint32_t *keys, const uint32_t *vals,
                    const uint32_t *useg, int64_t Btot, uint32_t *tmp, int warp_words, int num_sms,
                    cudaStream_t s, const std::function<void()> &before_kernel = {});
+
+// ---- normals (gpv_normals.cu) ----------------------------------------------------------------
+void launch_face_normals(const BatchDev &bd, cudaStream_t s);
+// Level1 normals of the U boundary voxels of the sorted meshes, then (any_l2) Level2 normals.
+void launch_normals(const BatchDev &bd, const uint32_t *keys, const uint32_t *vals,
+                    const uint32_t *useg, int64_t U, bool any_l2, int num_sms, cudaStream_t s);
 
 GridDev make_griddev(const GridHost &gh, const float *dtables);
 int64_t table_floats(const GridHost &gh);

@@ -44,25 +44,6 @@ __device__ __forceinline__ T warp_sum(T v) {
   return v;
 }
 
-// Sub-cells along one axis whose box can meet [tmin, tmax].  Cell p spans
-// [c2s[p] - h, c2s[p] + h] ~ [vmin + p g2, vmin + (p+1) g2]; a cell whose box misses
-// [tmin - delta, tmax + delta] is rejected by the SAT's own box-axis test (delta covers the
-// rounding of the coordinates and of this computation, the 1e-3 cell margin that of the
-// quotient).
-__device__ __forceinline__ void l2_range(float tmin, float tmax, float c0, float h, float inv_g2,
-                                         int n2, int &lo, int &hi) {
-  const float vmin = c0 - h;
-  const float delta = 8.f * EPS24 * (fabsf(tmin) + fabsf(tmax) + fabsf(vmin) + h) + 1e-30f;
-  // first p with vmin + (p+1) g2 >= tmin - delta, last p with vmin + p g2 <= tmax + delta
-  // (the reciprocal's rounding moves the quotients by far less than the 1e-3 cell margin)
-  float f0 = (tmin - delta - vmin) * inv_g2 - 1e-3f;
-  float f1 = (tmax + delta - vmin) * inv_g2 + 1e-3f;
-  f0 = fminf(fmaxf(f0, -4.f), (float)n2 + 4.f);
-  f1 = fminf(fmaxf(f1, -4.f), (float)n2 + 4.f);
-  lo = max((int)floorf(f0), 0);
-  hi = min((int)floorf(f1), n2 - 1);
-}
-
 // Slab of cell centres the triangle's plane test can accept.  For a cell centre c the SAT's
 // plane test (planeBoxOverlap on the box-relative, rounded edges) can only pass when
 //   |n_f . (V0 - c)| <= |n_f| . h + E,
@@ -96,11 +77,6 @@ __device__ __forceinline__ PlaneSlab plane_slab(const float *V, float cx0, float
 }
 
 // Bits of one Level2 column (n2z cells along z) start at bit (q*n2x + p)*n2z of a voxel's mask.
-__device__ __forceinline__ void or_column(uint32_t *m, int colidx, int n2z, uint32_t bits) {
-  const int off = colidx * n2z, sh = off & 31;
-  atomicOr(&m[off >> 5], bits << sh);
-  if (sh + n2z > 32) atomicOr(&m[(off >> 5) + 1], bits >> (32 - sh));
-}
 __device__ __forceinline__ void xor_column(uint32_t *m, int colidx, int n2z, uint32_t bits) {
   const int off = colidx * n2z, sh = off & 31;
   atomicXor(&m[off >> 5], bits << sh);
@@ -131,7 +107,12 @@ struct WarpScratch {
   float x[32][4];     // slab (SAT) or (1/det, well-conditioned flag) (fill)
   uint32_t rng[32];   // packed sub-cell ranges
   uint32_t pre[33];   // exclusive prefix of item counts
-  int jm[32];         // fill: voxels of the chunk below the triangle's topmost voxel
+  int jm[32];         // SAT: the triangle's voxel in the chunk; fill: voxels of the chunk below
+                      // the triangle's topmost voxel
+  uint32_t zrec[32];  // SAT: (triangle slot, p, q) of a sub-column item
+  uint32_t zmask[32]; // SAT: cells of that sub-column left for the full test
+  uint32_t zpre[33];  // SAT: exclusive prefix of the cell counts
+  uint32_t seg[33];   // SAT: first pair of each voxel of the chunk, and the end
 };
 
 // ---- item construction -----------------------------------------------------------------------
@@ -170,9 +151,10 @@ __global__ void k_itemflags(BatchDev bd, const uint32_t *__restrict__ cflag,
                             int64_t B, uint32_t *__restrict__ iflag) {
   const int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (u >= B) return;
-  const int CH = bd.md[mesh_of_u(bd.md, bd.nmesh, u)].ch;
+  const MeshDesc &d = bd.md[mesh_of_u(bd.md, bd.nmesh, u)];
   const uint32_t c = cord[u] + cflag[u] - 1u;
-  iflag[u] = ((u - colhead[c]) % CH == 0) ? 1u : 0u;
+  // meshes without a Level2 grid (sorted for their normals only) get no Level2 work items
+  iflag[u] = (d.has_l2 && (u - colhead[c]) % d.ch == 0) ? 1u : 0u;
 }
 
 __global__ void k_itemstarts(const uint32_t *__restrict__ iflag, const uint32_t *__restrict__ iord,
@@ -184,7 +166,7 @@ __global__ void k_itemstarts(const uint32_t *__restrict__ iflag, const uint32_t 
 }
 
 // ---- Level2 ------------------------------------------------------------------------------------
-__global__ void __launch_bounds__(kWarps * 32, 5) k_level2c(
+__global__ void __launch_bounds__(kWarps * 32, 6) k_level2c(
     BatchDev bd, const uint32_t *__restrict__ keys, const uint32_t *__restrict__ vals,
     const uint32_t *__restrict__ useg, const uint32_t *__restrict__ cflag,
     const uint32_t *__restrict__ cord, const uint32_t *__restrict__ colhead,
@@ -219,7 +201,9 @@ __global__ void __launch_bounds__(kWarps * 32, 5) k_level2c(
 
   const uint32_t ucol_end = colhead[cord[ua] + cflag[ua]];  // first voxel of the next column
   const int m = (int)min((uint32_t)CH, ucol_end - ua);
-  for (int w = lane; w < 2 * CH * W + CH * FW; w += 32) sat[w] = 0;
+  // clear the masks of the chunk's m voxels only (the arrays are sized for CH voxels)
+  for (int w = lane; w < m * W; w += 32) { sat[w] = 0; par[w] = 0; }
+  for (int w = lane; w < m * FW; w += 32) ft[w] = 0;
   const int nx = g.n[0], ny = g.n[1], nz = g.n[2];
   const uint32_t col = keys[useg[ua]] / (uint32_t)nz;
   const int ci = (int)(col % (uint32_t)nx), cj = (int)(col / (uint32_t)nx);
@@ -230,27 +214,33 @@ __global__ void __launch_bounds__(kWarps * 32, 5) k_level2c(
   const float *ox = g.o2[0] + (size_t)ci * n2x, *oy = g.o2[1] + (size_t)cj * n2y;
   const float sx0 = __ldg(sx), sx1 = __ldg(sx + n2x - 1), sy0 = __ldg(sy), sy1 = __ldg(sy + n2y - 1);
 
-  // ---------------- SAT of each voxel's own triangles
-  for (int jv = 0; jv < m; ++jv) {
-    const int k = kz[jv];
-    const float *sz = g.c2s[2] + (size_t)k * n2z;
-    const float sz0 = __ldg(sz), sz1 = __ldg(sz + n2z - 1);
-    const uint32_t s0 = useg[ua + jv], s1 = useg[ua + jv + 1];
-    uint32_t *satj = sat + jv * W;
-    for (uint32_t b0 = s0; b0 < s1; b0 += 32) {
+  // ---------------- SAT of each voxel's own triangles: the chunk's (voxel, triangle) pairs are
+  // contiguous in the sorted lists and are taken 32 at a time across voxel boundaries.
+  if ((int)lane < m) ws.seg[lane] = useg[ua + lane];
+  if (lane == 0) ws.seg[m] = useg[ua + m];
+  __syncwarp();
+  {
+    const uint32_t S0 = ws.seg[0], S1 = ws.seg[m];
+    for (uint32_t b0 = S0; b0 < S1; b0 += 32) {
       const uint32_t e = b0 + lane;
       uint32_t cnt = 0;
-      if (e < s1) {
+      if (e < S1) {
+        int jv = 0;  // last voxel whose segment starts at or before e
+#pragma unroll
+        for (int st = 16; st > 0; st >>= 1)
+          if (jv + st <= m - 1 && ws.seg[jv + st] <= e) jv += st;
+        const float *sz = g.c2s[2] + (size_t)kz[jv] * n2z;
+        const float sz0 = __ldg(sz), sz1 = __ldg(sz + n2z - 1);
         const uint32_t t = vals[e] & 0x7fffffffu;
         const float4 a0 = __ldg(ptri + 3 * (size_t)t), a1 = __ldg(ptri + 3 * (size_t)t + 1),
                      a2 = __ldg(ptri + 3 * (size_t)t + 2);
         const float V[9] = {a0.x, a0.y, a0.z, a1.x, a1.y, a1.z, a2.x, a2.y, a2.z};
         int p0, p1, q0, q1, r0, r1;
-        l2_range(fminf(V[0], fminf(V[3], V[6])), fmaxf(V[0], fmaxf(V[3], V[6])), sx0, g.e2[0],
+        l2_cell_range(fminf(V[0], fminf(V[3], V[6])), fmaxf(V[0], fmaxf(V[3], V[6])), sx0, g.e2[0],
                  g.inv_g2[0], n2x, p0, p1);
-        l2_range(fminf(V[1], fminf(V[4], V[7])), fmaxf(V[1], fmaxf(V[4], V[7])), sy0, g.e2[1],
+        l2_cell_range(fminf(V[1], fminf(V[4], V[7])), fmaxf(V[1], fmaxf(V[4], V[7])), sy0, g.e2[1],
                  g.inv_g2[1], n2y, q0, q1);
-        l2_range(fminf(V[2], fminf(V[5], V[8])), fmaxf(V[2], fmaxf(V[5], V[8])), sz0, g.e2[2],
+        l2_cell_range(fminf(V[2], fminf(V[5], V[8])), fmaxf(V[2], fmaxf(V[5], V[8])), sz0, g.e2[2],
                  g.inv_g2[2], n2z, r0, r1);
         if (p0 <= p1 && q0 <= q1 && r0 <= r1) {
           const PlaneSlab ps = plane_slab(V, sx0, sx1, sy0, sy1, sz0, sz1, g.e2);
@@ -260,6 +250,7 @@ __global__ void __launch_bounds__(kWarps * 32, 5) k_level2c(
           const int np = p1 - p0 + 1;
           ws.rng[lane] = (uint32_t)p0 | ((uint32_t)np << 6) | ((uint32_t)q0 << 12) |
                          ((uint32_t)r0 << 18) | ((uint32_t)r1 << 24);
+          ws.jm[lane] = jv;
           cnt = (uint32_t)(np * (q1 - q0 + 1));
         }
       }
@@ -267,55 +258,90 @@ __global__ void __launch_bounds__(kWarps * 32, 5) k_level2c(
       ws.pre[lane] = inc - cnt;
       const uint32_t tot = __shfl_sync(FULL, inc, 31);
       __syncwarp();
-      for (uint32_t w = lane; w < tot; w += 32) {
-        const int tl = batch_search(ws.pre, w);
-        const uint32_t loc = w - ws.pre[tl];
-        const uint32_t rg = ws.rng[tl];
-        const int np = (int)((rg >> 6) & 63u);
-        // loc / np by a float reciprocal: exact here (loc < 1024, np <= 32, so the quotient of
-        // loc + 1/2 stays at least 1/64 away from an integer, far above the rounding)
-        const int qq = __float2int_rz(((float)loc + 0.5f) * __frcp_rn((float)np));
-        const int p = (int)(rg & 63u) + (int)loc - qq * np;
-        const int q = (int)((rg >> 12) & 63u) + qq;
-        const int r0 = (int)((rg >> 18) & 63u), r1 = (int)((rg >> 24) & 63u);
-        float V[9];
+      // (triangle, sub-column) items, 32 at a time: z-invariant SAT part and the plane slab
+      // select the cells left for the full test; then those (triangle, cell) tests run 32 at a
+      // time so that the lanes stay busy whatever the per-column cell counts.
+      for (uint32_t wb = 0; wb < tot; wb += 32) {
+        const uint32_t w = wb + lane;
+        uint32_t zm = 0, rec = 0;
+        if (w < tot) {
+          const int tl = batch_search(ws.pre, w);
+          const uint32_t loc = w - ws.pre[tl];
+          const uint32_t rg = ws.rng[tl];
+          const int np = (int)((rg >> 6) & 63u);
+          // loc / np by a float reciprocal: exact here (loc < 1024, np <= 32, so the quotient of
+          // loc + 1/2 stays at least 1/64 away from an integer, far above the rounding)
+          const int qq = __float2int_rz(((float)loc + 0.5f) * __frcp_rn((float)np));
+          const int p = (int)(rg & 63u) + (int)loc - qq * np;
+          const int q = (int)((rg >> 12) & 63u) + qq;
+          const int r0 = (int)((rg >> 18) & 63u), r1 = (int)((rg >> 24) & 63u);
+          const int jv = ws.jm[tl];
+          const uint32_t *satj = sat + jv * W;
+          const float *sz = g.c2s[2] + (size_t)kz[jv] * n2z;
+          const float sz0 = __ldg(sz), sz1 = __ldg(sz + n2z - 1);
+          // cells of this column already marked by another triangle need no test (OR only)
+          const int off = (q * n2x + p) * n2z, sh = off & 31;
+          uint32_t done = satj[off >> 5] >> sh;
+          if (sh + n2z > 32) done |= satj[(off >> 5) + 1] << (32 - sh);
+          const uint32_t rmask = ((r1 - r0 + 1) >= 32 ? 0xffffffffu : ((1u << (r1 - r0 + 1)) - 1u)) << r0;
+          if ((~done & rmask) != 0) {
+            float V[9];
 #pragma unroll
-        for (int qq = 0; qq < 9; ++qq) V[qq] = ws.v[tl][qq];
-        // cells of this column already marked by another triangle need no test (OR only)
-        const int off = (q * n2x + p) * n2z, sh = off & 31;
-        uint32_t done = satj[off >> 5] >> sh;
-        if (sh + n2z > 32) done |= satj[(off >> 5) + 1] << (32 - sh);
-        const uint32_t rmask = ((r1 - r0 + 1) >= 32 ? 0xffffffffu : ((1u << (r1 - r0 + 1)) - 1u)) << r0;
-        if ((~done & rmask) == 0) continue;
-        const float cx = __ldg(sx + p), cy = __ldg(sy + q);
-        SatCol s;
-        if (!sat_col(V, cx, cy, g.e2, s)) continue;
-        const float nxs = ws.x[tl][0], nys = ws.x[tl][1], nzs = ws.x[tl][2], H = ws.x[tl][3];
-        const float sxy = fa(fm(nxs, fs(V[0], cx)), fm(nys, fs(V[1], cy)));
-        // The per-cell slab test |sxy + nz (V0z - cz)| <= H can only pass for cz within
-        // H/|nz| of V0z + sxy/nz; the interval is widened by the float error of that test (a few
-        // ulps of its terms, over |nz|) and one cell, and the exact per-cell test still runs.
-        int ra = r0, rb = r1;
-        if (fabsf(nzs) > 0.f) {
-          const float rnz = __frcp_rn(nzs);
-          const float zc = V[2] + sxy * rnz;
-          const float ext = (H + 8.f * EPS24 * (fabsf(sxy) + fabsf(nzs) * (fabsf(V[2]) + fabsf(sz0) +
-                                                                           fabsf(sz1)))) * fabsf(rnz);
-          const float igz = g.inv_g2[2];
-          const float fa0 = (zc - ext - sz0) * igz - 1.f, fb0 = (zc + ext - sz0) * igz + 1.f;
-          if (fa0 > -2.f) ra = max(ra, (int)floorf(fminf(fa0, (float)n2z + 2.f)));
-          if (fb0 < (float)n2z + 2.f) rb = min(rb, (int)ceilf(fmaxf(fb0, -2.f)));
+            for (int c = 0; c < 9; ++c) V[c] = ws.v[tl][c];
+            const float cx = __ldg(sx + p), cy = __ldg(sy + q);
+            SatCol sc;
+            if (sat_col(V, cx, cy, g.e2, sc)) {
+              const float nxs = ws.x[tl][0], nys = ws.x[tl][1], nzs = ws.x[tl][2], H = ws.x[tl][3];
+              const float sxy = fa(fm(nxs, fs(V[0], cx)), fm(nys, fs(V[1], cy)));
+              // The per-cell slab test |sxy + nz (V0z - cz)| <= H can only pass for cz within
+              // H/|nz| of V0z + sxy/nz; the interval is widened by the float error of that test
+              // (a few ulps of its terms, over |nz|) and one cell, and the exact per-cell test
+              // still runs.
+              int ra = r0, rb = r1;
+              if (fabsf(nzs) > 0.f) {
+                const float rnz = __frcp_rn(nzs);
+                const float zc = V[2] + sxy * rnz;
+                const float ext = (H + 8.f * EPS24 * (fabsf(sxy) + fabsf(nzs) * (fabsf(V[2]) + fabsf(sz0) +
+                                                                                 fabsf(sz1)))) * fabsf(rnz);
+                const float igz = g.inv_g2[2];
+                const float fa0 = (zc - ext - sz0) * igz - 1.f, fb0 = (zc + ext - sz0) * igz + 1.f;
+                if (fa0 > -2.f) ra = max(ra, (int)floorf(fminf(fa0, (float)n2z + 2.f)));
+                if (fb0 < (float)n2z + 2.f) rb = min(rb, (int)ceilf(fmaxf(fb0, -2.f)));
+              }
+              for (int r = ra; r <= rb; ++r) {
+                if ((done >> r) & 1u) continue;
+                if (fabsf(fa(sxy, fm(nzs, fs(V[2], __ldg(sz + r))))) <= H) zm |= 1u << r;
+              }
+              rec = (uint32_t)tl | ((uint32_t)p << 5) | ((uint32_t)q << 11);
+            }
+          }
         }
-        uint32_t bits = 0;
-        for (int r = ra; r <= rb; ++r) {
-          if ((done >> r) & 1u) continue;
-          const float cz = __ldg(sz + r);
-          if (fabsf(fa(sxy, fm(nzs, fs(V[2], cz)))) > H) continue;  // plane misses the cell
-          if (sat_z(s, V, cz, g.e2)) bits |= 1u << r;
+        const uint32_t zc = (uint32_t)__popc(zm);
+        const uint32_t zinc = warp_incl_scan(zc);
+        ws.zpre[lane] = zinc - zc;
+        ws.zrec[lane] = rec;
+        ws.zmask[lane] = zm;
+        const uint32_t ztot = __shfl_sync(FULL, zinc, 31);
+        __syncwarp();
+        for (uint32_t z = lane; z < ztot; z += 32) {
+          const int rl = batch_search(ws.zpre, z);
+          const uint32_t rc = ws.zrec[rl];
+          const int r = (int)__fns(ws.zmask[rl], 0u, (int)(z - ws.zpre[rl]) + 1);
+          const int tl = (int)(rc & 31u), p = (int)((rc >> 5) & 63u), q = (int)((rc >> 11) & 63u);
+          const int jv = ws.jm[tl];
+          const float *sz = g.c2s[2] + (size_t)kz[jv] * n2z;
+          float V[9];
+#pragma unroll
+          for (int c = 0; c < 9; ++c) V[c] = ws.v[tl][c];
+          SatCol sc;
+          sat_col_values(V, __ldg(sx + p), __ldg(sy + q), sc);
+          if (sat_z(sc, V, __ldg(sz + r), g.e2)) {
+            const int bi = (q * n2x + p) * n2z + r;
+            atomicOr(&sat[jv * W + (bi >> 5)], 1u << (bi & 31));
+          }
         }
-        if (bits) or_column(satj, q * n2x + p, n2z, bits);
+        __syncwarp();
       }
-      __syncwarp();
     }
   }
 
@@ -406,46 +432,34 @@ __global__ void __launch_bounds__(kWarps * 32, 5) k_level2c(
     __syncwarp();
   }
 
-  // ---------------- output, top voxel first so the full-hit toggles accumulate downwards
+  // ---------------- output, top voxel first so the full-hit toggles accumulate downwards.
+  // One lane per sub-column: its n2z SAT and parity bits are read once and written as n2z
+  // bytes at stride n2x*n2y (consecutive lanes write consecutive bytes of each z layer).
   for (int w = lane; w < FW; w += 32) ftacc[w] = 0;
   __syncwarp();
   unsigned long long nin = 0, nbd = 0;
-  const bool vec = (cells & 3) == 0;
-  const bool pow2 = ((n2x & (n2x - 1)) == 0) && ((n2y & (n2y - 1)) == 0);
-  const int lx = __ffs(n2x) - 1, ly = __ffs(n2y) - 1;
+  const uint32_t zmask_all = n2z >= 32 ? 0xffffffffu : ((1u << n2z) - 1u);
   for (int jv = m - 1; jv >= 0; --jv) {
     for (int w = lane; w < FW; w += 32) ftacc[w] ^= ft[jv * FW + w];
     __syncwarp();
     const int64_t vlin = ((int64_t)kz[jv] * ny + cj) * nx + ci;
     uint8_t *out = d.l2 + (size_t)d.prefix[vlin] * cells;
     const uint32_t *satj = sat + jv * W, *parj = par + jv * W;
-    for (int c4 = lane * 4; c4 < cells; c4 += 128) {
-      uint32_t word = 0;
-#pragma unroll
-      for (int d = 0; d < 4; ++d) {
-        const int c = c4 + d;
-        if (c >= cells) break;
-        int p, q, r;
-        if (pow2) {
-          p = c & (n2x - 1);
-          q = (c >> lx) & (n2y - 1);
-          r = c >> (lx + ly);
-        } else {
-          p = c % n2x;
-          q = (c / n2x) % n2y;
-          r = c / ncol2;
-        }
-        const int pq = q * n2x + p;
-        const int bi = pq * n2z + r;
-        const uint32_t sb = (satj[bi >> 5] >> (bi & 31)) & 1u;
-        const uint32_t pb = ((parj[bi >> 5] >> (bi & 31)) ^ (ftacc[pq >> 5] >> (pq & 31))) & 1u;
-        const uint32_t s = sb ? 254u : (pb ? 127u : 0u);
-        nin += (!sb && pb);
-        nbd += sb;
-        if (vec) word |= s << (8 * d);
-        else out[c] = (uint8_t)s;
+    for (int pq = lane; pq < ncol2; pq += 32) {
+      const int off = pq * n2z, sh = off & 31;
+      uint32_t sb = satj[off >> 5] >> sh, pb = parj[off >> 5] >> sh;
+      if (sh + n2z > 32) {
+        sb |= satj[(off >> 5) + 1] << (32 - sh);
+        pb |= parj[(off >> 5) + 1] << (32 - sh);
       }
-      if (vec) *reinterpret_cast<uint32_t *>(out + c4) = word;
+      sb &= zmask_all;
+      if ((ftacc[pq >> 5] >> (pq & 31)) & 1u) pb = ~pb;
+      const uint32_t ib = pb & ~sb & zmask_all;
+      nbd += (unsigned)__popc(sb);
+      nin += (unsigned)__popc(ib);
+      uint8_t *o = out + pq;
+      for (int r = 0; r < n2z; ++r)
+        o[(size_t)r * ncol2] = ((sb >> r) & 1u) ? (uint8_t)254 : (((ib >> r) & 1u) ? (uint8_t)127 : (uint8_t)0);
     }
     __syncwarp();
   }

@@ -354,6 +354,25 @@ int gpv_write_raw(const char *prefix, const gpv_result *res, const uint8_t *leve
   return GPV_OK;
 }
 
+int gpv_write_raw_normals(const char *prefix, const gpv_result *res, const uint8_t *level1_normal,
+                          const uint8_t *level2_normal) {
+  if (!prefix || !res || !level1_normal) return GPV_ERR_INVALID;
+  const std::string p(prefix);
+  const gpv_grid_spec &s = res->spec;
+  const bool l2 = s.ndiv2[0] > 0;
+  if (l2 && res->num_boundary && !level2_normal) return GPV_ERR_INVALID;
+  auto dump = [&](const std::string &name, const void *data, size_t bytes) -> int {
+    std::ofstream f(p + name, std::ios::binary);
+    if (!f.good()) return GPV_ERR_IO;
+    if (bytes) f.write((const char *)data, (std::streamsize)bytes);
+    return f.good() ? GPV_OK : GPV_ERR_IO;
+  };
+  int rc = dump("Level1Normal.raw", level1_normal, 3 * (size_t)res->num_level1);
+  if (rc || !l2) return rc;
+  const size_t cells = (size_t)s.ndiv2[0] * s.ndiv2[1] * s.ndiv2[2];
+  return dump("Level2Normal.raw", level2_normal, 3 * (size_t)res->num_boundary * cells);
+}
+
 // ---- generators ----------------------------------------------------------------------------------
 
 int64_t gpv_gen_uvsphere(uint64_t seed, int32_t nlon, int32_t nlat, const float center[3],

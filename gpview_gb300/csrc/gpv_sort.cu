@@ -179,9 +179,16 @@ __device__ __forceinline__ int64_t seg_in_base(const MeshDesc &d, bool emit) {
   return emit ? d.emit_base : d.pair_base;
 }
 
+// by_val: the digit comes from the value's triangle id (bit 31, the topmost flag, excluded)
+// instead of the key; value passes run before the key passes to order each voxel's triangles.
+__device__ __forceinline__ uint32_t seg_digit(uint32_t key, uint32_t val, bool by_val, int shift) {
+  return ((by_val ? (val & 0x7fffffffu) : key) >> shift) & 255u;
+}
+
 __global__ void k_radix_hist_seg(const MeshDesc *__restrict__ md, const SortTile *__restrict__ tiles,
                                  const int64_t *__restrict__ tb, const uint32_t *__restrict__ keys,
-                                 bool emit, int shift, uint32_t *__restrict__ hist) {
+                                 const uint32_t *__restrict__ vals, bool by_val, bool emit,
+                                 int shift, uint32_t *__restrict__ hist) {
   __shared__ uint32_t s_h[256];
   s_h[threadIdx.x] = 0;
   __syncthreads();
@@ -189,7 +196,9 @@ __global__ void k_radix_hist_seg(const MeshDesc *__restrict__ md, const SortTile
   const int64_t in0 = seg_in_base(md[st.mesh], emit) + (int64_t)st.j * kSortTile;
   for (int r = 0; r < kSortRounds; ++r) {
     const int i = r * kSortThreads + threadIdx.x;
-    if (i < st.count) atomicAdd(&s_h[(keys[in0 + i] >> shift) & 255u], 1u);
+    if (i < st.count)
+      atomicAdd(&s_h[by_val ? seg_digit(0u, vals[in0 + i], true, shift)
+                            : seg_digit(keys[in0 + i], 0u, false, shift)], 1u);
   }
   __syncthreads();
   const int64_t nt_m = tb[st.mesh + 1] - tb[st.mesh];
@@ -199,8 +208,9 @@ __global__ void k_radix_hist_seg(const MeshDesc *__restrict__ md, const SortTile
 __global__ void k_radix_scatter_seg(const MeshDesc *__restrict__ md,
                                     const SortTile *__restrict__ tiles,
                                     const int64_t *__restrict__ tb, const uint32_t *__restrict__ keys,
-                                    const uint32_t *__restrict__ vals, bool emit, int shift,
-                                    const uint32_t *__restrict__ hoff, uint32_t *__restrict__ kout,
+                                    const uint32_t *__restrict__ vals, bool by_val, bool emit,
+                                    int shift, const uint32_t *__restrict__ hoff,
+                                    uint32_t *__restrict__ kout,
                                     uint32_t *__restrict__ vout) {
   __shared__ uint32_t s_off[256];
   __shared__ uint32_t s_run[256];
@@ -223,7 +233,7 @@ __global__ void k_radix_scatter_seg(const MeshDesc *__restrict__ md,
     if (valid) {
       key = keys[in0 + i];
       val = vals[in0 + i];
-      digit = (key >> shift) & 255u;
+      digit = seg_digit(key, val, by_val, shift);
     }
     const unsigned peers = __match_any_sync(0xffffffffu, digit);
     const unsigned rank = __popc(peers & lt_mask);
@@ -313,27 +323,32 @@ int64_t sort_seg_temp_words(int64_t ntiles) {
 
 bool sort_pairs_seg(const BatchDev &bd, const SortTile *tiles, const int64_t *tile_base_dev,
                     int64_t ntiles, uint32_t *keys, uint32_t *vals, uint32_t *kalt, uint32_t *valt,
-                    int64_t Ptotal, int key_bits, uint32_t *temp, cudaStream_t s) {
+                    int64_t Ptotal, int key_bits, int val_bits, uint32_t *temp, cudaStream_t s) {
   static_assert(kSortTileItems == kSortTile, "tile size mismatch");
   if (Ptotal <= 0 || ntiles <= 0) return false;
   uint32_t *hist = temp;
   uint32_t *hoff = temp + 256 * ntiles;
   uint32_t *stmp = temp + 2 * 256 * ntiles;
   // Pass 0 always runs (it also moves the pairs from the emission segments to the dense
-  // layout), so the result lands in (kalt, valt) after an odd number of passes.
-  const int passes = std::max(1, (key_bits + 7) / 8);
+  // layout), so the result lands in (kalt, valt) after an odd number of passes.  Value passes
+  // (triangle id digits) come first, so the stable key passes leave each key's triangles in
+  // ascending order.
+  const int vpasses = val_bits > 0 ? (val_bits + 7) / 8 : 0;
+  const int kpasses = std::max(vpasses > 0 ? 0 : 1, (key_bits + 7) / 8);
   bool alt = false;
-  for (int ps = 0; ps < passes; ++ps) {
+  for (int ps = 0; ps < vpasses + kpasses; ++ps) {
+    const bool by_val = ps < vpasses;
+    const int shift = 8 * (by_val ? ps : ps - vpasses);
+    const bool emit = ps == 0;
     const uint32_t *ki = alt ? kalt : keys;
     const uint32_t *vi = alt ? valt : vals;
     uint32_t *ko = alt ? keys : kalt;
     uint32_t *vo = alt ? vals : valt;
-    const bool emit = ps == 0;
-    k_radix_hist_seg<<<(unsigned)ntiles, kSortThreads, 0, s>>>(bd.md, tiles, tile_base_dev, ki,
-                                                                emit, 8 * ps, hist);
+    k_radix_hist_seg<<<(unsigned)ntiles, kSortThreads, 0, s>>>(bd.md, tiles, tile_base_dev, ki, vi,
+                                                                by_val, emit, shift, hist);
     scan_u32(hist, hoff, 256 * ntiles, nullptr, stmp, s);
     k_radix_scatter_seg<<<(unsigned)ntiles, kSortThreads, 0, s>>>(
-        bd.md, tiles, tile_base_dev, ki, vi, emit, 8 * ps, hoff, ko, vo);
+        bd.md, tiles, tile_base_dev, ki, vi, by_val, emit, shift, hoff, ko, vo);
     count_launch(2);
     alt = !alt;
   }

@@ -84,6 +84,13 @@ typedef struct {
     int32_t *boundary_index;     /* device, num_boundary int32: boundaryIndex */
     uint8_t *level2_inout;       /* device, num_boundary * n2x*n2y*n2z bytes */
     uint64_t handle;             /* internal */
+    /* Normals (gpv_set_normals; NULL when off).  Three values per Level1 voxel (x fastest) and
+     * per Level2 cell (boundary order, cell order as level2_inout): bytes in the .raw encoding
+     * uint8(n * float(256/3) + 127) (src/Object.cpp:2940-2941, :3033-3035) or floats. */
+    void *level1_normal;         /* device, 3 * num_level1 values */
+    void *level2_normal;         /* device, 3 * num_boundary * n2x*n2y*n2z values */
+    int32_t normal_mode;         /* GPV_NORMALS_* the result was made with */
+    int32_t reserved;
 } gpv_result;
 
 /* A triangle soup on the host, as Object::CreateFlatTriangleData builds it
@@ -105,6 +112,14 @@ const char *gpv_last_error(gpv_ctx *ctx);
  * number of boundary voxels of one Level1 column that one Level2 work item takes (1..32). */
 int gpv_set_tile(gpv_ctx *ctx, int tris_per_tile);
 int gpv_set_level2_chunk(gpv_ctx *ctx, int max_voxels);
+/* Voxel normals (default off), the reference's Level1 and Level2 normal passes
+ * (src/Object.cpp:3219-3253, :2402-2424, :2715-2719): GPV_NORMALS_OFF, GPV_NORMALS_BYTES (the
+ * .raw encoding) or GPV_NORMALS_FLOAT.  With normals on, each voxel's triangles are also ordered
+ * by id (the reference CPU path's list order), which the float sums follow. */
+#define GPV_NORMALS_OFF 0
+#define GPV_NORMALS_BYTES 1
+#define GPV_NORMALS_FLOAT 2
+int gpv_set_normals(gpv_ctx *ctx, int mode);
 /* Record the Level1 and Level2 launch sequences of each voxelization as CUDA graphs (default on;
  * the executable graphs are cached in the context and updated in place). */
 int gpv_set_graphs(gpv_ctx *ctx, int on);
@@ -142,6 +157,10 @@ int gpv_voxelize_host(gpv_ctx *ctx, const float *h_tris, int64_t num_triangles,
 int gpv_result_copy_to_host(gpv_ctx *ctx, const gpv_result *res, uint8_t *level1_inout,
                             int32_t *level1_prefix, int32_t *boundary_index,
                             uint8_t *level2_inout, cudaStream_t stream);
+/* Copy a result's normals (3 bytes or 3 floats per voxel / cell, per normal_mode) to host
+ * buffers (either may be NULL) and wait for the stream. */
+int gpv_result_copy_normals_to_host(gpv_ctx *ctx, const gpv_result *res, void *level1_normal,
+                                    void *level2_normal, cudaStream_t stream);
 int gpv_result_release(gpv_ctx *ctx, gpv_result *res);
 
 /* Batched path: n meshes in one launch sequence (persistent work-queue kernels).
@@ -199,6 +218,11 @@ void gpv_mesh_free(gpv_mesh *mesh);
  * <prefix>VoxelConfig.txt, Level1InOut.raw, Level1BoundaryPrefixSum.raw, Level2InOut.raw. */
 int gpv_write_raw(const char *prefix, const gpv_result *res, const uint8_t *level1_inout,
                   const int32_t *level1_prefix, const uint8_t *level2_inout);
+/* The two normal files of Object::SaveVoxelization (src/Object.cpp:3032-3035, :3047-3049,
+ * :3058-3064): <prefix>Level1Normal.raw (3 * num_level1 bytes) and, with Level2,
+ * <prefix>Level2Normal.raw (3 * num_boundary * n2x*n2y*n2z bytes), from host byte normals. */
+int gpv_write_raw_normals(const char *prefix, const gpv_result *res, const uint8_t *level1_normal,
+                          const uint8_t *level2_normal);
 
 /* ---- seeded synthetic meshes (host) ---------------------------------------------------------- */
 /* Each returns the triangle count; with tris == NULL only the count is returned. */

@@ -5,7 +5,8 @@
                                TriBoxIntersection.cpp / TriRayIntersection.cpp, built only where
                                the reference sources are present (they are compiled where they
                                lie; nothing is copied into this repository)
-  oracle/_ref/libref_pred.so   the reference predicates alone, under C names
+  oracle/_ref/libref_pred.so   the reference predicates and its normal arithmetic
+                               (includes/FloatVector.h) alone, under C names
 
 Flags: -O2 -ffp-contract=off -fno-fast-math.  Contraction must stay off: a fused multiply-add
 changes the predicates' results (GCC fuses by default on aarch64).
@@ -16,6 +17,7 @@ import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 REF_SRC = os.environ.get("GPV_REFERENCE_SRC", "/root/reference/src")
+REF_INC = os.path.join(os.path.dirname(REF_SRC), "includes")
 FLAGS = ["-O2", "-ffp-contract=off", "-fno-fast-math", "-fPIC"]
 
 
@@ -36,21 +38,23 @@ def build(force=False):
     if force or _stale(out, [src]):
         _run(["gcc", *FLAGS, "-fopenmp", "-shared", "-o", out, src, "-lm"])
     ref_files = [os.path.join(REF_SRC, f) for f in ("TriBoxIntersection.cpp", "TriRayIntersection.cpp")]
-    if all(os.path.exists(f) for f in ref_files):
+    ref_hdr = os.path.join(REF_INC, "FloatVector.h")
+    if all(os.path.exists(f) for f in ref_files + [ref_hdr]):
         rdir = os.path.join(HERE, "_ref")
         os.makedirs(rdir, exist_ok=True)
         shim = os.path.join(HERE, "ref_shim.cpp")
         pred = os.path.join(rdir, "libref_pred.so")
-        if force or _stale(pred, ref_files + [shim]):
-            _run(["g++", *FLAGS, "-shared", "-o", pred, shim, *ref_files])
+        if force or _stale(pred, ref_files + [shim, ref_hdr]):
+            _run(["g++", *FLAGS, "-I", REF_INC, "-shared", "-o", pred, shim, *ref_files])
         oref = os.path.join(rdir, "liboracle_ref.so")
-        if force or _stale(oref, ref_files + [shim, src]):
+        if force or _stale(oref, ref_files + [shim, src, ref_hdr]):
             objs = []
             for f in [src]:
                 o = os.path.join(rdir, "gpv_oracle_ref.o")
                 _run(["gcc", *FLAGS, "-fopenmp", "-DORC_REF_PREDICATES", "-c", f, "-o", o])
                 objs.append(o)
-            _run(["g++", *FLAGS, "-fopenmp", "-shared", "-o", oref, *objs, shim, *ref_files, "-lm"])
+            _run(["g++", *FLAGS, "-I", REF_INC, "-fopenmp", "-shared", "-o", oref, *objs, shim, *ref_files,
+                  "-lm"])
     return out
 
 

@@ -43,6 +43,8 @@
 /* Built only in oracle/_ref: the reference's own TriBoxOverlap / triangle_ray_intersection,
  * compiled from its sources and exported through ref_shim.cpp. */
 int ref_tri_box(const float c[3], const float h[3], const float *tv);
+void ref_face_normal(const float *tv, float *out);
+void ref_average_normal(const float *sum, float count, float *out);
 int ref_tri_ray(const float *V1, const float *V2, const float *V3, const float *O,
                 const float *D, float *out);
 #endif
@@ -872,4 +874,120 @@ void orc_count_ops(const orc_run *r, int64_t b0, int64_t b1, int nthreads, int64
         }
     }
     out[0] = s1; out[1] = r1; out[2] = s2; out[3] = r2;
+}
+
+/* ------------------------------------------------------------------------------------------ */
+/* Normals                                                                                     */
+/* ------------------------------------------------------------------------------------------ */
+
+/* VectorNormalize (includes/FloatVector.h:333-342): float magnitude, divide when non-zero. */
+static void orc_normalize(float a[3])
+{
+    float mag = sqrtf(a[0] * a[0] + a[1] * a[1] + a[2] * a[2]);
+    if (mag != 0) {
+        a[0] /= mag;
+        a[1] /= mag;
+        a[2] /= mag;
+    }
+}
+
+/* Face normal of one triangle as the loader and Level1 pass compute it (src/Object.cpp:522-526,
+ * :3233-3239): VectorCrossProduct(v1 - v0, v2 - v0) (includes/FloatVector.h:293-296),
+ * normalised. */
+void orc_face_normal(const float *tv, float out[3])
+{
+#ifdef ORC_REF_PREDICATES
+    ref_face_normal(tv, out);
+    return;
+#endif
+    float a[3], b[3];
+    for (int c = 0; c < 3; ++c) { a[c] = tv[3 + c] - tv[c]; b[c] = tv[6 + c] - tv[c]; }
+    out[0] = a[1] * b[2] - b[1] * a[2];
+    out[1] = a[2] * b[0] - b[2] * a[0];
+    out[2] = a[0] * b[1] - b[0] * a[1];
+    orc_normalize(out);
+}
+
+/* sum / count componentwise, normalised (src/Object.cpp:3247-3248, :2410-2415). */
+static void orc_average(const float sum[3], float count, float out[3])
+{
+#ifdef ORC_REF_PREDICATES
+    ref_average_normal(sum, count, out);
+    return;
+#endif
+    out[0] = sum[0] / count; out[1] = sum[1] / count; out[2] = sum[2] / count;
+    orc_normalize(out);
+}
+
+/* Level1 normals (src/Object.cpp:3219-3253) into out[3*N1]: for every voxel with recorded
+ * triangles, the float sum of their face normals in list order (ascending triangle id, the order
+ * ClassifyTessellation records them, :2267-2340), divided by the count and normalised; 0 for the
+ * other voxels (:3151-3152). */
+void orc_level1_normals(const orc_run *r, float *out)
+{
+    memset(out, 0, sizeof(float) * 3 * (size_t)r->N1);
+    for (int64_t v = 0; v < r->N1; ++v) {
+        int64_t n = r->vstart[v + 1] - r->vstart[v];
+        if (n == 0) continue;
+        float sum[3] = {0.f, 0.f, 0.f};
+        for (int64_t e = r->vstart[v]; e < r->vstart[v + 1]; ++e) {
+            float fn[3];
+            orc_face_normal(r->tris + 9 * (int64_t)r->vtris[e], fn);
+            sum[0] += fn[0]; sum[1] += fn[1]; sum[2] += fn[2];
+        }
+        float avg[3];
+        orc_average(sum, (float)n, avg);
+        out[3 * v + 0] = avg[0]; out[3 * v + 1] = avg[1]; out[3 * v + 2] = avg[2];
+    }
+}
+
+/* Level2 normals of boundary voxels [b0, b1) into out[3*(b1-b0)*cells], cell order as the Level2
+ * states.  Every SAT pass of ClassifyTessellationLevel2 (src/Object.cpp:2374-2398) adds the
+ * triangle's face normal and 1 to the cell (AddPointToVoxel, :2715-2719), triangles in list
+ * order; the sums are divided by the count and normalised (:2402-2424); cells without a pass
+ * stay 0 (:3309-3310). */
+void orc_level2_normals(const orc_run *r, int64_t b0, int64_t b1, float *out, int nthreads)
+{
+    int nth = orc_threads(nthreads);
+    const int nx = r->s.n[0], ny = r->s.n[1];
+    const int n2x = r->s.n2[0], n2y = r->s.n2[1], n2z = r->s.n2[2];
+    const int64_t cells = (int64_t)n2x * n2y * n2z;
+    if (b1 > r->B) b1 = r->B;
+    if (b0 >= b1 || cells <= 0) return;
+#pragma omp parallel num_threads(nth)
+    {
+        float *acc = (float *)malloc(sizeof(float) * 4 * (size_t)cells);
+#pragma omp for schedule(dynamic, 16)
+        for (int64_t b = b0; b < b1; ++b) {
+            memset(acc, 0, sizeof(float) * 4 * (size_t)cells);
+            int64_t v = r->bindex[b];
+            int k = (int)(v / ((int64_t)nx * ny));
+            int64_t ij = v - (int64_t)k * nx * ny;
+            int j = (int)(ij / nx), i = (int)(ij % nx);
+            const float *sx = r->t.c2s[0] + (size_t)i * n2x;
+            const float *sy = r->t.c2s[1] + (size_t)j * n2y;
+            const float *sz = r->t.c2s[2] + (size_t)k * n2z;
+            for (int64_t e = r->vstart[v]; e < r->vstart[v + 1]; ++e) {
+                const float *tv = r->tris + 9 * (int64_t)r->vtris[e];
+                float fn[3];
+                orc_face_normal(tv, fn);
+                for (int p = 0; p < n2x; ++p)
+                    for (int q = 0; q < n2y; ++q)
+                        for (int rr = 0; rr < n2z; ++rr) {
+                            float c3[3] = {sx[p], sy[q], sz[rr]};
+                            if (!orc_tri_box(c3, r->t.e2, tv)) continue;
+                            float *a = acc + 4 * (((int64_t)rr * n2y + q) * n2x + p);
+                            a[0] += fn[0]; a[1] += fn[1]; a[2] += fn[2]; a[3] += 1;
+                        }
+            }
+            float *o = out + 3 * (b - b0) * cells;
+            for (int64_t c = 0; c < cells; ++c) {
+                float avg[3] = {0.f, 0.f, 0.f};
+                const float *a = acc + 4 * c;
+                if (a[3] > 0) orc_average(a, a[3], avg);
+                o[3 * c + 0] = avg[0]; o[3 * c + 1] = avg[1]; o[3 * c + 2] = avg[2];
+            }
+        }
+        free(acc);
+    }
 }

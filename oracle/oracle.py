@@ -53,6 +53,9 @@ def _load(ref=False):
     L.orc_voxel_tris.restype = i64
     L.orc_level2.argtypes = [vp, i64, i64, vp, C.c_int, C.POINTER(i64), C.POINTER(i64)]
     L.orc_count_ops.argtypes = [vp, i64, i64, C.c_int, vp]
+    L.orc_face_normal.argtypes = [vp, vp]
+    L.orc_level1_normals.argtypes = [vp, vp]
+    L.orc_level2_normals.argtypes = [vp, i64, i64, vp, C.c_int]
     L.orc_tri_box.argtypes = [vp, vp, vp]
     L.orc_tri_ray.argtypes = [vp, vp, vp, vp, vp, C.POINTER(C.c_float)]
     L.orc_tri_ray_z.argtypes = [vp, vp]
@@ -148,9 +151,38 @@ class Run:
         self.L.orc_count_ops(self.h, int(b0), int(b1), int(threads), _p(out))
         return dict(zip(("sat1", "ray1", "sat2", "ray2"), (int(x) for x in out)))
 
+    def level1_normals(self):
+        """float32 [N1, 3]: Level1 normals (zero where no triangle is recorded)."""
+        out = np.empty(self.N1 * 3, np.float32)
+        self.L.orc_level1_normals(self.h, _p(out))
+        return out.reshape(-1, 3)
+
+    def level2_normals(self, b0=0, b1=None, threads=0):
+        """float32 [(b1-b0)*cells, 3]: Level2 normals of boundary voxels [b0,b1)."""
+        b1 = self.B if b1 is None else b1
+        out = np.zeros(max(b1 - b0, 0) * self.cells * 3, np.float32)
+        if b1 > b0:
+            self.L.orc_level2_normals(self.h, int(b0), int(b1), _p(out), int(threads))
+        return out.reshape(-1, 3)
+
     def level2_bytes(self, b0=0, b1=None, threads=0):
         st, _, _ = self.level2_state(b0, b1, threads)
         return (st * 127).astype(np.uint8)
+
+
+def face_normal(tv, ref=False):
+    L = _load(ref)
+    tv = np.ascontiguousarray(tv, np.float32)
+    out = np.empty(3, np.float32)
+    L.orc_face_normal(_p(tv), _p(out))
+    return out
+
+
+def normal_bytes(n):
+    """The .raw encoding of normals (src/Object.cpp:2940-2941, :3033-3035): unsigned char of
+    n * float(256/3) + 127 in float."""
+    n = np.asarray(n, np.float32)
+    return (n * np.float32(256.0 / 3.0) + np.float32(127.0)).astype(np.int32).astype(np.uint8)
 
 
 def tri_box(c, h, tv, ref=False):

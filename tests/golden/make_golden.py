@@ -6,9 +6,12 @@ and src/TriRayIntersection.cpp) and writes:
 
   pred_sat.npz   triangle/box cases and TriBoxOverlap's answers
   pred_ray.npz   ray/triangle cases and triangle_ray_intersection's answers (hit, t)
+  normal_face.npz  face normals of the SAT-case triangles from the reference's own vector code
+                 (includes/FloatVector.h: VectorCrossProduct, VectorNormalize)
   mesh_*.npz     small meshes + grids and the full two-level outputs of the reference's CPU
                  composition (E3) evaluated with the reference's predicates, voxel by voxel
-                 (ClassifyInOutCPU semantics: every voxel centre against every triangle)
+                 (ClassifyInOutCPU semantics: every voxel centre against every triangle), plus
+                 the Level1 and Level2 normals with the reference's vector arithmetic
 
 The fixtures are small (tens of KB each) and travel with the repository; the GPU machine never
 needs the reference.
@@ -32,6 +35,7 @@ def _ref_pred():
     vp = C.c_void_p
     L.ref_tri_box.argtypes = [vp, vp, vp]
     L.ref_tri_ray.argtypes = [vp, vp, vp, vp, vp, C.POINTER(C.c_float)]
+    L.ref_face_normal.argtypes = [vp, vp]
     return L
 
 
@@ -122,6 +126,10 @@ def main():
         out[i] = L.ref_tri_box(_p(c[i]), _p(h[i]), _p(tv[i]))
     np.savez_compressed(os.path.join(HERE, "pred_sat.npz"), center=c, half=h, tri=tv, hit=out)
     print("pred_sat: pass rate", out.mean())
+    fn = np.empty((n, 3), np.float32)
+    for i in range(n):
+        L.ref_face_normal(_p(tv[i]), _p(fn[i]))
+    np.savez_compressed(os.path.join(HERE, "normal_face.npz"), tri=tv, normal=fn)
 
     v, o, d = ray_cases(rng, n)
     hit = np.empty(n, np.int8)
@@ -144,7 +152,8 @@ def main():
             bbox_min=np.array(spec.bbox_min, np.float32), bbox_max=np.array(spec.bbox_max, np.float32),
             ndiv=np.array(spec.ndiv, np.int32), ndiv2=np.array(spec.ndiv2, np.int32),
             level1=run.level1_state(), prefix=run.prefix(), bindex=run.boundary_index(), level2=st2,
-            work=np.array([run.sat1_tests(), s2, run.ray1_candidates(), r2], np.int64))
+            work=np.array([run.sat1_tests(), s2, run.ray1_candidates(), r2], np.int64),
+            level1_normal=run.level1_normals(), level2_normal=run.level2_normals())
         print(name, "T", tris.size // 9, "B", run.B, "level1", np.bincount(run.level1_state(), minlength=3))
 
 

@@ -97,3 +97,24 @@ def test_op_counts_fixture_sphere16k():
         for k, (lo, hi) in {"sat1": (27, 124), "sat2": (27, 124), "ray1": (20, 52), "ray2": (20, 52)}.items():
             e = fix[name][k]
             assert lo * e["tests"] <= e["ops"] <= hi * e["tests"], (name, k)
+
+
+def test_face_normals_match_reference_vectors():
+    z = np.load(os.path.join(GOLD, "normal_face.npz"))
+    got = np.stack([orc.face_normal(t) for t in z["tri"]])
+    np.testing.assert_array_equal(got, z["normal"])
+
+
+@pytest.mark.parametrize("path", sorted(glob.glob(os.path.join(GOLD, "mesh_*.npz"))),
+                         ids=lambda p: os.path.basename(p)[5:-4])
+def test_oracle_normals_match_golden_meshes(path):
+    z = np.load(path)
+    grid = (z["bbox_min"], z["bbox_max"], z["ndiv"], z["ndiv2"])
+    r = orc.Run(z["tris"], grid)
+    np.testing.assert_array_equal(r.level1_normals(), z["level1_normal"])
+    np.testing.assert_array_equal(r.level2_normals(), z["level2_normal"])
+
+
+def test_normal_bytes_encoding():
+    # n * float(256/3) + 127, truncated: -1 -> 41, 0 -> 127, 1 -> 212
+    assert list(orc.normal_bytes([-1.0, 0.0, 1.0, 0.5])) == [41, 127, 212, 169]
