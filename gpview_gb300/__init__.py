@@ -61,6 +61,14 @@ class Result(C.Structure):
 NORMALS_OFF, NORMALS_BYTES, NORMALS_FLOAT = 0, 1, 2
 
 
+class VoxelConfig(C.Structure):
+    _fields_ = [("bbox_min", C.c_float * 3), ("bbox_max", C.c_float * 3), ("ndiv", C.c_int32 * 3),
+                ("grid_size", C.c_float * 3), ("num_level1_inside", C.c_int64),
+                ("num_boundary", C.c_int64), ("has_level2", C.c_int32), ("ndiv2", C.c_int32 * 3),
+                ("grid_size2", C.c_float * 3), ("num_level2_inside", C.c_int64),
+                ("num_level2_boundary", C.c_int64)]
+
+
 class MeshC(C.Structure):
     _fields_ = [("tris", C.POINTER(C.c_float)), ("num_triangles", C.c_int64),
                 ("bbox_min", C.c_float * 3), ("bbox_max", C.c_float * 3),
@@ -102,6 +110,9 @@ def lib():
     L.gpv_write_raw.argtypes = [C.c_char_p, C.POINTER(Result), C.c_void_p, C.c_void_p, C.c_void_p]
     L.gpv_write_raw_normals.argtypes = [C.c_char_p, C.POINTER(Result), C.c_void_p, C.c_void_p]
     L.gpv_set_normals.argtypes = [C.c_void_p, C.c_int]
+    L.gpv_read_voxel_config.argtypes = [C.c_char_p, C.POINTER(VoxelConfig)]
+    L.gpv_read_raw.argtypes = [C.c_char_p, C.POINTER(VoxelConfig), C.c_void_p, C.c_void_p,
+                               C.c_void_p, C.c_void_p, C.c_void_p]
     L.gpv_result_copy_normals_to_host.argtypes = [C.c_void_p, C.POINTER(Result), C.c_void_p,
                                                   C.c_void_p, C.c_void_p]
     for name, extra in (("gpv_gen_uvsphere", [C.c_int32, C.c_int32, f3, C.c_float, C.c_float]),
@@ -396,6 +407,25 @@ class Object:
     def ReadOFFObject(self, path):
         self._load(lib().gpv_load_off, path)
 
+    def ReadRAWObject(self, fName):
+        """Object::ReadRAWObject (src/Object.cpp:319-392): a 48 x 64 x 64 Level1InOut file read as
+        the Level1 states; `solid` per voxel is int(value) % 2 (the grid spans bBoxMin..bBoxMax)."""
+        n = (48, 64, 64)
+        with open(fName, "rb") as f:
+            data = np.frombuffer(f.read(n[0] * n[1] * n[2]), np.uint8)
+        vd = VoxelData.__new__(VoxelData)
+        vd.numDivX, vd.numDivY, vd.numDivZ = n
+        if self.bBoxMin is not None:
+            span = (np.asarray(self.bBoxMax, np.float64) - np.asarray(self.bBoxMin, np.float64))
+            vd.gridSizeX, vd.gridSizeY, vd.gridSizeZ = (float(np.float32(span[a] / (n[a] * 1.0)))
+                                                        for a in range(3))
+        full = np.zeros(n[0] * n[1] * n[2], np.uint8)
+        full[:data.size] = data
+        vd.level1InOut = full
+        vd.solid = (full.astype(np.int32) % 2).astype(np.uint8)
+        self.voxelData = vd
+        return vd
+
     def CreateFlatTriangleData(self):
         self.flatCPUTriangleData = self._tris
         self.totalNumTriangles = self._tris.size // 9
@@ -445,6 +475,40 @@ class Object:
                                              n1.ctypes.data_as(C.c_void_p), n2.ctypes.data_as(C.c_void_p))
             if rc:
                 raise GpvError(rc, "SaveVoxelization (normals)")
+
+
+def read_voxel_config(prefix):
+    """Parses <prefix>VoxelConfig.txt (the line order of Object::SaveVoxelization)."""
+    cfg = VoxelConfig()
+    rc = lib().gpv_read_voxel_config(str(prefix).encode(), C.byref(cfg))
+    if rc:
+        raise GpvError(rc, f"{prefix}VoxelConfig.txt")
+    return cfg
+
+
+def read_raw(prefix, cfg=None, normals=True):
+    """Reads a saved voxelization back: dict of the config and the .raw arrays (Level1InOut,
+    Level1BoundaryPrefixSum, Level2InOut and, when present, the two normal files)."""
+    cfg = cfg or read_voxel_config(prefix)
+    n1 = int(np.prod(list(cfg.ndiv)))
+    cells = int(np.prod(list(cfg.ndiv2))) if cfg.has_level2 else 0
+    nb = int(cfg.num_boundary)
+    out = {"config": cfg, "level1InOut": np.empty(n1, np.uint8)}
+    if cfg.has_level2:
+        out["boundaryPrefixSum"] = np.empty(n1, np.int32)
+        out["level2InOut"] = np.empty(nb * cells, np.uint8)
+    have_n = normals and os.path.exists(f"{prefix}Level1Normal.raw")
+    if have_n:
+        out["level1Normal"] = np.empty((n1, 3), np.uint8)
+        if cfg.has_level2:
+            out["level2Normal"] = np.empty((nb * cells, 3), np.uint8)
+    ptr = lambda k: out[k].ctypes.data_as(C.c_void_p) if k in out else None  # noqa: E731
+    rc = lib().gpv_read_raw(str(prefix).encode(), C.byref(cfg), ptr("level1InOut"),
+                            ptr("boundaryPrefixSum"), ptr("level2InOut"), ptr("level1Normal"),
+                            ptr("level2Normal"))
+    if rc:
+        raise GpvError(rc, f"read_raw {prefix}")
+    return out
 
 
 def normal_bytes(n):

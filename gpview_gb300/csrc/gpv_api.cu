@@ -171,6 +171,7 @@ void gpv_destroy(gpv_ctx *ctx) {
   ctx->owned.clear();
   for (cudaGraphExec_t &ge : ctx->gexec)
     if (ge) cudaGraphExecDestroy(ge);
+  if (ctx->slab) cudaFree(ctx->slab);
   if (ctx->h_stats) cudaFreeHost(ctx->h_stats);
   if (ctx->h_md) cudaFreeHost(ctx->h_md);
   if (ctx->h_tiles) cudaFreeHost(ctx->h_tiles);

@@ -21,22 +21,55 @@ namespace gpv {
 
 namespace {
 
+// Per-call workspace carved from the context's slab (256-byte aligned pieces).  Pieces that do
+// not fit fall back to stream-ordered allocations, freed at the end of the call; the total need
+// is recorded so that the next call grows the slab first.
 struct Arena {
-  std::vector<void *> ptrs;
+  gpv_ctx *ctx;
   cudaStream_t s;
-  explicit Arena(cudaStream_t st) : s(st) {}
+  size_t off = 0;
+  std::vector<void *> extra;
+  Arena(gpv_ctx *c, cudaStream_t st) : ctx(c), s(st) {}
   template <typename T>
   cudaError_t get(T **p, size_t count) {
+    const size_t bytes = (std::max<size_t>(count * sizeof(T), 16) + 255) & ~size_t(255);
+    if (ctx->slab && off + bytes <= ctx->slab_cap) {
+      *p = reinterpret_cast<T *>(static_cast<char *>(ctx->slab) + off);
+      off += bytes;
+      return cudaSuccess;
+    }
+    off += bytes;
     void *q = nullptr;
-    cudaError_t e = cudaMallocAsync(&q, std::max<size_t>(count * sizeof(T), 16), s);
-    if (e == cudaSuccess) ptrs.push_back(q);
+    cudaError_t e = cudaMallocAsync(&q, bytes, s);
+    if (e == cudaSuccess) extra.push_back(q);
     *p = (T *)q;
     return e;
   }
   ~Arena() {
-    for (void *p : ptrs) cudaFreeAsync(p, s);
+    for (void *p : extra) cudaFreeAsync(p, s);
+    ctx->slab_want = std::max(ctx->slab_want, off);
   }
 };
+
+// Grows the slab to the need recorded by earlier calls (the slab is idle between calls).
+cudaError_t grow_slab(gpv_ctx *ctx, cudaStream_t s) {
+  if (ctx->slab_want <= ctx->slab_cap) return cudaSuccess;
+  if (ctx->slab) {
+    cudaError_t e = cudaFreeAsync(ctx->slab, s);
+    if (e != cudaSuccess) return e;
+    ctx->slab = nullptr;
+    ctx->slab_cap = 0;
+  }
+  const size_t want = ctx->slab_want + ctx->slab_want / 8;
+  cudaError_t e = cudaMallocAsync(&ctx->slab, want, s);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    ctx->slab = nullptr;
+    return cudaSuccess;  // keep going on per-call allocations
+  }
+  ctx->slab_cap = want;
+  return cudaSuccess;
+}
 
 size_t al16(size_t v) { return (v + 15) & ~size_t(15); }
 
@@ -150,7 +183,8 @@ int run_batch(gpv_ctx *ctx, int n, const float *const *d_tris, const int64_t *T,
   int val_bits = 1;  // bits of the largest triangle id (normals: the sort's value digits)
   while (val_bits < 31 && ((int64_t)1 << val_bits) < max_T) ++val_bits;
 
-  Arena ws(s);
+  CK(grow_slab(ctx, s));
+  Arena ws(ctx, s);
   // coordinate tables: one pinned staging copy
   CK(ctx_ensure_tables(ctx, (size_t)tab_off[n]));
   for (int m = 0; m < n; ++m) pack_tables(gh[m], ctx->h_tables + tab_off[m]);
@@ -247,32 +281,19 @@ int run_batch(gpv_ctx *ctx, int n, const float *const *d_tris, const int64_t *T,
     return ctx_fail(ctx, code, msg);
   };
 
-  // ---- phase A
-  mark(0);
-  launch_prep(bd, s);
-  mark(1);
-  CK(cudaGetLastError());
-  CK(cudaMemcpyAsync(ctx->h_stats, stats, n * sizeof(MeshStats), cudaMemcpyDeviceToHost, s));
-  CK(cudaStreamSynchronize(s));
-  int64_t caps = 0;
-  for (int m = 0; m < n; ++m) {
-    if (ctx->h_stats[m].status & ST_BAD_INPUT) return fail_all(GPV_ERR_INVALID, "non-finite vertex");
-    md[m].pair_cap = (int64_t)std::max<unsigned long long>(ctx->h_stats[m].sat1, 1);
-    md[m].emit_base = caps;
-    caps += md[m].pair_cap;
-  }
+  // ---- phase A+B (one recording): prep, per-mesh pair bases on the device (no host round trip:
+  // the pair buffer has the context's capacity hint; a mesh that does not fit raises
+  // ST_PAIR_OVERFLOW and the call re-runs with the exact capacity), Level1, fill finish,
+  // boundary scan.
+  const int64_t pair_cap = std::max<int64_t>(ctx->pair_hint, std::max<int64_t>(16 * tris, 1 << 16));
   uint32_t *keys, *vals;
-  CK(ws.get(&keys, (size_t)caps));
-  CK(ws.get(&vals, (size_t)caps));
-  for (int m = 0; m < n; ++m) {
-    md[m].keys = keys + md[m].emit_base;
-    md[m].vals = vals + md[m].emit_base;
-  }
-  std::memcpy(ctx->h_md, md.data(), n * sizeof(MeshDesc));
-  CK(cudaMemcpyAsync(d_md, ctx->h_md, n * sizeof(MeshDesc), cudaMemcpyHostToDevice, s));
-
-  // ---- phase B
+  CK(ws.get(&keys, (size_t)pair_cap));
+  CK(ws.get(&vals, (size_t)pair_cap));
   CK(run_phase(ctx, 0, s, capturing, [&] {
+    mark(0);
+    launch_prep(bd, s);
+    mark(1);
+    launch_pair_bases(bd, d_md, keys, vals, pair_cap, s);
     mark(2);
     launch_level1(bd, ctx->num_sms, s);
     mark(3);
@@ -284,6 +305,30 @@ int run_batch(gpv_ctx *ctx, int n, const float *const *d_tris, const int64_t *T,
   }));
   CK(cudaMemcpyAsync(ctx->h_stats, stats, n * sizeof(MeshStats), cudaMemcpyDeviceToHost, s));
   CK(cudaStreamSynchronize(s));
+  {
+    // the same bases the device computed, for the host copy of the descriptors
+    int64_t caps = 0, need = 0;
+    bool overflow = false;
+    for (int m = 0; m < n; ++m) {
+      const MeshStats &st = ctx->h_stats[m];
+      if (st.status & ST_BAD_INPUT) return fail_all(GPV_ERR_INVALID, "non-finite vertex");
+      overflow = overflow || (st.status & ST_PAIR_OVERFLOW);
+      const int64_t want = (int64_t)st.sat1;
+      md[m].emit_base = caps;
+      md[m].pair_cap = std::max<int64_t>(0, std::min<int64_t>(want, pair_cap - caps));
+      md[m].keys = keys + std::min<int64_t>(caps, pair_cap);
+      md[m].vals = vals + std::min<int64_t>(caps, pair_cap);
+      caps += want;
+      need += want;
+    }
+    if (overflow) {
+      if (ctx->pair_hint >= need) return fail_all(GPV_ERR_DEVICE, "pair buffer overflow");
+      ctx->pair_hint = need + need / 8;
+      fail_all(GPV_OK, "");
+      ctx->err.clear();
+      return run_batch(ctx, n, d_tris, T, specs, out, s);
+    }
+  }
   int64_t Btot = 0, l2bytes = 0, P2 = 0, ub = 0;
   std::vector<int64_t> l2off(n + 1, 0), boff(n + 1, 0);
   for (int m = 0; m < n; ++m) {

@@ -43,6 +43,13 @@ struct gpv_ctx {
   uint32_t *h_u32 = nullptr;           // pinned scratch (small)
   float *h_tables = nullptr;           // pinned staging for coordinate tables
   size_t h_tables_cap = 0;
+  // Device workspace kept across calls (grow-only): every intermediate of a voxelization is carved
+  // from this slab; requests beyond it fall back to stream-ordered allocations and the slab is
+  // grown to the recorded need at the next call.  Calls on one context run one at a time (each
+  // ends with a stream synchronisation), so the slab is idle between calls.
+  void *slab = nullptr;
+  size_t slab_cap = 0, slab_want = 0;
+  int64_t pair_hint = 0;               // pair-buffer capacity for the next call (grow-only)
   uint64_t next_handle = 1;
   std::mutex owned_mu;                 // results may be released from another host thread
   std::unordered_map<uint64_t, std::shared_ptr<gpv::ResultSet>> owned;

@@ -84,6 +84,9 @@ struct BatchDev {
 };
 
 void launch_prep(const BatchDev &bd, cudaStream_t s);
+// Device-side per-mesh pair segments (emit_base, pair_cap, keys, vals) from prep's sat1 counts.
+void launch_pair_bases(const BatchDev &bd, MeshDesc *d_md, uint32_t *keys, uint32_t *vals,
+                       int64_t cap, cudaStream_t s);
 void launch_level1(const BatchDev &bd, int num_sms, cudaStream_t s);
 void launch_fill_finish(const BatchDev &bd, cudaStream_t s);
 void launch_popc(const uint32_t *plane, int64_t nwords, uint32_t *cnt, cudaStream_t s);

@@ -197,6 +197,51 @@ __global__ void __launch_bounds__(256) k_prep(BatchDev bd) {
   warp_add(&d.stats->ray1, r1);
 }
 
+// Per-mesh pair emission segments from the candidate counts prep just produced: exclusive prefix
+// of sat1 over the meshes, capped by the buffer capacity (a mesh past the end gets a short or
+// empty segment; its Level1 then raises ST_PAIR_OVERFLOW).  One block; meshes in rounds of 1024.
+__global__ void __launch_bounds__(1024) k_pair_bases(int nmesh, MeshDesc *md, uint32_t *keys,
+                                                     uint32_t *vals, int64_t cap) {
+  __shared__ unsigned long long s_w[32];
+  __shared__ unsigned long long s_carry;
+  const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+  if (threadIdx.x == 0) s_carry = 0;
+  __syncthreads();
+  for (int m0 = 0; m0 < nmesh; m0 += 1024) {
+    const int m = m0 + (int)threadIdx.x;
+    const unsigned long long v = m < nmesh ? md[m].stats->sat1 : 0ull;
+    unsigned long long x = v;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+      const unsigned long long o = __shfl_up_sync(FULL, x, d);
+      if (lane >= (unsigned)d) x += o;
+    }
+    if (lane == 31) s_w[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+      unsigned long long w = s_w[lane];
+#pragma unroll
+      for (int d = 1; d < 32; d <<= 1) {
+        const unsigned long long o = __shfl_up_sync(FULL, w, d);
+        if (lane >= (unsigned)d) w += o;
+      }
+      s_w[lane] = w;
+    }
+    __syncthreads();
+    const unsigned long long base = s_carry + (warp ? s_w[warp - 1] : 0ull) + x - v;
+    if (m < nmesh) {
+      const int64_t b = (int64_t)base;
+      md[m].emit_base = b;
+      md[m].pair_cap = max((int64_t)0, min((int64_t)v, cap - b));
+      md[m].keys = keys + min(b, cap);
+      md[m].vals = vals + min(b, cap);
+    }
+    __syncthreads();
+    if (threadIdx.x == 1023) s_carry = base + v;
+    __syncthreads();
+  }
+}
+
 // ---------------------------------------------------------------------------------------------
 constexpr int kL1Threads = 256;
 constexpr int kL1Warps = kL1Threads / 32;
@@ -521,6 +566,12 @@ __global__ void k_useg(const uint32_t *__restrict__ flags, const uint32_t *__res
 void launch_prep(const BatchDev &bd, cudaStream_t s) {
   if (bd.total_tris <= 0) return;
   k_prep<<<(unsigned)((bd.total_tris + 255) / 256), 256, 0, s>>>(bd);
+  count_launch();
+}
+
+void launch_pair_bases(const BatchDev &bd, MeshDesc *d_md, uint32_t *keys, uint32_t *vals,
+                       int64_t cap, cudaStream_t s) {
+  k_pair_bases<<<1, 1024, 0, s>>>(bd.nmesh, d_md, keys, vals, cap);
   count_launch();
 }
 

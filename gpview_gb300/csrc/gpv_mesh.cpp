@@ -373,6 +373,63 @@ int gpv_write_raw_normals(const char *prefix, const gpv_result *res, const uint8
   return dump("Level2Normal.raw", level2_normal, 3 * (size_t)res->num_boundary * cells);
 }
 
+int gpv_read_voxel_config(const char *prefix, gpv_voxel_config *out) {
+  if (!prefix || !out) return GPV_ERR_INVALID;
+  std::memset(out, 0, sizeof(*out));
+  std::ifstream f(std::string(prefix) + "VoxelConfig.txt");
+  if (!f.good()) return GPV_ERR_IO;
+  std::string name;
+  if (!std::getline(f, name)) return GPV_ERR_PARSE;
+  auto rd3f = [&](float *v) { return static_cast<bool>(f >> v[0] >> v[1] >> v[2]); };
+  auto rd3i = [&](int32_t *v) { return static_cast<bool>(f >> v[0] >> v[1] >> v[2]); };
+  long long a = 0, b = 0;
+  if (!rd3f(out->bbox_min) || !rd3f(out->bbox_max) || !rd3i(out->ndiv) || !rd3f(out->grid_size) ||
+      !(f >> a >> b))
+    return GPV_ERR_PARSE;
+  out->num_level1_inside = a;
+  out->num_boundary = b;
+  for (int k = 0; k < 3; ++k)
+    if (out->ndiv[k] < 1) return GPV_ERR_PARSE;
+  int32_t n2[3];
+  if (rd3i(n2)) {  // the Level2 block is present
+    float g2[3];
+    if (!rd3f(g2) || !(f >> a >> b)) return GPV_ERR_PARSE;
+    for (int k = 0; k < 3; ++k) {
+      if (n2[k] < 1) return GPV_ERR_PARSE;
+      out->ndiv2[k] = n2[k];
+      out->grid_size2[k] = g2[k];
+    }
+    out->has_level2 = 1;
+    out->num_level2_inside = a;
+    out->num_level2_boundary = b;
+  }
+  return GPV_OK;
+}
+
+int gpv_read_raw(const char *prefix, const gpv_voxel_config *cfg, uint8_t *level1_inout,
+                 int32_t *level1_prefix, uint8_t *level2_inout, uint8_t *level1_normal,
+                 uint8_t *level2_normal) {
+  if (!prefix || !cfg) return GPV_ERR_INVALID;
+  const std::string p(prefix);
+  const size_t N1 = (size_t)cfg->ndiv[0] * cfg->ndiv[1] * cfg->ndiv[2];
+  const size_t cells = cfg->has_level2 ? (size_t)cfg->ndiv2[0] * cfg->ndiv2[1] * cfg->ndiv2[2] : 0;
+  const size_t L2 = (size_t)cfg->num_boundary * cells;
+  if ((level1_prefix || level2_inout || level2_normal) && !cfg->has_level2) return GPV_ERR_INVALID;
+  auto load = [&](const char *name, void *dst, size_t bytes) -> int {
+    if (!dst) return GPV_OK;
+    std::ifstream f(p + name, std::ios::binary);
+    if (!f.good()) return GPV_ERR_IO;
+    if (bytes) f.read(static_cast<char *>(dst), (std::streamsize)bytes);
+    return (size_t)f.gcount() == bytes ? GPV_OK : GPV_ERR_IO;
+  };
+  int rc = load("Level1InOut.raw", level1_inout, N1);
+  if (!rc) rc = load("Level1BoundaryPrefixSum.raw", level1_prefix, 4 * N1);
+  if (!rc) rc = load("Level2InOut.raw", level2_inout, L2);
+  if (!rc) rc = load("Level1Normal.raw", level1_normal, 3 * N1);
+  if (!rc) rc = load("Level2Normal.raw", level2_normal, 3 * L2);
+  return rc;
+}
+
 // ---- generators ----------------------------------------------------------------------------------
 
 int64_t gpv_gen_uvsphere(uint64_t seed, int32_t nlon, int32_t nlat, const float center[3],

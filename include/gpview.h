@@ -224,6 +224,31 @@ int gpv_write_raw(const char *prefix, const gpv_result *res, const uint8_t *leve
 int gpv_write_raw_normals(const char *prefix, const gpv_result *res, const uint8_t *level1_normal,
                           const uint8_t *level2_normal);
 
+/* Reading a saved voxelization back (host).  <prefix>VoxelConfig.txt, in the line order
+ * Object::SaveVoxelization writes (src/Object.cpp:3009-3022): prefix; bbox min; bbox max; Level1
+ * divisions; Level1 grid size; Level1 inside count; Level1 boundary count; and with Level2: Level2
+ * divisions; Level2 grid size; Level2 inside count; Level2 boundary count. */
+typedef struct {
+    float bbox_min[3], bbox_max[3];
+    int32_t ndiv[3];
+    float grid_size[3];
+    int64_t num_level1_inside;
+    int64_t num_boundary;        /* Level1 boundary voxels = Level2 blocks */
+    int32_t has_level2;
+    int32_t ndiv2[3];
+    float grid_size2[3];
+    int64_t num_level2_inside;
+    int64_t num_level2_boundary;
+} gpv_voxel_config;
+int gpv_read_voxel_config(const char *prefix, gpv_voxel_config *out);
+/* Reads the .raw files of a saved voxelization into host buffers sized from the config (any
+ * buffer may be NULL to skip its file): Level1InOut (N1 bytes), Level1BoundaryPrefixSum (N1
+ * int32), Level2InOut (B*n2^3 bytes), Level1Normal (3*N1 bytes), Level2Normal (3*B*n2^3 bytes).
+ * A file shorter than its size is GPV_ERR_IO. */
+int gpv_read_raw(const char *prefix, const gpv_voxel_config *cfg, uint8_t *level1_inout,
+                 int32_t *level1_prefix, uint8_t *level2_inout, uint8_t *level1_normal,
+                 uint8_t *level2_normal);
+
 /* ---- seeded synthetic meshes (host) ---------------------------------------------------------- */
 /* Each returns the triangle count; with tris == NULL only the count is returned. */
 int64_t gpv_gen_uvsphere(uint64_t seed, int32_t nlon, int32_t nlat, const float center[3],

@@ -150,3 +150,69 @@ def test_invalid_grid_rejected(built):
     gpv = built
     with pytest.raises(gpv.GpvError):
         gpv.grid_padded((0, 0, 0), (1, 1, 1), 2, 4)  # needs at least 3 cells per axis
+
+
+def test_raw_round_trip_and_config(built, tmp_path):
+    """gpv_write_raw + gpv_write_raw_normals, then gpv_read_voxel_config + gpv_read_raw give back
+    the same arrays and counts (the golden sphere's outputs)."""
+    import glob
+
+    gpv = built
+    z = np.load(sorted(glob.glob(os.path.join(ROOT, "tests", "golden", "mesh_sphere288.npz")))[0])
+    res = gpv.Result()
+    spec = res.spec
+    spec.bbox_min[:] = z["bbox_min"]
+    spec.bbox_max[:] = z["bbox_max"]
+    spec.ndiv[:] = z["ndiv"]
+    spec.ndiv2[:] = z["ndiv2"]
+    l1 = (z["level1"] * 127).astype(np.uint8)
+    l2 = (z["level2"] * 127).astype(np.uint8)
+    res.num_level1 = l1.size
+    res.num_boundary = z["bindex"].size
+    res.num_level1_inside = int((l1 == 127).sum())
+    res.num_level2_inside = int((l2 == 127).sum())
+    res.num_level2_boundary = int((l2 == 254).sum())
+    for a in range(3):
+        res.grid_size[a] = 0.125
+        res.grid_size2[a] = 0.03125
+    pre = z["prefix"].astype(np.int32)
+    n1 = gpv.normal_bytes(z["level1_normal"])
+    n2 = gpv.normal_bytes(z["level2_normal"])
+    p = str(tmp_path / "Obj-1")
+    L = gpv.lib()
+    v = lambda a: a.ctypes.data_as(C.c_void_p)  # noqa: E731
+    assert L.gpv_write_raw(p.encode(), C.byref(res), v(l1), v(pre), v(l2)) == 0
+    assert L.gpv_write_raw_normals(p.encode(), C.byref(res), v(n1), v(n2)) == 0
+    back = gpv.read_raw(p)
+    cfg = back["config"]
+    assert list(cfg.ndiv) == list(z["ndiv"]) and list(cfg.ndiv2) == list(z["ndiv2"])
+    assert cfg.num_boundary == res.num_boundary and cfg.has_level2 == 1
+    assert cfg.num_level1_inside == res.num_level1_inside
+    assert cfg.num_level2_boundary == res.num_level2_boundary
+    np.testing.assert_array_equal(back["level1InOut"], l1)
+    np.testing.assert_array_equal(back["boundaryPrefixSum"], pre)
+    np.testing.assert_array_equal(back["level2InOut"], l2)
+    np.testing.assert_array_equal(back["level1Normal"], n1)
+    np.testing.assert_array_equal(back["level2Normal"], n2)
+    # a truncated file is an I/O error, a missing config a parse/IO error
+    with open(p + "Level2InOut.raw", "r+b") as f:
+        f.truncate(10)
+    with pytest.raises(gpv.GpvError):
+        gpv.read_raw(p)
+    with pytest.raises(gpv.GpvError):
+        gpv.read_voxel_config(str(tmp_path / "nothing"))
+
+
+def test_read_raw_object_reference_layout(built, tmp_path):
+    """Object.ReadRAWObject: 48 x 64 x 64 bytes, solid = value % 2 (src/Object.cpp:319-392)."""
+    gpv = built
+    data = np.random.default_rng(3).choice(np.array([0, 127, 254], np.uint8), 48 * 64 * 64)
+    path = tmp_path / "x.raw"
+    data.tofile(path)
+    obj = gpv.Object()
+    obj.bBoxMin = np.zeros(3, np.float32)
+    obj.bBoxMax = np.ones(3, np.float32)
+    vd = obj.ReadRAWObject(str(path))
+    np.testing.assert_array_equal(vd.level1InOut, data)
+    np.testing.assert_array_equal(vd.solid, data % 2)
+    assert (vd.numDivX, vd.numDivY, vd.numDivZ) == (48, 64, 64)
