@@ -475,6 +475,7 @@ def main():
     launches = gpv.kernel_launches() - launches0
     clk = clocks.stop()
     calls, stage_ms = ctx.stage_times()
+    hcalls, host_ms = ctx.host_times()
     ctx.set_timing(False)
     if dist:
         dist.barrier()
@@ -537,7 +538,8 @@ def main():
             "voxels_per_s": (N1 + B * cells) * args.steps * world / t_total,
             "e2e": {"value": e2e_value, "unit": "tests/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h, "ms_per_step": e2e_t * 1e3 / args.steps},
-            "gpu_launches": launches, "roofline": roof, "clocks": clk}
+            "gpu_launches": launches, "roofline": roof, "clocks": clk,
+            "host_ms_per_call": {k: v / max(hcalls, 1) for k, v in host_ms.items()}}
     tuned = (128, 8)
     if args.batch > 0:
         line["batched"] = batch_bench(gpv, ctx, torch, stream, local, args)

@@ -94,6 +94,7 @@ def lib():
     L.gpv_set_tile.argtypes = [C.c_void_p, C.c_int]
     L.gpv_set_timing.argtypes = [C.c_void_p, C.c_int]
     L.gpv_stage_times.argtypes = [C.c_void_p, C.POINTER(C.c_double), C.c_int]
+    L.gpv_host_times.argtypes = [C.c_void_p, C.POINTER(C.c_double), C.c_int]
     L.gpv_kernel_launches.restype = C.c_uint64
     L.gpv_grid_padded.argtypes = [f3, f3, C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.POINTER(GridSpec)]
     L.gpv_grid_reference.argtypes = [f3, f3, C.c_float, C.c_int32, C.c_int32, C.POINTER(GridSpec)]
@@ -258,6 +259,14 @@ class Context:
         ms = (C.c_double * 9)()
         calls = lib().gpv_stage_times(self._h, ms, 9)
         return calls, {k: ms[i] for i, k in enumerate(self.STAGES)}
+
+    HOST_SEGMENTS = ("setup", "first_phase", "planning", "second_phase", "results")
+
+    def host_times(self):
+        """(calls, {segment: accumulated host ms}) from the host clock around each call."""
+        ms = (C.c_double * 5)()
+        calls = lib().gpv_host_times(self._h, ms, 5)
+        return calls, {k: ms[i] for i, k in enumerate(self.HOST_SEGMENTS)}
 
     def set_graphs(self, on=True):
         self._check(lib().gpv_set_graphs(self._h, int(bool(on))), "set_graphs")

@@ -191,6 +191,7 @@ int gpv_set_timing(gpv_ctx *ctx, int on) {
       if (cudaEventCreate(&ctx->ev[i]) != cudaSuccess) return GPV_ERR_CUDA;
   ctx->timing = on != 0;
   for (double &v : ctx->stage_ms) v = 0.0;
+  for (double &v : ctx->host_ms) v = 0.0;
   ctx->stage_calls = 0;
   return GPV_OK;
 }
@@ -198,6 +199,12 @@ int gpv_set_timing(gpv_ctx *ctx, int on) {
 int gpv_stage_times(gpv_ctx *ctx, double *ms, int n) {
   if (!ctx || !ms) return GPV_ERR_INVALID;
   for (int i = 0; i < n && i < gpv_ctx::kStages; ++i) ms[i] = ctx->stage_ms[i];
+  return (int)ctx->stage_calls;
+}
+
+int gpv_host_times(gpv_ctx *ctx, double *ms, int n) {
+  if (!ctx || !ms) return GPV_ERR_INVALID;
+  for (int i = 0; i < n && i < 5; ++i) ms[i] = ctx->host_ms[i];
   return (int)ctx->stage_calls;
 }
 
@@ -353,12 +360,16 @@ int gpv_result_release(gpv_ctx *ctx, gpv_result *res) {
   }
   cudaSetDevice(ctx->device);
   if (set) {
-    cudaFreeAsync(set->l1, 0);
-    cudaFreeAsync(set->prefix, 0);
-    cudaFreeAsync(set->bindex, 0);
-    cudaFreeAsync(set->l2, 0);
-    if (set->l1n) cudaFreeAsync(set->l1n, 0);
-    if (set->l2n) cudaFreeAsync(set->l2n, 0);
+    // freed on the stream that made them, so the next call on that stream reuses the memory
+    // directly (a free on another stream would make the pool map fresh memory for the next
+    // large result)
+    cudaStream_t fs = set->stream;
+    cudaFreeAsync(set->l1, fs);
+    cudaFreeAsync(set->prefix, fs);
+    cudaFreeAsync(set->bindex, fs);
+    cudaFreeAsync(set->l2, fs);
+    if (set->l1n) cudaFreeAsync(set->l1n, fs);
+    if (set->l2n) cudaFreeAsync(set->l2n, fs);
   }
   res->level1_inout = nullptr;
   res->level1_prefix = nullptr;

@@ -135,6 +135,9 @@ int run_batch(gpv_ctx *ctx, int n, const float *const *d_tris, const int64_t *T,
     if (e_ != cudaSuccess) return ctx_cuda_fail(ctx, e_, #call);    \
   } while (0)
   if (n <= 0) return ctx_fail(ctx, GPV_ERR_INVALID, "empty batch");
+  using HClock = std::chrono::steady_clock;
+  HClock::time_point ht[6];
+  ht[0] = HClock::now();
   std::vector<GridHost> gh(n);
   for (int m = 0; m < n; ++m) {
     if (grid_derive(specs[m], gh[m]) != GPV_OK)
@@ -289,6 +292,7 @@ int run_batch(gpv_ctx *ctx, int n, const float *const *d_tris, const int64_t *T,
   uint32_t *keys, *vals;
   CK(ws.get(&keys, (size_t)pair_cap));
   CK(ws.get(&vals, (size_t)pair_cap));
+  ht[1] = HClock::now();
   CK(run_phase(ctx, 0, s, capturing, [&] {
     mark(0);
     launch_prep(bd, s);
@@ -305,6 +309,7 @@ int run_batch(gpv_ctx *ctx, int n, const float *const *d_tris, const int64_t *T,
   }));
   CK(cudaMemcpyAsync(ctx->h_stats, stats, n * sizeof(MeshStats), cudaMemcpyDeviceToHost, s));
   CK(cudaStreamSynchronize(s));
+  ht[2] = HClock::now();
   {
     // the same bases the device computed, for the host copy of the descriptors
     int64_t caps = 0, need = 0;
@@ -393,6 +398,7 @@ int run_batch(gpv_ctx *ctx, int n, const float *const *d_tris, const int64_t *T,
     CK(cudaMemcpyAsync(d_tiles, ctx->h_tiles, ntiles * sizeof(SortTile), cudaMemcpyHostToDevice, s));
     CK(cudaMemcpyAsync(d_tb, ctx->h_tb, (n + 1) * sizeof(int64_t), cudaMemcpyHostToDevice, s));
   }
+  ht[3] = HClock::now();
   CK(run_phase(ctx, 1, s, capturing, [&] {
     mark(5);
     launch_expand(bd, wpre, s);
@@ -423,6 +429,7 @@ int run_batch(gpv_ctx *ctx, int n, const float *const *d_tris, const int64_t *T,
   CK(cudaMemcpyAsync(ctx->h_stats, stats, n * sizeof(MeshStats), cudaMemcpyDeviceToHost, s));
   CK(cudaMemcpyAsync(ctx->h_u32, wtot, 8, cudaMemcpyDeviceToHost, s));
   CK(cudaStreamSynchronize(s));
+  ht[4] = HClock::now();
   if (ctx->timing) {
     // stages: 0 prep, 1 level1, 2 fill finish + boundary scan, 3 expand, 4 sort + lists,
     // 5 level2 (work items + kernel), 6 the Level2 kernel alone
@@ -477,6 +484,11 @@ int run_batch(gpv_ctx *ctx, int n, const float *const *d_tris, const int64_t *T,
       r.level1_normal = static_cast<uint8_t *>(set->l1n) + res_l1n[m];
       r.level2_normal = static_cast<uint8_t *>(set->l2n) + 3 * l2off[m] * nsz;
     }
+  }
+  if (ctx->timing) {
+    ht[5] = HClock::now();
+    for (int k = 0; k < 5; ++k)
+      ctx->host_ms[k] += std::chrono::duration<double, std::milli>(ht[k + 1] - ht[k]).count();
   }
   return GPV_OK;
 #undef CK

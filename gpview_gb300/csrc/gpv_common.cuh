@@ -57,41 +57,6 @@ __device__ __forceinline__ float fm(float a, float b) { return __fmul_rn(a, b); 
 __device__ __forceinline__ float fa(float a, float b) { return __fadd_rn(a, b); }
 __device__ __forceinline__ float fs(float a, float b) { return __fsub_rn(a, b); }
 
-// ---- paired FP32: two IEEE round-to-nearest operations per instruction (the f32x2 forms of
-// sm_100 and later).  Each half rounds exactly as the scalar __fmul_rn/__fadd_rn/__fsub_rn, so a
-// predicate evaluated in pairs is bit-identical to its scalar evaluation.
-typedef unsigned long long f32x2;
-__device__ __forceinline__ f32x2 pk(float lo, float hi) {
-  f32x2 r;
-  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
-  return r;
-}
-__device__ __forceinline__ float lo_of(f32x2 v) {
-  float a, b;
-  asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(v));
-  return a;
-}
-__device__ __forceinline__ float hi_of(f32x2 v) {
-  float a, b;
-  asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(v));
-  return b;
-}
-__device__ __forceinline__ f32x2 fm2(f32x2 a, f32x2 b) {
-  f32x2 r;
-  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
-  return r;
-}
-__device__ __forceinline__ f32x2 fa2(f32x2 a, f32x2 b) {
-  f32x2 r;
-  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
-  return r;
-}
-__device__ __forceinline__ f32x2 fs2(f32x2 a, f32x2 b) {
-  f32x2 r;
-  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
-  return r;
-}
-
 // Level1 cell of a coordinate: int(((v-min)/(max-min))*n) with the decrement at v == max
 // (src/Object.cpp:2280-2306).  The quotient is clamped to [-1, n+1] before the conversion so
 // that vertices outside the grid (undefined in the reference) give a defined index.
@@ -226,63 +191,6 @@ __device__ __forceinline__ void l2_cell_range(float tmin, float tmax, float c0, 
   hi = min((int)floorf(f1), n2 - 1);
 }
 
-// sat_z with the paired projections: the two vertex projections of each edge-cross axis, the
-// radii of an edge's X and Y axes, the x/y normal components and the two plane dot products run
-// as f32x2 pairs; the operations and their order per value are those of sat_z.
-__device__ __forceinline__ bool sat_z2(const SatCol &s, const float *V, float cz,
-                                       const float h[3]) {
-  const f32x2 czz = pk(cz, cz);
-  const f32x2 z02 = fs2(pk(V[2], V[8]), czz);  // (v0z, v2z)
-  const float v0z = lo_of(z02), v2z = hi_of(z02), v1z = fs(V[5], cz);
-  const f32x2 ez01 = fs2(pk(v1z, v2z), pk(v0z, v1z));  // (e0z, e1z)
-  const float e0z = lo_of(ez01), e1z = hi_of(ez01), e2z = fs(v0z, v2z);
-  const f32x2 hyx = pk(h[1], h[0]), hzz = pk(h[2], h[2]);
-  {
-    const f32x2 y02 = pk(s.v0y, s.v2y), x02 = pk(s.v0x, s.v2x);
-    // edge 0: X01 and Y02 on (v0, v2)
-    f32x2 P = fs2(fm2(pk(e0z, e0z), y02), fm2(pk(s.e0y, s.e0y), z02));
-    f32x2 Q = fa2(fm2(pk(-e0z, -e0z), x02), fm2(pk(s.e0x, s.e0x), z02));
-    float fz = fabsf(e0z);
-    f32x2 R = fa2(fm2(pk(fz, fz), hyx), fm2(pk(fabsf(s.e0y), fabsf(s.e0x)), hzz));
-    if (sep(lo_of(P), hi_of(P), lo_of(R))) return false;
-    if (sep(lo_of(Q), hi_of(Q), hi_of(R))) return false;
-    // edge 1: X01 and Y02 on (v0, v2)
-    P = fs2(fm2(pk(e1z, e1z), y02), fm2(pk(s.e1y, s.e1y), z02));
-    Q = fa2(fm2(pk(-e1z, -e1z), x02), fm2(pk(s.e1x, s.e1x), z02));
-    fz = fabsf(e1z);
-    R = fa2(fm2(pk(fz, fz), hyx), fm2(pk(fabsf(s.e1y), fabsf(s.e1x)), hzz));
-    if (sep(lo_of(P), hi_of(P), lo_of(R))) return false;
-    if (sep(lo_of(Q), hi_of(Q), hi_of(R))) return false;
-  }
-  {
-    // edge 2: X2 and Y1 on (v0, v1)
-    const f32x2 z01 = pk(v0z, v1z), y01 = pk(s.v0y, s.v1y), x01 = pk(s.v0x, s.v1x);
-    const f32x2 P = fs2(fm2(pk(e2z, e2z), y01), fm2(pk(s.e2y, s.e2y), z01));
-    const f32x2 Q = fa2(fm2(pk(-e2z, -e2z), x01), fm2(pk(s.e2x, s.e2x), z01));
-    const float fz = fabsf(e2z);
-    const f32x2 R = fa2(fm2(pk(fz, fz), hyx), fm2(pk(fabsf(s.e2y), fabsf(s.e2x)), hzz));
-    if (sep(lo_of(P), hi_of(P), lo_of(R))) return false;
-    if (sep(lo_of(Q), hi_of(Q), hi_of(R))) return false;
-  }
-  // box z axis
-  float mn = v0z, mx = v0z;
-  if (v1z < mn) mn = v1z;
-  if (v1z > mx) mx = v1z;
-  if (v2z < mn) mn = v2z;
-  if (v2z > mx) mx = v2z;
-  if (mn > h[2] || mx < -h[2]) return false;
-  // plane: (nx, ny) paired, nz scalar; (dmin, dmax) paired
-  const f32x2 nxy = fs2(fm2(pk(s.e0y, e0z), pk(e1z, s.e1x)), fm2(pk(e0z, s.e0x), pk(s.e1y, e1z)));
-  const float nx = lo_of(nxy), ny = hi_of(nxy);
-  const float nz = fs(fm(s.e0x, s.e1y), fm(s.e0y, s.e1x));
-  const f32x2 L0 = fs2(nx > 0.0f ? pk(-h[0], h[0]) : pk(h[0], -h[0]), pk(s.v0x, s.v0x));
-  const f32x2 L1 = fs2(ny > 0.0f ? pk(-h[1], h[1]) : pk(h[1], -h[1]), pk(s.v0y, s.v0y));
-  const f32x2 L2 = fs2(nz > 0.0f ? pk(-h[2], h[2]) : pk(h[2], -h[2]), pk(v0z, v0z));
-  const f32x2 D = fa2(fa2(fm2(pk(nx, nx), L0), fm2(pk(ny, ny), L1)), fm2(pk(nz, nz), L2));
-  if (lo_of(D) > 0.0f) return false;
-  return hi_of(D) >= 0.0f;
-}
-
 __device__ __forceinline__ bool tri_box(const float *V, const float c[3], const float h[3]) {
   SatCol s;
   if (!sat_col(V, c[0], c[1], h, s)) return false;
@@ -337,30 +245,6 @@ __device__ __forceinline__ bool ray_t(const RayTri &r, const RayCol &c, float oz
   const float q2 = fs(fm(c.Tx, r.e1y), fm(c.Ty, r.e1x));
   const float t = fm(fa(fa(fm(r.e2x, q0), fm(r.e2y, q1)), fm(r.e2z, q2)), r.inv_det);
   return t > thr;
-}
-
-// ray_t over the n origin heights oz[0..n), two heights per f32x2 operation; bit r is set when
-// t > thr at oz[r].  Per height the operations and their order are those of ray_t.
-__device__ __forceinline__ uint32_t ray_t_bits(const RayTri &r, const RayCol &c, const float *oz,
-                                               int n, float thr) {
-  const float A = fm(c.Ty, r.e1z), B = fm(c.Tx, r.e1z);
-  const float q2 = fs(fm(c.Tx, r.e1y), fm(c.Ty, r.e1x));
-  const float C = fm(r.e2z, q2);
-  const f32x2 AA = pk(A, A), BB = pk(B, B), CC = pk(C, C), v1z = pk(r.v1z, r.v1z);
-  const f32x2 e1y = pk(r.e1y, r.e1y), e1x = pk(r.e1x, r.e1x);
-  const f32x2 e2x = pk(r.e2x, r.e2x), e2y = pk(r.e2y, r.e2y), inv = pk(r.inv_det, r.inv_det);
-  uint32_t bits = 0;
-  int k = 0;
-  for (; k + 1 < n; k += 2) {
-    const f32x2 Tz = fs2(pk(__ldg(oz + k), __ldg(oz + k + 1)), v1z);
-    const f32x2 q0 = fs2(AA, fm2(Tz, e1y));
-    const f32x2 q1 = fs2(fm2(Tz, e1x), BB);
-    const f32x2 t = fm2(fa2(fa2(fm2(e2x, q0), fm2(e2y, q1)), CC), inv);
-    bits |= (lo_of(t) > thr ? 1u : 0u) << k;
-    bits |= (hi_of(t) > thr ? 1u : 0u) << (k + 1);
-  }
-  if (k < n && ray_t(r, c, __ldg(oz + k), thr)) bits |= 1u << k;
-  return bits;
 }
 
 // ---- PTX helpers: mbarrier + bulk async copy (TMA, non-tensor) into this CTA's shared memory.

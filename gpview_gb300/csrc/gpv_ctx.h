@@ -1,5 +1,6 @@
 // gpv_ctx.h -- the library context (one per host thread) and helpers shared by the host files.
 #pragma once
+#include <chrono>
 #include <memory>
 #include <mutex>
 #include <string>
@@ -27,6 +28,10 @@ struct gpv_ctx {
   cudaEvent_t ev[kStages + 1] = {};
   double stage_ms[kStages] = {};       // accumulated stage durations
   uint64_t stage_calls = 0;
+  // host-side time per call segment (timing on): 0 setup up to the first recorded launch,
+  // 1 first launch to the first synchronisation returning, 2 planning between the
+  // synchronisations, 3 second launch to the last synchronisation returning, 4 result assembly
+  double host_ms[5] = {};
   std::string err;
   int tile = 128;                      // Level1 triangles per tile (autotuned)
   int l2_chunk_cap = 8;                // Level2 boundary voxels per chunk, upper bound (autotuned)

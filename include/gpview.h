@@ -135,6 +135,11 @@ int gpv_autotune(gpv_ctx *ctx, int32_t n, const float *const *d_tris, const int6
  * (up to 9 slots; unused slots stay 0). */
 int gpv_set_timing(gpv_ctx *ctx, int on);
 int gpv_stage_times(gpv_ctx *ctx, double *ms, int n);
+/* Host-side milliseconds per call segment, accumulated while timing is on: 0 setup up to the
+ * first recorded launch sequence, 1 from there to the first synchronisation returning, 2 planning
+ * between the synchronisations, 3 the second launch sequence to the last synchronisation
+ * returning, 4 result assembly.  Returns the number of timed calls. */
+int gpv_host_times(gpv_ctx *ctx, double *ms, int n);
 /* Number of kernels this library has launched in this process. */
 uint64_t gpv_kernel_launches(void);
 
@@ -161,6 +166,8 @@ int gpv_result_copy_to_host(gpv_ctx *ctx, const gpv_result *res, uint8_t *level1
  * buffers (either may be NULL) and wait for the stream. */
 int gpv_result_copy_normals_to_host(gpv_ctx *ctx, const gpv_result *res, void *level1_normal,
                                     void *level2_normal, cudaStream_t stream);
+/* Frees a result's device arrays (stream-ordered, on the stream the result was made on: release
+ * results before destroying that stream). */
 int gpv_result_release(gpv_ctx *ctx, gpv_result *res);
 
 /* Batched path: n meshes in one launch sequence (persistent work-queue kernels).
