@@ -55,7 +55,12 @@ class Result(C.Structure):
                 ("boundary_index", C.c_void_p), ("level2_inout", C.c_void_p),
                 ("handle", C.c_uint64), ("level1_normal", C.c_void_p),
                 ("level2_normal", C.c_void_p), ("normal_mode", C.c_int32),
-                ("reserved", C.c_int32)]
+                ("hierarchy_levels", C.c_int32), ("hierarchy", C.c_void_p)]
+
+
+# gpv_box: one node of the voxel box hierarchy
+BOX_DTYPE = np.dtype([("mid", np.float32, 3), ("half", np.float32, 3), ("solid", np.int32),
+                      ("child1", np.int32), ("child2", np.int32), ("index", np.int32)])
 
 
 NORMALS_OFF, NORMALS_BYTES, NORMALS_FLOAT = 0, 1, 2
@@ -111,6 +116,9 @@ def lib():
     L.gpv_write_raw.argtypes = [C.c_char_p, C.POINTER(Result), C.c_void_p, C.c_void_p, C.c_void_p]
     L.gpv_write_raw_normals.argtypes = [C.c_char_p, C.POINTER(Result), C.c_void_p, C.c_void_p]
     L.gpv_set_normals.argtypes = [C.c_void_p, C.c_int]
+    L.gpv_set_hierarchy.argtypes = [C.c_void_p, C.c_int]
+    L.gpv_result_copy_hierarchy_to_host.argtypes = [C.c_void_p, C.POINTER(Result), C.c_void_p,
+                                                    C.c_void_p]
     L.gpv_read_voxel_config.argtypes = [C.c_char_p, C.POINTER(VoxelConfig)]
     L.gpv_read_raw.argtypes = [C.c_char_p, C.POINTER(VoxelConfig), C.c_void_p, C.c_void_p,
                                C.c_void_p, C.c_void_p, C.c_void_p]
@@ -345,6 +353,18 @@ class Context:
             self._h, C.byref(res), l1.ctypes.data_as(C.c_void_p), l2.ctypes.data_as(C.c_void_p),
             C.c_void_p(stream)), "copy_normals_to_host")
         return l1, l2
+
+    def set_hierarchy(self, on=True):
+        """Build the voxel box hierarchy (Object::BuildHierarchy) with the next calls."""
+        self._check(lib().gpv_set_hierarchy(self._h, int(bool(on))), "set_hierarchy")
+
+    def fetch_hierarchy(self, res, stream=0):
+        """The result's hierarchy as a structured array of num_level1 - 1 boxes (BOX_DTYPE)."""
+        out = np.empty(max(res.num_level1 - 1, 1), BOX_DTYPE)
+        self._check(lib().gpv_result_copy_hierarchy_to_host(
+            self._h, C.byref(res), out.ctypes.data_as(C.c_void_p), C.c_void_p(stream)),
+            "copy_hierarchy_to_host")
+        return out[:res.num_level1 - 1]
 
     def release(self, res):
         self._check(lib().gpv_result_release(self._h, C.byref(res)), "release")

@@ -167,6 +167,7 @@ void gpv_destroy(gpv_ctx *ctx) {
     cudaFree(r->l2);
     if (r->l1n) cudaFree(r->l1n);
     if (r->l2n) cudaFree(r->l2n);
+    if (r->hier) cudaFree(r->hier);
   }
   ctx->owned.clear();
   for (cudaGraphExec_t &ge : ctx->gexec)
@@ -213,6 +214,24 @@ uint64_t gpv_kernel_launches(void) { return gpv::launch_count(); }
 int gpv_set_graphs(gpv_ctx *ctx, int on) {
   if (!ctx) return GPV_ERR_INVALID;
   ctx->graphs = on != 0;
+  return GPV_OK;
+}
+
+int gpv_set_hierarchy(gpv_ctx *ctx, int on) {
+  if (!ctx) return GPV_ERR_INVALID;
+  ctx->hierarchy = on != 0;
+  return GPV_OK;
+}
+
+int gpv_result_copy_hierarchy_to_host(gpv_ctx *ctx, const gpv_result *res, gpv_box *out,
+                                      cudaStream_t s) {
+  if (!ctx || !res || !out) return GPV_ERR_INVALID;
+  if (!res->hierarchy || res->num_level1 < 2)
+    return ctx_fail(ctx, GPV_ERR_INVALID, "the result has no hierarchy (gpv_set_hierarchy, power-of-two grid)");
+  cudaSetDevice(ctx->device);
+  GPV_CUDA(cudaMemcpyAsync(out, res->hierarchy, sizeof(gpv_box) * (res->num_level1 - 1),
+                           cudaMemcpyDeviceToHost, s));
+  GPV_CUDA(cudaStreamSynchronize(s));
   return GPV_OK;
 }
 
@@ -370,6 +389,7 @@ int gpv_result_release(gpv_ctx *ctx, gpv_result *res) {
     cudaFreeAsync(set->l2, fs);
     if (set->l1n) cudaFreeAsync(set->l1n, fs);
     if (set->l2n) cudaFreeAsync(set->l2n, fs);
+    if (set->hier) cudaFreeAsync(set->hier, fs);
   }
   res->level1_inout = nullptr;
   res->level1_prefix = nullptr;
@@ -377,6 +397,7 @@ int gpv_result_release(gpv_ctx *ctx, gpv_result *res) {
   res->level2_inout = nullptr;
   res->level1_normal = nullptr;
   res->level2_normal = nullptr;
+  res->hierarchy = nullptr;
   res->handle = 0;
   return GPV_OK;
 }

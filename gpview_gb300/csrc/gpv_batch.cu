@@ -152,7 +152,8 @@ int run_batch(gpv_ctx *ctx, int n, const float *const *d_tris, const int64_t *T,
   const size_t nsz = nmode == GPV_NORMALS_FLOAT ? sizeof(float) : 1;  // bytes per normal value
 
   // ---- sizes and per-mesh bases
-  std::vector<int64_t> tab_off(n + 1, 0), res_l1(n + 1, 0), res_pre(n + 1, 0), res_l1n(n + 1, 0);
+  std::vector<int64_t> tab_off(n + 1, 0), res_l1(n + 1, 0), res_pre(n + 1, 0), res_l1n(n + 1, 0),
+      res_hier(n + 1, 0);
   std::vector<MeshDesc> md(n);
   int64_t tris = 0, tiles = 0, fwarps = 0, rows = 0, words = 0, togg = 0;
   int max_keybits = 1, warp_words = 0;
@@ -178,6 +179,7 @@ int run_batch(gpv_ctx *ctx, int n, const float *const *d_tris, const int64_t *T,
     res_l1[m + 1] = res_l1[m] + (int64_t)al16(g.N1);
     res_pre[m + 1] = res_pre[m] + (int64_t)al16(g.N1);  // int32 elements, 64-byte aligned
     res_l1n[m + 1] = res_l1n[m] + (int64_t)al16(3 * g.N1 * nsz);  // bytes
+    res_hier[m + 1] = res_hier[m] + ((ctx->hierarchy && hierarchy_levels(g.N1)) ? g.N1 - 1 : 0);
     max_keybits = std::max(max_keybits, g.key_bits);
     max_T = std::max(max_T, T[m]);
     any_l2 = any_l2 || g.level2;
@@ -224,6 +226,7 @@ int run_batch(gpv_ctx *ctx, int n, const float *const *d_tris, const int64_t *T,
   set->stream = s;
   CK(cudaMallocAsync(&set->l1, std::max<int64_t>(res_l1[n], 16), s));
   CK(cudaMallocAsync(&set->prefix, 4 * std::max<int64_t>(res_pre[n], 16), s));
+  if (res_hier[n] > 0) CK(cudaMallocAsync(&set->hier, sizeof(gpv_box) * res_hier[n], s));
   if (nmode) {
     // voxels without recorded triangles keep the zero normal: 0.0f, or byte 127 (0 * scale + 127)
     CK(cudaMallocAsync(&set->l1n, std::max<int64_t>(res_l1n[n], 16), s));
@@ -280,7 +283,8 @@ int run_batch(gpv_ctx *ctx, int n, const float *const *d_tris, const int64_t *T,
     if (set->l2) cudaFreeAsync(set->l2, s);
     if (set->l1n) cudaFreeAsync(set->l1n, s);
     if (set->l2n) cudaFreeAsync(set->l2n, s);
-    set->l1 = set->prefix = set->bindex = set->l2 = set->l1n = set->l2n = nullptr;
+    if (set->hier) cudaFreeAsync(set->hier, s);
+    set->l1 = set->prefix = set->bindex = set->l2 = set->l1n = set->l2n = set->hier = nullptr;
     return ctx_fail(ctx, code, msg);
   };
 
@@ -402,6 +406,9 @@ int run_batch(gpv_ctx *ctx, int n, const float *const *d_tris, const int64_t *T,
   CK(run_phase(ctx, 1, s, capturing, [&] {
     mark(5);
     launch_expand(bd, wpre, s);
+    for (int m = 0; m < n; ++m)
+      if (res_hier[m + 1] > res_hier[m])
+        launch_hierarchy(md[m].g, md[m].iplane, static_cast<gpv_box *>(set->hier) + res_hier[m], s);
     mark(6);
     if (do_l2) {
       const bool in_alt = sort_pairs_seg(bd, d_tiles, d_tb, ntiles, keys, vals, kalt, valt, P2,
@@ -480,6 +487,10 @@ int run_batch(gpv_ctx *ctx, int n, const float *const *d_tris, const int64_t *T,
     r.level2_inout = static_cast<uint8_t *>(set->l2) + l2off[m];
     r.handle = handle;
     r.normal_mode = nmode;
+    if (res_hier[m + 1] > res_hier[m]) {
+      r.hierarchy = static_cast<gpv_box *>(set->hier) + res_hier[m];
+      r.hierarchy_levels = hierarchy_levels(gh[m].N1);
+    }
     if (nmode) {
       r.level1_normal = static_cast<uint8_t *>(set->l1n) + res_l1n[m];
       r.level2_normal = static_cast<uint8_t *>(set->l2n) + 3 * l2off[m] * nsz;

@@ -14,6 +14,7 @@ namespace gpv {
 struct ResultSet {
   void *l1 = nullptr, *prefix = nullptr, *bindex = nullptr, *l2 = nullptr;
   void *l1n = nullptr, *l2n = nullptr;  // normals (optional)
+  void *hier = nullptr;                 // voxel box hierarchy (optional)
   cudaStream_t stream = 0;
   int refs = 0;
 };
@@ -37,6 +38,7 @@ struct gpv_ctx {
   int l2_chunk_cap = 8;                // Level2 boundary voxels per chunk, upper bound (autotuned)
   bool graphs = true;                  // record phases B and C as CUDA graphs
   int normals = 0;                     // GPV_NORMALS_* for the next voxelizations
+  bool hierarchy = false;              // build the voxel box hierarchy
   cudaGraphExec_t gexec[2] = {};       // cached executable graphs of phases B and C
   uint64_t graph_launches = 0, graph_instantiations = 0;
   gpv::MeshStats *h_stats = nullptr;   // pinned, h_cap entries

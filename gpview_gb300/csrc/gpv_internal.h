@@ -123,6 +123,10 @@ void launch_face_normals(const BatchDev &bd, cudaStream_t s);
 void launch_normals(const BatchDev &bd, const uint32_t *keys, const uint32_t *vals,
                     const uint32_t *useg, int64_t U, bool any_l2, int num_sms, cudaStream_t s);
 
+// ---- voxel box hierarchy (gpv_hierarchy.cu) ----------------------------------------------------
+int hierarchy_levels(int64_t N1);  // 0 unless N1 is a power of two >= 2
+void launch_hierarchy(const GridDev &g, const uint32_t *iplane, gpv_box *out, cudaStream_t s);
+
 GridDev make_griddev(const GridHost &gh, const float *dtables);
 int64_t table_floats(const GridHost &gh);
 void pack_tables(const GridHost &gh, float *host);

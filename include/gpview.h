@@ -90,8 +90,18 @@ typedef struct {
     void *level1_normal;         /* device, 3 * num_level1 values */
     void *level2_normal;         /* device, 3 * num_boundary * n2x*n2y*n2z values */
     int32_t normal_mode;         /* GPV_NORMALS_* the result was made with */
-    int32_t reserved;
+    int32_t hierarchy_levels;    /* gpv_set_hierarchy: levels of `hierarchy`, else 0 */
+    struct gpv_box *hierarchy;   /* device, num_level1 - 1 boxes, or NULL */
 } gpv_result;
+
+/* One node of the voxel box hierarchy (BBoxData fields used by Object::BuildHierarchy,
+ * includes/Utilities.h:57-77): centre, half size, solid flag, the two children's indices and its
+ * own index.  Level-1 children index the Level1 voxels (x fastest); later levels index nodes. */
+typedef struct gpv_box {
+    float mid[3];
+    float half[3];
+    int32_t solid, child1, child2, index;
+} gpv_box;
 
 /* A triangle soup on the host, as Object::CreateFlatTriangleData builds it
  * (src/Object.cpp:3496-3527): float[num_triangles*9], vertex-major, file face order.
@@ -120,6 +130,12 @@ int gpv_set_level2_chunk(gpv_ctx *ctx, int max_voxels);
 #define GPV_NORMALS_BYTES 1
 #define GPV_NORMALS_FLOAT 2
 int gpv_set_normals(gpv_ctx *ctx, int mode);
+/* Voxel box hierarchy (Object::BuildHierarchy, src/Object.cpp:2750-2867; default off): a binary
+ * tree over the Level1 voxels, whose leaves are the voxel boxes with solid = the inside fill's
+ * parity.  Built for grids whose voxel count is a power of two; others get none. */
+int gpv_set_hierarchy(gpv_ctx *ctx, int on);
+int gpv_result_copy_hierarchy_to_host(gpv_ctx *ctx, const gpv_result *res, gpv_box *out,
+                                      cudaStream_t stream);
 /* Record the Level1 and Level2 launch sequences of each voxelization as CUDA graphs (default on;
  * the executable graphs are cached in the context and updated in place). */
 int gpv_set_graphs(gpv_ctx *ctx, int on);

@@ -391,6 +391,7 @@ typedef struct {
     int64_t T;
     int64_t N1, B;
     uint8_t *state1;     /* 0 outside, 1 inside, 2 boundary */
+    uint8_t *parity;     /* the inside fill alone (before the boundary marks), 0/1 */
     int32_t *prefix;     /* boundaryPrefixSum */
     int32_t *bindex;     /* boundaryIndex */
     int64_t *vstart;     /* per-voxel triangle list CSR (size N1+1) */
@@ -635,6 +636,8 @@ orc_run *orc_create(const float *tris, int64_t T, const orc_spec *s, int fill_mo
     r->N1 = (int64_t)s->n[0] * s->n[1] * s->n[2];
     r->state1 = (uint8_t *)calloc((size_t)r->N1, 1);
     orc_fill_level1(r, fill_mode, nth);
+    r->parity = (uint8_t *)malloc((size_t)r->N1);
+    memcpy(r->parity, r->state1, (size_t)r->N1);
     orc_sat_level1(r, nth);
     /* Compaction (src/Object.cpp:3271-3279): exclusive count of value 2 in linear order. */
     r->prefix = (int32_t *)malloc(sizeof(int32_t) * (size_t)r->N1);
@@ -673,7 +676,7 @@ void orc_free(orc_run *r)
 {
     if (!r) return;
     orc_tables_free(&r->t);
-    free(r->state1); free(r->prefix); free(r->bindex); free(r->vstart); free(r->vtris);
+    free(r->state1); free(r->parity); free(r->prefix); free(r->bindex); free(r->vstart); free(r->vtris);
     free(r);
 }
 
@@ -990,4 +993,101 @@ void orc_level2_normals(const orc_run *r, int64_t b0, int64_t b1, float *out, in
         }
         free(acc);
     }
+}
+
+/* ------------------------------------------------------------------------------------------ */
+/* Voxel box hierarchy                                                                         */
+/* ------------------------------------------------------------------------------------------ */
+
+typedef struct {
+    float mid[3], half[3];
+    int32_t solid, child1, child2, index;
+} orc_box;
+
+/* CombineBBox (src/Object.cpp:2750-2788): two empty boxes give an empty box; one solid box is
+ * copied; two solid boxes give their bounding box as (max+min)/2, (max-min)/2 in float. */
+static void orc_combine(const orc_box *a, int32_t ia, const orc_box *b, int32_t ib, orc_box *o)
+{
+    float mid[3] = {0.f, 0.f, 0.f}, half[3] = {0.f, 0.f, 0.f};
+    if (a->solid == 0 && b->solid == 0) {
+        o->solid = 0;
+    } else if (a->solid == 0) {
+        o->solid = 1;
+        memcpy(mid, b->mid, sizeof mid); memcpy(half, b->half, sizeof half);
+    } else if (b->solid == 0) {
+        o->solid = 1;
+        memcpy(mid, a->mid, sizeof mid); memcpy(half, a->half, sizeof half);
+    } else {
+        o->solid = 1;
+        for (int c = 0; c < 3; ++c) {
+            float amn = a->mid[c] - a->half[c], amx = a->mid[c] + a->half[c];
+            float bmn = b->mid[c] - b->half[c], bmx = b->mid[c] + b->half[c];
+            /* std::max / std::min: (a < b) ? b : a and (b < a) ? b : a */
+            float mx = (amx < bmx) ? bmx : amx, mn = (bmn < amn) ? bmn : amn;
+            mid[c] = (mx + mn) / 2.0f;
+            half[c] = (mx - mn) / 2.0f;
+        }
+    }
+    memcpy(o->mid, mid, sizeof mid);
+    memcpy(o->half, half, sizeof half);
+    o->child1 = ia;
+    o->child2 = ib;
+}
+
+/* Object::BuildHierarchy (src/Object.cpp:2790-2867) over the Level1 voxels: the leaves are the
+ * voxel boxes (centre, half size, solid = the inside fill's parity, :3176-3187); level 1 pairs
+ * x-neighbours, later levels pair along x, y, z in turn (level % 3) with the reference's fallback
+ * when that axis is already one box wide.  out receives N1-1 boxes; level-1 children are the
+ * leaf indices (2i, 2i+1).  Returns the number of levels, or -1 unless N1 is a power of two. */
+int orc_build_hierarchy(const orc_run *r, orc_box *out)
+{
+    const int64_t N1 = r->N1;
+    if (N1 < 2 || (N1 & (N1 - 1))) return -1;
+    int levels = 0;
+    for (int64_t x = N1; x > 1; x >>= 1) ++levels;
+    const int nx = r->s.n[0], ny = r->s.n[1];
+    memset(out, 0, sizeof(orc_box) * (size_t)(N1 - 1));
+    int64_t nlev = N1 / 2;
+    for (int64_t i = 0; i < nlev; ++i) {
+        orc_box leaf[2];
+        for (int h = 0; h < 2; ++h) {
+            const int64_t v = 2 * i + h;
+            const int k = (int)(v / ((int64_t)nx * ny)), j = (int)((v / nx) % ny), q = (int)(v % nx);
+            leaf[h].mid[0] = r->t.c1[0][q]; leaf[h].mid[1] = r->t.c1[1][j]; leaf[h].mid[2] = r->t.c1[2][k];
+            for (int c = 0; c < 3; ++c) leaf[h].half[c] = r->t.e1[c];
+            leaf[h].solid = r->parity[v] % 2;
+        }
+        orc_combine(&leaf[0], (int32_t)(2 * i), &leaf[1], (int32_t)(2 * i + 1), &out[i]);
+        out[i].index = (int32_t)i;
+    }
+    int dx = r->s.n[0] / 2, dy = r->s.n[1], dz = r->s.n[2];
+    int64_t prev = 0, cur = nlev;
+    nlev /= 2;
+    for (int level = 2; level < levels + 1; ++level) {
+        int is = (level % 3 == 1 && dx > 1) ? 2 : 1;
+        int js = (level % 3 == 2 && dy > 1) ? 2 : 1;
+        int ks = (level % 3 == 0 && dz > 1) ? 2 : 1;
+        if (is == 1 && js == 1 && ks == 1) {
+            if (dx > 1) is = 2;
+            else if (dy > 1) js = 2;
+            else if (dz > 1) ks = 2;
+        }
+        for (int k = 0; k < dz; k += ks)
+            for (int j = 0; j < dy; j += js)
+                for (int i = 0; i < dx; i += is) {
+                    const int64_t i1 = (int64_t)k * dy * dx + (int64_t)j * dx + i;
+                    const int64_t i2 = (int64_t)(k / ks) * (dy / js) * (dx / is) + (int64_t)(j / js) * (dx / is) + i / is;
+                    const int64_t sk = (int64_t)(ks - 1) * dy * dx + (int64_t)(js - 1) * dx + (is - 1);
+                    const orc_box *a = out + prev + i1, *b = out + prev + i1 + sk;
+                    orc_combine(a, a->index, b, b->index, out + cur + i2);
+                    out[cur + i2].index = (int32_t)(cur + i2);
+                }
+        if (is == 2) dx /= 2;
+        if (js == 2) dy /= 2;
+        if (ks == 2) dz /= 2;
+        prev += nlev * 2;
+        cur += nlev;
+        nlev /= 2;
+    }
+    return levels;
 }

@@ -54,6 +54,8 @@ def _load(ref=False):
     L.orc_level2.argtypes = [vp, i64, i64, vp, C.c_int, C.POINTER(i64), C.POINTER(i64)]
     L.orc_count_ops.argtypes = [vp, i64, i64, C.c_int, vp]
     L.orc_face_normal.argtypes = [vp, vp]
+    L.orc_build_hierarchy.argtypes = [vp, vp]
+    L.orc_build_hierarchy.restype = C.c_int
     L.orc_level1_normals.argtypes = [vp, vp]
     L.orc_level2_normals.argtypes = [vp, i64, i64, vp, C.c_int]
     L.orc_tri_box.argtypes = [vp, vp, vp]
@@ -165,9 +167,20 @@ class Run:
             self.L.orc_level2_normals(self.h, int(b0), int(b1), _p(out), int(threads))
         return out.reshape(-1, 3)
 
+    def hierarchy(self):
+        """Object::BuildHierarchy over the Level1 voxels: (levels, structured array of N1-1 boxes
+        with mid, half, solid, child1, child2, index); levels = -1 unless N1 is a power of two."""
+        out = np.zeros(max(self.N1 - 1, 1), dtype=BOX_DTYPE)
+        lv = int(self.L.orc_build_hierarchy(self.h, _p(out)))
+        return lv, out[:self.N1 - 1]
+
     def level2_bytes(self, b0=0, b1=None, threads=0):
         st, _, _ = self.level2_state(b0, b1, threads)
         return (st * 127).astype(np.uint8)
+
+
+BOX_DTYPE = np.dtype([("mid", np.float32, 3), ("half", np.float32, 3), ("solid", np.int32),
+                      ("child1", np.int32), ("child2", np.int32), ("index", np.int32)])
 
 
 def face_normal(tv, ref=False):

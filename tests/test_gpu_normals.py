@@ -122,3 +122,40 @@ def test_normals_files_written(ctx, tmp_path):
     np.testing.assert_array_equal(n1, orc.normal_bytes(ref.level1_normals()).reshape(-1))
     np.testing.assert_array_equal(n2, orc.normal_bytes(ref.level2_normals()).reshape(-1))
     np.testing.assert_array_equal(vd.level1Normal, ref.level1_normals())
+
+
+@pytest.mark.parametrize("ndiv", [(16, 8, 4), (32, 32, 32), (64, 64, 64)])
+def test_hierarchy_matches_oracle(ctx, ndiv):
+    """Object::BuildHierarchy on the device equals the oracle's restatement bit for bit."""
+    import gpview_gb300 as gpv
+
+    tris = gpv.gen_torus(41, 96, 48, (0.5, 0.5, 0.5), 0.3, 0.1, 0.01)
+    spec = gpv.grid_padded(*gpv.mesh_bounds(tris), ndiv, 4)
+    ctx.set_hierarchy(True)
+    try:
+        res = ctx.voxelize_host(tris, spec)
+    finally:
+        ctx.set_hierarchy(False)
+    h = ctx.fetch_hierarchy(res)
+    ref = orc.Run(tris, spec)
+    lv, want = ref.hierarchy()
+    assert res.hierarchy_levels == lv
+    for f in ("mid", "half", "solid", "child1", "child2", "index"):
+        np.testing.assert_array_equal(h[f], want[f], err_msg=f)
+    ctx.release(res)
+
+
+def test_hierarchy_absent_for_non_power_of_two(ctx):
+    import gpview_gb300 as gpv
+
+    tris = gpv.gen_uvsphere(42, 24, 12, (0.5, 0.5, 0.5), 0.4, 0.002)
+    spec = gpv.grid_padded(*gpv.mesh_bounds(tris), (12, 8, 8), 0)
+    ctx.set_hierarchy(True)
+    try:
+        res = ctx.voxelize_host(tris, spec)
+    finally:
+        ctx.set_hierarchy(False)
+    assert res.hierarchy_levels == 0 and not res.hierarchy
+    with pytest.raises(gpv.GpvError):
+        ctx.fetch_hierarchy(res)
+    ctx.release(res)

@@ -118,3 +118,32 @@ def test_oracle_normals_match_golden_meshes(path):
 def test_normal_bytes_encoding():
     # n * float(256/3) + 127, truncated: -1 -> 41, 0 -> 127, 1 -> 212
     assert list(orc.normal_bytes([-1.0, 0.0, 1.0, 0.5])) == [41, 127, 212, 169]
+
+
+def test_oracle_hierarchy_structure():
+    """Structural checks of the restated BuildHierarchy: N1-1 nodes, the root bounds every solid
+    leaf, children indices point one level down, empty nodes have zero boxes."""
+    import workloads as W
+
+    tris, spec = W.make(W.C1)
+    r = orc.Run(tris, spec)
+    lv, h = r.hierarchy()
+    assert lv == 18 and h.shape == (r.N1 - 1,)
+    assert (h["index"] == np.arange(r.N1 - 1)).all()
+    root = h[-1]
+    assert root["solid"] == 1
+    empty = h["solid"] == 0
+    assert (h["mid"][empty] == 0).all() and (h["half"][empty] == 0).all()
+    # level-1 children are leaf pairs (2i, 2i+1)
+    n1 = r.N1 // 2
+    assert (h["child1"][:n1] == 2 * np.arange(n1)).all() and (h["child2"][:n1] == 2 * np.arange(n1) + 1).all()
+    # every inside voxel (parity 1) lies in the root box
+    tab = orc.grid_tables(spec)
+    n = [int(x) for x in spec.ndiv]
+    st = r.level1_state().reshape(n[2], n[1], n[0])
+    k, j, i = np.nonzero(st == 1)
+    c = [tab["c1"][:n[0]][i], tab["c1"][n[0]:n[0] + n[1]][j], tab["c1"][n[0] + n[1]:][k]]
+    for a in range(3):
+        lo = root["mid"][a] - root["half"][a]
+        hi = root["mid"][a] + root["half"][a]
+        assert (c[a] - tab["e1"][a] >= lo - 1e-6).all() and (c[a] + tab["e1"][a] <= hi + 1e-6).all()
