@@ -18,6 +18,7 @@ bounded sample of the same workload and reports the same metric.
 Multi-GPU: replicas only (each rank voxelizes its own copy; the path has no exchange step).
 """
 import argparse
+import faulthandler
 import json
 import os
 import statistics
@@ -158,6 +159,7 @@ def batch_bench(gpv, ctx, torch, stream, local, args):
     t0 = time.perf_counter()
     meshes = W.batch4096(args.batch)
     gen_s = time.perf_counter() - t0
+    progress(f"batch generated ({len(meshes)} meshes, {gen_s:.1f} s)")
     counts = [t.size // 9 for t, _ in meshes]
     specs = [s for _, s in meshes]
     offs, o = [], 0
@@ -174,6 +176,7 @@ def batch_bench(gpv, ctx, torch, stream, local, args):
         # autotuner on a sample of the batch
         ns = min(256, len(ptrs))
         tile, chunk, tune_ms = ctx.autotune(ptrs[:ns], counts[:ns], specs[:ns], sp)
+        progress(f"autotuned: tile {tile}, chunk {chunk}")
         # plain path: one voxelization (full launch sequence, host syncs) per mesh
         torch.cuda.synchronize()
         tp = time.perf_counter()
@@ -184,6 +187,7 @@ def batch_bench(gpv, ctx, torch, stream, local, args):
             ctx.release(r)
         torch.cuda.synchronize()
         plain_s = time.perf_counter() - tp
+        progress(f"plain loop {plain_s:.2f} s")
         # batched path
         times = []
         for k in range(args.batch_reps + 1):
@@ -401,7 +405,13 @@ def roofline(name, per_call, work, stats, spec, T, peaks, peak_kind, clk):
     return out
 
 
+def progress(msg):
+    """Section markers on stderr (the JSON line goes to stdout at the end)."""
+    print(f"[bench] {msg}", file=sys.stderr, flush=True)
+
+
 def main():
+    faulthandler.enable()
     args = parse()
     if args.impl == "reference":
         run_reference(args)
@@ -541,12 +551,16 @@ def main():
             "gpu_launches": launches, "roofline": roof, "clocks": clk,
             "host_ms_per_call": {k: v / max(hcalls, 1) for k, v in host_ms.items()}}
     tuned = (128, 8)
+    progress("plain path done")
     if args.batch > 0:
+        progress("batched section")
         line["batched"] = batch_bench(gpv, ctx, torch, stream, local, args)
         tuned = (line["batched"]["tile"], line["batched"]["level2_chunk"])
     if args.serve_seconds > 0:
+        progress("served section")
         line["served"] = served_bench(gpv, torch, local, args, tuned)
     if rank == 0 and not args.no_cpu_baseline:
+        progress("cpu baseline")
         line["cpu_baseline"] = cpu_baseline(tris, spec, tests_per_step, args.cpu_seconds,
                                             os.cpu_count() or 1)
         line["cpu_baseline"].pop("sec_per_mesh", None)

@@ -95,6 +95,37 @@ __device__ __forceinline__ void warp_add(unsigned long long *dst, unsigned long 
   }
 }
 
+// The four prep counters of a 256-thread block: one atomic each per block when every thread of
+// the block works on the same mesh (the common case), else per warp.  Thousands of per-warp
+// atomics on one counter serialise at L2.
+__device__ __forceinline__ void block_add_prep(MeshStats *st, unsigned long long a,
+                                               unsigned long long b, unsigned long long c,
+                                               unsigned long long d) {
+  __shared__ unsigned long long s_acc[4][8];
+  __shared__ MeshStats *s_first;
+  if (threadIdx.x == 0) s_first = st;
+  __syncthreads();
+  if (__syncthreads_and(st == s_first)) {
+    a = warp_sum(a); b = warp_sum(b); c = warp_sum(c); d = warp_sum(d);
+    const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+    if (lane == 0) { s_acc[0][warp] = a; s_acc[1][warp] = b; s_acc[2][warp] = c; s_acc[3][warp] = d; }
+    __syncthreads();
+    if (threadIdx.x < 4) {
+      unsigned long long v = 0;
+#pragma unroll
+      for (int w = 0; w < 8; ++w) v += s_acc[threadIdx.x][w];
+      unsigned long long *dst = threadIdx.x == 0 ? &st->sat1 : threadIdx.x == 1 ? &st->sat_units
+                                : threadIdx.x == 2 ? &st->fill_units : &st->ray1;
+      if (v) atomicAdd(dst, v);
+    }
+  } else {
+    warp_add(&st->sat1, a);
+    warp_add(&st->sat_units, b);
+    warp_add(&st->fill_units, c);
+    warp_add(&st->ray1, d);
+  }
+}
+
 // Conservative x/y box of the columns whose +z ray can pass the u/v tests of this triangle.
 // Outside the box every column fails them in float arithmetic; ill-conditioned projections get
 // the whole plane; triangles failing the |det| test get an empty box.
@@ -191,10 +222,7 @@ __global__ void __launch_bounds__(256) k_prep(BatchDev bd) {
                          (int)pack2(lo[2], hi[2]), 0);
     d.fbox[t] = fb;
   }
-  warp_add(&d.stats->sat1, sat1);
-  warp_add(&d.stats->sat_units, su);
-  warp_add(&d.stats->fill_units, fu);
-  warp_add(&d.stats->ray1, r1);
+  block_add_prep(d.stats, sat1, su, fu, r1);
 }
 
 // Per-mesh pair emission segments from the candidate counts prep just produced: exclusive prefix

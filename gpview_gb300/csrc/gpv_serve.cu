@@ -73,6 +73,9 @@ struct gpv_server {
   std::vector<std::thread> workers;
   std::vector<gpv_ctx *> ctxs;
   std::vector<cudaStream_t> streams;
+  // results released by clients, freed by their worker between batches: a worker's stream is
+  // recorded into CUDA graphs while it runs a batch, so no other thread may enqueue on it
+  std::vector<std::vector<gpv_result>> to_free;
   uint64_t batches = 0, served = 0;
 };
 
@@ -82,16 +85,24 @@ void worker_loop(gpv_server *srv, int w) {
   cudaSetDevice(srv->device);
   gpv_ctx *ctx = srv->ctxs[w];
   cudaStream_t s = srv->streams[w];
+  std::vector<gpv_result> frees;
   for (;;) {
     std::vector<Request *> batch;
     int64_t bytes = 0;
     {
       std::unique_lock<std::mutex> lk(srv->mu);
       srv->cv_work.wait(lk, [&] {
-        return srv->stop || (!srv->pending.empty() &&
-                             srv->in_use + srv->pending.front()->pred <= srv->budget);
+        return srv->stop || !srv->to_free[w].empty() ||
+               (!srv->pending.empty() && srv->in_use + srv->pending.front()->pred <= srv->budget);
       });
-      if (srv->stop) return;
+      if (srv->stop) return;  // the destroy call frees what is left
+      frees.swap(srv->to_free[w]);
+      if (!frees.empty()) {
+        lk.unlock();
+        for (gpv_result &r : frees) gpv_result_release(ctx, &r);
+        frees.clear();
+        continue;
+      }
       while (!srv->pending.empty() && (int)batch.size() < srv->max_batch) {
         Request *r = srv->pending.front();
         if (srv->in_use + bytes + r->pred > srv->budget) break;
@@ -179,6 +190,7 @@ int gpv_server_create(int device, int64_t budget_bytes, int32_t workers, int32_t
     srv->ctxs.push_back(ctx);
     srv->streams.push_back(s);
   }
+  srv->to_free.resize(workers);
   for (int w = 0; w < workers; ++w) srv->workers.emplace_back(worker_loop, srv, w);
   *out = srv;
   return GPV_OK;
@@ -250,8 +262,8 @@ int gpv_server_release(gpv_server *srv, uint64_t ticket) {
     r = std::move(it->second);
     srv->all.erase(it);
     if (r->status == GPV_OK) srv->in_use -= r->res_bytes;
+    if (r->status == GPV_OK && r->worker >= 0) srv->to_free[r->worker].push_back(r->res);
   }
-  if (r->status == GPV_OK && r->worker >= 0) gpv_result_release(srv->ctxs[r->worker], &r->res);
   srv->cv_work.notify_all();
   return GPV_OK;
 }
@@ -276,6 +288,7 @@ void gpv_server_destroy(gpv_server *srv) {
   srv->cv_work.notify_all();
   for (auto &t : srv->workers) t.join();
   for (size_t k = 0; k < srv->ctxs.size(); ++k) {
+    for (gpv_result &r : srv->to_free[k]) gpv_result_release(srv->ctxs[k], &r);
     cudaStreamSynchronize(srv->streams[k]);
     gpv_destroy(srv->ctxs[k]);
     cudaStreamDestroy(srv->streams[k]);

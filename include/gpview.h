@@ -183,7 +183,8 @@ int gpv_result_copy_to_host(gpv_ctx *ctx, const gpv_result *res, uint8_t *level1
 int gpv_result_copy_normals_to_host(gpv_ctx *ctx, const gpv_result *res, void *level1_normal,
                                     void *level2_normal, cudaStream_t stream);
 /* Frees a result's device arrays (stream-ordered, on the stream the result was made on: release
- * results before destroying that stream). */
+ * results before destroying that stream, and from the thread that uses the context -- a stream
+ * being recorded into a graph by another thread must not receive the frees). */
 int gpv_result_release(gpv_ctx *ctx, gpv_result *res);
 
 /* Batched path: n meshes in one launch sequence (persistent work-queue kernels).
