@@ -337,7 +337,9 @@ def run_reference(args):
 # Warp instructions one launch of the Level2 kernel executes on each single-mesh workload, from
 # `ncu --metrics smsp__inst_executed.sum` on the current kernel (profiles/k_level2c_*.md give the
 # commands).  The count is a property of the kernel's code and the input, not of the clock.
-LEVEL2_INST_PER_LAUNCH = {"torus262k": 575574987}
+LEVEL2_INST_PER_LAUNCH = {"torus262k": 438334456, "sphere16k": 28080689}
+# DRAM bytes read + written by one launch of the Level2 kernel (same captures)
+LEVEL2_TRAFFIC = {"torus262k": 30657280 + 13406720, "sphere16k": 2824960}
 
 
 def max_over_ranks(seconds, dist, device):
@@ -385,11 +387,10 @@ def roofline(name, per_call, work, stats, spec, T, peaks, peak_kind, clk):
         out["achieved"] = out["frac"] = None
     cells = spec.ndiv2[0] * spec.ndiv2[1] * spec.ndiv2[2]
     B, P = stats["boundary"], stats["pairs"]
-    # DRAM bytes per launch from the ncu capture of the same kernel and workload (torus262k:
-    # 30.6 MB read + 6.0 MB written); the algorithmic bytes are the sorted pairs read once,
-    # the triangles (48 B of prepared vertices) gathered once per pair and the Level2 blocks
-    # written once.
-    out["traffic"] = {"torus262k": 36611840}.get(name)
+    # DRAM bytes per launch from the ncu capture of the same kernel and workload; the
+    # algorithmic bytes are the sorted pairs read once, the triangles (48 B of prepared
+    # vertices) gathered once per pair and the Level2 blocks written once.
+    out["traffic"] = LEVEL2_TRAFFIC.get(name)
     out["algorithmic_bytes"] = P * 8 + P * 48 + B * cells
     try:
         with open(os.path.join(ROOT, "tests", "golden", "op_counts.json")) as f:

@@ -92,6 +92,28 @@ __device__ __forceinline__ float ray_tval(const RayTri &r, const RayCol &c, floa
   return fm(fa(fa(fm(r.e2x, q0), fm(r.e2y, q1)), fm(r.e2z, q2)), r.inv_det);
 }
 
+// First index i in [0, n] with tab[i] >= x, and last index in [-1, n-1] with tab[i] <= x, for an
+// increasing table of spacing ~1/inv: an arithmetic estimate corrected by table comparisons
+// (the result is exactly the table's, the estimate only saves the scan).
+__device__ __forceinline__ int tab_first_ge(const float *tab, int n, float x, float inv) {
+  const float t0 = __ldg(tab);
+  if (!(x > t0)) return 0;                       // also x = -inf
+  const float f = fminf((x - t0) * inv, (float)n);  // +inf and huge x clamp to n
+  int i = (int)ceilf(f);
+  while (i > 0 && __ldg(tab + i - 1) >= x) --i;
+  while (i < n && __ldg(tab + i) < x) ++i;
+  return i;
+}
+__device__ __forceinline__ int tab_last_le(const float *tab, int n, float x, float inv) {
+  const float t0 = __ldg(tab);
+  if (x < t0) return -1;
+  const float f = fminf((x - t0) * inv, (float)(n - 1));
+  int i = (int)floorf(f);
+  while (i < n - 1 && __ldg(tab + i + 1) <= x) ++i;
+  while (i >= 0 && __ldg(tab + i) > x) --i;
+  return i;
+}
+
 // last index tl in [0,31] with pre[tl] <= it (pre nondecreasing, pre[0] = 0)
 __device__ __forceinline__ int batch_search(const uint32_t *pre, uint32_t it) {
   int lo = 0, hi = 31;
@@ -104,15 +126,14 @@ __device__ __forceinline__ int batch_search(const uint32_t *pre, uint32_t it) {
 
 struct WarpScratch {
   float v[32][9];     // triangle vertices of the current batch
-  float x[32][4];     // slab (SAT) or (1/det, well-conditioned flag) (fill)
+  float x[32][5];     // slab (SAT) or (1/det, well-conditioned flag) (fill); odd row stride: no bank conflicts
   uint32_t rng[32];   // packed sub-cell ranges
   uint32_t pre[33];   // exclusive prefix of item counts
   int jm[32];         // SAT: the triangle's voxel in the chunk; fill: voxels of the chunk below
                       // the triangle's topmost voxel
   uint32_t zrec[32];  // SAT: (triangle slot, p, q) of a sub-column item
-  uint32_t zmask[32]; // SAT: cells of that sub-column left for the full test
-  uint32_t zpre[33];  // SAT: exclusive prefix of the cell counts
   uint32_t seg[33];   // SAT: first pair of each voxel of the chunk, and the end
+  uint32_t zown[64];  // SAT: (record lane, cell) of each (triangle, cell) item of a window
 };
 
 // ---- item construction -----------------------------------------------------------------------
@@ -260,7 +281,9 @@ __global__ void __launch_bounds__(kWarps * 32, 6) k_level2c(
       __syncwarp();
       // (triangle, sub-column) items, 32 at a time: z-invariant SAT part and the plane slab
       // select the cells left for the full test; then those (triangle, cell) tests run 32 at a
-      // time so that the lanes stay busy whatever the per-column cell counts.
+      // time so that the lanes stay busy whatever the per-column cell counts.  Each item lane
+      // lists its cells in a window of 64 slots (its lane and the cell's z), so a test lane
+      // reads its work from one slot.
       for (uint32_t wb = 0; wb < tot; wb += 32) {
         const uint32_t w = wb + lane;
         uint32_t zm = 0, rec = 0;
@@ -318,29 +341,40 @@ __global__ void __launch_bounds__(kWarps * 32, 6) k_level2c(
         }
         const uint32_t zc = (uint32_t)__popc(zm);
         const uint32_t zinc = warp_incl_scan(zc);
-        ws.zpre[lane] = zinc - zc;
         ws.zrec[lane] = rec;
-        ws.zmask[lane] = zm;
         const uint32_t ztot = __shfl_sync(FULL, zinc, 31);
-        __syncwarp();
-        for (uint32_t z = lane; z < ztot; z += 32) {
-          const int rl = batch_search(ws.zpre, z);
-          const uint32_t rc = ws.zrec[rl];
-          const int r = (int)__fns(ws.zmask[rl], 0u, (int)(z - ws.zpre[rl]) + 1);
-          const int tl = (int)(rc & 31u), p = (int)((rc >> 5) & 63u), q = (int)((rc >> 11) & 63u);
-          const int jv = ws.jm[tl];
-          const float *sz = g.c2s[2] + (size_t)kz[jv] * n2z;
-          float V[9];
-#pragma unroll
-          for (int c = 0; c < 9; ++c) V[c] = ws.v[tl][c];
-          SatCol sc;
-          sat_col_values(V, __ldg(sx + p), __ldg(sy + q), sc);
-          if (sat_z(sc, V, __ldg(sz + r), g.e2)) {
-            const int bi = (q * n2x + p) * n2z + r;
-            atomicOr(&sat[jv * W + (bi >> 5)], 1u << (bi & 31));
+        for (uint32_t w0 = 0; w0 < ztot; w0 += 64) {
+          // each record lane lists its cells of this window: (record lane, cell r) per slot
+          {
+            uint32_t mm = zm, pos = zinc - zc;
+            while (mm && pos < w0) { mm &= mm - 1u; ++pos; }
+            while (mm && pos < w0 + 64u) {
+              ws.zown[pos - w0] = lane | ((uint32_t)(__ffs(mm) - 1) << 5);
+              mm &= mm - 1u;
+              ++pos;
+            }
           }
+          __syncwarp();
+          const uint32_t wn = min(64u, ztot - w0);
+          for (uint32_t z = lane; z < wn; z += 32) {
+            const uint32_t own = ws.zown[z];
+            const uint32_t rc = ws.zrec[own & 31u];
+            const int r = (int)(own >> 5);
+            const int tl = (int)(rc & 31u), p = (int)((rc >> 5) & 63u), q = (int)((rc >> 11) & 63u);
+            const int jv = ws.jm[tl];
+            const float *sz = g.c2s[2] + (size_t)kz[jv] * n2z;
+            float V[9];
+#pragma unroll
+            for (int c = 0; c < 9; ++c) V[c] = ws.v[tl][c];
+            SatCol sc;
+            sat_col_values(V, __ldg(sx + p), __ldg(sy + q), sc);
+            if (sat_z(sc, V, __ldg(sz + r), g.e2)) {
+              const int bi = (q * n2x + p) * n2z + r;
+              atomicOr(&sat[jv * W + (bi >> 5)], 1u << (bi & 31));
+            }
+          }
+          __syncwarp();
         }
-        __syncwarp();
       }
     }
   }
@@ -363,11 +397,11 @@ __global__ void __launch_bounds__(kWarps * 32, 6) k_level2c(
       nun += (uint64_t)jm;
       const float4 fb = __ldg(fbox + t);
       if (jm > 0 && fb.x <= fb.z) {
-        int p0 = 0, p1 = n2x - 1, q0 = 0, q1 = n2y - 1;
-        while (p0 <= p1 && __ldg(ox + p0) < fb.x) ++p0;
-        while (p1 >= p0 && __ldg(ox + p1) > fb.z) --p1;
-        while (q0 <= q1 && __ldg(oy + q0) < fb.y) ++q0;
-        while (q1 >= q0 && __ldg(oy + q1) > fb.w) --q1;
+        // sub-columns whose origin lies in the box: first origin >= lo, last origin <= hi
+        const int p0 = tab_first_ge(ox, n2x, fb.x, g.inv_g2[0]);
+        const int p1 = tab_last_le(ox, n2x, fb.z, g.inv_g2[0]);
+        const int q0 = tab_first_ge(oy, n2y, fb.y, g.inv_g2[1]);
+        const int q1 = tab_last_le(oy, n2y, fb.w, g.inv_g2[1]);
         if (p0 <= p1 && q0 <= q1) {
           const float4 a0 = __ldg(ptri + 3 * (size_t)t), a1 = __ldg(ptri + 3 * (size_t)t + 1),
                        a2 = __ldg(ptri + 3 * (size_t)t + 2);

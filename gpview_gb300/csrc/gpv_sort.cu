@@ -2,7 +2,9 @@
 // triangle lists (the reference builds them on the host, src/Object.cpp:2146-2180, and
 // compacts boundary voxels there too, :3271-3279).
 //
-// scan_u32:  reduce-then-scan, three launches, no inter-block waiting.
+// scan_u32:  reduce-then-scan, no inter-block waiting: tile sums, then a down-sweep in which every
+//            block adds up the sums of the tiles before it (up to 1024 tiles; beyond that a
+//            separate single-block scan of the tile sums runs in between).
 // sort_pairs: stable LSD radix sort of (u32 key, u32 value), 8-bit digits; per pass a tile
 //             histogram, a scan of the digit-major histogram, and a stable scatter whose
 //             in-tile ranks come from __match_any_sync peer masks.
@@ -101,6 +103,41 @@ __global__ void k_scan_down(const uint32_t *__restrict__ in, int64_t n,
     if (i < n) out[i] = ex;
     ex += v[k];
   }
+}
+
+// Down-sweep that also finds its own tile offset: the sum of the partials of the tiles before it
+// (for up to kFusedTiles tiles, where that sum is cheap), so the partials need no separate scan.
+constexpr int64_t kFusedTiles = 1024;
+
+__global__ void k_scan_down_fused(const uint32_t *__restrict__ in, int64_t n,
+                                  const uint32_t *__restrict__ part, uint32_t *__restrict__ out,
+                                  uint32_t *__restrict__ total) {
+  __shared__ uint32_t s_base;
+  uint32_t acc = 0;
+  for (int64_t k = threadIdx.x; k < blockIdx.x; k += kScanThreads) acc += part[k];
+  uint32_t sum;
+  block_excl_scan<kScanThreads>(acc, sum);
+  if (threadIdx.x == 0) s_base = sum;
+  __syncthreads();
+  const int64_t base = (int64_t)blockIdx.x * kScanTile;
+  uint32_t v[kScanItems];
+  uint32_t s = 0;
+  const int64_t tb = base + (int64_t)threadIdx.x * kScanItems;
+#pragma unroll
+  for (int k = 0; k < kScanItems; ++k) {
+    int64_t i = tb + k;
+    v[k] = i < n ? in[i] : 0u;
+    s += v[k];
+  }
+  uint32_t tot;
+  uint32_t ex = block_excl_scan<kScanThreads>(s, tot) + s_base;
+#pragma unroll
+  for (int k = 0; k < kScanItems; ++k) {
+    int64_t i = tb + k;
+    if (i < n) out[i] = ex;
+    ex += v[k];
+  }
+  if (total && blockIdx.x == gridDim.x - 1 && threadIdx.x == 0) *total = s_base + tot;
 }
 
 // ---- radix sort ---------------------------------------------------------------------------
@@ -279,6 +316,11 @@ void scan_u32(const uint32_t *in, uint32_t *out, int64_t n, uint32_t *d_total, u
   }
   const int64_t nb = (n + kScanTile - 1) / kScanTile;
   k_scan_reduce<<<(unsigned)nb, kScanThreads, 0, s>>>(in, n, temp);
+  if (nb <= kFusedTiles) {
+    k_scan_down_fused<<<(unsigned)nb, kScanThreads, 0, s>>>(in, n, temp, out, d_total);
+    count_launch(2);
+    return;
+  }
   k_scan_partials<<<1, 1024, 0, s>>>(temp, nb, d_total);
   k_scan_down<<<(unsigned)nb, kScanThreads, 0, s>>>(in, n, temp, out);
   count_launch(3);
