@@ -9,8 +9,9 @@ Default workload (one step = one voxelization of one mesh through the plain path
 value    tri-voxel tests/s on device-resident triangles (results stay on the device), timed with
          CUDA events on the launching stream; L2 is flushed (256 MiB write) between steps,
          outside the timed spans.
-e2e      the same metric through the public host API: H2D of the step's triangles from pinned
-         memory, voxelization, D2H of every result array, timed on the host around each step.
+e2e      the same metric through the public host API (gpv_voxelize_to_host): H2D of the step's
+         triangles from pinned memory, voxelization, D2H of every result array into pinned
+         buffers (overlapped with the Level2 slabs), timed on the host around each step.
 tests    = sat1 + sat2 + ray1 + ray2 counted from the reference algorithm (see include/gpview.h).
 
 --impl reference times the reference's CPU path (the oracle restatement, all host threads) on a
@@ -41,6 +42,8 @@ def parse():
     p.add_argument("--workload", default="torus262k", choices=["sphere16k", "torus262k", "star1310k"])
     p.add_argument("--tile", type=int, default=0)
     p.add_argument("--no-graphs", action="store_true")
+    p.add_argument("--slabs", type=int, default=0,
+                   help="z slabs of the e2e path's Level2 launch (0: by the Level2 output size)")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--cpu-seconds", type=float, default=15.0)
     p.add_argument("--batch", type=int, default=4096, help="meshes of the batched workload (0: skip)")
@@ -504,21 +507,16 @@ def main():
     h_bi = torch.empty(max(stats["boundary"], 1), dtype=torch.int32).pin_memory()
     h_l2 = torch.empty(max(stats["boundary"] * cells, 1), dtype=torch.uint8).pin_memory()
     e2e_times = []
-    import ctypes as C
-
     for k in range(args.warmup + args.steps):
         with torch.cuda.stream(stream):
             flush.zero_()
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        res = gpv.Result()
-        rc = gpv.lib().gpv_voxelize_host(ctx._h, C.c_void_p(h_tris.data_ptr()), T, C.byref(spec),
-                                          C.byref(res), C.c_void_p(sp))
-        if rc:
-            raise gpv.GpvError(rc, ctx.error())
-        rc = gpv.lib().gpv_result_copy_to_host(ctx._h, C.byref(res), C.c_void_p(h_l1.data_ptr()),
-                                               C.c_void_p(h_pre.data_ptr()), C.c_void_p(h_bi.data_ptr()),
-                                               C.c_void_p(h_l2.data_ptr()), C.c_void_p(sp))
+        # host triangles in, host outputs out: H2D, voxelization, and the D2H of every output
+        # (Level1 arrays as soon as they exist, Level2 slab by slab while later slabs compute)
+        rc, res = ctx.voxelize_to_host(h_tris.data_ptr(), T, spec, h_l1.data_ptr(),
+                                       h_pre.data_ptr(), h_bi.data_ptr(), h_l2.data_ptr(),
+                                       h_l2.numel(), args.slabs, sp)
         if rc:
             raise gpv.GpvError(rc, ctx.error())
         t1 = time.perf_counter()

@@ -109,6 +109,9 @@ def lib():
                                     C.POINTER(Result), C.c_void_p]
     L.gpv_result_copy_to_host.argtypes = [C.c_void_p, C.POINTER(Result), C.c_void_p, C.c_void_p,
                                           C.c_void_p, C.c_void_p, C.c_void_p]
+    L.gpv_voxelize_to_host.argtypes = [C.c_void_p, C.c_void_p, C.c_int64, C.POINTER(GridSpec),
+                                       C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64,
+                                       C.c_int32, C.POINTER(Result), C.c_void_p]
     L.gpv_result_release.argtypes = [C.c_void_p, C.POINTER(Result)]
     L.gpv_load_obj.argtypes = [C.c_char_p, C.POINTER(MeshC)]
     L.gpv_load_off.argtypes = [C.c_char_p, C.POINTER(MeshC)]
@@ -303,6 +306,20 @@ class Context:
                                             tris.size // 9, C.byref(spec), C.byref(res),
                                             C.c_void_p(stream)), "gpv_voxelize_host")
         return res
+
+    def voxelize_to_host(self, tris_ptr, num_triangles, spec, l1_ptr, prefix_ptr, bindex_ptr,
+                         l2_ptr, l2_bytes, slabs=0, stream=0):
+        """Host triangles in, host outputs out (pointers, ideally page-locked), copies overlapped
+        with the computation.  Returns (status, result); status GPV_ERR_BUDGET (-7) when the
+        Level2 buffer is too small (the result is still complete and must be released)."""
+        res = Result()
+        rc = lib().gpv_voxelize_to_host(self._h, C.c_void_p(tris_ptr), int(num_triangles),
+                                        C.byref(spec), C.c_void_p(l1_ptr), C.c_void_p(prefix_ptr),
+                                        C.c_void_p(bindex_ptr), C.c_void_p(l2_ptr), int(l2_bytes),
+                                        int(slabs), C.byref(res), C.c_void_p(stream))
+        if rc not in (0, -7):
+            raise GpvError(rc, f"gpv_voxelize_to_host: {self.error()}")
+        return rc, res
 
     def voxelize_batch(self, d_ptrs, counts, specs, stream=0):
         n = len(d_ptrs)

@@ -172,6 +172,17 @@ void gpv_destroy(gpv_ctx *ctx) {
   ctx->owned.clear();
   for (cudaGraphExec_t &ge : ctx->gexec)
     if (ge) cudaGraphExecDestroy(ge);
+  if (ctx->cstream) {
+    cudaStreamSynchronize(ctx->cstream);
+    cudaStreamDestroy(ctx->cstream);
+  }
+  for (cudaEvent_t &e : ctx->cev)
+    if (e) cudaEventDestroy(e);
+  for (cudaStream_t &x : ctx->slab_aux.st)
+    if (x) { cudaStreamSynchronize(x); cudaStreamDestroy(x); }
+  if (ctx->slab_aux.fork) cudaEventDestroy(ctx->slab_aux.fork);
+  for (cudaEvent_t &e : ctx->slab_aux.join)
+    if (e) cudaEventDestroy(e);
   if (ctx->slab) cudaFree(ctx->slab);
   if (ctx->h_stats) cudaFreeHost(ctx->h_stats);
   if (ctx->h_md) cudaFreeHost(ctx->h_md);
@@ -325,6 +336,30 @@ int gpv_voxelize_host(gpv_ctx *ctx, const float *h_tris, int64_t num_triangles,
   }
   const float *dp = d;
   int rc = run_batch(ctx, 1, &dp, &num_triangles, spec, out, stream);
+  cudaFreeAsync(d, stream);
+  return rc;
+}
+
+int gpv_voxelize_to_host(gpv_ctx *ctx, const float *h_tris, int64_t num_triangles,
+                         const gpv_grid_spec *spec, uint8_t *h_l1, int32_t *h_prefix,
+                         int32_t *h_bindex, uint8_t *h_l2, int64_t h_l2_bytes, int32_t slabs,
+                         gpv_result *out, cudaStream_t stream) {
+  if (!ctx || !spec || !out || num_triangles < 0 || (num_triangles > 0 && !h_tris) ||
+      h_l2_bytes < 0)
+    return GPV_ERR_INVALID;
+  cudaSetDevice(ctx->device);
+  float *d = nullptr;
+  const size_t bytes = (size_t)std::max<int64_t>(num_triangles, 1) * 9 * sizeof(float);
+  cudaError_t e = cudaMallocAsync((void **)&d, bytes, stream);
+  if (e != cudaSuccess) return ctx_cuda_fail(ctx, e, "cudaMallocAsync");
+  if (num_triangles > 0) {
+    e = cudaMemcpyAsync(d, h_tris, (size_t)num_triangles * 9 * sizeof(float),
+                        cudaMemcpyHostToDevice, stream);
+    if (e != cudaSuccess) { cudaFreeAsync(d, stream); return ctx_cuda_fail(ctx, e, "cudaMemcpyAsync"); }
+  }
+  HostSink sink{h_l1, h_prefix, h_bindex, h_l2, h_l2_bytes, std::max(slabs, 0)};
+  const float *dp = d;
+  int rc = run_batch(ctx, 1, &dp, &num_triangles, spec, out, stream, &sink);
   cudaFreeAsync(d, stream);
   return rc;
 }

@@ -78,8 +78,9 @@ size_t al16(size_t v) { return (v + 15) & ~size_t(15); }
 // recording has the same topology; otherwise it is re-instantiated.  If recording fails the
 // launches run directly.
 template <typename F>
-cudaError_t run_phase(gpv_ctx *ctx, int phase, cudaStream_t s, bool &capturing, F &&launches) {
-  if (!ctx->graphs) {
+cudaError_t run_phase(gpv_ctx *ctx, int phase, cudaStream_t s, bool &capturing, F &&launches,
+                      bool allow_graph = true) {
+  if (!ctx->graphs || !allow_graph) {
     launches();
     return cudaGetLastError();
   }
@@ -128,13 +129,14 @@ cudaError_t run_phase(gpv_ctx *ctx, int phase, cudaStream_t s, bool &capturing, 
 }  // namespace
 
 int run_batch(gpv_ctx *ctx, int n, const float *const *d_tris, const int64_t *T,
-              const gpv_grid_spec *specs, gpv_result *out, cudaStream_t s) {
+              const gpv_grid_spec *specs, gpv_result *out, cudaStream_t s, const HostSink *sink) {
 #define CK(call)                                                    \
   do {                                                              \
     cudaError_t e_ = (call);                                        \
     if (e_ != cudaSuccess) return ctx_cuda_fail(ctx, e_, #call);    \
   } while (0)
   if (n <= 0) return ctx_fail(ctx, GPV_ERR_INVALID, "empty batch");
+  if (sink && n != 1) return ctx_fail(ctx, GPV_ERR_INVALID, "host outputs take one mesh");
   using HClock = std::chrono::steady_clock;
   HClock::time_point ht[6];
   ht[0] = HClock::now();
@@ -212,7 +214,18 @@ int run_batch(gpv_ctx *ctx, int n, const float *const *d_tris, const int64_t *T,
   CK(ws.get(&wpre, (size_t)words));
   CK(ws.get(&wtot, 4));
   CK(ws.get(&stmp, (size_t)scan_temp_words(words)));
-  CK(ws.get(&queue, 4));
+  CK(ws.get(&queue, 16));  // [0] Level1 tickets, [1 + k] Level2 tickets of slab k
+  // z slabs of the Level2 launch when the outputs go to the host (one mesh): the boundary ranks
+  // at up to kMaxSlabs fine slab starts are read with the first phase's counts; the launch then
+  // groups fine slabs into as many slabs as the Level2 output size calls for
+  int fslab = 1, fz = 0, nslab = 1, zslab = 0;
+  uint32_t *d_slab = nullptr;
+  if (sink && gh[0].level2) {
+    fslab = std::min(kMaxSlabs, gh[0].n[2]);
+    fz = (gh[0].n[2] + fslab - 1) / fslab;
+    fslab = (gh[0].n[2] + fz - 1) / fz;
+    CK(ws.get(&d_slab, 16));
+  }
   CK(ws.get(&stats, (size_t)n));
   CK(ws.get(&d_md, (size_t)n));
   CK(cudaMemsetAsync(stats, 0, n * sizeof(MeshStats), s));
@@ -309,8 +322,12 @@ int run_batch(gpv_ctx *ctx, int n, const float *const *d_tris, const int64_t *T,
     launch_popc(bplane, words, wcnt, s);
     scan_u32(wcnt, wpre, words, wtot, stmp, s);
     launch_boundary_counts(bd, wpre, wtot, s);
+    if (d_slab)
+      launch_slab_offsets(wpre, wtot, (int64_t)gh[0].n[1] * gh[0].nxw, gh[0].n[2], fz, fslab,
+                          d_slab, s);
     mark(4);
   }));
+  if (d_slab) CK(cudaMemcpyAsync(ctx->h_u32 + 4, d_slab, 4 * (fslab + 1), cudaMemcpyDeviceToHost, s));
   CK(cudaMemcpyAsync(ctx->h_stats, stats, n * sizeof(MeshStats), cudaMemcpyDeviceToHost, s));
   CK(cudaStreamSynchronize(s));
   ht[2] = HClock::now();
@@ -403,9 +420,45 @@ int run_batch(gpv_ctx *ctx, int n, const float *const *d_tris, const int64_t *T,
     CK(cudaMemcpyAsync(d_tb, ctx->h_tb, (n + 1) * sizeof(int64_t), cudaMemcpyHostToDevice, s));
   }
   ht[3] = HClock::now();
+  // host outputs: Level1 arrays copied as soon as the expansion has written them, Level2 slab by
+  // slab, on the context's copy stream (this phase then runs without a graph)
+  bool l2_copied = true;
+  if (sink) {
+    if (!ctx->cstream) CK(cudaStreamCreateWithFlags(&ctx->cstream, cudaStreamNonBlocking));
+    for (cudaEvent_t &e : ctx->cev)
+      if (!e) CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    if (!ctx->slab_aux.st[0]) {
+      for (cudaStream_t &x : ctx->slab_aux.st) CK(cudaStreamCreateWithFlags(&x, cudaStreamNonBlocking));
+      CK(cudaEventCreateWithFlags(&ctx->slab_aux.fork, cudaEventDisableTiming));
+      for (cudaEvent_t &e : ctx->slab_aux.join) CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    }
+    l2_copied = !gh[0].level2 || (sink->l2 && sink->l2_cap >= l2bytes);
+  }
+  cudaStream_t cs = ctx->cstream;
+  uint32_t slab_off[kMaxSlabs + 1] = {};
+  if (d_slab) {
+    // slab count: the caller's, or one per 12 MB of Level2 output (the copy of each slab then
+    // overlaps the computation of the next; smaller slabs cost more than they hide)
+    int want = sink->nslab > 0 ? sink->nslab
+                               : (int)std::min<int64_t>(kMaxSlabs, l2bytes / (12ll << 20));
+    want = std::max(1, std::min(want, fslab));
+    const int gsz = (fslab + want - 1) / want;
+    zslab = gsz * fz;
+    nslab = (fslab + gsz - 1) / gsz;
+    for (int k = 0; k <= nslab; ++k) slab_off[k] = ctx->h_u32[4 + std::min(k * gsz, fslab)];
+  }
   CK(run_phase(ctx, 1, s, capturing, [&] {
     mark(5);
     launch_expand(bd, wpre, s);
+    if (sink) {
+      cudaEventRecord(ctx->cev[0], s);
+      cudaStreamWaitEvent(cs, ctx->cev[0], 0);
+      if (sink->l1) cudaMemcpyAsync(sink->l1, set->l1, gh[0].N1, cudaMemcpyDeviceToHost, cs);
+      if (sink->prefix)
+        cudaMemcpyAsync(sink->prefix, set->prefix, 4 * gh[0].N1, cudaMemcpyDeviceToHost, cs);
+      if (sink->bindex && Btot)
+        cudaMemcpyAsync(sink->bindex, set->bindex, 4 * Btot, cudaMemcpyDeviceToHost, cs);
+    }
     for (int m = 0; m < n; ++m)
       if (res_hier[m + 1] > res_hier[m])
         launch_hierarchy(md[m].g, md[m].iplane, static_cast<gpv_box *>(set->hier) + res_hier[m], s);
@@ -420,7 +473,17 @@ int run_batch(gpv_ctx *ctx, int n, const float *const *d_tris, const int64_t *T,
       launch_useg(flags, uidx, P2, useg, s);
       mark(7);
       if (any_l2)
-        launch_level2(bd, sk, sv, useg, ub, l2tmp, warp_words, ctx->num_sms, s, [&] { mark(9); });
+        launch_level2(bd, sk, sv, useg, ub, l2tmp, warp_words, ctx->num_sms, s, [&] { mark(9); },
+                      zslab, nslab, [&](int k, cudaStream_t ls) {
+                        if (!sink || !l2_copied) return;
+                        cudaEventRecord(ctx->cev[1 + k], ls);
+                        cudaStreamWaitEvent(cs, ctx->cev[1 + k], 0);
+                        const int64_t a = (int64_t)slab_off[k] * gh[0].cells;
+                        const int64_t b = (int64_t)slab_off[k + 1] * gh[0].cells;
+                        if (b > a)
+                          cudaMemcpyAsync(sink->l2 + a, static_cast<uint8_t *>(set->l2) + a, b - a,
+                                          cudaMemcpyDeviceToHost, cs);
+                      }, gh[0].n[2], sink ? &ctx->slab_aux : nullptr);
       else
         mark(9);
       if (nmode) {
@@ -432,7 +495,11 @@ int run_batch(gpv_ctx *ctx, int n, const float *const *d_tris, const int64_t *T,
       mark(9);
     }
     mark(8);
-  }));
+  }, !sink));
+  if (sink) {
+    CK(cudaEventRecord(ctx->cev[kMaxSlabs + 1], cs));
+    CK(cudaStreamWaitEvent(s, ctx->cev[kMaxSlabs + 1], 0));
+  }
   CK(cudaMemcpyAsync(ctx->h_stats, stats, n * sizeof(MeshStats), cudaMemcpyDeviceToHost, s));
   CK(cudaMemcpyAsync(ctx->h_u32, wtot, 8, cudaMemcpyDeviceToHost, s));
   CK(cudaStreamSynchronize(s));
@@ -495,6 +562,10 @@ int run_batch(gpv_ctx *ctx, int n, const float *const *d_tris, const int64_t *T,
       r.level1_normal = static_cast<uint8_t *>(set->l1n) + res_l1n[m];
       r.level2_normal = static_cast<uint8_t *>(set->l2n) + 3 * l2off[m] * nsz;
     }
+  }
+  if (!l2_copied) {
+    ctx_fail(ctx, GPV_ERR_BUDGET, "host Level2 buffer too small: nothing copied there (result kept)");
+    return GPV_ERR_BUDGET;
   }
   if (ctx->timing) {
     ht[5] = HClock::now();

@@ -10,6 +10,8 @@
 
 namespace gpv {
 
+constexpr int kMaxSlabs = 8;  // z slabs of gpv_voxelize_to_host's Level2 launch, at most
+
 // Result arrays of one batch; every result of the batch holds a reference.
 struct ResultSet {
   void *l1 = nullptr, *prefix = nullptr, *bindex = nullptr, *l2 = nullptr;
@@ -57,6 +59,9 @@ struct gpv_ctx {
   void *slab = nullptr;
   size_t slab_cap = 0, slab_want = 0;
   int64_t pair_hint = 0;               // pair-buffer capacity for the next call (grow-only)
+  cudaStream_t cstream = nullptr;      // copy stream of gpv_voxelize_to_host (lazily created)
+  cudaEvent_t cev[gpv::kMaxSlabs + 2] = {};  // its ordering events
+  gpv::SlabStreams slab_aux = {};      // two streams for overlapping Level2 slab launches
   uint64_t next_handle = 1;
   std::mutex owned_mu;                 // results may be released from another host thread
   std::unordered_map<uint64_t, std::shared_ptr<gpv::ResultSet>> owned;
@@ -119,8 +124,19 @@ inline cudaError_t ctx_ensure_host_tiles(gpv_ctx *ctx, size_t ntiles, size_t ntb
   return e;
 }
 
+// Host destinations of gpv_voxelize_to_host (one mesh): the Level1 outputs are copied on the
+// context's copy stream as soon as they exist, the Level2 outputs slab by slab while later slabs
+// compute.
+struct HostSink {
+  uint8_t *l1;
+  int32_t *prefix, *bindex;
+  uint8_t *l2;
+  int64_t l2_cap;  // bytes available at l2
+  int nslab;       // z slabs of the Level2 launch (0: by the Level2 output size)
+};
 int run_batch(gpv_ctx *ctx, int n, const float *const *d_tris, const int64_t *T,
-              const gpv_grid_spec *specs, gpv_result *out, cudaStream_t s);
+              const gpv_grid_spec *specs, gpv_result *out, cudaStream_t s,
+              const HostSink *sink = nullptr);
 int autotune(gpv_ctx *ctx, int n, const float *const *d_tris, const int64_t *T,
              const gpv_grid_spec *specs, cudaStream_t s, int reps, int *best_tile,
              int *best_chunk, float *best_ms);

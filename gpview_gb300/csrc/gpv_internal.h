@@ -84,6 +84,9 @@ struct BatchDev {
 };
 
 void launch_prep(const BatchDev &bd, cudaStream_t s);
+// Boundary rank at each z-slab start of a single mesh (nslab + 1 values into out).
+void launch_slab_offsets(const uint32_t *wpre, const uint32_t *wtot, int64_t words_per_layer,
+                         int nz, int zslab, int nslab, uint32_t *out, cudaStream_t s);
 // Device-side per-mesh pair segments (emit_base, pair_cap, keys, vals) from prep's sat1 counts.
 void launch_pair_bases(const BatchDev &bd, MeshDesc *d_md, uint32_t *keys, uint32_t *vals,
                        int64_t cap, cudaStream_t s);
@@ -113,9 +116,19 @@ int level2_warp_words(const GridDev &g, int cap = 32);
 int64_t level2_temp_words(int64_t Btot);
 // before_kernel (optional) runs on the host between the work-item launches and the Level2
 // kernel's launch, e.g. to record an event that times the kernel alone.
+// With zslab > 0 and nslab > 1 the Level2 kernel runs once per slab of zslab Level1 layers (one
+// mesh with slab_nz Level1 layers): the outputs of slab k are contiguous and complete after the
+// work after_slab(k, stream) sees on `stream`, so a copy of them can start while the next slab
+// computes.  With aux, slab launches alternate between aux's two streams (joined back into s).
+struct SlabStreams {  // two streams and their events for overlapping slab launches
+  cudaStream_t st[2];
+  cudaEvent_t fork, join[2];
+};
 void launch_level2(const BatchDev &bd, const uint32_t *keys, const uint32_t *vals,
                    const uint32_t *useg, int64_t Btot, uint32_t *tmp, int warp_words, int num_sms,
-                   cudaStream_t s, const std::function<void()> &before_kernel = {});
+                   cudaStream_t s, const std::function<void()> &before_kernel = {}, int zslab = 0,
+                   int nslab = 1, const std::function<void(int, cudaStream_t)> &after_slab = {},
+                   int slab_nz = 0, const SlabStreams *aux = nullptr);
 
 // ---- normals (gpv_normals.cu) ----------------------------------------------------------------
 void launch_face_normals(const BatchDev &bd, cudaStream_t s);

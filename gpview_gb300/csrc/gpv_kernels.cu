@@ -597,6 +597,23 @@ void launch_prep(const BatchDev &bd, cudaStream_t s) {
   count_launch();
 }
 
+// Boundary-voxel rank at the start of each z slab of one mesh (slab k = layers [k*zslab,
+// (k+1)*zslab)): the exclusive word prefix at the slab's first word, the total past the end.
+__global__ void k_slab_offsets(const uint32_t *__restrict__ wpre, const uint32_t *__restrict__ wtot,
+                               int64_t words_per_layer, int nz, int zslab, int nslab,
+                               uint32_t *__restrict__ out) {
+  const int t = (int)threadIdx.x;
+  if (t > nslab) return;
+  const int z0 = min(t * zslab, nz);
+  out[t] = z0 >= nz ? *wtot : wpre[(int64_t)z0 * words_per_layer];
+}
+
+void launch_slab_offsets(const uint32_t *wpre, const uint32_t *wtot, int64_t words_per_layer,
+                         int nz, int zslab, int nslab, uint32_t *out, cudaStream_t s) {
+  k_slab_offsets<<<1, 32, 0, s>>>(wpre, wtot, words_per_layer, nz, zslab, nslab, out);
+  count_launch();
+}
+
 void launch_pair_bases(const BatchDev &bd, MeshDesc *d_md, uint32_t *keys, uint32_t *vals,
                        int64_t cap, cudaStream_t s) {
   k_pair_bases<<<1, 1024, 0, s>>>(bd.nmesh, d_md, keys, vals, cap);

@@ -167,15 +167,23 @@ __global__ void k_colheads(const uint32_t *__restrict__ cflag, const uint32_t *_
   if (u == B - 1) colhead[cord[u] + cflag[u]] = (uint32_t)B;
 }
 
-__global__ void k_itemflags(BatchDev bd, const uint32_t *__restrict__ cflag,
+// An item starts every CH voxels from its column's first boundary voxel and, with z slabs
+// (zslab > 0), also where the column enters a new slab of zslab Level1 layers.
+__global__ void k_itemflags(BatchDev bd, const uint32_t *__restrict__ keys,
+                            const uint32_t *__restrict__ useg, const uint32_t *__restrict__ cflag,
                             const uint32_t *__restrict__ cord, const uint32_t *__restrict__ colhead,
-                            int64_t B, uint32_t *__restrict__ iflag) {
+                            int64_t B, int zslab, uint32_t *__restrict__ iflag) {
   const int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (u >= B) return;
   const MeshDesc &d = bd.md[mesh_of_u(bd.md, bd.nmesh, u)];
   const uint32_t c = cord[u] + cflag[u] - 1u;
+  bool start = (u - colhead[c]) % d.ch == 0;
+  if (zslab > 0 && !start) {
+    const uint32_t nz = (uint32_t)d.g.n[2];
+    start = (keys[useg[u]] % nz) / (uint32_t)zslab != (keys[useg[u - 1]] % nz) / (uint32_t)zslab;
+  }
   // meshes without a Level2 grid (sorted for their normals only) get no Level2 work items
-  iflag[u] = (d.has_l2 && (u - colhead[c]) % d.ch == 0) ? 1u : 0u;
+  iflag[u] = (d.has_l2 && start) ? 1u : 0u;
 }
 
 __global__ void k_itemstarts(const uint32_t *__restrict__ iflag, const uint32_t *__restrict__ iord,
@@ -186,23 +194,58 @@ __global__ void k_itemstarts(const uint32_t *__restrict__ iflag, const uint32_t 
   if (u == B - 1) *nitems = iord[u] + iflag[u];
 }
 
+// Items of one mesh ordered by z slab (order within a slab is free): per-slab counts, their
+// exclusive prefix (ioff[0..nslab]), then each item placed in its slab's range.
+__global__ void k_item_slab_count(const uint32_t *__restrict__ istart,
+                                  const uint32_t *__restrict__ nitems, const uint32_t *__restrict__ keys,
+                                  const uint32_t *__restrict__ useg, int nz, int zslab,
+                                  uint32_t *__restrict__ cnt) {
+  const int64_t it = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (it >= (int64_t)*nitems) return;
+  atomicAdd(&cnt[(keys[useg[istart[it]]] % (uint32_t)nz) / (uint32_t)zslab], 1u);
+}
+
+__global__ void k_item_slab_offsets(uint32_t *__restrict__ cnt, int nslab, uint32_t *__restrict__ ioff) {
+  if (threadIdx.x != 0) return;
+  uint32_t a = 0;
+  for (int k = 0; k < nslab; ++k) {
+    ioff[k] = a;
+    a += cnt[k];
+    cnt[k] = ioff[k];  // becomes the slab's placement cursor
+  }
+  ioff[nslab] = a;
+}
+
+__global__ void k_item_slab_place(const uint32_t *__restrict__ istart,
+                                  const uint32_t *__restrict__ nitems, const uint32_t *__restrict__ keys,
+                                  const uint32_t *__restrict__ useg, int nz, int zslab,
+                                  uint32_t *__restrict__ cur, uint32_t *__restrict__ ilist) {
+  const int64_t it = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (it >= (int64_t)*nitems) return;
+  const uint32_t sl = (keys[useg[istart[it]]] % (uint32_t)nz) / (uint32_t)zslab;
+  ilist[atomicAdd(&cur[sl], 1u)] = (uint32_t)it;
+}
+
 // ---- Level2 ------------------------------------------------------------------------------------
 __global__ void __launch_bounds__(kWarps * 32, 6) k_level2c(
     BatchDev bd, const uint32_t *__restrict__ keys, const uint32_t *__restrict__ vals,
     const uint32_t *__restrict__ useg, const uint32_t *__restrict__ cflag,
     const uint32_t *__restrict__ cord, const uint32_t *__restrict__ colhead,
-    const uint32_t *__restrict__ istart, const uint32_t *__restrict__ nitems, int per_warp) {
+    const uint32_t *__restrict__ istart, const uint32_t *__restrict__ nitems, int per_warp,
+    int slab, int zslab, const uint32_t *__restrict__ ilist, const uint32_t *__restrict__ ioff) {
   extern __shared__ uint32_t sm[];
   const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
   uint32_t *base = sm + (size_t)warp * per_warp;
-  const int64_t NI = (int64_t)*nitems;
+  // all items, or (z slabs) this launch's slab of the slab-ordered item list
+  const int64_t i0 = ilist ? (int64_t)ioff[slab] : 0;
+  const int64_t NI = ilist ? (int64_t)ioff[slab + 1] - i0 : (int64_t)*nitems;
   for (;;) {
   // ---- pull the next chunk item from the queue (one ticket per warp)
   uint32_t tk = 0;
-  if (lane == 0) tk = atomicAdd(&bd.queue[1], 1u);
+  if (lane == 0) tk = atomicAdd(&bd.queue[1 + slab], 1u);
   const int64_t it = (int64_t)__shfl_sync(FULL, tk, 0);
   if (it >= NI) return;
-  const uint32_t ua = istart[it];
+  const uint32_t ua = ilist ? istart[ilist[i0 + it]] : istart[it];
   const MeshDesc &d = bd.md[mesh_of_u(bd.md, bd.nmesh, ua)];
   const GridDev &g = d.g;
   const float4 *__restrict__ ptri = d.ptri;
@@ -221,12 +264,24 @@ __global__ void __launch_bounds__(kWarps * 32, 6) k_level2c(
   WarpScratch &ws = *reinterpret_cast<WarpScratch *>(ftacc + FW);
 
   const uint32_t ucol_end = colhead[cord[ua] + cflag[ua]];  // first voxel of the next column
-  const int m = (int)min((uint32_t)CH, ucol_end - ua);
+  const int nx = g.n[0], ny = g.n[1], nz = g.n[2];
+  const uint32_t col = keys[useg[ua]] / (uint32_t)nz;
+  int m = (int)min((uint32_t)CH, ucol_end - ua);
+  if (zslab > 0) {
+    // this launch takes one slab of zslab Level1 layers; an item ends at the slab's edge and at
+    // the next CH-aligned item start of its column
+    const uint32_t chead = colhead[cord[ua] + cflag[ua] - 1u];
+    bool ok = false;
+    if ((int)lane < m) {
+      const int zl = (int)(keys[useg[ua + lane]] - col * (uint32_t)nz);
+      ok = zl / zslab == slab && (lane == 0 || (ua + lane - chead) % (uint32_t)CH != 0);
+    }
+    m = __ffs(~__ballot_sync(FULL, ok)) - 1;  // leading run of voxels of this item
+    if (m < 0) m = 32;
+  }
   // clear the masks of the chunk's m voxels only (the arrays are sized for CH voxels)
   for (int w = lane; w < m * W; w += 32) { sat[w] = 0; par[w] = 0; }
   for (int w = lane; w < m * FW; w += 32) ft[w] = 0;
-  const int nx = g.n[0], ny = g.n[1], nz = g.n[2];
-  const uint32_t col = keys[useg[ua]] / (uint32_t)nz;
   const int ci = (int)(col % (uint32_t)nx), cj = (int)(col / (uint32_t)nx);
   if ((int)lane < m) kz[lane] = (int)(keys[useg[ua + lane]] - col * (uint32_t)nz);
   __syncwarp();
@@ -528,21 +583,25 @@ int level2_warp_words(const GridDev &g, int cap) {
 
 size_t level2_smem_bytes(int warp_words) { return (size_t)warp_words * 4 * kWarps; }
 
-int64_t level2_temp_words(int64_t B) { return 6 * B + 8 + scan_temp_words(B); }
+int64_t level2_temp_words(int64_t B) { return 7 * B + 32 + scan_temp_words(B); }
 
 // Builds the chunk items from the sorted pair lists and runs the persistent Level2 kernel.
 void launch_level2(const BatchDev &bd, const uint32_t *keys, const uint32_t *vals,
                    const uint32_t *useg, int64_t B, uint32_t *tmp, int warp_words, int num_sms,
-                   cudaStream_t s, const std::function<void()> &before_kernel) {
+                   cudaStream_t s, const std::function<void()> &before_kernel, int zslab,
+                   int nslab, const std::function<void(int, cudaStream_t)> &after_slab, int slab_nz,
+                   const SlabStreams *aux) {
   if (B <= 0) return;
   uint32_t *cflag = tmp, *cord = cflag + B, *colhead = cord + B, *iflag = colhead + B + 1,
            *iord = iflag + B, *istart = iord + B, *nitems = istart + B + 1,
-           *stmp = nitems + 4;
+           *slabcnt = nitems + 4, *ioff = slabcnt + 12, *ilist = ioff + 12,
+           *stmp = ilist + B;
+  if (nslab <= 1) zslab = 0;
   const unsigned nb = (unsigned)((B + 255) / 256);
   k_colflags<<<nb, 256, 0, s>>>(bd, keys, useg, B, cflag);
   scan_u32(cflag, cord, B, nullptr, stmp, s);
   k_colheads<<<nb, 256, 0, s>>>(cflag, cord, B, colhead);
-  k_itemflags<<<nb, 256, 0, s>>>(bd, cflag, cord, colhead, B, iflag);
+  k_itemflags<<<nb, 256, 0, s>>>(bd, keys, useg, cflag, cord, colhead, B, zslab, iflag);
   scan_u32(iflag, iord, B, nullptr, stmp, s);
   k_itemstarts<<<nb, 256, 0, s>>>(iflag, iord, B, istart, nitems);
   count_launch(4);
@@ -556,11 +615,40 @@ void launch_level2(const BatchDev &bd, const uint32_t *keys, const uint32_t *val
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_level2c, kWarps * 32, smem);
   per_sm = std::max(per_sm, 1);
   const int64_t grid = std::min<int64_t>((B + kWarps - 1) / kWarps, (int64_t)num_sms * per_sm);
-  cudaMemsetAsync(bd.queue + 1, 0, sizeof(uint32_t), s);
+  const int nz = slab_nz;
+  if (zslab > 0) {
+    // single mesh: order the items by slab so that each launch takes only its own
+    cudaMemsetAsync(slabcnt, 0, 12 * sizeof(uint32_t), s);
+    k_item_slab_count<<<nb, 256, 0, s>>>(istart, nitems, keys, useg, nz, zslab, slabcnt);
+    k_item_slab_offsets<<<1, 32, 0, s>>>(slabcnt, nslab, ioff);
+    k_item_slab_place<<<nb, 256, 0, s>>>(istart, nitems, keys, useg, nz, zslab, slabcnt, ilist);
+    count_launch(3);
+  }
   if (before_kernel) before_kernel();
-  k_level2c<<<(unsigned)grid, kWarps * 32, smem, s>>>(bd, keys, vals, useg, cflag, cord, colhead,
-                                                      istart, nitems, warp_words);
-  count_launch();
+  // one launch, or one per z slab over that slab's items; slab launches alternate between two
+  // streams (when given) so that one slab's tail overlaps the next slab's start
+  const int launches = zslab > 0 ? nslab : 1;
+  const bool two = zslab > 0 && launches > 1 && aux;
+  cudaMemsetAsync(bd.queue + 1, 0, (size_t)launches * sizeof(uint32_t), s);
+  if (two) {
+    cudaEventRecord(aux->fork, s);
+    cudaStreamWaitEvent(aux->st[0], aux->fork, 0);
+    cudaStreamWaitEvent(aux->st[1], aux->fork, 0);
+  }
+  for (int sl = 0; sl < launches; ++sl) {
+    cudaStream_t ls = two ? aux->st[sl & 1] : s;
+    k_level2c<<<(unsigned)grid, kWarps * 32, smem, ls>>>(bd, keys, vals, useg, cflag, cord, colhead,
+                                                         istart, nitems, warp_words, sl, zslab,
+                                                         zslab > 0 ? ilist : nullptr, ioff);
+    count_launch();
+    if (after_slab) after_slab(sl, ls);
+  }
+  if (two) {
+    cudaEventRecord(aux->join[0], aux->st[0]);
+    cudaEventRecord(aux->join[1], aux->st[1]);
+    cudaStreamWaitEvent(s, aux->join[0], 0);
+    cudaStreamWaitEvent(s, aux->join[1], 0);
+  }
 }
 
 }  // namespace gpv

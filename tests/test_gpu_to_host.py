@@ -1,0 +1,81 @@
+"""gpv_voxelize_to_host: host outputs copied while the Level2 slabs compute equal the plain path's
+(and the oracle's) for any slab count; a Level2 buffer that is too small is reported, not
+overrun."""
+import numpy as np
+import pytest
+
+from oracle import oracle as orc
+import workloads as W
+
+pytestmark = pytest.mark.gpu
+
+
+def _to_host(ctx, tris, spec, slabs, l2_bytes=None):
+    import torch
+
+    n1 = int(np.prod(list(spec.ndiv)))
+    cells = int(np.prod(list(spec.ndiv2))) if spec.ndiv2[0] else 0
+    ref = ctx.voxelize_host(tris, spec)  # sizes
+    B = ref.num_boundary
+    ctx.release(ref)
+    h_tris = torch.from_numpy(tris).pin_memory()
+    l1 = torch.empty(n1, dtype=torch.uint8).pin_memory()
+    pre = torch.empty(n1, dtype=torch.int32).pin_memory()
+    bi = torch.empty(max(B, 1), dtype=torch.int32).pin_memory()
+    need = B * cells
+    l2 = torch.full((max(need, 1),), 77, dtype=torch.uint8).pin_memory()
+    rc, res = ctx.voxelize_to_host(h_tris.data_ptr(), tris.size // 9, spec, l1.data_ptr(),
+                                   pre.data_ptr(), bi.data_ptr(), l2.data_ptr(),
+                                   need if l2_bytes is None else l2_bytes, slabs)
+    return rc, res, l1.numpy().copy(), pre.numpy().copy(), bi.numpy()[:B].copy(), l2.numpy()[:need].copy()
+
+
+@pytest.mark.parametrize("slabs", [1, 3, 4, 8])
+def test_to_host_equals_oracle_sphere16k(ctx, slabs):
+    tris, spec = W.make(W.C1)
+    rc, res, l1, pre, bi, l2 = _to_host(ctx, tris, spec, slabs)
+    assert rc == 0
+    ref = orc.Run(tris, spec)
+    np.testing.assert_array_equal(l1, ref.level1_bytes())
+    np.testing.assert_array_equal(pre, ref.prefix())
+    np.testing.assert_array_equal(bi, ref.boundary_index())
+    np.testing.assert_array_equal(l2, ref.level2_bytes())
+    # the returned device result matches too
+    d1, dpre, dbi, dl2 = ctx.fetch(res)
+    np.testing.assert_array_equal(dl2, l2)
+    ctx.release(res)
+
+
+def test_to_host_equals_plain_torus262k(ctx):
+    tris, spec = W.make(W.C2)
+    rc, res, l1, pre, bi, l2 = _to_host(ctx, tris, spec, 4)
+    assert rc == 0
+    ctx.release(res)
+    plain = ctx.voxelize_host(tris, spec)
+    p1, ppre, pbi, pl2 = ctx.fetch(plain)
+    ctx.release(plain)
+    np.testing.assert_array_equal(l1, p1)
+    np.testing.assert_array_equal(pre, ppre)
+    np.testing.assert_array_equal(bi, pbi)
+    np.testing.assert_array_equal(l2, pl2)
+
+
+def test_to_host_small_buffer_is_reported(ctx):
+    tris, spec = W.make(W.C1)
+    rc, res, l1, pre, bi, l2 = _to_host(ctx, tris, spec, 4, l2_bytes=100)
+    assert rc == -7  # GPV_ERR_BUDGET: nothing copied to the Level2 buffer
+    assert (l2 == 77).all()
+    ref = orc.Run(tris, spec)
+    np.testing.assert_array_equal(l1, ref.level1_bytes())  # Level1 outputs still delivered
+    ctx.release(res)
+
+
+def test_to_host_level1_only(ctx):
+    import gpview_gb300 as gpv
+
+    tris = gpv.gen_uvsphere(51, 32, 16, (0.5, 0.5, 0.5), 0.4, 0.002)
+    spec = gpv.grid_padded(*gpv.mesh_bounds(tris), 24, 0)
+    rc, res, l1, pre, bi, l2 = _to_host(ctx, tris, spec, 4)
+    assert rc == 0
+    np.testing.assert_array_equal(l1, orc.Run(tris, spec).level1_bytes())
+    ctx.release(res)
