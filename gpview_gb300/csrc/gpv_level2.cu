@@ -15,7 +15,9 @@
 //            once per (triangle, sub-column) for the whole chunk.  Voxels that lie certainly below
 //            the triangle (t at their top origin exceeds 1e-6 by twice a float error bound) are
 //            entirely hit: one "full hit" toggle marks the highest of them and a suffix XOR over
-//            the chunk's voxels expands it.  The remaining voxels evaluate t per origin.
+//            the chunk's voxels expands it.  In the remaining voxels t at each origin follows
+//            from t at the top origin (exact t falls by the rise of the origin); only origins
+//            within the error band of the crossing evaluate their own t.
 #include "gpv_internal.h"
 
 namespace gpv {
@@ -507,14 +509,34 @@ __global__ void __launch_bounds__(kWarps * 32, 6) k_level2c(
       }
       for (int jv = ws.jm[tl] - 1; jv >= 0; --jv) {
         const float *oz = ozt + (size_t)kz[jv] * n2z;
-        if (well && ray_tval(rt, rc, __ldg(oz + n2z - 1)) > g.thr + E2) {
-          // this voxel and every lower voxel of the chunk are hit at every origin
-          atomicXor(&ft[jv * FW + (pq >> 5)], 1u << (pq & 31));
-          break;
-        }
         uint32_t bits = 0;
-        for (int r = 0; r < n2z; ++r)
-          if (ray_t(rt, rc, __ldg(oz + r), g.thr)) bits |= 1u << r;
+        if (well) {
+          const float otop = __ldg(oz + n2z - 1);
+          const float ttop = ray_tval(rt, rc, otop);
+          if (ttop > g.thr + E2) {
+            // this voxel and every lower voxel of the chunk are hit at every origin
+            atomicXor(&ft[jv * FW + (pq >> 5)], 1u << (pq & 31));
+            break;
+          }
+          // Along +z, t* (exact) grows by exactly the drop of the origin below otop:
+          // t*(oz) = t*(otop) + (otop - oz), and the float t at every origin and at otop lies
+          // within E2/2 of t*.  So with d = otop - oz, the float t exceeds thr when
+          // d > thr - ttop + E2 and does not when d <= thr - ttop - E2; the thresholds carry the
+          // rounding of d and of themselves (K bounds every magnitude involved).  Origins
+          // between the two run the exact test.
+          const float dmax = otop - __ldg(oz);
+          const float K = fabsf(ttop) + dmax + g.thr;
+          const float slack = E2 * 1.0001f + 8.f * EPS24 * K + 1e-30f;
+          const float dhit = (g.thr - ttop) + slack, dmiss = (g.thr - ttop) - slack;
+          for (int r = 0; r < n2z; ++r) {
+            const float ozr = __ldg(oz + r);
+            const float d = otop - ozr;
+            if (d > dhit || (d > dmiss && ray_t(rt, rc, ozr, g.thr))) bits |= 1u << r;
+          }
+        } else {
+          for (int r = 0; r < n2z; ++r)
+            if (ray_t(rt, rc, __ldg(oz + r), g.thr)) bits |= 1u << r;
+        }
         if (bits) xor_column(par + jv * W, pq, n2z, bits);
       }
     }

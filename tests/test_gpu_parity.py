@@ -117,6 +117,20 @@ def _spec_exact(mn, mx, n, n2):
     return s
 
 
+def test_vertices_on_cell_lattice(ctx):
+    """Vertices snapped to Level2 cell centres and faces: SAT and ray tests at exact ties, where
+    the kernel's certified SAT decisions and slab bounds are closest to their margins."""
+    import gpview_gb300 as gpv
+
+    tris = gpv.gen_torus(9, 48, 24, (0.5, 0.5, 0.5), 0.3, 0.12, 0.0).reshape(-1, 3)
+    for mn, mx, n, n2 in (((0, 0, 0), (1, 1, 1), (16, 16, 16), (4, 4, 4)),
+                          ((-0.25, -0.5, 0.0), (1.25, 1.5, 1.0), (12, 20, 10), (3, 5, 2))):
+        mn32, mx32 = np.float32(mn), np.float32(mx)
+        half = ((mx32 - mn32) / (np.array(n) * np.array(n2)).astype(np.float32) / 2).astype(np.float32)
+        snapped = (mn32 + np.round((tris - mn32) / half).astype(np.float32) * half).astype(np.float32)
+        _check_full(ctx, snapped.reshape(-1), _spec_exact(mn, mx, n, n2), fill=orc.FILL_VOXEL)
+
+
 def test_nonuniform_divisions_and_odd_sizes(ctx):
     import gpview_gb300 as gpv
 
