@@ -64,6 +64,9 @@ BOX_DTYPE = np.dtype([("mid", np.float32, 3), ("half", np.float32, 3), ("solid",
 
 
 NORMALS_OFF, NORMALS_BYTES, NORMALS_FLOAT = 0, 1, 2
+# inside fill: +z ray parity (ClassifyInOutCPU / ClassifyInOutLevel2CPU) or the rasterised
+# stencil parity (ClassifyInOut2x / ClassifyInOut2xLevel2)
+FILL_RAY, FILL_STENCIL = 0, 1
 
 
 class VoxelConfig(C.Structure):
@@ -120,6 +123,7 @@ def lib():
     L.gpv_write_raw_normals.argtypes = [C.c_char_p, C.POINTER(Result), C.c_void_p, C.c_void_p]
     L.gpv_set_normals.argtypes = [C.c_void_p, C.c_int]
     L.gpv_set_hierarchy.argtypes = [C.c_void_p, C.c_int]
+    L.gpv_set_fill.argtypes = [C.c_void_p, C.c_int]
     L.gpv_result_copy_hierarchy_to_host.argtypes = [C.c_void_p, C.POINTER(Result), C.c_void_p,
                                                     C.c_void_p]
     L.gpv_read_voxel_config.argtypes = [C.c_char_p, C.POINTER(VoxelConfig)]
@@ -371,6 +375,10 @@ class Context:
             C.c_void_p(stream)), "copy_normals_to_host")
         return l1, l2
 
+    def set_fill(self, mode):
+        """FILL_RAY (default) or FILL_STENCIL for the next calls."""
+        self._check(lib().gpv_set_fill(self._h, int(mode)), "set_fill")
+
     def set_hierarchy(self, on=True):
         """Build the voxel box hierarchy (Object::BuildHierarchy) with the next calls."""
         self._check(lib().gpv_set_hierarchy(self._h, int(bool(on))), "set_hierarchy")
@@ -476,10 +484,12 @@ class Object:
         self.flatCPUTriangleData = self._tris
         self.totalNumTriangles = self._tris.size // 9
 
-    def PerformVoxelization(self, glParam, bufferSize=-1, spec=None, normals=True):
+    def PerformVoxelization(self, glParam, bufferSize=-1, spec=None, normals=True, fill=FILL_RAY):
         """Voxelizes on the GPU.  `spec` overrides the reference sizing (explicit grids).  Normals
         are computed as the reference does (float, src/Object.cpp:3219-3253, :2402-2424) unless
-        `normals` is False."""
+        `normals` is False.  `fill` picks the inside fill: FILL_RAY, the CPU path
+        (ClassifyInOutCPU, :3159), or FILL_STENCIL, the rasterised path the reference calls at
+        :3158 and :3297 (ClassifyInOut2x, ClassifyInOut2xLevel2)."""
         del bufferSize  # the device path has no fixed per-voxel buffer
         if self.flatCPUTriangleData is None:
             self.CreateFlatTriangleData()
@@ -489,10 +499,12 @@ class Object:
             spec = grid_reference(self.bBoxMin, self.bBoxMax, self.maxModelSize,
                                   glParam.voxelCount, glParam.voxelCount2 if glParam.level2Voxels else 0)
         self.ctx.set_normals(NORMALS_FLOAT if normals else NORMALS_OFF)
+        self.ctx.set_fill(fill)
         try:
             res = self.ctx.voxelize_host(self.flatCPUTriangleData, spec)
         finally:
             self.ctx.set_normals(NORMALS_OFF)
+            self.ctx.set_fill(FILL_RAY)
         try:
             l1, pre, bi, l2 = self.ctx.fetch(res)
             nrm = self.ctx.fetch_normals(res) if normals else (None, None)

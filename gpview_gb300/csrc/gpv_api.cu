@@ -70,6 +70,11 @@ int grid_derive(const gpv_grid_spec &spec, GridHost &gh, const float *ext1_overr
       }
     }
   }
+  // stencil fill clip heights (slice + 0.5)*gridSizeZ + bBoxMin[2] in double, float in GL
+  // (src/Object.cpp:1534)
+  gh.sp1.resize(gh.n[2]);
+  for (int k = 0; k < gh.n[2]; ++k)
+    gh.sp1[k] = (float)((k + 0.5) * (double)gh.g[2] + (double)spec.bbox_min[2]);
   gh.nxw = (gh.n[0] + 31) / 32;
   gh.nzw = (gh.n[2] + 31) / 32;
   int kb = 1;
@@ -85,7 +90,7 @@ int grid_derive(const gpv_grid_spec &spec, GridHost &gh, const float *ext1_overr
 int64_t table_floats(const GridHost &gh) {
   int64_t n = 0;
   for (int a = 0; a < 3; ++a) n += (int64_t)gh.c1[a].size() + 2 * (int64_t)gh.c2s[a].size();
-  return n;
+  return n + (int64_t)gh.sp1.size();
 }
 
 void pack_tables(const GridHost &gh, float *host) {
@@ -93,6 +98,7 @@ void pack_tables(const GridHost &gh, float *host) {
   for (int a = 0; a < 3; ++a) { std::memcpy(host + o, gh.c1[a].data(), 4 * gh.c1[a].size()); o += gh.c1[a].size(); }
   for (int a = 0; a < 3; ++a) { std::memcpy(host + o, gh.c2s[a].data(), 4 * gh.c2s[a].size()); o += gh.c2s[a].size(); }
   for (int a = 0; a < 3; ++a) { std::memcpy(host + o, gh.o2[a].data(), 4 * gh.o2[a].size()); o += gh.o2[a].size(); }
+  std::memcpy(host + o, gh.sp1.data(), 4 * gh.sp1.size());
 }
 
 GridDev make_griddev(const GridHost &gh, const float *dt) {
@@ -111,6 +117,7 @@ GridDev make_griddev(const GridHost &gh, const float *dt) {
   for (int a = 0; a < 3; ++a) { g.c1[a] = dt + o; o += gh.c1[a].size(); }
   for (int a = 0; a < 3; ++a) { g.c2s[a] = dt + o; o += gh.c2s[a].size(); }
   for (int a = 0; a < 3; ++a) { g.o2[a] = dt + o; o += gh.o2[a].size(); }
+  g.sp1 = dt + o;
   g.nxw = gh.nxw;
   g.nzw = gh.nzw;
   g.key_bits = gh.key_bits;
@@ -231,6 +238,13 @@ int gpv_set_graphs(gpv_ctx *ctx, int on) {
 int gpv_set_hierarchy(gpv_ctx *ctx, int on) {
   if (!ctx) return GPV_ERR_INVALID;
   ctx->hierarchy = on != 0;
+  return GPV_OK;
+}
+
+int gpv_set_fill(gpv_ctx *ctx, int mode) {
+  if (!ctx || (mode != GPV_FILL_RAY && mode != GPV_FILL_STENCIL))
+    return ctx_fail(ctx, GPV_ERR_INVALID, "fill mode must be GPV_FILL_RAY or GPV_FILL_STENCIL");
+  ctx->fill = mode;
   return GPV_OK;
 }
 

@@ -151,13 +151,14 @@ int run_batch(gpv_ctx *ctx, int n, const float *const *d_tris, const int64_t *T,
   }
   const int tile = ctx->tile;
   const int nmode = ctx->normals;
+  const bool stencil = ctx->fill == GPV_FILL_STENCIL;
   const size_t nsz = nmode == GPV_NORMALS_FLOAT ? sizeof(float) : 1;  // bytes per normal value
 
   // ---- sizes and per-mesh bases
   std::vector<int64_t> tab_off(n + 1, 0), res_l1(n + 1, 0), res_pre(n + 1, 0), res_l1n(n + 1, 0),
       res_hier(n + 1, 0);
   std::vector<MeshDesc> md(n);
-  int64_t tris = 0, tiles = 0, fwarps = 0, rows = 0, words = 0, togg = 0;
+  int64_t tris = 0, tiles = 0, fwarps = 0, rows = 0, words = 0, togg = 0, stgw = 0;
   int max_keybits = 1, warp_words = 0;
   int64_t max_T = 1;
   bool any_l2 = false;
@@ -177,6 +178,7 @@ int run_batch(gpv_ctx *ctx, int n, const float *const *d_tris, const int64_t *T,
     rows += (int64_t)g.n[2] * g.n[1];
     words += (int64_t)g.n[2] * g.n[1] * g.nxw;
     togg += (int64_t)g.n[0] * g.n[1] * g.nzw;
+    if (stencil) stgw += 4 * (int64_t)g.n[0] * g.n[1] * g.nzw;
     tab_off[m + 1] = tab_off[m] + table_floats(g);
     res_l1[m + 1] = res_l1[m] + (int64_t)al16(g.N1);
     res_pre[m + 1] = res_pre[m] + (int64_t)al16(g.N1);  // int32 elements, 64-byte aligned
@@ -231,6 +233,11 @@ int run_batch(gpv_ctx *ctx, int n, const float *const *d_tris, const int64_t *T,
   CK(cudaMemsetAsync(stats, 0, n * sizeof(MeshStats), s));
   CK(cudaMemsetAsync(bplane, 0, words * 4, s));
   CK(cudaMemsetAsync(toggles, 0, togg * 4, s));
+  uint32_t *stg = nullptr;  // stencil fill: Level1 sample-column toggles
+  if (stencil) {
+    CK(ws.get(&stg, (size_t)stgw));
+    CK(cudaMemsetAsync(stg, 0, stgw * 4, s));
+  }
   float4 *fnorm = nullptr;
   if (nmode) CK(ws.get(&fnorm, (size_t)std::max<int64_t>(tris, 1)));
 
@@ -246,7 +253,7 @@ int run_batch(gpv_ctx *ctx, int n, const float *const *d_tris, const int64_t *T,
     CK(cudaMemsetAsync(set->l1n, nmode == GPV_NORMALS_FLOAT ? 0 : 127, res_l1n[n], s));
   }
 
-  int64_t togg_off = 0;
+  int64_t togg_off = 0, stg_off = 0;
   for (int m = 0; m < n; ++m) {
     MeshDesc &d = md[m];
     const GridHost &g = gh[m];
@@ -259,6 +266,10 @@ int run_batch(gpv_ctx *ctx, int n, const float *const *d_tris, const int64_t *T,
     d.iplane = iplane + d.word_base;
     d.toggles = toggles + togg_off;
     togg_off += (int64_t)g.n[0] * g.n[1] * g.nzw;
+    if (stg) {
+      d.stg = stg + stg_off;
+      stg_off += 4 * (int64_t)g.n[0] * g.n[1] * g.nzw;
+    }
     d.stats = stats + m;
     d.l1 = static_cast<uint8_t *>(set->l1) + res_l1[m];
     d.prefix = static_cast<int32_t *>(set->prefix) + res_pre[m];
@@ -266,7 +277,8 @@ int run_batch(gpv_ctx *ctx, int n, const float *const *d_tris, const int64_t *T,
     d.has_l2 = g.level2 ? 1 : 0;
     d.fnorm = fnorm ? fnorm + d.tri_base : nullptr;
     d.l1n = nmode ? static_cast<uint8_t *>(set->l1n) + res_l1n[m] : nullptr;
-    if (g.level2) warp_words = std::max(warp_words, level2_warp_words(d.g, ctx->l2_chunk_cap));
+    if (g.level2)
+      warp_words = std::max(warp_words, level2_warp_words(d.g, ctx->l2_chunk_cap, stencil));
   }
   BatchDev bd;
   bd.md = d_md;
@@ -279,6 +291,7 @@ int run_batch(gpv_ctx *ctx, int n, const float *const *d_tris, const int64_t *T,
   bd.total_words = words;
   bd.queue = queue;
   bd.normals = nmode;
+  bd.fill = ctx->fill;
   CK(ctx_ensure_host(ctx, (size_t)n));
   std::memcpy(ctx->h_md, md.data(), n * sizeof(MeshDesc));
   CK(cudaMemcpyAsync(d_md, ctx->h_md, n * sizeof(MeshDesc), cudaMemcpyHostToDevice, s));
@@ -317,6 +330,7 @@ int run_batch(gpv_ctx *ctx, int n, const float *const *d_tris, const int64_t *T,
     launch_pair_bases(bd, d_md, keys, vals, pair_cap, s);
     mark(2);
     launch_level1(bd, ctx->num_sms, s);
+    if (stencil) launch_stencil1(bd, s);
     mark(3);
     launch_fill_finish(bd, s);
     launch_popc(bplane, words, wcnt, s);

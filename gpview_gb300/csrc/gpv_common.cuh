@@ -51,6 +51,7 @@ struct GridDev {
   float thr;            // largest float below 1e-6
   int oz_monotone;      // Level2 ray-origin heights strictly increase along every column
   float inv_g2[3];      // 1 / gridSize2 (range arithmetic only, never inside a predicate)
+  const float *sp1;     // stencil fill: Level1 slice clip heights [k] (Level2 uses o2[2])
 };
 
 __device__ __forceinline__ float fm(float a, float b) { return __fmul_rn(a, b); }
@@ -290,5 +291,87 @@ __device__ __forceinline__ void fence_mbar_init() {
 }
 
 __device__ __forceinline__ unsigned lane_id() { return threadIdx.x & 31u; }
+
+// ---- stencil fill (ClassifyInOut2x, src/Object.cpp:1446-1649; ClassifyInOut2xLevel2,
+// :1210-1444): the triangles are drawn into an orthographic viewport of SW x SH pixels over
+// [lx, hx] x [ly, hy]; a pixel (sample) counts a triangle when its centre is covered and the
+// surface there lies at or below the slice's clip height (glClipPlane (0, 0, -1, c) keeps
+// z <= c).  Window coordinates are snapped to 1/256 pixel (8 sub-pixel bits, clamped to
+// +-2^21 pixels), coverage is decided by exact integer edge functions with a top-left rule
+// (a sample on an edge shared by two triangles counts once), and the height is interpolated
+// from the barycentric weights in float.
+struct StTri {
+  int32_t X[3], Y[3];  // snapped window coordinates, counter-clockwise
+  float z[3];
+  float rA;            // 1 / (twice the snapped area)
+  int sx0, sx1, sy0, sy1;  // samples whose centres lie in the snapped bounding box
+};
+
+__device__ __forceinline__ int32_t st_snap(float v, float lo, float hi, int npx) {
+  float w = fm(__fdiv_rn(fs(v, lo), fs(hi, lo)), (float)npx);
+  w = (w > -2097152.0f) ? fminf(w, 2097152.0f) : -2097152.0f;  // NaN to the low clamp
+  return (int32_t)__float2ll_rn(fm(w, 256.0f));
+}
+
+// false: zero snapped area, or no sample centre inside the viewport and the triangle's box.
+__device__ __forceinline__ bool st_setup(const float *V, float lx, float hx, float ly, float hy,
+                                         int SW, int SH, StTri &t) {
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    t.X[i] = st_snap(V[3 * i], lx, hx, SW);
+    t.Y[i] = st_snap(V[3 * i + 1], ly, hy, SH);
+    t.z[i] = V[3 * i + 2];
+  }
+  long long A = (long long)(t.X[1] - t.X[0]) * (t.Y[2] - t.Y[0]) -
+                (long long)(t.Y[1] - t.Y[0]) * (t.X[2] - t.X[0]);
+  if (A == 0) return false;
+  if (A < 0) {
+    int32_t a = t.X[1]; t.X[1] = t.X[2]; t.X[2] = a;
+    a = t.Y[1]; t.Y[1] = t.Y[2]; t.Y[2] = a;
+    const float f = t.z[1]; t.z[1] = t.z[2]; t.z[2] = f;
+    A = -A;
+  }
+  t.rA = __frcp_rn(__ll2float_rn(A));
+  const int32_t xmn = min(t.X[0], min(t.X[1], t.X[2])), xmx = max(t.X[0], max(t.X[1], t.X[2]));
+  const int32_t ymn = min(t.Y[0], min(t.Y[1], t.Y[2])), ymx = max(t.Y[0], max(t.Y[1], t.Y[2]));
+  // sample centres 256 s + 128 within [mn, mx]: ceil((mn - 128) / 256) .. floor((mx - 128) / 256)
+  t.sx0 = max(-((128 - xmn) >> 8), 0);
+  t.sx1 = min((xmx - 128) >> 8, SW - 1);
+  t.sy0 = max(-((128 - ymn) >> 8), 0);
+  t.sy1 = min((ymx - 128) >> 8, SH - 1);
+  return t.sx0 <= t.sx1 && t.sy0 <= t.sy1;
+}
+
+__device__ __forceinline__ bool st_edge_in(long long w, int32_t dx, int32_t dy) {
+  return w > 0 || (w == 0 && (dy < 0 || (dy == 0 && dx > 0)));
+}
+
+// Coverage of sample (sx, sy) and the interpolated surface height there.
+__device__ __forceinline__ bool st_cover(const StTri &t, int sx, int sy, float &zs) {
+  const long long px = (long long)sx * 256 + 128, py = (long long)sy * 256 + 128;
+  const int32_t dx0 = t.X[2] - t.X[1], dy0 = t.Y[2] - t.Y[1];
+  const long long w0 = (long long)dx0 * (py - t.Y[1]) - (long long)dy0 * (px - t.X[1]);
+  if (!st_edge_in(w0, dx0, dy0)) return false;
+  const int32_t dx1 = t.X[0] - t.X[2], dy1 = t.Y[0] - t.Y[2];
+  const long long w1 = (long long)dx1 * (py - t.Y[2]) - (long long)dy1 * (px - t.X[2]);
+  if (!st_edge_in(w1, dx1, dy1)) return false;
+  const int32_t dx2 = t.X[1] - t.X[0], dy2 = t.Y[1] - t.Y[0];
+  const long long w2 = (long long)dx2 * (py - t.Y[0]) - (long long)dy2 * (px - t.X[0]);
+  if (!st_edge_in(w2, dx2, dy2)) return false;
+  zs = fa(fa(fm(fm(__ll2float_rn(w0), t.rA), t.z[0]), fm(fm(__ll2float_rn(w1), t.rA), t.z[1])),
+          fm(fm(__ll2float_rn(w2), t.rA), t.z[2]));
+  return true;
+}
+
+// First index in [0, n] with tab[i] >= x (tab increasing): the lowest slice whose clip height
+// keeps a surface point at height x.
+__device__ __forceinline__ int st_first_slice(const float *tab, int n, float x) {
+  int lo = 0, hi = n;
+  while (lo < hi) {
+    const int mid = (lo + hi) >> 1;
+    if (__ldg(tab + mid) >= x) hi = mid; else lo = mid + 1;
+  }
+  return lo;
+}
 
 }  // namespace gpv

@@ -41,6 +41,7 @@ struct gpv_ctx {
   bool graphs = true;                  // record phases B and C as CUDA graphs
   int normals = 0;                     // GPV_NORMALS_* for the next voxelizations
   bool hierarchy = false;              // build the voxel box hierarchy
+  int fill = GPV_FILL_RAY;             // inside fill of both levels
   cudaGraphExec_t gexec[2] = {};       // cached executable graphs of phases B and C
   uint64_t graph_launches = 0, graph_instantiations = 0;
   gpv::MeshStats *h_stats = nullptr;   // pinned, h_cap entries

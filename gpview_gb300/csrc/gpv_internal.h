@@ -29,6 +29,7 @@ struct GridHost {
   int n[3], n2[3];
   float g[3], e1[3], g2[3], e2[3];
   std::vector<float> c1[3], c2s[3], o2[3];
+  std::vector<float> sp1;  // stencil fill: Level1 slice clip heights
   int64_t N1 = 0, cells = 0;
   int nxw = 0, nzw = 0, key_bits = 0;
   bool level2 = false;
@@ -72,6 +73,7 @@ struct MeshDesc {
   int32_t has_l2;        // the mesh has a Level2 grid
   float4 *fnorm;         // normals on: normalised face normal per triangle
   void *l1n, *l2n;       // normals on: Level1 / Level2 normal outputs (bytes or floats)
+  uint32_t *stg;         // stencil fill: Level1 sample-column toggles, (2nx * 2ny) x nzw words
 };
 
 struct BatchDev {
@@ -81,6 +83,7 @@ struct BatchDev {
   int64_t total_tris, total_tiles, total_fwarps, total_rows, total_words;
   uint32_t *queue;       // work-queue tickets, zeroed before each persistent launch
   int normals;           // GPV_NORMALS_* of this batch
+  int fill;              // GPV_FILL_* of this batch
 };
 
 void launch_prep(const BatchDev &bd, cudaStream_t s);
@@ -92,6 +95,9 @@ void launch_pair_bases(const BatchDev &bd, MeshDesc *d_md, uint32_t *keys, uint3
                        int64_t cap, cudaStream_t s);
 void launch_level1(const BatchDev &bd, int num_sms, cudaStream_t s);
 void launch_fill_finish(const BatchDev &bd, cudaStream_t s);
+// Stencil fill, Level1 (gpv_stencil.cu): per-sample-column slice toggles of every triangle into
+// MeshDesc::stg (zeroed by the caller); launch_fill_finish then reduces them.
+void launch_stencil1(const BatchDev &bd, cudaStream_t s);
 void launch_popc(const uint32_t *plane, int64_t nwords, uint32_t *cnt, cudaStream_t s);
 void launch_boundary_counts(const BatchDev &bd, const uint32_t *wpre, const uint32_t *wtotal,
                             cudaStream_t s);
@@ -112,7 +118,7 @@ bool sort_pairs_seg(const BatchDev &bd, const SortTile *tiles, const int64_t *ti
 constexpr int kSortTileItems = 2048;
 
 int level2_chunk(const GridDev &g, int cap = 32);
-int level2_warp_words(const GridDev &g, int cap = 32);
+int level2_warp_words(const GridDev &g, int cap = 32, bool stencil = false);
 int64_t level2_temp_words(int64_t Btot);
 // before_kernel (optional) runs on the host between the work-item launches and the Level2
 // kernel's launch, e.g. to record an event that times the kernel alone.

@@ -213,6 +213,11 @@ __global__ void __launch_bounds__(256) k_prep(BatchDev bd) {
     }
     if (fx0 <= fx1 && fy0 <= fy1) fu = (unsigned long long)(fx1 - fx0 + 1) * (fy1 - fy0 + 1);
     else { fx0 = 1; fx1 = 0; fy0 = 1; fy1 = 0; }
+    if (bd.fill == GPV_FILL_STENCIL) {  // the stencil kernel fills instead of the ray units
+      fx0 = 1; fx1 = 0; fy0 = 1; fy1 = 0;
+      fu = 0;
+      r1 = 0;
+    }
     // 1/det of the +z ray test (src/TriRayIntersection.cpp:310), shared by every column
     const float det = fa(fm(fs(V[3], V[0]), -fs(V[7], V[1])), fm(fs(V[4], V[1]), fs(V[6], V[0])));
     d.ptri[3 * t + 0] = make_float4(V[0], V[1], V[2], __uint_as_float(pack2(fx0, fx1)));
@@ -474,6 +479,9 @@ __global__ void __launch_bounds__(kL1Threads) k_level1(BatchDev bd) {
 // ---------------------------------------------------------------------------------------------
 // One warp per (mesh, row j, 32-column group): suffix XOR of each column's toggles gives the
 // parity of every voxel; 32 ballots per word transpose it into the linear inside plane.
+// Stencil fill: the parity of each of the voxel column's four sample columns is the prefix XOR
+// of its slice toggles (lowest slice first), and a voxel is inside where at least three of the
+// four are odd.
 __global__ void __launch_bounds__(256) k_fill_finish(BatchDev bd) {
   const int64_t gw = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const unsigned lane = threadIdx.x & 31u;
@@ -487,13 +495,42 @@ __global__ void __launch_bounds__(256) k_fill_finish(BatchDev bd) {
   const int i = ig * 32 + (int)lane;
   const bool valid = i < nx;
   const size_t col = (size_t)j * nx + i;
+  const bool stencil = bd.fill == GPV_FILL_STENCIL;
+  const uint32_t *sc[4] = {nullptr, nullptr, nullptr, nullptr};
+  uint32_t tot = 0, above = 0;  // bit a: toggle parity of sample column a, in all / higher words
+  if (stencil && valid) {
+    const size_t SW = 2 * (size_t)nx;
+    sc[0] = d.stg + ((size_t)(2 * j) * SW + 2 * (size_t)i) * g.nzw;
+    sc[1] = sc[0] + g.nzw;
+    sc[2] = sc[0] + SW * g.nzw;
+    sc[3] = sc[2] + g.nzw;
+    for (int w = 0; w < g.nzw; ++w)
+#pragma unroll
+      for (int a = 0; a < 4; ++a) tot ^= (uint32_t)(__popc(sc[a][w]) & 1) << a;
+  }
   uint32_t carry = 0;
   for (int w = g.nzw - 1; w >= 0; --w) {
-    const uint32_t D = valid ? d.toggles[col * g.nzw + w] : 0u;
-    uint32_t s = D;
-    s ^= s >> 1; s ^= s >> 2; s ^= s >> 4; s ^= s >> 8; s ^= s >> 16;
-    if (carry) s = ~s;
-    carry ^= (uint32_t)(__popc(D) & 1);
+    uint32_t s;
+    if (stencil) {
+      uint32_t x[4];
+#pragma unroll
+      for (int a = 0; a < 4; ++a) {
+        const uint32_t D = valid ? sc[a][w] : 0u;
+        const uint32_t pd = (uint32_t)(__popc(D) & 1);
+        uint32_t y = D;  // prefix XOR from the lowest slice of the word
+        y ^= y << 1; y ^= y << 2; y ^= y << 4; y ^= y << 8; y ^= y << 16;
+        if ((((tot ^ above) >> a) & 1u) ^ pd) y = ~y;  // odd toggles in the words below
+        above ^= pd << a;
+        x[a] = y;
+      }
+      s = (x[0] & x[1] & (x[2] | x[3])) | (x[2] & x[3] & (x[0] | x[1]));
+    } else {
+      const uint32_t D = valid ? d.toggles[col * g.nzw + w] : 0u;
+      s = D;
+      s ^= s >> 1; s ^= s >> 2; s ^= s >> 4; s ^= s >> 8; s ^= s >> 16;
+      if (carry) s = ~s;
+      carry ^= (uint32_t)(__popc(D) & 1);
+    }
     uint32_t mine = 0;
 #pragma unroll
     for (int bb = 0; bb < 32; ++bb) {

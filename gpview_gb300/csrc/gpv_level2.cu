@@ -79,6 +79,11 @@ __device__ __forceinline__ PlaneSlab plane_slab(const float *V, float cx0, float
 }
 
 // Bits of one Level2 column (n2z cells along z) start at bit (q*n2x + p)*n2z of a voxel's mask.
+__device__ __forceinline__ void or_column(uint32_t *m, int colidx, int n2z, uint32_t bits) {
+  const int off = colidx * n2z, sh = off & 31;
+  atomicOr(&m[off >> 5], bits << sh);
+  if (sh + n2z > 32) atomicOr(&m[(off >> 5) + 1], bits >> (32 - sh));
+}
 __device__ __forceinline__ void xor_column(uint32_t *m, int colidx, int n2z, uint32_t bits) {
   const int off = colidx * n2z, sh = off & 31;
   atomicXor(&m[off >> 5], bits << sh);
@@ -228,7 +233,17 @@ __global__ void k_item_slab_place(const uint32_t *__restrict__ istart,
   ilist[atomicAdd(&cur[sl], 1u)] = (uint32_t)it;
 }
 
+// n2z bits of a Level2 column starting at bit `off` of a mask.
+__device__ __forceinline__ uint32_t column_bits(const uint32_t *m, int off, int n2z) {
+  const int sh = off & 31;
+  uint32_t b = m[off >> 5] >> sh;
+  if (sh + n2z > 32) b |= m[(off >> 5) + 1] << (32 - sh);
+  return b;
+}
+
 // ---- Level2 ------------------------------------------------------------------------------------
+// ST: the stencil fill (ClassifyInOut2xLevel2) instead of the ray fill.
+template <bool ST>
 __global__ void __launch_bounds__(kWarps * 32, 6) k_level2c(
     BatchDev bd, const uint32_t *__restrict__ keys, const uint32_t *__restrict__ vals,
     const uint32_t *__restrict__ useg, const uint32_t *__restrict__ cflag,
@@ -264,6 +279,9 @@ __global__ void __launch_bounds__(kWarps * 32, 6) k_level2c(
   int *kz = (int *)(ft + CH * FW);
   uint32_t *ftacc = (uint32_t *)(kz + CH);
   WarpScratch &ws = *reinterpret_cast<WarpScratch *>(ftacc + FW);
+  // stencil fill: per voxel, (2 n2x * 2 n2y) sample columns of n2z slice toggle bits
+  uint32_t *stg = reinterpret_cast<uint32_t *>(&ws + 1);
+  const int SWd = 4 * W;
 
   const uint32_t ucol_end = colhead[cord[ua] + cflag[ua]];  // first voxel of the next column
   const int nx = g.n[0], ny = g.n[1], nz = g.n[2];
@@ -284,6 +302,8 @@ __global__ void __launch_bounds__(kWarps * 32, 6) k_level2c(
   // clear the masks of the chunk's m voxels only (the arrays are sized for CH voxels)
   for (int w = lane; w < m * W; w += 32) { sat[w] = 0; par[w] = 0; }
   for (int w = lane; w < m * FW; w += 32) ft[w] = 0;
+  if (ST)
+    for (int w = lane; w < m * SWd; w += 32) stg[w] = 0;
   const int ci = (int)(col % (uint32_t)nx), cj = (int)(col / (uint32_t)nx);
   if ((int)lane < m) kz[lane] = (int)(keys[useg[ua + lane]] - col * (uint32_t)nz);
   __syncwarp();
@@ -436,12 +456,103 @@ __global__ void __launch_bounds__(kWarps * 32, 6) k_level2c(
     }
   }
 
+  uint64_t nun = 0;
+  if (ST) {
+    // ---------------- stencil fill: the triangles recorded anywhere in the Level1 column (the
+    // voxel strip of CreateVoxelStripDisplayLists, src/Object.cpp:605-633: each once, at its
+    // topmost record) are drawn into 2 n2x x 2 n2y samples over the Level1 voxel's x/y extent
+    // (glOrtho over [i*gridSizeX + bBoxMin, + gridSizeX], :1241-1266).  Slice s of voxel k clips
+    // at the Level2 ray-origin height o2z[k][s] (minZ + (s + 0.5)*gridSizeZ2, :1297), so a
+    // covered sample at height zs counts in every slice from the first with o2z >= zs: one
+    // toggle bit there, expanded by a prefix XOR below.
+    const uint32_t chead = colhead[cord[ua] + cflag[ua] - 1u];
+    const uint32_t g0 = useg[chead], g1 = useg[ucol_end];
+    const int SW = 2 * n2x, SH = 2 * n2y;
+    const float lx = fa(fm((float)ci, g.g[0]), g.bmin[0]), hx = fa(lx, g.g[0]);
+    const float ly = fa(fm((float)cj, g.g[1]), g.bmin[1]), hy = fa(ly, g.g[1]);
+    const float *ozt = g.o2[2];
+    for (uint32_t b0 = g0; b0 < g1; b0 += 32) {
+      const uint32_t e = b0 + lane;
+      const uint32_t vv = e < g1 ? vals[e] : 0u;
+      uint32_t cnt = 0;
+      if (vv & 0x80000000u) {
+        const uint32_t t = vv & 0x7fffffffu;
+        const float4 a0 = __ldg(ptri + 3 * (size_t)t), a1 = __ldg(ptri + 3 * (size_t)t + 1),
+                     a2 = __ldg(ptri + 3 * (size_t)t + 2);
+        const float V[9] = {a0.x, a0.y, a0.z, a1.x, a1.y, a1.z, a2.x, a2.y, a2.z};
+        StTri st;
+        if (st_setup(V, lx, hx, ly, hy, SW, SH, st)) {
+#pragma unroll
+          for (int c = 0; c < 3; ++c) {
+            ws.v[lane][2 * c] = __int_as_float(st.X[c]);
+            ws.v[lane][2 * c + 1] = __int_as_float(st.Y[c]);
+            ws.v[lane][6 + c] = st.z[c];
+          }
+          ws.x[lane][0] = st.rA;
+          const int nsx = st.sx1 - st.sx0 + 1;
+          ws.rng[lane] = (uint32_t)st.sx0 | ((uint32_t)nsx << 7) | ((uint32_t)st.sy0 << 14);
+          cnt = (uint32_t)(nsx * (st.sy1 - st.sy0 + 1));
+        }
+      }
+      const uint32_t inc = warp_incl_scan(cnt);
+      ws.pre[lane] = inc - cnt;
+      const uint32_t tot = __shfl_sync(FULL, inc, 31);
+      __syncwarp();
+      for (uint32_t w = lane; w < tot; w += 32) {
+        const int tl = batch_search(ws.pre, w);
+        const uint32_t loc = w - ws.pre[tl];
+        const uint32_t rg = ws.rng[tl];
+        const uint32_t nsx = (rg >> 7) & 127u;
+        const uint32_t row = loc / nsx;
+        StTri st;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+          st.X[c] = __float_as_int(ws.v[tl][2 * c]);
+          st.Y[c] = __float_as_int(ws.v[tl][2 * c + 1]);
+          st.z[c] = ws.v[tl][6 + c];
+        }
+        st.rA = ws.x[tl][0];
+        const int sx = (int)(rg & 127u) + (int)(loc - row * nsx), sy = (int)((rg >> 14) & 127u) + (int)row;
+        float zs;
+        if (!st_cover(st, sx, sy, zs)) continue;
+        const int sbit = (sy * SW + sx) * n2z;
+        for (int jv = m - 1; jv >= 0; --jv) {
+          const int s0 = st_first_slice(ozt + (size_t)kz[jv] * n2z, n2z, zs);
+          if (s0 < n2z) {
+            const int b = sbit + s0;
+            atomicXor(&stg[jv * SWd + (b >> 5)], 1u << (b & 31));
+          }
+          // lower voxels clip lower still: none of their slices keeps this sample
+          if (s0 > 0 && g.oz_monotone) break;
+        }
+      }
+      __syncwarp();
+    }
+    // a cell is inside when at least 3 of its 4 samples are odd (ClassifyInOut2xLevel2,
+    // :1383-1401): parity per slice = prefix XOR of the sample column's toggles
+    const uint32_t zmask = n2z >= 32 ? 0xffffffffu : ((1u << n2z) - 1u);
+    for (int jv = 0; jv < m; ++jv) {
+      const uint32_t *sj = stg + jv * SWd;
+      for (int pq = lane; pq < ncol2; pq += 32) {
+        const int q = pq / n2x, p = pq - q * n2x;
+        uint32_t x[4];
+#pragma unroll
+        for (int a = 0; a < 4; ++a) {
+          uint32_t y = column_bits(sj, ((2 * q + (a >> 1)) * SW + 2 * p + (a & 1)) * n2z, n2z);
+          y ^= y << 1; y ^= y << 2; y ^= y << 4; y ^= y << 8; y ^= y << 16;
+          x[a] = y;
+        }
+        const uint32_t in = ((x[0] & x[1] & (x[2] | x[3])) | (x[2] & x[3] & (x[0] | x[1]))) & zmask;
+        if (in) or_column(par + jv * W, pq, n2z, in);
+      }
+    }
+    __syncwarp();
+  } else {
   // ---------------- fill: u/v once per (triangle, sub-column) for the whole chunk
   const uint32_t f0 = useg[ua], f1 = useg[ucol_end];
   const float *ozt = g.o2[2];
   const float oz_lo = __ldg(ozt + (size_t)kz[0] * n2z);
   const float oz_hi = __ldg(ozt + (size_t)kz[m - 1] * n2z + n2z - 1);
-  uint64_t nun = 0;
   for (uint32_t b0 = f0; b0 < f1; b0 += 32) {
     const uint32_t e = b0 + lane;
     const uint32_t vv = e < f1 ? vals[e] : 0u;
@@ -543,6 +654,8 @@ __global__ void __launch_bounds__(kWarps * 32, 6) k_level2c(
     __syncwarp();
   }
 
+  }
+
   // ---------------- output, top voxel first so the full-hit toggles accumulate downwards.
   // One lane per sub-column: its n2z SAT and parity bits are read once and written as n2z
   // bytes at stride n2x*n2y (consecutive lanes write consecutive bytes of each z layer).
@@ -595,12 +708,12 @@ int level2_chunk(const GridDev &g, int cap) {
 }
 
 // Shared-memory words one warp needs for a mesh with this grid.
-int level2_warp_words(const GridDev &g, int cap) {
+int level2_warp_words(const GridDev &g, int cap, bool stencil) {
   const int cells = g.n2[0] * g.n2[1] * g.n2[2];
   const int W = (cells + 31) >> 5;
   const int FW = (g.n2[0] * g.n2[1] + 31) >> 5;
   const int CH = level2_chunk(g, cap);
-  return 2 * CH * W + CH * FW + CH + FW + (int)(sizeof(WarpScratch) / 4);
+  return 2 * CH * W + CH * FW + CH + FW + (int)(sizeof(WarpScratch) / 4) + (stencil ? 4 * CH * W : 0);
 }
 
 size_t level2_smem_bytes(int warp_words) { return (size_t)warp_words * 4 * kWarps; }
@@ -628,13 +741,15 @@ void launch_level2(const BatchDev &bd, const uint32_t *keys, const uint32_t *val
   k_itemstarts<<<nb, 256, 0, s>>>(iflag, iord, B, istart, nitems);
   count_launch(4);
   const size_t smem = level2_smem_bytes(warp_words);
-  static bool attr_set = false;
-  if (!attr_set) {
-    cudaFuncSetAttribute(k_level2c, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-    attr_set = true;
+  const bool st = bd.fill == GPV_FILL_STENCIL;
+  auto kern = st ? k_level2c<true> : k_level2c<false>;
+  static bool attr_set[2] = {false, false};
+  if (!attr_set[st]) {
+    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    attr_set[st] = true;
   }
   int per_sm = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_level2c, kWarps * 32, smem);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kWarps * 32, smem);
   per_sm = std::max(per_sm, 1);
   const int64_t grid = std::min<int64_t>((B + kWarps - 1) / kWarps, (int64_t)num_sms * per_sm);
   const int nz = slab_nz;
@@ -659,9 +774,9 @@ void launch_level2(const BatchDev &bd, const uint32_t *keys, const uint32_t *val
   }
   for (int sl = 0; sl < launches; ++sl) {
     cudaStream_t ls = two ? aux->st[sl & 1] : s;
-    k_level2c<<<(unsigned)grid, kWarps * 32, smem, ls>>>(bd, keys, vals, useg, cflag, cord, colhead,
-                                                         istart, nitems, warp_words, sl, zslab,
-                                                         zslab > 0 ? ilist : nullptr, ioff);
+    kern<<<(unsigned)grid, kWarps * 32, smem, ls>>>(bd, keys, vals, useg, cflag, cord, colhead, istart,
+                                                    nitems, warp_words, sl, zslab,
+                                                    zslab > 0 ? ilist : nullptr, ioff);
     count_launch();
     if (after_slab) after_slab(sl, ls);
   }

@@ -136,6 +136,26 @@ int gpv_set_normals(gpv_ctx *ctx, int mode);
 int gpv_set_hierarchy(gpv_ctx *ctx, int on);
 int gpv_result_copy_hierarchy_to_host(gpv_ctx *ctx, const gpv_result *res, gpv_box *out,
                                       cudaStream_t stream);
+/* Inside fill of both levels (default GPV_FILL_RAY):
+ *   GPV_FILL_RAY      +z ray parity from each voxel centre / Level2 ray origin, the CPU path
+ *                     ClassifyInOutCPU + ClassifyInOutLevel2CPU (src/Object.cpp:716-779,
+ *                     :1111-1207), bit for bit.
+ *   GPV_FILL_STENCIL  the rasterised stencil-parity fill ClassifyInOut2x + ClassifyInOut2xLevel2
+ *                     (src/Object.cpp:1446-1649, :1210-1444), which the reference runs through
+ *                     OpenGL, as CUDA kernels: per z slice, 2x2 samples per voxel (pixel centres
+ *                     of an orthographic viewport over the bounding box, or over the Level1
+ *                     voxel's x/y extent for Level2), each counting the triangles that cover it
+ *                     with their surface at or below the slice's clip plane; a voxel is inside
+ *                     when at least 3 of its 4 counts are odd.  Level1 draws every triangle,
+ *                     Level2 the triangles recorded in the voxel's Level1 column.  Coverage uses
+ *                     vertices snapped to 1/256 pixel, exact integer edge functions and a
+ *                     top-left tie rule; the surface height is interpolated in float.  A GPU
+ *                     rasteriser's own sub-pixel and clipping arithmetic can differ, so bit
+ *                     equality holds against this restatement, not against a GL driver.
+ * The work counts ray1 and ray2 are 0 with the stencil fill. */
+#define GPV_FILL_RAY 0
+#define GPV_FILL_STENCIL 1
+int gpv_set_fill(gpv_ctx *ctx, int mode);
 /* Record the Level1 and Level2 launch sequences of each voxelization as CUDA graphs (default on;
  * the executable graphs are cached in the context and updated in place). */
 int gpv_set_graphs(gpv_ctx *ctx, int on);

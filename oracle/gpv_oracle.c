@@ -30,6 +30,12 @@
  *                       if the column centre lies inside the triangle's x/y bounding box grown by
  *                       a generous margin (or always, for triangles whose x/y projection is
  *                       ill-conditioned).  Checked equal to ORC_FILL_COLUMN by the tests.
+ *   ORC_FILL_STENCIL -- both levels filled by the rasterised stencil parity of ClassifyInOut2x
+ *                       (src/Object.cpp:1446-1649) and ClassifyInOut2xLevel2 (:1210-1444), which
+ *                       the reference runs through OpenGL.  No graphics stack exists here, so the
+ *                       rasterisation is restated (orc_st_* below) and parity for this mode is
+ *                       unpinned: it is pinned to the restatement, and the tests check the
+ *                       restatement against a literal slice-by-slice form of the two functions.
  */
 #include <math.h>
 #include <stdint.h>
@@ -52,6 +58,7 @@ int ref_tri_ray(const float *V1, const float *V2, const float *V3, const float *
 #define ORC_FILL_VOXEL 0
 #define ORC_FILL_COLUMN 1
 #define ORC_FILL_CAND 2
+#define ORC_FILL_STENCIL 3
 
 /* ------------------------------------------------------------------------------------------ */
 /* Predicates                                                                                  */
@@ -398,7 +405,134 @@ typedef struct {
     int32_t *vtris;      /* triangle ids in objTriangleID order within each voxel */
     int64_t sat1_tests;  /* sum over triangles of the candidate box size */
     int64_t ray1_cand;   /* (column,triangle) pairs in the triangles' exact x/y boxes, times nz */
+    int fill;            /* ORC_FILL_* */
 } orc_run;
+
+/* ---- Stencil fill --------------------------------------------------------------------------
+ * One rendering of the reference draws triangles into an orthographic viewport of W x H pixels
+ * over [lx, hx] x [ly, hy] with the clip plane (0, 0, -1, c) (keeps z <= c), GL_INCR on the
+ * stencil of every fragment.  Restated: window coordinates ((v - lo) / (hi - lo)) * W in float,
+ * snapped to 1/256 pixel (clamped to +-2^21 pixels); a pixel centre (s + 1/2) is covered when
+ * the three integer edge functions of the counter-clockwise snapped triangle are positive, or
+ * zero on a left edge (dy < 0) or a bottom edge (dy == 0, dx > 0); the height there is
+ * sum_i (w_i * (1/A)) * z_i in float; the fragment survives the clip when height <= c. */
+static int orc_first_ge(const float *tab, int n, float x);
+
+typedef struct {
+    int32_t X[3], Y[3];
+    float z[3];
+    float rA;
+    int sx0, sx1, sy0, sy1;
+} orc_sttri;
+
+static int32_t orc_st_snap(float v, float lo, float hi, int npx)
+{
+    float w = ((v - lo) / (hi - lo)) * (float)npx;
+    if (!(w > -2097152.0f)) w = -2097152.0f;
+    else if (w > 2097152.0f) w = 2097152.0f;
+    return (int32_t)llrintf(w * 256.0f);
+}
+
+static int32_t orc_floor256(int32_t x) { return x >= 0 ? x / 256 : -((-x + 255) / 256); }
+
+static int orc_st_setup(const float *tv, float lx, float hx, float ly, float hy, int W, int H,
+                        orc_sttri *t)
+{
+    for (int i = 0; i < 3; ++i) {
+        t->X[i] = orc_st_snap(tv[3 * i], lx, hx, W);
+        t->Y[i] = orc_st_snap(tv[3 * i + 1], ly, hy, H);
+        t->z[i] = tv[3 * i + 2];
+    }
+    int64_t A = (int64_t)(t->X[1] - t->X[0]) * (t->Y[2] - t->Y[0]) -
+                (int64_t)(t->Y[1] - t->Y[0]) * (t->X[2] - t->X[0]);
+    if (A == 0) return 0; /* zero area: no fragments */
+    if (A < 0) {
+        int32_t a = t->X[1]; t->X[1] = t->X[2]; t->X[2] = a;
+        a = t->Y[1]; t->Y[1] = t->Y[2]; t->Y[2] = a;
+        float f = t->z[1]; t->z[1] = t->z[2]; t->z[2] = f;
+        A = -A;
+    }
+    t->rA = 1.0f / (float)A;
+    int32_t xmn = t->X[0], xmx = t->X[0], ymn = t->Y[0], ymx = t->Y[0];
+    for (int i = 1; i < 3; ++i) {
+        if (t->X[i] < xmn) xmn = t->X[i];
+        if (t->X[i] > xmx) xmx = t->X[i];
+        if (t->Y[i] < ymn) ymn = t->Y[i];
+        if (t->Y[i] > ymx) ymx = t->Y[i];
+    }
+    t->sx0 = -orc_floor256(128 - xmn);
+    t->sx1 = orc_floor256(xmx - 128);
+    t->sy0 = -orc_floor256(128 - ymn);
+    t->sy1 = orc_floor256(ymx - 128);
+    if (t->sx0 < 0) t->sx0 = 0;
+    if (t->sy0 < 0) t->sy0 = 0;
+    if (t->sx1 > W - 1) t->sx1 = W - 1;
+    if (t->sy1 > H - 1) t->sy1 = H - 1;
+    return t->sx0 <= t->sx1 && t->sy0 <= t->sy1;
+}
+
+static int orc_st_edge(int64_t w, int32_t dx, int32_t dy)
+{
+    return w > 0 || (w == 0 && (dy < 0 || (dy == 0 && dx > 0)));
+}
+
+static int orc_st_cover(const orc_sttri *t, int sx, int sy, float *zs)
+{
+    int64_t px = (int64_t)sx * 256 + 128, py = (int64_t)sy * 256 + 128;
+    int64_t w[3];
+    for (int e = 0; e < 3; ++e) {
+        int a = (e + 1) % 3, b = (e + 2) % 3; /* edge opposite vertex e, counter-clockwise */
+        int32_t dx = t->X[b] - t->X[a], dy = t->Y[b] - t->Y[a];
+        w[e] = (int64_t)dx * (py - t->Y[a]) - (int64_t)dy * (px - t->X[a]);
+        if (!orc_st_edge(w[e], dx, dy)) return 0;
+    }
+    *zs = ((float)w[0] * t->rA) * t->z[0] + ((float)w[1] * t->rA) * t->z[1];
+    *zs = *zs + ((float)w[2] * t->rA) * t->z[2];
+    return 1;
+}
+
+static int orc_tri_finite(const float *tv)
+{
+    for (int k = 0; k < 9; ++k)
+        if (!isfinite(tv[k])) return 0;
+    return 1;
+}
+
+/* ClassifyInOut2x: per slice k the stencil counts of the 2nx x 2ny samples over the bounding
+ * box, clip height (k + 0.5)*gridSizeZ + bBoxMin[2] (double, stored as float); a voxel is inside
+ * when more than 2 of its 4 counts are odd.  A fragment at height zs counts in slices k >= k0
+ * (the first clip height >= zs), so the counts are accumulated per (sample, slice) parity. */
+static void orc_fill_stencil1(orc_run *r)
+{
+    const int nx = r->s.n[0], ny = r->s.n[1], nz = r->s.n[2];
+    const int W = 2 * nx, H = 2 * ny;
+    float *clip = (float *)malloc(sizeof(float) * (size_t)nz);
+    for (int k = 0; k < nz; ++k) clip[k] = (float)((k + 0.5) * (double)r->t.g[2] + (double)r->s.bmin[2]);
+    uint8_t *par = (uint8_t *)calloc((size_t)W * H * nz, 1);
+    for (int64_t t = 0; t < r->T; ++t) {
+        const float *tv = r->tris + 9 * t;
+        orc_sttri st;
+        if (!orc_tri_finite(tv)) continue;
+        if (!orc_st_setup(tv, r->s.bmin[0], r->s.bmax[0], r->s.bmin[1], r->s.bmax[1], W, H, &st)) continue;
+        for (int sy = st.sy0; sy <= st.sy1; ++sy)
+            for (int sx = st.sx0; sx <= st.sx1; ++sx) {
+                float zs;
+                if (!orc_st_cover(&st, sx, sy, &zs)) continue;
+                uint8_t *c = par + ((size_t)sy * W + sx) * nz;
+                for (int k = orc_first_ge(clip, nz, zs); k < nz; ++k) c[k] ^= 1;
+            }
+    }
+    for (int k = 0; k < nz; ++k)
+        for (int j = 0; j < ny; ++j)
+            for (int i = 0; i < nx; ++i) {
+                int cnt = 0;
+                for (int l = 0; l < 2; ++l)
+                    for (int m = 0; m < 2; ++m) cnt += par[((size_t)(2 * j + l) * W + 2 * i + m) * nz + k];
+                r->state1[((int64_t)k * ny + j) * nx + i] = cnt > 2 ? 1 : 0;
+            }
+    free(par);
+    free(clip);
+}
 
 static int orc_threads(int req)
 {
@@ -635,7 +769,9 @@ orc_run *orc_create(const float *tris, int64_t T, const orc_spec *s, int fill_mo
     orc_tables_build(s, &r->t);
     r->N1 = (int64_t)s->n[0] * s->n[1] * s->n[2];
     r->state1 = (uint8_t *)calloc((size_t)r->N1, 1);
-    orc_fill_level1(r, fill_mode, nth);
+    r->fill = fill_mode;
+    if (fill_mode == ORC_FILL_STENCIL) orc_fill_stencil1(r);
+    else orc_fill_level1(r, fill_mode, nth);
     r->parity = (uint8_t *)malloc((size_t)r->N1);
     memcpy(r->parity, r->state1, (size_t)r->N1);
     orc_sat_level1(r, nth);
@@ -668,7 +804,7 @@ orc_run *orc_create(const float *tris, int64_t T, const orc_spec *s, int fill_mo
         }
         rc += (int64_t)cnt[0] * cnt[1];
     }
-    r->ray1_cand = rc * s->n[2];
+    r->ray1_cand = fill_mode == ORC_FILL_STENCIL ? 0 : rc * s->n[2];
     return r;
 }
 
@@ -696,6 +832,51 @@ int64_t orc_voxel_tris(const orc_run *r, int64_t v, int32_t *out, int64_t cap)
     int64_t n = r->vstart[v + 1] - r->vstart[v];
     for (int64_t e = 0; e < n && e < cap; ++e) out[e] = r->vtris[r->vstart[v] + e];
     return n;
+}
+
+/* ClassifyInOut2xLevel2 for the boundary voxel (i, j, k): 2 n2x x 2 n2y samples over the voxel's
+ * x/y extent (minX = i*gridSizeX + bBoxMin[0] in float, maxX = minX + gridSizeX, :1241-1266),
+ * slice s clipped at minZ + (s + 0.5)*gridSizeZ2 (double, stored as float: the Level2 ray-origin
+ * heights), drawing the triangles recorded in the Level1 column (i, j) -- the strip display list
+ * of CreateVoxelStripDisplayLists (:605-633), each triangle once.  blk receives 1 for inside. */
+static void orc_fill_stencil2(const orc_run *r, int i, int j, int k, uint8_t *blk)
+{
+    const int nx = r->s.n[0], ny = r->s.n[1], nz = r->s.n[2];
+    const int n2x = r->s.n2[0], n2y = r->s.n2[1], n2z = r->s.n2[2];
+    const int W = 2 * n2x, H = 2 * n2y;
+    const float lx = i * r->t.g[0] + r->s.bmin[0], hx = lx + r->t.g[0];
+    const float ly = j * r->t.g[1] + r->s.bmin[1], hy = ly + r->t.g[1];
+    const float *clip = r->t.o2[2] + (size_t)k * n2z;
+    uint8_t *par = (uint8_t *)calloc((size_t)W * H * n2z, 1);
+    uint8_t *seen = (uint8_t *)calloc((size_t)r->T + 1, 1);
+    const int64_t ij = (int64_t)j * nx + i;
+    for (int z = 0; z < nz; ++z) {
+        const int64_t w = (int64_t)z * nx * ny + ij;
+        for (int64_t e = r->vstart[w]; e < r->vstart[w + 1]; ++e) {
+            const int32_t t = r->vtris[e];
+            if (seen[t]) continue;
+            seen[t] = 1;
+            orc_sttri st;
+            if (!orc_st_setup(r->tris + 9 * (int64_t)t, lx, hx, ly, hy, W, H, &st)) continue;
+            for (int sy = st.sy0; sy <= st.sy1; ++sy)
+                for (int sx = st.sx0; sx <= st.sx1; ++sx) {
+                    float zs;
+                    if (!orc_st_cover(&st, sx, sy, &zs)) continue;
+                    uint8_t *c = par + ((size_t)sy * W + sx) * n2z;
+                    for (int s2 = orc_first_ge(clip, n2z, zs); s2 < n2z; ++s2) c[s2] ^= 1;
+                }
+        }
+    }
+    for (int s2 = 0; s2 < n2z; ++s2)
+        for (int q = 0; q < n2y; ++q)
+            for (int p = 0; p < n2x; ++p) {
+                int cnt = 0;
+                for (int l = 0; l < 2; ++l)
+                    for (int m = 0; m < 2; ++m) cnt += par[((size_t)(2 * q + l) * W + 2 * p + m) * n2z + s2];
+                if (cnt > 2) blk[((int64_t)s2 * n2y + q) * n2x + p] = 1;
+            }
+    free(seen);
+    free(par);
 }
 
 /* Level2 of boundary voxels [b0, b1): ClassifyInOutLevel2CPU then ClassifyTessellationLevel2.
@@ -739,6 +920,10 @@ void orc_level2(const orc_run *r, int64_t b0, int64_t b1, uint8_t *out, int nthr
                 }
             }
             for (int64_t e = 0; e < nu; ++e) mark[uni[e]] = 0;
+            if (r->fill == ORC_FILL_STENCIL) {
+                orc_fill_stencil2(r, i, j, k, blk);
+                goto level2_sat;
+            }
             r2 += nu * cells;
             const float *ox = r->t.o2[0] + (size_t)i * n2x;
             const float *oy = r->t.o2[1] + (size_t)j * n2y;
@@ -754,6 +939,7 @@ void orc_level2(const orc_run *r, int64_t b0, int64_t b1, uint8_t *out, int nthr
                     for (int rr = 0; rr < n2z; ++rr)
                         if (par[rr]) blk[((int64_t)rr * n2y + q) * n2x + p] = 1;
                 }
+        level2_sat:
             /* Level2 SAT over every sub-cell for every triangle of the voxel (:2374-2398). */
             const float *sx = r->t.c2s[0] + (size_t)i * n2x;
             const float *sy = r->t.c2s[1] + (size_t)j * n2y;

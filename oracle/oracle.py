@@ -10,7 +10,7 @@ import os
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-FILL_VOXEL, FILL_COLUMN, FILL_CAND = 0, 1, 2
+FILL_VOXEL, FILL_COLUMN, FILL_CAND, FILL_STENCIL = 0, 1, 2, 3
 
 
 class Spec(C.Structure):
