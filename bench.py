@@ -409,6 +409,49 @@ def roofline(name, per_call, work, stats, spec, T, peaks, peak_kind, clk):
     return out
 
 
+def stencil_bench(gpv, ctx, torch, stream, step_device, flush, args, tris, spec, cpu):
+    """The same workload with the rasterised stencil fill (GPV_FILL_STENCIL) instead of the ray
+    fill: device time per step and per stage, and (cpu) the oracle's restatement on the host."""
+    ctx.set_fill(gpv.FILL_STENCIL)
+    try:
+        with torch.cuda.stream(stream):
+            for _ in range(args.warmup):
+                ctx.release(step_device())
+        torch.cuda.synchronize()
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+              for _ in range(args.steps)]
+        ctx.set_timing(True)
+        torch.cuda.synchronize()
+        with torch.cuda.stream(stream):
+            for k in range(args.steps):
+                flush.zero_()
+                ev[k][0].record(stream)
+                r = step_device()
+                ev[k][1].record(stream)
+                if k == 0:
+                    counts = dict(l1_inside=r.num_level1_inside, l2_inside=r.num_level2_inside,
+                                  l2_boundary=r.num_level2_boundary)
+                ctx.release(r)
+        torch.cuda.synchronize()
+        calls, stage_ms = ctx.stage_times()
+        ctx.set_timing(False)
+    finally:
+        ctx.set_fill(gpv.FILL_RAY)
+    ms = sum(a.elapsed_time(b) for a, b in ev) / args.steps
+    out = {"fill": "stencil (ClassifyInOut2x + ClassifyInOut2xLevel2 as CUDA kernels)",
+           "ms_per_step": ms, "meshes_per_s": 1e3 / ms,
+           "stage_ms_per_step": {k: v / max(calls, 1) for k, v in stage_ms.items()}, **counts}
+    if cpu:
+        from oracle import oracle as orc
+
+        t0 = time.perf_counter()
+        run = orc.Run(tris, spec, fill=orc.FILL_STENCIL, threads=os.cpu_count() or 1)
+        run.level2_state(threads=os.cpu_count() or 1)
+        out["cpu_oracle_s_per_mesh"] = time.perf_counter() - t0
+        out["cpu_oracle_cores"] = os.cpu_count() or 1
+    return out
+
+
 def progress(msg):
     """Section markers on stderr (the JSON line goes to stdout at the end)."""
     print(f"[bench] {msg}", file=sys.stderr, flush=True)
@@ -551,6 +594,9 @@ def main():
             "host_ms_per_call": {k: v / max(hcalls, 1) for k, v in host_ms.items()}}
     tuned = (128, 8)
     progress("plain path done")
+    progress("stencil fill section")
+    line["stencil_fill"] = stencil_bench(gpv, ctx, torch, stream, step_device, flush, args, tris,
+                                         spec, rank == 0 and not args.no_cpu_baseline)
     if args.batch > 0:
         progress("batched section")
         line["batched"] = batch_bench(gpv, ctx, torch, stream, local, args)

@@ -408,10 +408,13 @@ __global__ void __launch_bounds__(kWarps * 32, 6) k_level2c(
                 if (fa0 > -2.f) ra = max(ra, (int)floorf(fminf(fa0, (float)n2z + 2.f)));
                 if (fb0 < (float)n2z + 2.f) rb = min(rb, (int)ceilf(fmaxf(fb0, -2.f)));
               }
-              for (int r = ra; r <= rb; ++r) {
-                if ((done >> r) & 1u) continue;
-                if (fabsf(fa(sxy, fm(nzs, fs(V[2], __ldg(sz + r))))) <= H) zm |= 1u << r;
-              }
+              // The slab value is monotone in cz (each operation on cz is a monotone rounding:
+              // V0z - cz, then times nz, then plus sxy), so the cells passing |value| <= H are
+              // one interval of [ra, rb]; its ends are found by testing inwards from both ends.
+              while (ra <= rb && !(fabsf(fa(sxy, fm(nzs, fs(V[2], __ldg(sz + ra))))) <= H)) ++ra;
+              while (rb > ra && !(fabsf(fa(sxy, fm(nzs, fs(V[2], __ldg(sz + rb))))) <= H)) --rb;
+              if (ra <= rb)
+                zm = ((rb - ra + 1 >= 32) ? 0xffffffffu : ((1u << (rb - ra + 1)) - 1u)) << ra & ~done;
               rec = (uint32_t)tl | ((uint32_t)p << 5) | ((uint32_t)q << 11);
             }
           }
