@@ -133,7 +133,8 @@ __device__ __forceinline__ int batch_search(const uint32_t *pre, uint32_t it) {
 
 struct WarpScratch {
   float v[32][9];     // triangle vertices of the current batch
-  float x[32][5];     // slab (SAT) or (1/det, well-conditioned flag) (fill); odd row stride: no bank conflicts
+  float x[32][7];     // SAT: slab normal, H, 1/(sub-columns per row), 1/nz, slab bound; fill: 1/det,
+                      // well-conditioned flag, 1/(sub-columns per row).  Odd row stride: no bank conflicts
   uint32_t rng[32];   // packed sub-cell ranges
   uint32_t pre[33];   // exclusive prefix of item counts
   int jm[32];         // SAT: the triangle's voxel in the chunk; fill: voxels of the chunk below
@@ -346,6 +347,10 @@ __global__ void __launch_bounds__(kWarps * 32, 6) k_level2c(
           for (int q = 0; q < 9; ++q) ws.v[lane][q] = V[q];
           ws.x[lane][0] = ps.nx; ws.x[lane][1] = ps.ny; ws.x[lane][2] = ps.nz; ws.x[lane][3] = ps.H;
           const int np = p1 - p0 + 1;
+          // per-triangle factors of the (triangle, sub-column) items below
+          ws.x[lane][4] = __frcp_rn((float)np);
+          ws.x[lane][5] = fabsf(ps.nz) > 0.f ? __frcp_rn(ps.nz) : 0.f;
+          ws.x[lane][6] = ps.H + 8.f * EPS24 * fabsf(ps.nz) * (fabsf(V[2]) + fabsf(sz0) + fabsf(sz1));
           ws.rng[lane] = (uint32_t)p0 | ((uint32_t)np << 6) | ((uint32_t)q0 << 12) |
                          ((uint32_t)r0 << 18) | ((uint32_t)r1 << 24);
           ws.jm[lane] = jv;
@@ -371,7 +376,7 @@ __global__ void __launch_bounds__(kWarps * 32, 6) k_level2c(
           const int np = (int)((rg >> 6) & 63u);
           // loc / np by a float reciprocal: exact here (loc < 1024, np <= 32, so the quotient of
           // loc + 1/2 stays at least 1/64 away from an integer, far above the rounding)
-          const int qq = __float2int_rz(((float)loc + 0.5f) * __frcp_rn((float)np));
+          const int qq = __float2int_rz(((float)loc + 0.5f) * ws.x[tl][4]);
           const int p = (int)(rg & 63u) + (int)loc - qq * np;
           const int q = (int)((rg >> 12) & 63u) + qq;
           const int r0 = (int)((rg >> 18) & 63u), r1 = (int)((rg >> 24) & 63u);
@@ -398,11 +403,10 @@ __global__ void __launch_bounds__(kWarps * 32, 6) k_level2c(
               // (a few ulps of its terms, over |nz|) and one cell, and the exact per-cell test
               // still runs.
               int ra = r0, rb = r1;
-              if (fabsf(nzs) > 0.f) {
-                const float rnz = __frcp_rn(nzs);
+              const float rnz = ws.x[tl][5];
+              if (rnz != 0.f) {
                 const float zc = V[2] + sxy * rnz;
-                const float ext = (H + 8.f * EPS24 * (fabsf(sxy) + fabsf(nzs) * (fabsf(V[2]) + fabsf(sz0) +
-                                                                                 fabsf(sz1)))) * fabsf(rnz);
+                const float ext = (ws.x[tl][6] + 8.f * EPS24 * fabsf(sxy)) * fabsf(rnz);
                 const float igz = g.inv_g2[2];
                 const float fa0 = (zc - ext - sz0) * igz - 1.f, fb0 = (zc + ext - sz0) * igz + 1.f;
                 if (fa0 > -2.f) ra = max(ra, (int)floorf(fminf(fa0, (float)n2z + 2.f)));
@@ -583,6 +587,7 @@ __global__ void __launch_bounds__(kWarps * 32, 6) k_level2c(
           // an unbounded box marks an ill-conditioned x/y projection: no certification there
           ws.x[lane][1] = (isinf(fb.x) || isinf(fb.z)) ? 0.f : 1.f;
           const int np = p1 - p0 + 1;
+          ws.x[lane][2] = __frcp_rn((float)np);
           ws.rng[lane] = (uint32_t)p0 | ((uint32_t)np << 6) | ((uint32_t)q0 << 12);
           ws.jm[lane] = jm;
           cnt = (uint32_t)(np * (q1 - q0 + 1));
@@ -598,7 +603,7 @@ __global__ void __launch_bounds__(kWarps * 32, 6) k_level2c(
       const uint32_t loc = w - ws.pre[tl];
       const uint32_t rg = ws.rng[tl];
       const int np = (int)((rg >> 6) & 63u);
-      const int qq = __float2int_rz(((float)loc + 0.5f) * __frcp_rn((float)np));
+      const int qq = __float2int_rz(((float)loc + 0.5f) * ws.x[tl][2]);
       const int p = (int)(rg & 63u) + (int)loc - qq * np;
       const int q = (int)((rg >> 12) & 63u) + qq;
       float V[9];
