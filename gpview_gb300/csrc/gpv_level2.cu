@@ -121,6 +121,21 @@ __device__ __forceinline__ int tab_last_le(const float *tab, int n, float x, flo
   return i;
 }
 
+// Number of origins r in [0, n) with otop - oz[r] > dthr (float subtraction), for an increasing
+// table oz of spacing ~1/inv: the count is a prefix length because otop - oz[r] rounds
+// monotonically; an arithmetic estimate is corrected by table comparisons.
+__device__ __forceinline__ int count_drop_above(const float *oz, int n, float otop, float dthr,
+                                                float inv) {
+  const float f = (otop - dthr - __ldg(oz)) * inv;
+  int i;
+  if (!(f > 0.f)) i = 0;
+  else if (f >= (float)n) i = n;
+  else i = (int)ceilf(f);
+  while (i > 0 && !(otop - __ldg(oz + i - 1) > dthr)) --i;
+  while (i < n && otop - __ldg(oz + i) > dthr) ++i;
+  return i;
+}
+
 // last index tl in [0,31] with pre[tl] <= it (pre nondecreasing, pre[0] = 0)
 __device__ __forceinline__ int batch_search(const uint32_t *pre, uint32_t it) {
   int lo = 0, hi = 31;
@@ -580,12 +595,30 @@ __global__ void __launch_bounds__(kWarps * 32, 6) k_level2c(
         if (p0 <= p1 && q0 <= q1) {
           const float4 a0 = __ldg(ptri + 3 * (size_t)t), a1 = __ldg(ptri + 3 * (size_t)t + 1),
                        a2 = __ldg(ptri + 3 * (size_t)t + 2);
-          ws.v[lane][0] = a0.x; ws.v[lane][1] = a0.y; ws.v[lane][2] = a0.z;
-          ws.v[lane][3] = a1.x; ws.v[lane][4] = a1.y; ws.v[lane][5] = a1.z;
-          ws.v[lane][6] = a2.x; ws.v[lane][7] = a2.y; ws.v[lane][8] = a2.z;
-          ws.x[lane][0] = a2.w;  // 1/det
-          // an unbounded box marks an ill-conditioned x/y projection: no certification there
-          ws.x[lane][1] = (isinf(fb.x) || isinf(fb.z)) ? 0.f : 1.f;
+          const float V[9] = {a0.x, a0.y, a0.z, a1.x, a1.y, a1.z, a2.x, a2.y, a2.z};
+          RayTri rt;
+          ray_tri_pre(V, a2.w, rt);
+          ws.v[lane][0] = rt.v1x; ws.v[lane][1] = rt.v1y; ws.v[lane][2] = rt.v1z;
+          ws.v[lane][3] = rt.e1x; ws.v[lane][4] = rt.e1y; ws.v[lane][5] = rt.e1z;
+          ws.v[lane][6] = rt.e2x; ws.v[lane][7] = rt.e2y; ws.v[lane][8] = rt.e2z;
+          ws.x[lane][0] = rt.inv_det;
+          // Certification bound E2 (below), or 0 where there is none: an unbounded box marks an
+          // ill-conditioned x/y projection.  |t - t*| <= 8.2 eps M1 |1/det| for every origin of
+          // the chunk (t* exact, affine and decreasing in the origin height), with M1 taken at
+          // the largest |Tx|, |Ty| over the triangle's sub-columns (Tx = ox - v1x rounds
+          // monotonically in ox, so the extremes sit at the range ends) and the largest |Tz|
+          // over the chunk's origins; 16 eps gives the float evaluation room.
+          float E2 = 0.f;
+          if (g.oz_monotone && !isinf(fb.x) && !isinf(fb.z)) {
+            const float Zm = fmaxf(fabsf(oz_lo - rt.v1z), fabsf(oz_hi - rt.v1z)) * 1.0001f;
+            const float atx = fmaxf(fabsf(fs(__ldg(ox + p0), rt.v1x)), fabsf(fs(__ldg(ox + p1), rt.v1x)));
+            const float aty = fmaxf(fabsf(fs(__ldg(oy + q0), rt.v1y)), fabsf(fs(__ldg(oy + q1), rt.v1y)));
+            const float M1 = fabsf(rt.e2x) * (aty * fabsf(rt.e1z) + Zm * fabsf(rt.e1y)) +
+                             fabsf(rt.e2y) * (Zm * fabsf(rt.e1x) + atx * fabsf(rt.e1z)) +
+                             fabsf(rt.e2z) * (atx * fabsf(rt.e1y) + aty * fabsf(rt.e1x));
+            E2 = 2.f * 16.f * EPS24 * M1 * fabsf(rt.inv_det) * 1.0001f;
+          }
+          ws.x[lane][1] = E2;
           const int np = p1 - p0 + 1;
           ws.x[lane][2] = __frcp_rn((float)np);
           ws.rng[lane] = (uint32_t)p0 | ((uint32_t)np << 6) | ((uint32_t)q0 << 12);
@@ -606,26 +639,17 @@ __global__ void __launch_bounds__(kWarps * 32, 6) k_level2c(
       const int qq = __float2int_rz(((float)loc + 0.5f) * ws.x[tl][2]);
       const int p = (int)(rg & 63u) + (int)loc - qq * np;
       const int q = (int)((rg >> 12) & 63u) + qq;
-      float V[9];
-#pragma unroll
-      for (int qq = 0; qq < 9; ++qq) V[qq] = ws.v[tl][qq];
       RayTri rt;
-      ray_tri_pre(V, ws.x[tl][0], rt);
+      rt.v1x = ws.v[tl][0]; rt.v1y = ws.v[tl][1]; rt.v1z = ws.v[tl][2];
+      rt.e1x = ws.v[tl][3]; rt.e1y = ws.v[tl][4]; rt.e1z = ws.v[tl][5];
+      rt.e2x = ws.v[tl][6]; rt.e2y = ws.v[tl][7]; rt.e2z = ws.v[tl][8];
+      rt.inv_det = ws.x[tl][0];
+      rt.ok = true;
       RayCol rc;
       if (!ray_col(rt, __ldg(ox + p), __ldg(oy + q), rc)) continue;
       const int pq = q * n2x + p;
-      const bool well = g.oz_monotone && ws.x[tl][1] != 0.f;
-      float E2 = 0.f;
-      if (well) {
-        // |t - t*| <= 8.2 eps M1 |1/det| for every origin with |Tz| <= Zm (t* exact, affine and
-        // decreasing in the origin height); 16 eps gives the float evaluation room.
-        const float Zm = fmaxf(fabsf(oz_lo - rt.v1z), fabsf(oz_hi - rt.v1z)) * 1.0001f;
-        const float atx = fabsf(rc.Tx), aty = fabsf(rc.Ty);
-        const float M1 = fabsf(rt.e2x) * (aty * fabsf(rt.e1z) + Zm * fabsf(rt.e1y)) +
-                         fabsf(rt.e2y) * (Zm * fabsf(rt.e1x) + atx * fabsf(rt.e1z)) +
-                         fabsf(rt.e2z) * (atx * fabsf(rt.e1y) + aty * fabsf(rt.e1x));
-        E2 = 2.f * 16.f * EPS24 * M1 * fabsf(rt.inv_det) * 1.0001f;
-      }
+      const float E2 = ws.x[tl][1];
+      const bool well = E2 > 0.f;
       for (int jv = ws.jm[tl] - 1; jv >= 0; --jv) {
         const float *oz = ozt + (size_t)kz[jv] * n2z;
         uint32_t bits = 0;
@@ -647,11 +671,13 @@ __global__ void __launch_bounds__(kWarps * 32, 6) k_level2c(
           const float K = fabsf(ttop) + dmax + g.thr;
           const float slack = E2 * 1.0001f + 8.f * EPS24 * K + 1e-30f;
           const float dhit = (g.thr - ttop) + slack, dmiss = (g.thr - ttop) - slack;
-          for (int r = 0; r < n2z; ++r) {
-            const float ozr = __ldg(oz + r);
-            const float d = otop - ozr;
-            if (d > dhit || (d > dmiss && ray_t(rt, rc, ozr, g.thr))) bits |= 1u << r;
-          }
+          // d = otop - oz rounds monotonically and falls as r grows, so the certain hits are the
+          // origins r < rh and the exact tests the band rh <= r < rm
+          const int rh = count_drop_above(oz, n2z, otop, dhit, g.inv_g2[2]);
+          const int rm = count_drop_above(oz, n2z, otop, dmiss, g.inv_g2[2]);
+          bits = rh >= 32 ? 0xffffffffu : ((1u << rh) - 1u);
+          for (int r = rh; r < rm; ++r)
+            if (ray_t(rt, rc, __ldg(oz + r), g.thr)) bits |= 1u << r;
         } else {
           for (int r = 0; r < n2z; ++r)
             if (ray_t(rt, rc, __ldg(oz + r), g.thr)) bits |= 1u << r;
