@@ -45,6 +45,7 @@ def parse():
     p.add_argument("--slabs", type=int, default=0,
                    help="z slabs of the e2e path's Level2 launch (0: by the Level2 output size)")
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-stencil", action="store_true", help="skip the stencil-fill section")
     p.add_argument("--cpu-seconds", type=float, default=15.0)
     p.add_argument("--batch", type=int, default=4096, help="meshes of the batched workload (0: skip)")
     p.add_argument("--batch-reps", type=int, default=3)
@@ -594,9 +595,10 @@ def main():
             "host_ms_per_call": {k: v / max(hcalls, 1) for k, v in host_ms.items()}}
     tuned = (128, 8)
     progress("plain path done")
-    progress("stencil fill section")
-    line["stencil_fill"] = stencil_bench(gpv, ctx, torch, stream, step_device, flush, args, tris,
-                                         spec, rank == 0 and not args.no_cpu_baseline)
+    if not args.no_stencil:
+        progress("stencil fill section")
+        line["stencil_fill"] = stencil_bench(gpv, ctx, torch, stream, step_device, flush, args,
+                                             tris, spec, rank == 0 and not args.no_cpu_baseline)
     if args.batch > 0:
         progress("batched section")
         line["batched"] = batch_bench(gpv, ctx, torch, stream, local, args)

@@ -157,6 +157,8 @@ struct WarpScratch {
   uint32_t zrec[32];  // SAT: (triangle slot, p, q) of a sub-column item
   uint32_t seg[33];   // SAT: first pair of each voxel of the chunk, and the end
   uint32_t zown[64];  // SAT: (record lane, cell) of each (triangle, cell) item of a window
+  uint32_t brec[64];  // SAT: queued (triangle slot, p, q) records of sub-columns passing the
+                      // z-invariant axes
 };
 
 // ---- item construction -----------------------------------------------------------------------
@@ -376,68 +378,55 @@ __global__ void __launch_bounds__(kWarps * 32, 6) k_level2c(
       ws.pre[lane] = inc - cnt;
       const uint32_t tot = __shfl_sync(FULL, inc, 31);
       __syncwarp();
-      // (triangle, sub-column) items, 32 at a time: z-invariant SAT part and the plane slab
-      // select the cells left for the full test; then those (triangle, cell) tests run 32 at a
-      // time so that the lanes stay busy whatever the per-column cell counts.  Each item lane
-      // lists its cells in a window of 64 slots (its lane and the cell's z), so a test lane
-      // reads its work from one slot.
-      for (uint32_t wb = 0; wb < tot; wb += 32) {
-        const uint32_t w = wb + lane;
+      // (triangle, sub-column) items, 32 at a time (B1): the z-invariant SAT part; the items that
+      // pass are queued as records.  Every 32 records (B2): the plane slab selects the cells left
+      // for the full test, so that those lanes all work; then the (triangle, cell) tests run 32
+      // at a time whatever the per-column cell counts.  Each record lane lists its cells in a
+      // window of 64 slots (its lane and the cell's z), so a test lane reads its work from one
+      // slot.
+      uint32_t nrec = 0;
+      auto run_records = [&](uint32_t nr) {
         uint32_t zm = 0, rec = 0;
-        if (w < tot) {
-          const int tl = batch_search(ws.pre, w);
-          const uint32_t loc = w - ws.pre[tl];
+        if (lane < nr) {
+          rec = ws.brec[lane];
+          const int tl = (int)(rec & 31u), p = (int)((rec >> 5) & 63u), q = (int)((rec >> 11) & 63u);
           const uint32_t rg = ws.rng[tl];
-          const int np = (int)((rg >> 6) & 63u);
-          // loc / np by a float reciprocal: exact here (loc < 1024, np <= 32, so the quotient of
-          // loc + 1/2 stays at least 1/64 away from an integer, far above the rounding)
-          const int qq = __float2int_rz(((float)loc + 0.5f) * ws.x[tl][4]);
-          const int p = (int)(rg & 63u) + (int)loc - qq * np;
-          const int q = (int)((rg >> 12) & 63u) + qq;
           const int r0 = (int)((rg >> 18) & 63u), r1 = (int)((rg >> 24) & 63u);
           const int jv = ws.jm[tl];
           const uint32_t *satj = sat + jv * W;
           const float *sz = g.c2s[2] + (size_t)kz[jv] * n2z;
-          const float sz0 = __ldg(sz), sz1 = __ldg(sz + n2z - 1);
+          const float sz0 = __ldg(sz);
           // cells of this column already marked by another triangle need no test (OR only)
           const int off = (q * n2x + p) * n2z, sh = off & 31;
           uint32_t done = satj[off >> 5] >> sh;
           if (sh + n2z > 32) done |= satj[(off >> 5) + 1] << (32 - sh);
-          const uint32_t rmask = ((r1 - r0 + 1) >= 32 ? 0xffffffffu : ((1u << (r1 - r0 + 1)) - 1u)) << r0;
-          if ((~done & rmask) != 0) {
-            float V[9];
-#pragma unroll
-            for (int c = 0; c < 9; ++c) V[c] = ws.v[tl][c];
-            const float cx = __ldg(sx + p), cy = __ldg(sy + q);
-            SatCol sc;
-            if (sat_col(V, cx, cy, g.e2, sc)) {
-              const float nxs = ws.x[tl][0], nys = ws.x[tl][1], nzs = ws.x[tl][2], H = ws.x[tl][3];
-              const float sxy = fa(fm(nxs, fs(V[0], cx)), fm(nys, fs(V[1], cy)));
-              // The per-cell slab test |sxy + nz (V0z - cz)| <= H can only pass for cz within
-              // H/|nz| of V0z + sxy/nz; the interval is widened by the float error of that test
-              // (a few ulps of its terms, over |nz|) and one cell, and the exact per-cell test
-              // still runs.
-              int ra = r0, rb = r1;
-              const float rnz = ws.x[tl][5];
-              if (rnz != 0.f) {
-                const float zc = V[2] + sxy * rnz;
-                const float ext = (ws.x[tl][6] + 8.f * EPS24 * fabsf(sxy)) * fabsf(rnz);
-                const float igz = g.inv_g2[2];
-                const float fa0 = (zc - ext - sz0) * igz - 1.f, fb0 = (zc + ext - sz0) * igz + 1.f;
-                if (fa0 > -2.f) ra = max(ra, (int)floorf(fminf(fa0, (float)n2z + 2.f)));
-                if (fb0 < (float)n2z + 2.f) rb = min(rb, (int)ceilf(fmaxf(fb0, -2.f)));
-              }
-              // The slab value is monotone in cz (each operation on cz is a monotone rounding:
-              // V0z - cz, then times nz, then plus sxy), so the cells passing |value| <= H are
-              // one interval of [ra, rb]; its ends are found by testing inwards from both ends.
-              while (ra <= rb && !(fabsf(fa(sxy, fm(nzs, fs(V[2], __ldg(sz + ra))))) <= H)) ++ra;
-              while (rb > ra && !(fabsf(fa(sxy, fm(nzs, fs(V[2], __ldg(sz + rb))))) <= H)) --rb;
-              if (ra <= rb)
-                zm = ((rb - ra + 1 >= 32) ? 0xffffffffu : ((1u << (rb - ra + 1)) - 1u)) << ra & ~done;
-              rec = (uint32_t)tl | ((uint32_t)p << 5) | ((uint32_t)q << 11);
-            }
+          const float V0 = ws.v[tl][0], V1 = ws.v[tl][1], V2 = ws.v[tl][2];
+          const float cx = __ldg(sx + p), cy = __ldg(sy + q);
+          const float nxs = ws.x[tl][0], nys = ws.x[tl][1], nzs = ws.x[tl][2], H = ws.x[tl][3];
+          const float sxy = fa(fm(nxs, fs(V0, cx)), fm(nys, fs(V1, cy)));
+          // The per-cell slab test |sxy + nz (V0z - cz)| <= H can only pass for cz within
+          // H/|nz| of V0z + sxy/nz; the interval is widened by the float error of that test
+          // (a few ulps of its terms, over |nz|) and one cell, and the exact per-cell test
+          // still runs.
+          int ra = r0, rb = r1;
+          const float rnz = ws.x[tl][5];
+          if (rnz != 0.f) {
+            const float zc = V2 + sxy * rnz;
+            const float ext = (ws.x[tl][6] + 8.f * EPS24 * fabsf(sxy)) * fabsf(rnz);
+            const float igz = g.inv_g2[2];
+            const float fa0 = (zc - ext - sz0) * igz - 1.f, fb0 = (zc + ext - sz0) * igz + 1.f;
+            if (fa0 > -2.f) ra = max(ra, (int)floorf(fminf(fa0, (float)n2z + 2.f)));
+            if (fb0 < (float)n2z + 2.f) rb = min(rb, (int)ceilf(fmaxf(fb0, -2.f)));
           }
+          // The slab value is monotone in cz (each operation on cz is a monotone rounding:
+          // V0z - cz, then times nz, then plus sxy), so the cells passing |value| <= H are
+          // one interval of [ra, rb]; its ends are found by testing inwards from both ends.
+          while (ra <= rb && !(fabsf(fa(sxy, fm(nzs, fs(V2, __ldg(sz + ra))))) <= H)) ++ra;
+          while (rb > ra && !(fabsf(fa(sxy, fm(nzs, fs(V2, __ldg(sz + rb))))) <= H)) --rb;
+          if (ra <= rb)
+            zm = ((rb - ra + 1 >= 32) ? 0xffffffffu : ((1u << (rb - ra + 1)) - 1u)) << ra & ~done;
         }
+        __syncwarp();  // records read: the queue may be refilled
         const uint32_t zc = (uint32_t)__popc(zm);
         const uint32_t zinc = warp_incl_scan(zc);
         ws.zrec[lane] = rec;
@@ -472,6 +461,54 @@ __global__ void __launch_bounds__(kWarps * 32, 6) k_level2c(
               atomicOr(&sat[jv * W + (bi >> 5)], 1u << (bi & 31));
             }
           }
+          __syncwarp();
+        }
+      };
+      // one call site for the record work (the last rounds only drain the queue)
+      for (uint32_t wb = 0; wb < tot || nrec > 0; wb += 32) {
+        const uint32_t w = wb + lane;
+        bool pass = false;
+        uint32_t rec = 0;
+        if (w < tot) {
+          const int tl = batch_search(ws.pre, w);
+          const uint32_t loc = w - ws.pre[tl];
+          const uint32_t rg = ws.rng[tl];
+          const int np = (int)((rg >> 6) & 63u);
+          // loc / np by a float reciprocal: exact here (loc < 1024, np <= 32, so the quotient of
+          // loc + 1/2 stays at least 1/64 away from an integer, far above the rounding)
+          const int qq = __float2int_rz(((float)loc + 0.5f) * ws.x[tl][4]);
+          const int p = (int)(rg & 63u) + (int)loc - qq * np;
+          const int q = (int)((rg >> 12) & 63u) + qq;
+          const int r0 = (int)((rg >> 18) & 63u), r1 = (int)((rg >> 24) & 63u);
+          const uint32_t *satj = sat + ws.jm[tl] * W;
+          // sub-columns whose cells are all marked already need no test (OR only)
+          const int off = (q * n2x + p) * n2z, sh = off & 31;
+          uint32_t done = satj[off >> 5] >> sh;
+          if (sh + n2z > 32) done |= satj[(off >> 5) + 1] << (32 - sh);
+          const uint32_t rmask = ((r1 - r0 + 1) >= 32 ? 0xffffffffu : ((1u << (r1 - r0 + 1)) - 1u)) << r0;
+          if ((~done & rmask) != 0) {
+            float V[9];
+#pragma unroll
+            for (int c = 0; c < 9; ++c) V[c] = ws.v[tl][c];
+            SatCol sc;
+            if (sat_col(V, __ldg(sx + p), __ldg(sy + q), g.e2, sc)) {
+              pass = true;
+              rec = (uint32_t)tl | ((uint32_t)p << 5) | ((uint32_t)q << 11);
+            }
+          }
+        }
+        const uint32_t bal = __ballot_sync(FULL, pass);
+        if (pass) ws.brec[nrec + __popc(bal & ((1u << lane) - 1u))] = rec;
+        nrec += (uint32_t)__popc(bal);
+        __syncwarp();
+        if (nrec >= 32 || (wb + 32 >= tot && nrec > 0)) {
+          const uint32_t nr = min(nrec, 32u);
+          run_records(nr);
+          // move the records beyond the first nr to the front
+          const uint32_t rest = (lane + nr < nrec) ? ws.brec[nr + lane] : 0u;
+          __syncwarp();
+          if (lane + nr < nrec) ws.brec[lane] = rest;
+          nrec -= nr;
           __syncwarp();
         }
       }
