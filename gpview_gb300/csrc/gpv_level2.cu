@@ -297,9 +297,12 @@ __global__ void __launch_bounds__(kWarps * 32, 6) k_level2c(
   int *kz = (int *)(ft + CH * FW);
   uint32_t *ftacc = (uint32_t *)(kz + CH);
   WarpScratch &ws = *reinterpret_cast<WarpScratch *>(ftacc + FW);
-  // stencil fill: per voxel, (2 n2x * 2 n2y) sample columns of n2z slice toggle bits
+  // stencil fill: per voxel, (2 n2x * 2 n2y) sample columns of n2z slice toggle bits; per voxel
+  // one bit per sample toggling every slice of that voxel and of the voxels above it
   uint32_t *stg = reinterpret_cast<uint32_t *>(&ws + 1);
   const int SWd = 4 * W;
+  const int FWS = (4 * ncol2 + 31) >> 5;
+  uint32_t *sft = stg + CH * SWd, *sftacc = sft + CH * FWS;
 
   const uint32_t ucol_end = colhead[cord[ua] + cflag[ua]];  // first voxel of the next column
   const int nx = g.n[0], ny = g.n[1], nz = g.n[2];
@@ -320,8 +323,11 @@ __global__ void __launch_bounds__(kWarps * 32, 6) k_level2c(
   // clear the masks of the chunk's m voxels only (the arrays are sized for CH voxels)
   for (int w = lane; w < m * W; w += 32) { sat[w] = 0; par[w] = 0; }
   for (int w = lane; w < m * FW; w += 32) ft[w] = 0;
-  if (ST)
+  if (ST) {
     for (int w = lane; w < m * SWd; w += 32) stg[w] = 0;
+    for (int w = lane; w < m * FWS; w += 32) sft[w] = 0;
+    for (int w = lane; w < FWS; w += 32) sftacc[w] = 0;
+  }
   const int ci = (int)(col % (uint32_t)nx), cj = (int)(col / (uint32_t)nx);
   if ((int)lane < m) kz[lane] = (int)(keys[useg[ua + lane]] - col * (uint32_t)nz);
   __syncwarp();
@@ -530,6 +536,8 @@ __global__ void __launch_bounds__(kWarps * 32, 6) k_level2c(
     const float lx = fa(fm((float)ci, g.g[0]), g.bmin[0]), hx = fa(lx, g.g[0]);
     const float ly = fa(fm((float)cj, g.g[1]), g.bmin[1]), hy = fa(ly, g.g[1]);
     const float *ozt = g.o2[2];
+    // with increasing clip heights, the chunk's highest one is its top voxel's last slice
+    const float top_clip = __ldg(ozt + (size_t)kz[m - 1] * n2z + n2z - 1);
     for (uint32_t b0 = g0; b0 < g1; b0 += 32) {
       const uint32_t e = b0 + lane;
       const uint32_t vv = e < g1 ? vals[e] : 0u;
@@ -539,8 +547,14 @@ __global__ void __launch_bounds__(kWarps * 32, 6) k_level2c(
         const float4 a0 = __ldg(ptri + 3 * (size_t)t), a1 = __ldg(ptri + 3 * (size_t)t + 1),
                      a2 = __ldg(ptri + 3 * (size_t)t + 2);
         const float V[9] = {a0.x, a0.y, a0.z, a1.x, a1.y, a1.z, a2.x, a2.y, a2.z};
+        // The interpolated height of a covered sample is a convex combination of the vertex
+        // heights up to 7 eps max|z| of rounding, so a triangle whose lowest vertex lies more
+        // than 16 eps max|z| above the chunk's highest clip height counts in none of its slices.
+        const float zmn = fminf(V[2], fminf(V[5], V[8]));
+        const float zmag = fmaxf(fabsf(V[2]), fmaxf(fabsf(V[5]), fabsf(V[8])));
+        const bool above = g.oz_monotone && zmn - 16.f * EPS24 * zmag > top_clip;
         StTri st;
-        if (st_setup(V, lx, hx, ly, hy, SW, SH, st)) {
+        if (!above && st_setup(V, lx, hx, ly, hy, SW, SH, st)) {
 #pragma unroll
           for (int c = 0; c < 3; ++c) {
             ws.v[lane][2 * c] = __int_as_float(st.X[c]);
@@ -574,15 +588,26 @@ __global__ void __launch_bounds__(kWarps * 32, 6) k_level2c(
         const int sx = (int)(rg & 127u) + (int)(loc - row * nsx), sy = (int)((rg >> 14) & 127u) + (int)row;
         float zs;
         if (!st_cover(st, sx, sy, zs)) continue;
-        const int sbit = (sy * SW + sx) * n2z;
-        for (int jv = m - 1; jv >= 0; --jv) {
-          const int s0 = st_first_slice(ozt + (size_t)kz[jv] * n2z, n2z, zs);
-          if (s0 < n2z) {
-            const int b = sbit + s0;
+        const int sidx = sy * SW + sx, sbit = sidx * n2z;
+        if (g.oz_monotone) {
+          // clip heights increase through the chunk: the lowest voxel whose top clip keeps zs
+          // gets its toggle at the first such slice, and every voxel above it keeps zs in all
+          // slices (one bit in its sample-toggle row, accumulated upwards)
+          int jv = 0;
+          while (jv < m && !(__ldg(ozt + (size_t)kz[jv] * n2z + n2z - 1) >= zs)) ++jv;
+          if (jv < m) {
+            const int b = sbit + st_first_slice(ozt + (size_t)kz[jv] * n2z, n2z, zs);
             atomicXor(&stg[jv * SWd + (b >> 5)], 1u << (b & 31));
+            if (jv + 1 < m) atomicXor(&sft[(jv + 1) * FWS + (sidx >> 5)], 1u << (sidx & 31));
           }
-          // lower voxels clip lower still: none of their slices keeps this sample
-          if (s0 > 0 && g.oz_monotone) break;
+        } else {
+          for (int jv = m - 1; jv >= 0; --jv) {
+            const int s0 = st_first_slice(ozt + (size_t)kz[jv] * n2z, n2z, zs);
+            if (s0 < n2z) {
+              const int b = sbit + s0;
+              atomicXor(&stg[jv * SWd + (b >> 5)], 1u << (b & 31));
+            }
+          }
         }
       }
       __syncwarp();
@@ -591,14 +616,19 @@ __global__ void __launch_bounds__(kWarps * 32, 6) k_level2c(
     // :1383-1401): parity per slice = prefix XOR of the sample column's toggles
     const uint32_t zmask = n2z >= 32 ? 0xffffffffu : ((1u << n2z) - 1u);
     for (int jv = 0; jv < m; ++jv) {
+      // samples toggled in every slice of this voxel: the XOR of the rows of it and below
+      for (int w = lane; w < FWS; w += 32) sftacc[w] ^= sft[jv * FWS + w];
+      __syncwarp();
       const uint32_t *sj = stg + jv * SWd;
       for (int pq = lane; pq < ncol2; pq += 32) {
         const int q = pq / n2x, p = pq - q * n2x;
         uint32_t x[4];
 #pragma unroll
         for (int a = 0; a < 4; ++a) {
-          uint32_t y = column_bits(sj, ((2 * q + (a >> 1)) * SW + 2 * p + (a & 1)) * n2z, n2z);
+          const int sidx = (2 * q + (a >> 1)) * SW + 2 * p + (a & 1);
+          uint32_t y = column_bits(sj, sidx * n2z, n2z);
           y ^= y << 1; y ^= y << 2; y ^= y << 4; y ^= y << 8; y ^= y << 16;
+          if ((sftacc[sidx >> 5] >> (sidx & 31)) & 1u) y = ~y;
           x[a] = y;
         }
         const uint32_t in = ((x[0] & x[1] & (x[2] | x[3])) | (x[2] & x[3] & (x[0] | x[1]))) & zmask;
@@ -784,7 +814,9 @@ int level2_warp_words(const GridDev &g, int cap, bool stencil) {
   const int W = (cells + 31) >> 5;
   const int FW = (g.n2[0] * g.n2[1] + 31) >> 5;
   const int CH = level2_chunk(g, cap);
-  return 2 * CH * W + CH * FW + CH + FW + (int)(sizeof(WarpScratch) / 4) + (stencil ? 4 * CH * W : 0);
+  const int FWS = (4 * g.n2[0] * g.n2[1] + 31) >> 5;
+  return 2 * CH * W + CH * FW + CH + FW + (int)(sizeof(WarpScratch) / 4) +
+         (stencil ? 4 * CH * W + CH * FWS + FWS : 0);
 }
 
 size_t level2_smem_bytes(int warp_words) { return (size_t)warp_words * 4 * kWarps; }
