@@ -171,7 +171,7 @@ void gpv_destroy(gpv_ctx *ctx) {
     cudaFree(r->l1);
     cudaFree(r->prefix);
     cudaFree(r->bindex);
-    cudaFree(r->l2);
+    if (!r->l2_external) cudaFree(r->l2);
     if (r->l1n) cudaFree(r->l1n);
     if (r->l2n) cudaFree(r->l2n);
     if (r->hier) cudaFree(r->hier);
@@ -371,7 +371,16 @@ int gpv_voxelize_to_host(gpv_ctx *ctx, const float *h_tris, int64_t num_triangle
                         cudaMemcpyHostToDevice, stream);
     if (e != cudaSuccess) { cudaFreeAsync(d, stream); return ctx_cuda_fail(ctx, e, "cudaMemcpyAsync"); }
   }
-  HostSink sink{h_l1, h_prefix, h_bindex, h_l2, h_l2_bytes, std::max(slabs, 0)};
+  // slabs == 0 with a pinned Level2 buffer: the Level2 kernel writes it directly
+  uint8_t *l2_dev = nullptr;
+  if (slabs == 0 && h_l2) {
+    cudaPointerAttributes pa;
+    if (cudaPointerGetAttributes(&pa, h_l2) == cudaSuccess && pa.type == cudaMemoryTypeHost &&
+        pa.devicePointer)
+      l2_dev = static_cast<uint8_t *>(pa.devicePointer);
+    cudaGetLastError();  // an unknown pointer only means: not pinned
+  }
+  HostSink sink{h_l1, h_prefix, h_bindex, h_l2, h_l2_bytes, std::max(slabs, 0), l2_dev};
   const float *dp = d;
   int rc = run_batch(ctx, 1, &dp, &num_triangles, spec, out, stream, &sink);
   cudaFreeAsync(d, stream);
@@ -391,9 +400,10 @@ int gpv_result_copy_to_host(gpv_ctx *ctx, const gpv_result *res, uint8_t *l1, in
   if (bindex && res->num_boundary)
     GPV_CUDA(cudaMemcpyAsync(bindex, res->boundary_index, 4 * res->num_boundary,
                              cudaMemcpyDeviceToHost, s));
+  // cudaMemcpyDefault: a result of gpv_voxelize_to_host may hold its Level2 bytes in host memory
   if (l2 && res->num_boundary && cells)
-    GPV_CUDA(cudaMemcpyAsync(l2, res->level2_inout, res->num_boundary * cells,
-                             cudaMemcpyDeviceToHost, s));
+    GPV_CUDA(cudaMemcpyAsync(l2, res->level2_inout, res->num_boundary * cells, cudaMemcpyDefault,
+                             s));
   GPV_CUDA(cudaStreamSynchronize(s));
   return GPV_OK;
 }
@@ -435,7 +445,7 @@ int gpv_result_release(gpv_ctx *ctx, gpv_result *res) {
     cudaFreeAsync(set->l1, fs);
     cudaFreeAsync(set->prefix, fs);
     cudaFreeAsync(set->bindex, fs);
-    cudaFreeAsync(set->l2, fs);
+    if (!set->l2_external) cudaFreeAsync(set->l2, fs);
     if (set->l1n) cudaFreeAsync(set->l1n, fs);
     if (set->l2n) cudaFreeAsync(set->l2n, fs);
     if (set->hier) cudaFreeAsync(set->hier, fs);

@@ -306,7 +306,7 @@ int run_batch(gpv_ctx *ctx, int n, const float *const *d_tris, const int64_t *T,
     cudaFreeAsync(set->l1, s);
     cudaFreeAsync(set->prefix, s);
     if (set->bindex) cudaFreeAsync(set->bindex, s);
-    if (set->l2) cudaFreeAsync(set->l2, s);
+    if (set->l2 && !set->l2_external) cudaFreeAsync(set->l2, s);
     if (set->l1n) cudaFreeAsync(set->l1n, s);
     if (set->l2n) cudaFreeAsync(set->l2n, s);
     if (set->hier) cudaFreeAsync(set->hier, s);
@@ -387,8 +387,16 @@ int run_batch(gpv_ctx *ctx, int n, const float *const *d_tris, const int64_t *T,
     l2off[m + 1] = l2off[m] + (gh[m].level2 ? (int64_t)st.boundary * gh[m].cells : 0);
   }
   l2bytes = l2off[n];
+  // host outputs into pinned memory: the Level2 kernel writes its bytes there itself (over the
+  // CPU-GPU link while it computes) instead of into device memory followed by copies
+  const bool l2_direct = sink && sink->l2_dev && gh[0].level2 && sink->l2_cap >= l2bytes;
   CK(cudaMallocAsync(&set->bindex, 4 * std::max<int64_t>(Btot, 4), s));
-  CK(cudaMallocAsync(&set->l2, std::max<int64_t>(l2bytes, 16), s));
+  if (l2_direct) {
+    set->l2 = sink->l2_dev;
+    set->l2_external = true;
+  } else {
+    CK(cudaMallocAsync(&set->l2, std::max<int64_t>(l2bytes, 16), s));
+  }
   if (nmode) {
     CK(cudaMallocAsync(&set->l2n, std::max<int64_t>(3 * l2bytes * (int64_t)nsz, 16), s));
     for (int m = 0; m < n; ++m) md[m].l2n = static_cast<uint8_t *>(set->l2n) + 3 * l2off[m] * nsz;
@@ -446,7 +454,7 @@ int run_batch(gpv_ctx *ctx, int n, const float *const *d_tris, const int64_t *T,
       CK(cudaEventCreateWithFlags(&ctx->slab_aux.fork, cudaEventDisableTiming));
       for (cudaEvent_t &e : ctx->slab_aux.join) CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
     }
-    l2_copied = !gh[0].level2 || (sink->l2 && sink->l2_cap >= l2bytes);
+    l2_copied = !gh[0].level2 || l2_direct || (sink->l2 && sink->l2_cap >= l2bytes);
   }
   cudaStream_t cs = ctx->cstream;
   uint32_t slab_off[kMaxSlabs + 1] = {};
@@ -454,6 +462,7 @@ int run_batch(gpv_ctx *ctx, int n, const float *const *d_tris, const int64_t *T,
     // slab count: the caller's, or one per 12 MB of Level2 output (the copy of each slab then
     // overlaps the computation of the next; smaller slabs cost more than they hide)
     int want = sink->nslab > 0 ? sink->nslab
+               : l2_direct     ? 1
                                : (int)std::min<int64_t>(kMaxSlabs, l2bytes / (12ll << 20));
     want = std::max(1, std::min(want, fslab));
     const int gsz = (fslab + want - 1) / want;
@@ -489,7 +498,7 @@ int run_batch(gpv_ctx *ctx, int n, const float *const *d_tris, const int64_t *T,
       if (any_l2)
         launch_level2(bd, sk, sv, useg, ub, l2tmp, warp_words, ctx->num_sms, s, [&] { mark(9); },
                       zslab, nslab, [&](int k, cudaStream_t ls) {
-                        if (!sink || !l2_copied) return;
+                        if (!sink || !l2_copied || l2_direct) return;
                         cudaEventRecord(ctx->cev[1 + k], ls);
                         cudaStreamWaitEvent(cs, ctx->cev[1 + k], 0);
                         const int64_t a = (int64_t)slab_off[k] * gh[0].cells;

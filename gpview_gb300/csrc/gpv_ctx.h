@@ -17,6 +17,7 @@ struct ResultSet {
   void *l1 = nullptr, *prefix = nullptr, *bindex = nullptr, *l2 = nullptr;
   void *l1n = nullptr, *l2n = nullptr;  // normals (optional)
   void *hier = nullptr;                 // voxel box hierarchy (optional)
+  bool l2_external = false;             // l2 is the caller's pinned host buffer (not freed)
   cudaStream_t stream = 0;
   int refs = 0;
 };
@@ -134,6 +135,8 @@ struct HostSink {
   uint8_t *l2;
   int64_t l2_cap;  // bytes available at l2
   int nslab;       // z slabs of the Level2 launch (0: by the Level2 output size)
+  uint8_t *l2_dev; // device address of l2 when it is pinned host memory the Level2 kernel may
+                   // write directly (no copy), else null
 };
 int run_batch(gpv_ctx *ctx, int n, const float *const *d_tris, const int64_t *T,
               const gpv_grid_spec *specs, gpv_result *out, cudaStream_t s,

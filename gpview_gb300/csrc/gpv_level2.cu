@@ -251,6 +251,48 @@ __global__ void k_item_slab_place(const uint32_t *__restrict__ istart,
   ilist[atomicAdd(&cur[sl], 1u)] = (uint32_t)it;
 }
 
+// 4 bits -> 4 bytes holding 0 or 1 (bit j to byte j; the shifted copies land on distinct bits).
+__device__ __forceinline__ uint32_t byte_flags4(uint32_t x) { return (x * 0x00204081u) & 0x01010101u; }
+
+// Output bytes of one boundary voxel when n2z is 8 or 16 and a z layer holds a multiple of 16
+// sub-columns: each lane builds 16 consecutive bytes (16 sub-columns of one layer) from the mask
+// words, where layer r of a sub-column is bit r of its n2z-bit field, and writes them with one
+// 16-byte store (a warp covers 512 contiguous bytes per instruction).
+template <int NZ>
+__device__ __forceinline__ void write_block_vec(uint8_t *out, const uint32_t *satj,
+                                                const uint32_t *parj, const uint32_t *ftacc,
+                                                int ncol2, unsigned lane, unsigned long long &nbd,
+                                                unsigned long long &nin) {
+  const int chunks = NZ * ncol2 / 16;
+  for (int c = (int)lane; c < chunks; c += 32) {
+    const int byte0 = c * 16;
+    const int r = byte0 / ncol2, pq0 = byte0 - r * ncol2;
+    const uint32_t f16 = (ftacc[pq0 >> 5] >> (pq0 & 31)) & 0xffffu;
+    uint32_t o[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {  // sub-columns pq0 + 4k .. pq0 + 4k + 3
+      uint32_t sf, pf;
+      if (NZ == 8) {  // four sub-columns per word
+        const int w = (pq0 >> 2) + k;
+        sf = (satj[w] >> r) & 0x01010101u;
+        pf = (parj[w] >> r) & 0x01010101u;
+      } else {  // two sub-columns per word: layer bits at 0 and 16 of each
+        const int w = (pq0 >> 1) + 2 * k;
+        const uint32_t a = satj[w] >> r, b = satj[w + 1] >> r;
+        sf = (a & 1u) | ((a >> 8) & 0x100u) | ((b & 1u) << 16) | ((b << 8) & 0x1000000u);
+        const uint32_t c2 = parj[w] >> r, d2 = parj[w + 1] >> r;
+        pf = (c2 & 1u) | ((c2 >> 8) & 0x100u) | ((d2 & 1u) << 16) | ((d2 << 8) & 0x1000000u);
+      }
+      pf ^= byte_flags4((f16 >> (4 * k)) & 0xfu);
+      const uint32_t inf = pf & ~sf;
+      nbd += (unsigned)__popc(sf);
+      nin += (unsigned)__popc(inf);
+      o[k] = sf * 254u + inf * 127u;  // flags are 0/1 per byte and disjoint: no carries
+    }
+    *reinterpret_cast<uint4 *>(out + byte0) = make_uint4(o[0], o[1], o[2], o[3]);
+  }
+}
+
 // n2z bits of a Level2 column starting at bit `off` of a mask.
 __device__ __forceinline__ uint32_t column_bits(const uint32_t *m, int off, int n2z) {
   const int sh = off & 31;
@@ -764,12 +806,21 @@ __global__ void __launch_bounds__(kWarps * 32, 6) k_level2c(
   __syncwarp();
   unsigned long long nin = 0, nbd = 0;
   const uint32_t zmask_all = n2z >= 32 ? 0xffffffffu : ((1u << n2z) - 1u);
+  // 16-byte stores where the layout allows them (also the fast pattern into pinned host memory)
+  const bool vec = (n2z == 8 || n2z == 16) && (ncol2 & 15) == 0 &&
+                   (reinterpret_cast<uintptr_t>(d.l2) & 15) == 0;
   for (int jv = m - 1; jv >= 0; --jv) {
     for (int w = lane; w < FW; w += 32) ftacc[w] ^= ft[jv * FW + w];
     __syncwarp();
     const int64_t vlin = ((int64_t)kz[jv] * ny + cj) * nx + ci;
     uint8_t *out = d.l2 + (size_t)d.prefix[vlin] * cells;
     const uint32_t *satj = sat + jv * W, *parj = par + jv * W;
+    if (vec) {
+      if (n2z == 8) write_block_vec<8>(out, satj, parj, ftacc, ncol2, lane, nbd, nin);
+      else write_block_vec<16>(out, satj, parj, ftacc, ncol2, lane, nbd, nin);
+      __syncwarp();
+      continue;
+    }
     for (int pq = lane; pq < ncol2; pq += 32) {
       const int off = pq * n2z, sh = off & 31;
       uint32_t sb = satj[off >> 5] >> sh, pb = parj[off >> 5] >> sh;

@@ -194,15 +194,20 @@ int gpv_voxelize(gpv_ctx *ctx, const float *d_tris, int64_t num_triangles,
 /* Same, from host triangles (copied in on the stream). */
 int gpv_voxelize_host(gpv_ctx *ctx, const float *h_tris, int64_t num_triangles,
                       const gpv_grid_spec *spec, gpv_result *out, cudaStream_t stream);
-/* Host triangles in, host outputs out, with the copies overlapped with the computation: the
- * Level1 arrays are copied as soon as they exist and the Level2 blocks z-slab by z-slab (the
- * Level2 launch is split into `slabs` slabs of Level1 layers, <= 8; 0 picks one slab per 12 MB
- * of Level2 output; slab launches alternate between two streams so their tails overlap) while
- * later slabs compute, on a copy stream of the context.  Any host pointer may be NULL; page-locked
- * buffers give the full copy rate.  The result is also returned (device arrays valid until
- * gpv_result_release).  If h_l2_bytes < num_boundary * n2^3 nothing is copied to h_l2 and
- * GPV_ERR_BUDGET is returned with the result complete (release it; num_boundary gives the
- * size needed). */
+/* Host triangles in, host outputs out, with the transfers overlapped with the computation.  The
+ * Level1 arrays are copied on a copy stream of the context as soon as they exist.  The Level2
+ * blocks:
+ *   slabs == 0 and h_level2_inout page-locked (cudaMallocHost / cudaHostRegister): the Level2
+ *     kernel writes them into h_level2_inout itself while it computes (no device copy, no D2H);
+ *     the result's level2_inout is then that buffer's device address and is not freed;
+ *   otherwise: z-slab by z-slab -- the Level2 launch is split into `slabs` slabs of Level1
+ *     layers (<= 8; 0 picks one slab per 12 MB of Level2 output; slab launches alternate
+ *     between two streams so their tails overlap) and each slab is copied while later slabs
+ *     compute.
+ * Any host pointer may be NULL; page-locked buffers give the full transfer rate.  The result is
+ * also returned (device arrays valid until gpv_result_release).  If h_l2_bytes < num_boundary *
+ * n2^3 nothing is written to h_l2 and GPV_ERR_BUDGET is returned with the result complete
+ * (release it; num_boundary gives the size needed). */
 int gpv_voxelize_to_host(gpv_ctx *ctx, const float *h_tris, int64_t num_triangles,
                          const gpv_grid_spec *spec, uint8_t *h_level1_inout,
                          int32_t *h_level1_prefix, int32_t *h_boundary_index, uint8_t *h_level2_inout,

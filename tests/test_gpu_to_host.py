@@ -1,6 +1,7 @@
-"""gpv_voxelize_to_host: host outputs copied while the Level2 slabs compute equal the plain path's
-(and the oracle's) for any slab count; a Level2 buffer that is too small is reported, not
-overrun."""
+"""gpv_voxelize_to_host: host outputs equal the plain path's (and the oracle's) whether the Level2
+kernel writes a pinned buffer directly (slabs = 0) or each z slab is copied while later slabs
+compute (any slab count, or a pageable buffer); a Level2 buffer that is too small is reported,
+not overrun."""
 import numpy as np
 import pytest
 
@@ -30,7 +31,7 @@ def _to_host(ctx, tris, spec, slabs, l2_bytes=None):
     return rc, res, l1.numpy().copy(), pre.numpy().copy(), bi.numpy()[:B].copy(), l2.numpy()[:need].copy()
 
 
-@pytest.mark.parametrize("slabs", [1, 3, 4, 8])
+@pytest.mark.parametrize("slabs", [0, 1, 3, 4, 8])
 def test_to_host_equals_oracle_sphere16k(ctx, slabs):
     tris, spec = W.make(W.C1)
     rc, res, l1, pre, bi, l2 = _to_host(ctx, tris, spec, slabs)
@@ -46,9 +47,10 @@ def test_to_host_equals_oracle_sphere16k(ctx, slabs):
     ctx.release(res)
 
 
-def test_to_host_equals_plain_torus262k(ctx):
+@pytest.mark.parametrize("slabs", [0, 4])
+def test_to_host_equals_plain_torus262k(ctx, slabs):
     tris, spec = W.make(W.C2)
-    rc, res, l1, pre, bi, l2 = _to_host(ctx, tris, spec, 4)
+    rc, res, l1, pre, bi, l2 = _to_host(ctx, tris, spec, slabs)
     assert rc == 0
     ctx.release(res)
     plain = ctx.voxelize_host(tris, spec)
@@ -60,13 +62,34 @@ def test_to_host_equals_plain_torus262k(ctx):
     np.testing.assert_array_equal(l2, pl2)
 
 
-def test_to_host_small_buffer_is_reported(ctx):
+@pytest.mark.parametrize("slabs", [0, 4])
+def test_to_host_small_buffer_is_reported(ctx, slabs):
     tris, spec = W.make(W.C1)
-    rc, res, l1, pre, bi, l2 = _to_host(ctx, tris, spec, 4, l2_bytes=100)
+    rc, res, l1, pre, bi, l2 = _to_host(ctx, tris, spec, slabs, l2_bytes=100)
     assert rc == -7  # GPV_ERR_BUDGET: nothing copied to the Level2 buffer
     assert (l2 == 77).all()
     ref = orc.Run(tris, spec)
     np.testing.assert_array_equal(l1, ref.level1_bytes())  # Level1 outputs still delivered
+    ctx.release(res)
+
+
+def test_to_host_pageable_buffers(ctx):
+    """Pageable host buffers: the Level2 bytes come through the slab copies."""
+    tris, spec = W.make(W.C1)
+    ref = orc.Run(tris, spec)
+    cells = int(np.prod(list(spec.ndiv2)))
+    n1 = int(np.prod(list(spec.ndiv)))
+    l1 = np.zeros(n1, np.uint8)
+    pre = np.zeros(n1, np.int32)
+    bi = np.zeros(ref.B, np.int32)
+    l2 = np.zeros(ref.B * cells, np.uint8)
+    rc, res = ctx.voxelize_to_host(tris.ctypes.data, tris.size // 9, spec, l1.ctypes.data,
+                                   pre.ctypes.data, bi.ctypes.data, l2.ctypes.data, l2.size, 0)
+    assert rc == 0
+    np.testing.assert_array_equal(l1, ref.level1_bytes())
+    np.testing.assert_array_equal(pre, ref.prefix())
+    np.testing.assert_array_equal(bi, ref.boundary_index())
+    np.testing.assert_array_equal(l2, ref.level2_bytes())
     ctx.release(res)
 
 
