@@ -79,18 +79,29 @@ size_t al16(size_t v) { return (v + 15) & ~size_t(15); }
 // launches run directly.
 template <typename F>
 cudaError_t run_phase(gpv_ctx *ctx, int phase, cudaStream_t s, bool &capturing, F &&launches,
-                      bool allow_graph = true) {
+                      bool allow_graph = true, const std::vector<uint64_t> *sig = nullptr) {
   if (!ctx->graphs || !allow_graph) {
     launches();
     return cudaGetLastError();
   }
+  cudaGraphExec_t &ge = ctx->gexec[phase];
+  if (sig && ge && ctx->gsig[phase] == *sig) {
+    // same arguments as the cached graph: replay it (recording and updating it again would
+    // only reproduce it, while the GPU waits)
+    count_launch(ctx->glaunch[phase]);
+    ctx->graph_launches++;
+    return cudaGraphLaunch(ge, s);
+  }
+  ctx->gsig[phase].clear();
   if (cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
     cudaGetLastError();
     launches();
     return cudaGetLastError();
   }
   capturing = true;
+  const uint64_t l0 = launch_count();
   launches();
+  const uint64_t nl = launch_count() - l0;
   capturing = false;
   cudaGraph_t graph = nullptr;
   cudaError_t e = cudaStreamEndCapture(s, &graph);
@@ -100,7 +111,6 @@ cudaError_t run_phase(gpv_ctx *ctx, int phase, cudaStream_t s, bool &capturing, 
     launches();
     return cudaGetLastError();
   }
-  cudaGraphExec_t &ge = ctx->gexec[phase];
   bool ok = false;
   if (ge) {
     cudaGraphExecUpdateResultInfo info;
@@ -123,6 +133,10 @@ cudaError_t run_phase(gpv_ctx *ctx, int phase, cudaStream_t s, bool &capturing, 
   e = cudaGraphLaunch(ge, s);
   ctx->graph_launches++;
   cudaGraphDestroy(graph);
+  if (e == cudaSuccess && sig) {
+    ctx->gsig[phase] = *sig;
+    ctx->glaunch[phase] = nl;
+  }
   return e;
 }
 
@@ -323,6 +337,24 @@ int run_batch(gpv_ctx *ctx, int n, const float *const *d_tris, const int64_t *T,
   CK(ws.get(&keys, (size_t)pair_cap));
   CK(ws.get(&vals, (size_t)pair_cap));
   ht[1] = HClock::now();
+  // every value the phase's launches take (the per-mesh data reaches the kernels through d_md)
+  auto bd_sig = [&](std::vector<uint64_t> &v) {
+    for (uint64_t x : {(uint64_t)(uintptr_t)bd.md, (uint64_t)bd.nmesh, (uint64_t)bd.tile,
+                       (uint64_t)bd.total_tris, (uint64_t)bd.total_tiles, (uint64_t)bd.total_fwarps,
+                       (uint64_t)bd.total_rows, (uint64_t)bd.total_words,
+                       (uint64_t)(uintptr_t)bd.queue, (uint64_t)bd.normals, (uint64_t)bd.fill,
+                       (uint64_t)ctx->timing, (uint64_t)ctx->num_sms})
+      v.push_back(x);
+  };
+  std::vector<uint64_t> sig0;
+  bd_sig(sig0);
+  for (uint64_t x : {(uint64_t)(uintptr_t)d_md, (uint64_t)(uintptr_t)keys, (uint64_t)(uintptr_t)vals,
+                     (uint64_t)pair_cap, (uint64_t)(uintptr_t)bplane, (uint64_t)words,
+                     (uint64_t)(uintptr_t)wcnt, (uint64_t)(uintptr_t)wpre, (uint64_t)(uintptr_t)wtot,
+                     (uint64_t)(uintptr_t)stmp, (uint64_t)(uintptr_t)d_slab,
+                     (uint64_t)(d_slab ? (int64_t)gh[0].n[1] * gh[0].nxw : 0),
+                     (uint64_t)(d_slab ? gh[0].n[2] : 0), (uint64_t)fz, (uint64_t)fslab})
+    sig0.push_back(x);
   CK(run_phase(ctx, 0, s, capturing, [&] {
     mark(0);
     launch_prep(bd, s);
@@ -340,7 +372,7 @@ int run_batch(gpv_ctx *ctx, int n, const float *const *d_tris, const int64_t *T,
       launch_slab_offsets(wpre, wtot, (int64_t)gh[0].n[1] * gh[0].nxw, gh[0].n[2], fz, fslab,
                           d_slab, s);
     mark(4);
-  }));
+  }, true, &sig0));
   if (d_slab) CK(cudaMemcpyAsync(ctx->h_u32 + 4, d_slab, 4 * (fslab + 1), cudaMemcpyDeviceToHost, s));
   CK(cudaMemcpyAsync(ctx->h_stats, stats, n * sizeof(MeshStats), cudaMemcpyDeviceToHost, s));
   CK(cudaStreamSynchronize(s));
@@ -470,6 +502,19 @@ int run_batch(gpv_ctx *ctx, int n, const float *const *d_tris, const int64_t *T,
     nslab = (fslab + gsz - 1) / gsz;
     for (int k = 0; k <= nslab; ++k) slab_off[k] = ctx->h_u32[4 + std::min(k * gsz, fslab)];
   }
+  std::vector<uint64_t> sig1;
+  bool any_hier = false;
+  for (int m = 0; m < n; ++m) any_hier = any_hier || res_hier[m + 1] > res_hier[m];
+  bd_sig(sig1);
+  for (uint64_t x : {(uint64_t)(uintptr_t)wpre, (uint64_t)do_l2, (uint64_t)(uintptr_t)d_tiles,
+                     (uint64_t)(uintptr_t)d_tb, (uint64_t)ntiles, (uint64_t)(uintptr_t)keys,
+                     (uint64_t)(uintptr_t)vals, (uint64_t)(uintptr_t)kalt, (uint64_t)(uintptr_t)valt,
+                     (uint64_t)P2, (uint64_t)max_keybits, (uint64_t)nmode, (uint64_t)val_bits,
+                     (uint64_t)(uintptr_t)sortmp, (uint64_t)(uintptr_t)flags, (uint64_t)(uintptr_t)uidx,
+                     (uint64_t)(uintptr_t)wtot, (uint64_t)(uintptr_t)useg, (uint64_t)any_l2,
+                     (uint64_t)ub, (uint64_t)(uintptr_t)l2tmp, (uint64_t)warp_words, (uint64_t)zslab,
+                     (uint64_t)nslab, (uint64_t)gh[0].n[2]})
+    sig1.push_back(x);
   CK(run_phase(ctx, 1, s, capturing, [&] {
     mark(5);
     launch_expand(bd, wpre, s);
@@ -518,7 +563,7 @@ int run_batch(gpv_ctx *ctx, int n, const float *const *d_tris, const int64_t *T,
       mark(9);
     }
     mark(8);
-  }, !sink));
+  }, !sink, any_hier ? nullptr : &sig1));
   if (sink) {
     CK(cudaEventRecord(ctx->cev[kMaxSlabs + 1], cs));
     CK(cudaStreamWaitEvent(s, ctx->cev[kMaxSlabs + 1], 0));

@@ -5,6 +5,7 @@
 #include <mutex>
 #include <string>
 #include <unordered_map>
+#include <vector>
 
 #include "gpv_internal.h"
 
@@ -44,6 +45,11 @@ struct gpv_ctx {
   bool hierarchy = false;              // build the voxel box hierarchy
   int fill = GPV_FILL_RAY;             // inside fill of both levels
   cudaGraphExec_t gexec[2] = {};       // cached executable graphs of phases B and C
+  // Launch signature of each cached graph (every value its kernels and copies take as
+  // arguments: workspace pointers, sizes, flags) and its kernel count: a call whose signature
+  // matches replays the graph without recording it again.
+  std::vector<uint64_t> gsig[2];
+  uint64_t glaunch[2] = {};
   uint64_t graph_launches = 0, graph_instantiations = 0;
   gpv::MeshStats *h_stats = nullptr;   // pinned, h_cap entries
   gpv::MeshDesc *h_md = nullptr;       // pinned, h_cap entries
