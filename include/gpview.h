@@ -191,7 +191,8 @@ int gpv_grid_reference(const float bbox_min[3], const float bbox_max[3], float m
 /* Plain path: one mesh, device triangles (16-byte aligned), results stay on the device. */
 int gpv_voxelize(gpv_ctx *ctx, const float *d_tris, int64_t num_triangles,
                  const gpv_grid_spec *spec, gpv_result *out, cudaStream_t stream);
-/* Same, from host triangles (copied in on the stream). */
+/* Same, from host triangles: page-locked, 16-byte aligned triangles are read in place by the
+ * first kernel (which packs them into device memory); others are copied in on the stream. */
 int gpv_voxelize_host(gpv_ctx *ctx, const float *h_tris, int64_t num_triangles,
                       const gpv_grid_spec *spec, gpv_result *out, cudaStream_t stream);
 /* Host triangles in, host outputs out, with the transfers overlapped with the computation.  The

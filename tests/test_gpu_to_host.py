@@ -93,6 +93,29 @@ def test_to_host_pageable_buffers(ctx):
     ctx.release(res)
 
 
+def test_pinned_triangles_read_in_place(ctx):
+    """gpv_voxelize_host on page-locked triangles (read by the kernels in place) equals the
+    pageable path."""
+    import ctypes as C
+
+    import torch
+    import gpview_gb300 as gpv
+
+    tris, spec = W.make(W.C1)
+    h = torch.from_numpy(tris).pin_memory()
+    res = gpv.Result()
+    rc = gpv.lib().gpv_voxelize_host(ctx._h, C.c_void_p(h.data_ptr()), tris.size // 9,
+                                     C.byref(spec), C.byref(res), C.c_void_p(0))
+    assert rc == 0
+    a = ctx.fetch(res)
+    ctx.release(res)
+    ref = ctx.voxelize_host(tris, spec)
+    b = ctx.fetch(ref)
+    ctx.release(ref)
+    for x, y in zip(a, b):
+        np.testing.assert_array_equal(x, y)
+
+
 def test_to_host_level1_only(ctx):
     import gpview_gb300 as gpv
 
