@@ -131,6 +131,22 @@ GridDev make_griddev(const GridHost &gh, const float *dt) {
 
 using namespace gpv;
 
+namespace {
+// Device address of a page-locked, 16-byte aligned host buffer (which kernels may read and write
+// in place), or null for any other pointer.
+template <typename T>
+T *pinned_alias(T *h) {
+  if (!h || (reinterpret_cast<uintptr_t>(h) & 15u)) return nullptr;
+  cudaPointerAttributes pa;
+  if (cudaPointerGetAttributes(&pa, h) != cudaSuccess) {
+    cudaGetLastError();  // an unknown pointer only means: not pinned
+    return nullptr;
+  }
+  return pa.type == cudaMemoryTypeHost && pa.devicePointer ? static_cast<T *>(pa.devicePointer)
+                                                           : nullptr;
+}
+}  // namespace
+
 #define GPV_CUDA(call)                                        \
   do {                                                        \
     cudaError_t e_ = (call);                                  \
@@ -339,6 +355,8 @@ int gpv_voxelize_host(gpv_ctx *ctx, const float *h_tris, int64_t num_triangles,
   if (!ctx || !spec || !out || num_triangles < 0 || (num_triangles > 0 && !h_tris))
     return GPV_ERR_INVALID;
   cudaSetDevice(ctx->device);
+  if (const float *dp = pinned_alias(h_tris))
+    return run_batch(ctx, 1, &dp, &num_triangles, spec, out, stream);
   float *d = nullptr;
   const size_t bytes = (size_t)std::max<int64_t>(num_triangles, 1) * 9 * sizeof(float);
   cudaError_t e = cudaMallocAsync((void **)&d, bytes, stream);
@@ -362,28 +380,28 @@ int gpv_voxelize_to_host(gpv_ctx *ctx, const float *h_tris, int64_t num_triangle
       h_l2_bytes < 0)
     return GPV_ERR_INVALID;
   cudaSetDevice(ctx->device);
+  // page-locked triangles are read by the prep kernel in place (it packs them into device
+  // memory for every later stage), so no device copy is made
+  const float *pin = pinned_alias(h_tris);
   float *d = nullptr;
-  const size_t bytes = (size_t)std::max<int64_t>(num_triangles, 1) * 9 * sizeof(float);
-  cudaError_t e = cudaMallocAsync((void **)&d, bytes, stream);
-  if (e != cudaSuccess) return ctx_cuda_fail(ctx, e, "cudaMallocAsync");
-  if (num_triangles > 0) {
-    e = cudaMemcpyAsync(d, h_tris, (size_t)num_triangles * 9 * sizeof(float),
-                        cudaMemcpyHostToDevice, stream);
-    if (e != cudaSuccess) { cudaFreeAsync(d, stream); return ctx_cuda_fail(ctx, e, "cudaMemcpyAsync"); }
+  if (!pin) {
+    const size_t bytes = (size_t)std::max<int64_t>(num_triangles, 1) * 9 * sizeof(float);
+    cudaError_t e = cudaMallocAsync((void **)&d, bytes, stream);
+    if (e != cudaSuccess) return ctx_cuda_fail(ctx, e, "cudaMallocAsync");
+    if (num_triangles > 0) {
+      e = cudaMemcpyAsync(d, h_tris, (size_t)num_triangles * 9 * sizeof(float),
+                          cudaMemcpyHostToDevice, stream);
+      if (e != cudaSuccess) { cudaFreeAsync(d, stream); return ctx_cuda_fail(ctx, e, "cudaMemcpyAsync"); }
+    }
   }
   // slabs == 0 with a pinned Level2 buffer: the Level2 kernel writes it directly
-  uint8_t *l2_dev = nullptr;
-  if (slabs == 0 && h_l2) {
-    cudaPointerAttributes pa;
-    if (cudaPointerGetAttributes(&pa, h_l2) == cudaSuccess && pa.type == cudaMemoryTypeHost &&
-        pa.devicePointer)
-      l2_dev = static_cast<uint8_t *>(pa.devicePointer);
-    cudaGetLastError();  // an unknown pointer only means: not pinned
-  }
-  HostSink sink{h_l1, h_prefix, h_bindex, h_l2, h_l2_bytes, std::max(slabs, 0), l2_dev};
-  const float *dp = d;
+  uint8_t *l2_dev = slabs == 0 ? pinned_alias(h_l2) : nullptr;
+  const bool l1_pinned = (!h_l1 || pinned_alias(h_l1)) && (!h_prefix || pinned_alias(h_prefix)) &&
+                         (!h_bindex || pinned_alias(h_bindex));
+  HostSink sink{h_l1, h_prefix, h_bindex, h_l2, h_l2_bytes, std::max(slabs, 0), l2_dev, l1_pinned};
+  const float *dp = pin ? pin : d;
   int rc = run_batch(ctx, 1, &dp, &num_triangles, spec, out, stream, &sink);
-  cudaFreeAsync(d, stream);
+  if (d) cudaFreeAsync(d, stream);
   return rc;
 }
 

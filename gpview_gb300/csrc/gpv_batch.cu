@@ -502,6 +502,8 @@ int run_batch(gpv_ctx *ctx, int n, const float *const *d_tris, const int64_t *T,
     nslab = (fslab + gsz - 1) / gsz;
     for (int k = 0; k <= nslab; ++k) slab_off[k] = ctx->h_u32[4 + std::min(k * gsz, fslab)];
   }
+  // host outputs: recorded too when only page-locked Level1 copies ride along (direct Level2)
+  const bool phase1_graph = !sink || (l2_direct && sink->l1_pinned);
   std::vector<uint64_t> sig1;
   bool any_hier = false;
   for (int m = 0; m < n; ++m) any_hier = any_hier || res_hier[m + 1] > res_hier[m];
@@ -513,7 +515,12 @@ int run_batch(gpv_ctx *ctx, int n, const float *const *d_tris, const int64_t *T,
                      (uint64_t)(uintptr_t)sortmp, (uint64_t)(uintptr_t)flags, (uint64_t)(uintptr_t)uidx,
                      (uint64_t)(uintptr_t)wtot, (uint64_t)(uintptr_t)useg, (uint64_t)any_l2,
                      (uint64_t)ub, (uint64_t)(uintptr_t)l2tmp, (uint64_t)warp_words, (uint64_t)zslab,
-                     (uint64_t)nslab, (uint64_t)gh[0].n[2]})
+                     (uint64_t)nslab, (uint64_t)gh[0].n[2], (uint64_t)(sink != nullptr),
+                     (uint64_t)(uintptr_t)(sink ? sink->l1 : nullptr),
+                     (uint64_t)(uintptr_t)(sink ? sink->prefix : nullptr),
+                     (uint64_t)(uintptr_t)(sink ? sink->bindex : nullptr), (uint64_t)gh[0].N1,
+                     (uint64_t)Btot, (uint64_t)(uintptr_t)set->l1, (uint64_t)(uintptr_t)set->prefix,
+                     (uint64_t)(uintptr_t)set->bindex, (uint64_t)(uintptr_t)cs})
     sig1.push_back(x);
   CK(run_phase(ctx, 1, s, capturing, [&] {
     mark(5);
@@ -563,11 +570,11 @@ int run_batch(gpv_ctx *ctx, int n, const float *const *d_tris, const int64_t *T,
       mark(9);
     }
     mark(8);
-  }, !sink, any_hier ? nullptr : &sig1));
-  if (sink) {
-    CK(cudaEventRecord(ctx->cev[kMaxSlabs + 1], cs));
-    CK(cudaStreamWaitEvent(s, ctx->cev[kMaxSlabs + 1], 0));
-  }
+    if (sink) {  // join the copy stream back
+      cudaEventRecord(ctx->cev[kMaxSlabs + 1], cs);
+      cudaStreamWaitEvent(s, ctx->cev[kMaxSlabs + 1], 0);
+    }
+  }, phase1_graph, any_hier ? nullptr : &sig1));
   CK(cudaMemcpyAsync(ctx->h_stats, stats, n * sizeof(MeshStats), cudaMemcpyDeviceToHost, s));
   CK(cudaMemcpyAsync(ctx->h_u32, wtot, 8, cudaMemcpyDeviceToHost, s));
   CK(cudaStreamSynchronize(s));

@@ -143,6 +143,7 @@ struct HostSink {
   int nslab;       // z slabs of the Level2 launch (0: by the Level2 output size)
   uint8_t *l2_dev; // device address of l2 when it is pinned host memory the Level2 kernel may
                    // write directly (no copy), else null
+  bool l1_pinned;  // the Level1 destinations are page-locked (their copies can be recorded)
 };
 int run_batch(gpv_ctx *ctx, int n, const float *const *d_tris, const int64_t *T,
               const gpv_grid_spec *specs, gpv_result *out, cudaStream_t s,
