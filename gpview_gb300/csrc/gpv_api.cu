@@ -301,7 +301,7 @@ int gpv_autotune(gpv_ctx *ctx, int32_t n, const float *const *d_tris, const int6
 }
 
 int gpv_set_tile(gpv_ctx *ctx, int t) {
-  if (!ctx || (t != 32 && t != 64 && t != 128 && t != 256)) return GPV_ERR_INVALID;
+  if (!ctx || (t != 0 && t != 32 && t != 64 && t != 128 && t != 256)) return GPV_ERR_INVALID;
   ctx->tile = t;
   return GPV_OK;
 }

@@ -163,7 +163,16 @@ int run_batch(gpv_ctx *ctx, int n, const float *const *d_tris, const int64_t *T,
     if (T[m] > 0 && (reinterpret_cast<uintptr_t>(d_tris[m]) & 15u))
       return ctx_fail(ctx, GPV_ERR_INVALID, "triangle buffers must be 16-byte aligned");
   }
-  const int tile = ctx->tile;
+  // Level1 tile: the caller's (or the autotuner's), else the largest that still gives every SM
+  // three tiles -- larger tiles amortise the per-tile staging and barriers, but a small mesh
+  // needs small ones to occupy the GPU (torus262k: 256; a 16k-triangle sphere: 32)
+  int tile = ctx->tile;
+  if (tile <= 0) {
+    int64_t total = 0;
+    for (int m = 0; m < n; ++m) total += T[m];
+    tile = 256;
+    while (tile > 32 && total < (int64_t)tile * 3 * ctx->num_sms) tile >>= 1;
+  }
   const int nmode = ctx->normals;
   const bool stencil = ctx->fill == GPV_FILL_STENCIL;
   const size_t nsz = nmode == GPV_NORMALS_FLOAT ? sizeof(float) : 1;  // bytes per normal value

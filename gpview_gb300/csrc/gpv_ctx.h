@@ -38,7 +38,7 @@ struct gpv_ctx {
   // synchronisations, 3 second launch to the last synchronisation returning, 4 result assembly
   double host_ms[5] = {};
   std::string err;
-  int tile = 128;                      // Level1 triangles per tile (autotuned)
+  int tile = 0;                        // Level1 triangles per tile (autotuned; 0: by mesh size)
   int l2_chunk_cap = 8;                // Level2 boundary voxels per chunk, upper bound (autotuned)
   bool graphs = true;                  // record phases B and C as CUDA graphs
   int normals = 0;                     // GPV_NORMALS_* for the next voxelizations

@@ -150,7 +150,7 @@ def test_superellipsoids_and_tiles(ctx):
         q, _ = np.linalg.qr(rng.normal(size=(3, 3)))
         tris = gpv.gen_superellipsoid(k, 40, 20, (0.5, 0.5, 0.5), semi, e1, e2, q.astype(np.float32))
         _check_full(ctx, tris, _pad_spec(tris, 40, 4))
-    ctx.set_tile(128)
+    ctx.set_tile(0)
 
 
 def test_reference_grid_sizing(ctx):
