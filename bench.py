@@ -41,6 +41,8 @@ def parse():
     p.add_argument("--impl", default="gpv", choices=["gpv", "reference"])
     p.add_argument("--workload", default="torus262k", choices=["sphere16k", "torus262k", "star1310k"])
     p.add_argument("--tile", type=int, default=0)
+    p.add_argument("--level2", type=int, default=0, help="override the workload's Level2 divisions")
+    p.add_argument("--chunk", type=int, default=0, help="Level2 chunk of the plain path (0: default)")
     p.add_argument("--no-graphs", action="store_true")
     p.add_argument("--slabs", type=int, default=0,
                    help="z slabs of the e2e path's Level2 launch (0: by the Level2 output size)")
@@ -49,6 +51,8 @@ def parse():
     p.add_argument("--cpu-seconds", type=float, default=15.0)
     p.add_argument("--batch", type=int, default=4096, help="meshes of the batched workload (0: skip)")
     p.add_argument("--batch-reps", type=int, default=3)
+    p.add_argument("--batch-tile", type=int, default=0, help="fixed Level1 tile (0: autotune)")
+    p.add_argument("--batch-chunk", type=int, default=0, help="fixed Level2 chunk (0: autotune)")
     p.add_argument("--serve-seconds", type=float, default=60.0, help="served stream length (0: skip)")
     p.add_argument("--serve-pool", type=int, default=256)
     p.add_argument("--serve-rate", type=float, nargs=2, default=(100.0, 5000.0))
@@ -177,10 +181,15 @@ def batch_bench(gpv, ctx, torch, stream, local, args):
     ptrs = [dev.data_ptr() + 4 * off for off in offs]
     sp = stream.cuda_stream
     with torch.cuda.stream(stream):
-        # autotuner on a sample of the batch
-        ns = min(256, len(ptrs))
-        tile, chunk, tune_ms = ctx.autotune(ptrs[:ns], counts[:ns], specs[:ns], sp)
-        progress(f"autotuned: tile {tile}, chunk {chunk}")
+        if args.batch_tile and args.batch_chunk:
+            tile, chunk, tune_ms = args.batch_tile, args.batch_chunk, 0.0
+            ctx.set_tile(tile)
+            ctx.set_level2_chunk(chunk)
+        else:
+            # autotuner on a sample of the batch
+            ns = min(256, len(ptrs))
+            tile, chunk, tune_ms = ctx.autotune(ptrs[:ns], counts[:ns], specs[:ns], sp)
+            progress(f"autotuned: tile {tile}, chunk {chunk}")
         # plain path: one voxelization (full launch sequence, host syncs) per mesh
         torch.cuda.synchronize()
         tp = time.perf_counter()
@@ -310,6 +319,8 @@ def run_reference(args):
     import workloads as W
 
     cfg = WORKLOADS[args.workload]
+    if args.level2:
+        cfg = dict(cfg, level2=args.level2)
     tris, spec = W.make(cfg)
     from oracle import oracle as orc
 
@@ -482,11 +493,17 @@ def main():
     import workloads as W
 
     cfg = WORKLOADS[args.workload]
+    if args.level2:
+        cfg = dict(cfg, level2=args.level2)
+    # the recorded per-launch counters of the roofline belong to the workloads as defined
+    rname = cfg["name"] + (f"-l2x{args.level2}" if args.level2 else "")
     tris, spec = W.make(cfg)
     T = tris.size // 9
     ctx = gpv.Context(local)
     if args.tile:
         ctx.set_tile(args.tile)
+    if args.chunk:
+        ctx.set_level2_chunk(args.chunk)
     ctx.set_graphs(not args.no_graphs)
     stream = torch.cuda.Stream(device=local)
     sp = stream.cuda_stream
@@ -576,7 +593,7 @@ def main():
     # roofline of the dominant kernel (the Level2 kernel: instruction-issue-bound integer/FP32 work)
     per_call = {k: v / max(calls, 1) for k, v in stage_ms.items()}
     N1, B = stats["level1"], stats["boundary"]
-    roof = roofline(cfg["name"], per_call, work, stats, spec, T, peaks, peak_kind, clk)
+    roof = roofline(rname, per_call, work, stats, spec, T, peaks, peak_kind, clk)
 
     line = {"metric": "tri-voxel tests/s", "value": value, "unit": "tests/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_total * 1e3 / args.steps,

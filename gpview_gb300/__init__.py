@@ -291,6 +291,10 @@ class Context:
         if rc:
             raise GpvError(rc, "set_tile")
 
+    def set_level2_chunk(self, max_voxels):
+        """Largest number of boundary voxels of one Level1 column per Level2 work item."""
+        self._check(lib().gpv_set_level2_chunk(self._h, int(max_voxels)), "set_level2_chunk")
+
     def _check(self, rc, what):
         if rc:
             raise GpvError(rc, f"{what}: {self.error()}")

@@ -513,6 +513,12 @@ int run_batch(gpv_ctx *ctx, int n, const float *const *d_tris, const int64_t *T,
   }
   // host outputs: recorded too when only page-locked Level1 copies ride along (direct Level2)
   const bool phase1_graph = !sink || (l2_direct && sink->l1_pinned);
+  bool l2_queue = true;
+  {
+    std::unique_ptr<bool[]> has_l2(new bool[n]);
+    for (int m = 0; m < n; ++m) has_l2[m] = gh[m].level2;
+    l2_queue = level2_queue_pays(ctx->h_stats, has_l2.get(), n);
+  }
   std::vector<uint64_t> sig1;
   bool any_hier = false;
   for (int m = 0; m < n; ++m) any_hier = any_hier || res_hier[m + 1] > res_hier[m];
@@ -529,7 +535,7 @@ int run_batch(gpv_ctx *ctx, int n, const float *const *d_tris, const int64_t *T,
                      (uint64_t)(uintptr_t)(sink ? sink->prefix : nullptr),
                      (uint64_t)(uintptr_t)(sink ? sink->bindex : nullptr), (uint64_t)gh[0].N1,
                      (uint64_t)Btot, (uint64_t)(uintptr_t)set->l1, (uint64_t)(uintptr_t)set->prefix,
-                     (uint64_t)(uintptr_t)set->bindex, (uint64_t)(uintptr_t)cs})
+                     (uint64_t)(uintptr_t)set->bindex, (uint64_t)(uintptr_t)cs, (uint64_t)l2_queue})
     sig1.push_back(x);
   CK(run_phase(ctx, 1, s, capturing, [&] {
     mark(5);
@@ -567,7 +573,7 @@ int run_batch(gpv_ctx *ctx, int n, const float *const *d_tris, const int64_t *T,
                         if (b > a)
                           cudaMemcpyAsync(sink->l2 + a, static_cast<uint8_t *>(set->l2) + a, b - a,
                                           cudaMemcpyDeviceToHost, cs);
-                      }, gh[0].n[2], sink ? &ctx->slab_aux : nullptr);
+                      }, gh[0].n[2], sink ? &ctx->slab_aux : nullptr, l2_queue);
       else
         mark(9);
       if (nmode) {

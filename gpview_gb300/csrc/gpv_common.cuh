@@ -32,6 +32,8 @@ struct MeshStats {
   unsigned long long l2_boundary; // Level2 cells with state 2
   unsigned long long ray2;        // sum |U(b)| * cells
   unsigned long long pair_cap;    // capacity of the pair buffer
+  unsigned long long xycells;     // sum over triangles of (x extent + 1)(y extent + 1) in Level2
+                                  // cells, times 16: with pairs, the density of Level2 SAT items
   unsigned int status;
   unsigned int pad;
 };

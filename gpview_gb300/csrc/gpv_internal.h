@@ -134,7 +134,10 @@ void launch_level2(const BatchDev &bd, const uint32_t *keys, const uint32_t *val
                    const uint32_t *useg, int64_t Btot, uint32_t *tmp, int warp_words, int num_sms,
                    cudaStream_t s, const std::function<void()> &before_kernel = {}, int zslab = 0,
                    int nslab = 1, const std::function<void(int, cudaStream_t)> &after_slab = {},
-                   int slab_nz = 0, const SlabStreams *aux = nullptr);
+                   int slab_nz = 0, const SlabStreams *aux = nullptr, bool queue = true);
+// Level2 SAT organisation for a batch (see k_level2c): queued records when most of the pair work
+// belongs to meshes whose pairs carry many (triangle, sub-column) items.
+bool level2_queue_pays(const MeshStats *stats, const bool *has_l2, int n);
 
 // ---- normals (gpv_normals.cu) ----------------------------------------------------------------
 void launch_face_normals(const BatchDev &bd, cudaStream_t s);

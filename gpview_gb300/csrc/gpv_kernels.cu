@@ -100,22 +100,26 @@ __device__ __forceinline__ void warp_add(unsigned long long *dst, unsigned long 
 // atomics on one counter serialise at L2.
 __device__ __forceinline__ void block_add_prep(MeshStats *st, unsigned long long a,
                                                unsigned long long b, unsigned long long c,
-                                               unsigned long long d) {
-  __shared__ unsigned long long s_acc[4][8];
+                                               unsigned long long d, unsigned long long e) {
+  __shared__ unsigned long long s_acc[5][8];
   __shared__ MeshStats *s_first;
   if (threadIdx.x == 0) s_first = st;
   __syncthreads();
   if (__syncthreads_and(st == s_first)) {
-    a = warp_sum(a); b = warp_sum(b); c = warp_sum(c); d = warp_sum(d);
+    a = warp_sum(a); b = warp_sum(b); c = warp_sum(c); d = warp_sum(d); e = warp_sum(e);
     const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
-    if (lane == 0) { s_acc[0][warp] = a; s_acc[1][warp] = b; s_acc[2][warp] = c; s_acc[3][warp] = d; }
+    if (lane == 0) {
+      s_acc[0][warp] = a; s_acc[1][warp] = b; s_acc[2][warp] = c; s_acc[3][warp] = d;
+      s_acc[4][warp] = e;
+    }
     __syncthreads();
-    if (threadIdx.x < 4) {
+    if (threadIdx.x < 5) {
       unsigned long long v = 0;
 #pragma unroll
       for (int w = 0; w < 8; ++w) v += s_acc[threadIdx.x][w];
       unsigned long long *dst = threadIdx.x == 0 ? &st->sat1 : threadIdx.x == 1 ? &st->sat_units
-                                : threadIdx.x == 2 ? &st->fill_units : &st->ray1;
+                                : threadIdx.x == 2 ? &st->fill_units : threadIdx.x == 3 ? &st->ray1
+                                : &st->xycells;
       if (v) atomicAdd(dst, v);
     }
   } else {
@@ -123,6 +127,7 @@ __device__ __forceinline__ void block_add_prep(MeshStats *st, unsigned long long
     warp_add(&st->sat_units, b);
     warp_add(&st->fill_units, c);
     warp_add(&st->ray1, d);
+    warp_add(&st->xycells, e);
   }
 }
 
@@ -165,7 +170,7 @@ __global__ void __launch_bounds__(256) k_prep(BatchDev bd) {
   const int m = find_mesh<&MeshDesc::tri_base>(bd.md, bd.nmesh, live ? gi : bd.total_tris - 1);
   const MeshDesc &d = bd.md[m];
   const GridDev &g = d.g;
-  unsigned long long sat1 = 0, su = 0, fu = 0, r1 = 0;
+  unsigned long long sat1 = 0, su = 0, fu = 0, r1 = 0, xy = 0;
   if (live) {
     const int64_t t = gi - d.tri_base;
     float V[9];
@@ -203,6 +208,10 @@ __global__ void __launch_bounds__(256) k_prep(BatchDev bd) {
       const int ay = last_le(g.c1[1], g.n[1], mxy, g.c1[1][0], g.g[1]) -
                      first_ge(g.c1[1], g.n[1], mny, g.c1[1][0], g.g[1]) + 1;
       if (ax > 0 && ay > 0) r1 = (unsigned long long)ax * ay * g.n[2];
+      if (g.n2[0] > 0) {  // x/y extent in Level2 cells (the density of the Level2 SAT items)
+        const float ex = fminf((mxx - mnx) * g.inv_g2[0], 1e6f), ey = fminf((mxy - mny) * g.inv_g2[1], 1e6f);
+        xy = (unsigned long long)((ex + 1.f) * (ey + 1.f) * 16.f);
+      }
     }
     const bool sat_ok = lo[0] <= hi[0] && lo[1] <= hi[1] && lo[2] <= hi[2];
     if (sat_ok) {
@@ -227,7 +236,7 @@ __global__ void __launch_bounds__(256) k_prep(BatchDev bd) {
                          (int)pack2(lo[2], hi[2]), 0);
     d.fbox[t] = fb;
   }
-  block_add_prep(d.stats, sat1, su, fu, r1);
+  block_add_prep(d.stats, sat1, su, fu, r1, xy);
 }
 
 // Per-mesh pair emission segments from the candidate counts prep just produced: exclusive prefix

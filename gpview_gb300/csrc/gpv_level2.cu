@@ -302,8 +302,11 @@ __device__ __forceinline__ uint32_t column_bits(const uint32_t *m, int off, int 
 }
 
 // ---- Level2 ------------------------------------------------------------------------------------
-// ST: the stencil fill (ClassifyInOut2xLevel2) instead of the ray fill.
-template <bool ST>
+// ST: the stencil fill (ClassifyInOut2xLevel2) instead of the ray fill.  QUEUE: the (triangle,
+// sub-column) items passing the z-invariant axes are queued and their slab work done 32 records
+// at a time (pays off when a pair has many items: triangles large against the Level2 cells);
+// otherwise each item lane does its own slab work.
+template <bool ST, bool QUEUE>
 __global__ void __launch_bounds__(kWarps * 32, 6) k_level2c(
     BatchDev bd, const uint32_t *__restrict__ keys, const uint32_t *__restrict__ vals,
     const uint32_t *__restrict__ useg, const uint32_t *__restrict__ cflag,
@@ -426,6 +429,7 @@ __global__ void __launch_bounds__(kWarps * 32, 6) k_level2c(
       ws.pre[lane] = inc - cnt;
       const uint32_t tot = __shfl_sync(FULL, inc, 31);
       __syncwarp();
+      if constexpr (QUEUE) {
       // (triangle, sub-column) items, 32 at a time (B1): the z-invariant SAT part; the items that
       // pass are queued as records.  Every 32 records (B2): the plane slab selects the cells left
       // for the full test, so that those lanes all work; then the (triangle, cell) tests run 32
@@ -559,6 +563,107 @@ __global__ void __launch_bounds__(kWarps * 32, 6) k_level2c(
           nrec -= nr;
           __syncwarp();
         }
+      }
+      } else {
+      // (triangle, sub-column) items, 32 at a time: z-invariant SAT part and the plane slab
+      // select the cells left for the full test; then those (triangle, cell) tests run 32 at a
+      // time so that the lanes stay busy whatever the per-column cell counts.  Each item lane
+      // lists its cells in a window of 64 slots (its lane and the cell's z), so a test lane
+      // reads its work from one slot.
+      for (uint32_t wb = 0; wb < tot; wb += 32) {
+        const uint32_t w = wb + lane;
+        uint32_t zm = 0, rec = 0;
+        if (w < tot) {
+          const int tl = batch_search(ws.pre, w);
+          const uint32_t loc = w - ws.pre[tl];
+          const uint32_t rg = ws.rng[tl];
+          const int np = (int)((rg >> 6) & 63u);
+          // loc / np by a float reciprocal: exact here (loc < 1024, np <= 32, so the quotient of
+          // loc + 1/2 stays at least 1/64 away from an integer, far above the rounding)
+          const int qq = __float2int_rz(((float)loc + 0.5f) * ws.x[tl][4]);
+          const int p = (int)(rg & 63u) + (int)loc - qq * np;
+          const int q = (int)((rg >> 12) & 63u) + qq;
+          const int r0 = (int)((rg >> 18) & 63u), r1 = (int)((rg >> 24) & 63u);
+          const int jv = ws.jm[tl];
+          const uint32_t *satj = sat + jv * W;
+          const float *sz = g.c2s[2] + (size_t)kz[jv] * n2z;
+          const float sz0 = __ldg(sz), sz1 = __ldg(sz + n2z - 1);
+          // cells of this column already marked by another triangle need no test (OR only)
+          const int off = (q * n2x + p) * n2z, sh = off & 31;
+          uint32_t done = satj[off >> 5] >> sh;
+          if (sh + n2z > 32) done |= satj[(off >> 5) + 1] << (32 - sh);
+          const uint32_t rmask = ((r1 - r0 + 1) >= 32 ? 0xffffffffu : ((1u << (r1 - r0 + 1)) - 1u)) << r0;
+          if ((~done & rmask) != 0) {
+            float V[9];
+#pragma unroll
+            for (int c = 0; c < 9; ++c) V[c] = ws.v[tl][c];
+            const float cx = __ldg(sx + p), cy = __ldg(sy + q);
+            SatCol sc;
+            if (sat_col(V, cx, cy, g.e2, sc)) {
+              const float nxs = ws.x[tl][0], nys = ws.x[tl][1], nzs = ws.x[tl][2], H = ws.x[tl][3];
+              const float sxy = fa(fm(nxs, fs(V[0], cx)), fm(nys, fs(V[1], cy)));
+              // The per-cell slab test |sxy + nz (V0z - cz)| <= H can only pass for cz within
+              // H/|nz| of V0z + sxy/nz; the interval is widened by the float error of that test
+              // (a few ulps of its terms, over |nz|) and one cell, and the exact per-cell test
+              // still runs.
+              int ra = r0, rb = r1;
+              const float rnz = ws.x[tl][5];
+              if (rnz != 0.f) {
+                const float zc = V[2] + sxy * rnz;
+                const float ext = (ws.x[tl][6] + 8.f * EPS24 * fabsf(sxy)) * fabsf(rnz);
+                const float igz = g.inv_g2[2];
+                const float fa0 = (zc - ext - sz0) * igz - 1.f, fb0 = (zc + ext - sz0) * igz + 1.f;
+                if (fa0 > -2.f) ra = max(ra, (int)floorf(fminf(fa0, (float)n2z + 2.f)));
+                if (fb0 < (float)n2z + 2.f) rb = min(rb, (int)ceilf(fmaxf(fb0, -2.f)));
+              }
+              // The slab value is monotone in cz (each operation on cz is a monotone rounding:
+              // V0z - cz, then times nz, then plus sxy), so the cells passing |value| <= H are
+              // one interval of [ra, rb]; its ends are found by testing inwards from both ends.
+              while (ra <= rb && !(fabsf(fa(sxy, fm(nzs, fs(V[2], __ldg(sz + ra))))) <= H)) ++ra;
+              while (rb > ra && !(fabsf(fa(sxy, fm(nzs, fs(V[2], __ldg(sz + rb))))) <= H)) --rb;
+              if (ra <= rb)
+                zm = ((rb - ra + 1 >= 32) ? 0xffffffffu : ((1u << (rb - ra + 1)) - 1u)) << ra & ~done;
+              rec = (uint32_t)tl | ((uint32_t)p << 5) | ((uint32_t)q << 11);
+            }
+          }
+        }
+        const uint32_t zc = (uint32_t)__popc(zm);
+        const uint32_t zinc = warp_incl_scan(zc);
+        ws.zrec[lane] = rec;
+        const uint32_t ztot = __shfl_sync(FULL, zinc, 31);
+        for (uint32_t w0 = 0; w0 < ztot; w0 += 64) {
+          // each record lane lists its cells of this window: (record lane, cell r) per slot
+          {
+            uint32_t mm = zm, pos = zinc - zc;
+            while (mm && pos < w0) { mm &= mm - 1u; ++pos; }
+            while (mm && pos < w0 + 64u) {
+              ws.zown[pos - w0] = lane | ((uint32_t)(__ffs(mm) - 1) << 5);
+              mm &= mm - 1u;
+              ++pos;
+            }
+          }
+          __syncwarp();
+          const uint32_t wn = min(64u, ztot - w0);
+          for (uint32_t z = lane; z < wn; z += 32) {
+            const uint32_t own = ws.zown[z];
+            const uint32_t rc = ws.zrec[own & 31u];
+            const int r = (int)(own >> 5);
+            const int tl = (int)(rc & 31u), p = (int)((rc >> 5) & 63u), q = (int)((rc >> 11) & 63u);
+            const int jv = ws.jm[tl];
+            const float *sz = g.c2s[2] + (size_t)kz[jv] * n2z;
+            float V[9];
+#pragma unroll
+            for (int c = 0; c < 9; ++c) V[c] = ws.v[tl][c];
+            SatCol sc;
+            sat_col_values(V, __ldg(sx + p), __ldg(sy + q), sc);
+            if (sat_z(sc, V, __ldg(sz + r), g.e2)) {
+              const int bi = (q * n2x + p) * n2z + r;
+              atomicOr(&sat[jv * W + (bi >> 5)], 1u << (bi & 31));
+            }
+          }
+          __syncwarp();
+        }
+      }
       }
     }
   }
@@ -806,8 +911,10 @@ __global__ void __launch_bounds__(kWarps * 32, 6) k_level2c(
   __syncwarp();
   unsigned long long nin = 0, nbd = 0;
   const uint32_t zmask_all = n2z >= 32 ? 0xffffffffu : ((1u << n2z) - 1u);
-  // 16-byte stores where the layout allows them (also the fast pattern into pinned host memory)
-  const bool vec = (n2z == 8 || n2z == 16) && (ncol2 & 15) == 0 &&
+  // 16-byte stores where the layout allows them (also the fast pattern into pinned host memory);
+  // measured faster with the queued organisation (torus262k: -6%) and slower with the per-lane
+  // one on the mixed batch (+3%), so only the former uses them
+  const bool vec = QUEUE && (n2z == 8 || n2z == 16) && (ncol2 & 15) == 0 &&
                    (reinterpret_cast<uintptr_t>(d.l2) & 15) == 0;
   for (int jv = m - 1; jv >= 0; --jv) {
     for (int w = lane; w < FW; w += 32) ftacc[w] ^= ft[jv * FW + w];
@@ -870,6 +977,22 @@ int level2_warp_words(const GridDev &g, int cap, bool stencil) {
          (stencil ? 4 * CH * W + CH * FWS + FWS : 0);
 }
 
+// Measured on one GB300: the queued records win (3-10%) where the triangles span several Level2
+// cells in x and y (xycells / pairs >= 4: torus262k at 8^3, a 16k sphere at 4^3); the per-lane
+// slab work wins (10-16%) where they span about one (the same torus at 2^3 and 4^3), and on
+// mixed batches.
+bool level2_queue_pays(const MeshStats *stats, const bool *has_l2, int n) {
+  double dense = 0.0, all = 0.0;
+  for (int m = 0; m < n; ++m) {
+    if (!has_l2[m]) continue;
+    const double p = (double)stats[m].pairs;
+    all += p;
+    if ((double)stats[m].xycells >= 64.0 * p) dense += p;  // xycells carries a factor 16
+  }
+  // mixed launches do better with the per-lane organisation (the 4096-mesh mix: +3%)
+  return dense > 0.9 * all;
+}
+
 size_t level2_smem_bytes(int warp_words) { return (size_t)warp_words * 4 * kWarps; }
 
 int64_t level2_temp_words(int64_t B) { return 7 * B + 32 + scan_temp_words(B); }
@@ -879,7 +1002,7 @@ void launch_level2(const BatchDev &bd, const uint32_t *keys, const uint32_t *val
                    const uint32_t *useg, int64_t B, uint32_t *tmp, int warp_words, int num_sms,
                    cudaStream_t s, const std::function<void()> &before_kernel, int zslab,
                    int nslab, const std::function<void(int, cudaStream_t)> &after_slab, int slab_nz,
-                   const SlabStreams *aux) {
+                   const SlabStreams *aux, bool queue) {
   if (B <= 0) return;
   uint32_t *cflag = tmp, *cord = cflag + B, *colhead = cord + B, *iflag = colhead + B + 1,
            *iord = iflag + B, *istart = iord + B, *nitems = istart + B + 1,
@@ -896,11 +1019,13 @@ void launch_level2(const BatchDev &bd, const uint32_t *keys, const uint32_t *val
   count_launch(4);
   const size_t smem = level2_smem_bytes(warp_words);
   const bool st = bd.fill == GPV_FILL_STENCIL;
-  auto kern = st ? k_level2c<true> : k_level2c<false>;
-  static bool attr_set[2] = {false, false};
-  if (!attr_set[st]) {
+  auto kern = st ? (queue ? k_level2c<true, true> : k_level2c<true, false>)
+                 : (queue ? k_level2c<false, true> : k_level2c<false, false>);
+  const int kv = (st ? 2 : 0) + (queue ? 1 : 0);
+  static bool attr_set[4] = {false, false, false, false};
+  if (!attr_set[kv]) {
     cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-    attr_set[st] = true;
+    attr_set[kv] = true;
   }
   int per_sm = 0;
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kWarps * 32, smem);
