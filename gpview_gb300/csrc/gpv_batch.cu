@@ -315,6 +315,8 @@ int run_batch(gpv_ctx *ctx, int n, const float *const *d_tris, const int64_t *T,
   bd.queue = queue;
   bd.normals = nmode;
   bd.fill = ctx->fill;
+  bd.stp = nullptr;
+  bd.stp_words = 0;
   CK(ctx_ensure_host(ctx, (size_t)n));
   std::memcpy(ctx->h_md, md.data(), n * sizeof(MeshDesc));
   CK(cudaMemcpyAsync(d_md, ctx->h_md, n * sizeof(MeshDesc), cudaMemcpyHostToDevice, s));
@@ -352,6 +354,7 @@ int run_batch(gpv_ctx *ctx, int n, const float *const *d_tris, const int64_t *T,
                        (uint64_t)bd.total_tris, (uint64_t)bd.total_tiles, (uint64_t)bd.total_fwarps,
                        (uint64_t)bd.total_rows, (uint64_t)bd.total_words,
                        (uint64_t)(uintptr_t)bd.queue, (uint64_t)bd.normals, (uint64_t)bd.fill,
+                       (uint64_t)(uintptr_t)bd.stp, (uint64_t)bd.stp_words,
                        (uint64_t)ctx->timing, (uint64_t)ctx->num_sms})
       v.push_back(x);
   };
@@ -479,6 +482,11 @@ int run_batch(gpv_ctx *ctx, int n, const float *const *d_tris, const int64_t *T,
     CK(ws.get(&useg, (size_t)ub + 1));
     CK(ws.get(&sortmp, (size_t)std::max(sort_seg_temp_words(ntiles), scan_temp_words(P2))));
     CK(ws.get(&l2tmp, (size_t)level2_temp_words(ub)));
+    if (stencil && any_l2) {  // per boundary voxel: the column prefix of sample coverage
+      for (int m = 0; m < n; ++m)
+        if (gh[m].level2) bd.stp_words = std::max(bd.stp_words, (4 * gh[m].n2[0] * gh[m].n2[1] + 31) / 32);
+      CK(ws.get(&bd.stp, (size_t)std::max<int64_t>(ub, 1) * bd.stp_words));
+    }
     CK(cudaMemcpyAsync(d_tiles, ctx->h_tiles, ntiles * sizeof(SortTile), cudaMemcpyHostToDevice, s));
     CK(cudaMemcpyAsync(d_tb, ctx->h_tb, (n + 1) * sizeof(int64_t), cudaMemcpyHostToDevice, s));
   }

@@ -84,6 +84,8 @@ struct BatchDev {
   uint32_t *queue;       // work-queue tickets, zeroed before each persistent launch
   int normals;           // GPV_NORMALS_* of this batch
   int fill;              // GPV_FILL_* of this batch
+  uint32_t *stp;         // stencil fill: per boundary voxel, the sample-coverage parity of the
+  int stp_words;         //   column's triangles recorded only below it (stp_words words each)
 };
 
 void launch_prep(const BatchDev &bd, cudaStream_t s);

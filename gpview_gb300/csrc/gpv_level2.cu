@@ -301,6 +301,102 @@ __device__ __forceinline__ uint32_t column_bits(const uint32_t *m, int off, int 
   return b;
 }
 
+// ---- stencil fill, column prefix ------------------------------------------------------------------
+// A triangle whose topmost record in a Level1 column lies below voxel v is not recorded in any
+// voxel from v up, so within the column's x/y extent it lies below v's bottom face (up to the
+// SAT's rounding, far less than the half Level2 cell to v's first clip height): every covered
+// sample keeps it in every slice of v and above.  One warp per column walks the column's records
+// in z order once, XOR-ing each triangle's sample coverage into a running mask, and stores the
+// mask reached at each boundary voxel; a Level2 chunk then starts from its first voxel's mask and
+// draws only the triangles recorded from that voxel up (otherwise every chunk of a tall column
+// would draw all the triangles below it again).
+constexpr int kPrefixWarps = 4;
+constexpr int kPrefixMaskWords = 128;  // 4 * 32 * 32 samples / 32
+
+__global__ void __launch_bounds__(kPrefixWarps * 32) k_stencil_prefix(
+    BatchDev bd, const uint32_t *__restrict__ keys, const uint32_t *__restrict__ vals,
+    const uint32_t *__restrict__ useg, const uint32_t *__restrict__ cflag,
+    const uint32_t *__restrict__ cord, const uint32_t *__restrict__ colhead,
+    const uint32_t *__restrict__ iflag, int64_t B) {
+  __shared__ uint32_t s_mask[kPrefixWarps][kPrefixMaskWords];
+  __shared__ StTri s_t[kPrefixWarps][32];
+  __shared__ uint32_t s_pre[kPrefixWarps][32];
+  const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+  const int64_t c = (int64_t)blockIdx.x * kPrefixWarps + warp;
+  const int64_t ncols = (int64_t)cord[B - 1] + cflag[B - 1];
+  if (c >= ncols) return;
+  const uint32_t u0 = colhead[c], u1 = colhead[c + 1];
+  const MeshDesc &d = bd.md[mesh_of_u(bd.md, bd.nmesh, u0)];
+  if (!d.has_l2) return;
+  // only the column's later work-item starts read a mask: a one-item column needs none, and
+  // the records from the last start up are not needed
+  uint32_t ulast = u0;
+  for (uint32_t u = u0 + 1 + lane; u < u1; u += 32)
+    if (iflag[u]) ulast = max(ulast, u);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) ulast = max(ulast, __shfl_xor_sync(FULL, ulast, o));
+  if (ulast == u0) return;
+  const GridDev &g = d.g;
+  const int n2x = g.n2[0], n2y = g.n2[1], nz = g.n[2], nx = g.n[0];
+  const int SW = 2 * n2x, SH = 2 * n2y;
+  const int FWS = (4 * n2x * n2y + 31) >> 5;
+  const uint32_t col = keys[useg[u0]] / (uint32_t)nz;
+  const int ci = (int)(col % (uint32_t)nx), cj = (int)(col / (uint32_t)nx);
+  const float lx = fa(fm((float)ci, g.g[0]), g.bmin[0]), hx = fa(lx, g.g[0]);
+  const float ly = fa(fm((float)cj, g.g[1]), g.bmin[1]), hy = fa(ly, g.g[1]);
+  uint32_t *mask = s_mask[warp];
+  for (int w = lane; w < FWS; w += 32) mask[w] = 0;
+  __syncwarp();
+  const float4 *__restrict__ ptri = d.ptri;
+  for (uint32_t u = u0; u <= ulast; ++u) {
+    if (u == u0 || iflag[u]) {
+      uint32_t *out = bd.stp + (size_t)u * bd.stp_words;
+      for (int w = lane; w < FWS; w += 32) out[w] = mask[w];
+    }
+    if (u == ulast) break;
+    const uint32_t e0 = useg[u], e1 = useg[u + 1];
+    for (uint32_t b0 = e0; b0 < e1; b0 += 32) {
+      const uint32_t e = b0 + lane;
+      const uint32_t vv = e < e1 ? vals[e] : 0u;
+      uint32_t cnt = 0;
+      if (vv & 0x80000000u) {  // the triangle's topmost record in the column
+        const uint32_t t = vv & 0x7fffffffu;
+        const float4 a0 = __ldg(ptri + 3 * (size_t)t), a1 = __ldg(ptri + 3 * (size_t)t + 1),
+                     a2 = __ldg(ptri + 3 * (size_t)t + 2);
+        const float V[9] = {a0.x, a0.y, a0.z, a1.x, a1.y, a1.z, a2.x, a2.y, a2.z};
+        StTri st;
+        if (st_setup(V, lx, hx, ly, hy, SW, SH, st)) {
+          s_t[warp][lane] = st;
+          cnt = (uint32_t)((st.sx1 - st.sx0 + 1) * (st.sy1 - st.sy0 + 1));
+        }
+      }
+      uint32_t inc = cnt;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t x = __shfl_up_sync(FULL, inc, o);
+        if (lane >= (unsigned)o) inc += x;
+      }
+      s_pre[warp][lane] = inc - cnt;
+      const uint32_t tot = __shfl_sync(FULL, inc, 31);
+      __syncwarp();
+      for (uint32_t w = lane; w < tot; w += 32) {
+        const int tl = batch_search(s_pre[warp], w);
+        const StTri &st = s_t[warp][tl];
+        const uint32_t loc = w - s_pre[warp][tl];
+        const uint32_t nsx = (uint32_t)(st.sx1 - st.sx0 + 1);
+        const uint32_t row = loc / nsx;
+        const int sx = st.sx0 + (int)(loc - row * nsx), sy = st.sy0 + (int)row;
+        float zs;
+        if (st_cover(st, sx, sy, zs)) {
+          const int sidx = sy * SW + sx;
+          atomicXor(&mask[sidx >> 5], 1u << (sidx & 31));
+        }
+      }
+      __syncwarp();
+    }
+  }
+}
+
 // ---- Level2 ------------------------------------------------------------------------------------
 // ST: the stencil fill (ClassifyInOut2xLevel2) instead of the ray fill.  QUEUE: the (triangle,
 // sub-column) items passing the z-invariant axes are queued and their slab work done 32 records
@@ -371,7 +467,10 @@ __global__ void __launch_bounds__(kWarps * 32, 6) k_level2c(
   if (ST) {
     for (int w = lane; w < m * SWd; w += 32) stg[w] = 0;
     for (int w = lane; w < m * FWS; w += 32) sft[w] = 0;
-    for (int w = lane; w < FWS; w += 32) sftacc[w] = 0;
+    // the coverage parity of the column's triangles recorded only below the chunk (none below a
+    // column's first voxel; the prefix pass writes the masks of the later chunk starts)
+    const bool first = colhead[cord[ua] + cflag[ua] - 1u] == ua;
+    for (int w = lane; w < FWS; w += 32) sftacc[w] = first ? 0u : bd.stp[(size_t)ua * bd.stp_words + w];
   }
   const int ci = (int)(col % (uint32_t)nx), cj = (int)(col / (uint32_t)nx);
   if ((int)lane < m) kz[lane] = (int)(keys[useg[ua + lane]] - col * (uint32_t)nz);
@@ -677,8 +776,8 @@ __global__ void __launch_bounds__(kWarps * 32, 6) k_level2c(
     // at the Level2 ray-origin height o2z[k][s] (minZ + (s + 0.5)*gridSizeZ2, :1297), so a
     // covered sample at height zs counts in every slice from the first with o2z >= zs: one
     // toggle bit there, expanded by a prefix XOR below.
-    const uint32_t chead = colhead[cord[ua] + cflag[ua] - 1u];
-    const uint32_t g0 = useg[chead], g1 = useg[ucol_end];
+    // triangles recorded from the chunk's first voxel up (those below are in the prefix)
+    const uint32_t g0 = useg[ua], g1 = useg[ucol_end];
     const int SW = 2 * n2x, SH = 2 * n2y;
     const float lx = fa(fm((float)ci, g.g[0]), g.bmin[0]), hx = fa(lx, g.g[0]);
     const float ly = fa(fm((float)cj, g.g[1]), g.bmin[1]), hy = fa(ly, g.g[1]);
@@ -1017,6 +1116,11 @@ void launch_level2(const BatchDev &bd, const uint32_t *keys, const uint32_t *val
   scan_u32(iflag, iord, B, nullptr, stmp, s);
   k_itemstarts<<<nb, 256, 0, s>>>(iflag, iord, B, istart, nitems);
   count_launch(4);
+  if (bd.fill == GPV_FILL_STENCIL && bd.stp) {
+    k_stencil_prefix<<<(unsigned)((B + kPrefixWarps - 1) / kPrefixWarps), kPrefixWarps * 32, 0, s>>>(
+        bd, keys, vals, useg, cflag, cord, colhead, iflag, B);
+    count_launch();
+  }
   const size_t smem = level2_smem_bytes(warp_words);
   const bool st = bd.fill == GPV_FILL_STENCIL;
   auto kern = st ? (queue ? k_level2c<true, true> : k_level2c<true, false>)
