@@ -352,9 +352,9 @@ def run_reference(args):
 # Warp instructions one launch of the Level2 kernel executes on each single-mesh workload, from
 # `ncu --metrics smsp__inst_executed.sum` on the current kernel (profiles/k_level2c_*.md give the
 # commands).  The count is a property of the kernel's code and the input, not of the clock.
-LEVEL2_INST_PER_LAUNCH = {"torus262k": 401801132, "sphere16k": 27392400}
+LEVEL2_INST_PER_LAUNCH = {"torus262k": 384583248, "sphere16k": 27545565}
 # DRAM bytes read + written by one launch of the Level2 kernel (same captures)
-LEVEL2_TRAFFIC = {"torus262k": 30704384 + 9126997, "sphere16k": 2835029}
+LEVEL2_TRAFFIC = {"torus262k": 30674603 + 6144341, "sphere16k": 2841685}
 
 
 def max_over_ranks(seconds, dist, device):
