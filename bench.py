@@ -214,6 +214,13 @@ def batch_bench(gpv, ctx, torch, stream, local, args):
                 ctx.release(r)
             if k > 0:
                 times.append(dt)
+        # one more call with host timing on: where the host time of a batch call goes
+        ctx.set_timing(True)
+        for r in ctx.voxelize_batch(ptrs, counts, specs, sp):
+            ctx.release(r)
+        torch.cuda.synchronize()
+        hcalls, host_ms = ctx.host_times()
+        ctx.set_timing(False)
     batch_s = sum(times) / len(times)
     assert bwork == work, (bwork, work)
     n = len(meshes)
@@ -222,7 +229,8 @@ def batch_bench(gpv, ctx, torch, stream, local, args):
             "tile": tile, "level2_chunk": chunk, "autotune_sample_ms": tune_ms,
             "plain_meshes_per_s": n / plain_s, "batched_meshes_per_s": n / batch_s,
             "batched_vs_plain": plain_s / batch_s, "batched_tests_per_s": work / batch_s,
-            "plain_s": plain_s, "batched_s": batch_s, "generate_s": gen_s}
+            "plain_s": plain_s, "batched_s": batch_s, "generate_s": gen_s,
+            "batched_host_ms_per_call": {k: v / max(hcalls, 1) for k, v in host_ms.items()}}
 
 
 def served_bench(gpv, torch, local, args, tuned):

@@ -13,11 +13,35 @@
 #include <cstring>
 #include <memory>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "gpv_ctx.h"
 
 namespace gpv {
+
+// Runs f(i) for i in [0, n) on up to the machine's hardware threads when n is large enough to
+// repay the thread start (the per-mesh host work of a batch); inline otherwise.
+template <typename F>
+void host_parallel_for(int n, F &&f) {
+  if (n < 128) {  // below two threads' worth: inline (and no query of the machine)
+    for (int i = 0; i < n; ++i) f(i);
+    return;
+  }
+  static const int hw = (int)std::max(1u, std::thread::hardware_concurrency());
+  const int nt = std::min(std::min(hw, 16), n / 64);
+  if (nt <= 1) {
+    for (int i = 0; i < n; ++i) f(i);
+    return;
+  }
+  std::vector<std::thread> th;
+  th.reserve(nt);
+  for (int t = 0; t < nt; ++t)
+    th.emplace_back([&, t] {
+      for (int i = t; i < n; i += nt) f(i);
+    });
+  for (std::thread &x : th) x.join();
+}
 
 namespace {
 
@@ -155,8 +179,18 @@ int run_batch(gpv_ctx *ctx, int n, const float *const *d_tris, const int64_t *T,
   HClock::time_point ht[6];
   ht[0] = HClock::now();
   std::vector<GridHost> gh(n);
+  std::vector<int> grc(n, GPV_OK);
+  if (n == 1 && ctx->last_gh && std::memcmp(&ctx->last_spec, &specs[0], sizeof(gpv_grid_spec)) == 0) {
+    gh[0] = *ctx->last_gh;  // the same grid as the previous single-mesh call
+  } else {
+    host_parallel_for(n, [&](int m) { grc[m] = grid_derive(specs[m], gh[m]); });
+    if (n == 1 && grc[0] == GPV_OK) {
+      ctx->last_spec = specs[0];
+      ctx->last_gh = std::make_shared<GridHost>(gh[0]);
+    }
+  }
   for (int m = 0; m < n; ++m) {
-    if (grid_derive(specs[m], gh[m]) != GPV_OK)
+    if (grc[m] != GPV_OK)
       return ctx_fail(ctx, GPV_ERR_INVALID, ("invalid grid specification for mesh " + std::to_string(m)).c_str());
     if (T[m] < 0 || T[m] >= ((int64_t)1 << 31) || (T[m] > 0 && !d_tris[m]))
       return ctx_fail(ctx, GPV_ERR_INVALID, "bad triangle count or pointer");
@@ -219,7 +253,7 @@ int run_batch(gpv_ctx *ctx, int n, const float *const *d_tris, const int64_t *T,
   Arena ws(ctx, s);
   // coordinate tables: one pinned staging copy
   CK(ctx_ensure_tables(ctx, (size_t)tab_off[n]));
-  for (int m = 0; m < n; ++m) pack_tables(gh[m], ctx->h_tables + tab_off[m]);
+  host_parallel_for(n, [&](int m) { pack_tables(gh[m], ctx->h_tables + tab_off[m]); });
   float *d_tab;
   CK(ws.get(&d_tab, (size_t)tab_off[n]));
   CK(cudaMemcpyAsync(d_tab, ctx->h_tables, tab_off[n] * sizeof(float), cudaMemcpyHostToDevice, s));

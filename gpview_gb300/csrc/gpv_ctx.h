@@ -70,6 +70,8 @@ struct gpv_ctx {
   cudaStream_t cstream = nullptr;      // copy stream of gpv_voxelize_to_host (lazily created)
   cudaEvent_t cev[gpv::kMaxSlabs + 2] = {};  // its ordering events
   gpv::SlabStreams slab_aux = {};      // two streams for overlapping Level2 slab launches
+  gpv_grid_spec last_spec = {};        // grid of the previous single-mesh call, derived
+  std::shared_ptr<gpv::GridHost> last_gh;
   uint64_t next_handle = 1;
   std::mutex owned_mu;                 // results may be released from another host thread
   std::unordered_map<uint64_t, std::shared_ptr<gpv::ResultSet>> owned;

@@ -82,3 +82,24 @@ def test_golden_fixtures_on_gpu(ctx):
         np.testing.assert_array_equal(l2, (z["level2"] * 127).astype(np.uint8), err_msg=path)
         assert [r.work.sat1, r.work.sat2, r.work.ray1, r.work.ray2] == z["work"].tolist()
         ctx.release(r)
+
+
+def test_large_batch_host_work_in_threads(ctx):
+    """A batch of 200 meshes: the per-mesh grid derivation and table packing run on several host
+    threads; every sampled mesh still equals its single-mesh result."""
+    torch = pytest.importorskip("torch")
+    import gpview_gb300 as gpv
+
+    meshes = _mixed_meshes(gpv, 200, seed=11)
+    dev = [torch.from_numpy(np.ascontiguousarray(t) if t.size else np.zeros(9, np.float32)).cuda()
+           for t, _ in meshes]
+    res = ctx.voxelize_batch([d.data_ptr() for d in dev], [t.size // 9 for t, _ in meshes],
+                             [s for _, s in meshes])
+    for i in range(0, len(meshes), 17):
+        t, spec = meshes[i]
+        ra = ctx.voxelize_host(t, spec)
+        for x, y in zip(ctx.fetch(res[i]), ctx.fetch(ra)):
+            np.testing.assert_array_equal(x, y)
+        ctx.release(ra)
+    for rb in res:
+        ctx.release(rb)

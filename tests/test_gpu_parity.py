@@ -162,3 +162,27 @@ def test_reference_grid_sizing(ctx):
     pad = np.float32(0.001) * np.linalg.norm(mx - mn)
     spec = gpv.grid_reference(mn - pad, mx + pad, float((mx - mn).max() + 2 * pad), 32, 4)
     _check_full(ctx, tris, spec)
+
+
+def test_graph_replay_with_other_mesh_data(ctx):
+    """Back-to-back calls whose launch arguments are identical (same sizes and counts) replay the
+    recorded graphs with the new mesh's data: a torus and its copy shifted by a whole number of
+    voxels (exact in float) give equal counts, and both must match the oracle."""
+    import gpview_gb300 as gpv
+
+    t = gpv.gen_torus(12, 96, 48, (0.5, 0.5, 0.5), 0.3, 0.1, 0.004)
+    t = (np.round(t * 65536.0) / 65536.0).astype(np.float32)  # shifts by 1.0 stay exact
+    u = t.reshape(-1, 3).copy()
+    u[:, 0] += np.float32(1.0)
+    spec = _spec_exact((0, 0, 0), (2, 1, 1), (32, 16, 16), (4, 4, 4))
+    refs = []
+    for tris in (t, u.reshape(-1), t):
+        res = ctx.voxelize_host(tris, spec)
+        l1, pre, bi, l2 = ctx.fetch(res)
+        ref = orc.Run(tris, spec)
+        np.testing.assert_array_equal(l1, ref.level1_bytes())
+        np.testing.assert_array_equal(bi, ref.boundary_index())
+        np.testing.assert_array_equal(l2, ref.level2_bytes())
+        refs.append((res.num_pairs, res.num_boundary))
+        ctx.release(res)
+    assert refs[0] == refs[1] == refs[2]  # identical sizes: the graphs were replayed
