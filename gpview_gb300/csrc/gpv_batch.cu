@@ -256,7 +256,6 @@ int run_batch(gpv_ctx *ctx, int n, const float *const *d_tris, const int64_t *T,
   host_parallel_for(n, [&](int m) { pack_tables(gh[m], ctx->h_tables + tab_off[m]); });
   float *d_tab;
   CK(ws.get(&d_tab, (size_t)tab_off[n]));
-  CK(cudaMemcpyAsync(d_tab, ctx->h_tables, tab_off[n] * sizeof(float), cudaMemcpyHostToDevice, s));
 
   float4 *ptri, *fbox;
   int4 *rng;
@@ -287,14 +286,8 @@ int run_batch(gpv_ctx *ctx, int n, const float *const *d_tris, const int64_t *T,
   }
   CK(ws.get(&stats, (size_t)n));
   CK(ws.get(&d_md, (size_t)n));
-  CK(cudaMemsetAsync(stats, 0, n * sizeof(MeshStats), s));
-  CK(cudaMemsetAsync(bplane, 0, words * 4, s));
-  CK(cudaMemsetAsync(toggles, 0, togg * 4, s));
   uint32_t *stg = nullptr;  // stencil fill: Level1 sample-column toggles
-  if (stencil) {
-    CK(ws.get(&stg, (size_t)stgw));
-    CK(cudaMemsetAsync(stg, 0, stgw * 4, s));
-  }
+  if (stencil) CK(ws.get(&stg, (size_t)stgw));
   float4 *fnorm = nullptr;
   if (nmode) CK(ws.get(&fnorm, (size_t)std::max<int64_t>(tris, 1)));
 
@@ -353,7 +346,6 @@ int run_batch(gpv_ctx *ctx, int n, const float *const *d_tris, const int64_t *T,
   bd.stp_words = 0;
   CK(ctx_ensure_host(ctx, (size_t)n));
   std::memcpy(ctx->h_md, md.data(), n * sizeof(MeshDesc));
-  CK(cudaMemcpyAsync(d_md, ctx->h_md, n * sizeof(MeshDesc), cudaMemcpyHostToDevice, s));
 
   bool capturing = false;
   auto mark = [&](int i) {
@@ -399,9 +391,21 @@ int run_batch(gpv_ctx *ctx, int n, const float *const *d_tris, const int64_t *T,
                      (uint64_t)(uintptr_t)wcnt, (uint64_t)(uintptr_t)wpre, (uint64_t)(uintptr_t)wtot,
                      (uint64_t)(uintptr_t)stmp, (uint64_t)(uintptr_t)d_slab,
                      (uint64_t)(d_slab ? (int64_t)gh[0].n[1] * gh[0].nxw : 0),
-                     (uint64_t)(d_slab ? gh[0].n[2] : 0), (uint64_t)fz, (uint64_t)fslab})
+                     (uint64_t)(d_slab ? gh[0].n[2] : 0), (uint64_t)fz, (uint64_t)fslab,
+                     (uint64_t)(uintptr_t)d_tab, (uint64_t)(uintptr_t)ctx->h_tables,
+                     (uint64_t)tab_off[n], (uint64_t)(uintptr_t)ctx->h_md,
+                     (uint64_t)(uintptr_t)ctx->h_stats, (uint64_t)(uintptr_t)ctx->h_u32,
+                     (uint64_t)(uintptr_t)stats, (uint64_t)(uintptr_t)toggles, (uint64_t)togg,
+                     (uint64_t)(uintptr_t)stg, (uint64_t)stgw})
     sig0.push_back(x);
   CK(run_phase(ctx, 0, s, capturing, [&] {
+    // this call's tables and descriptors in (from page-locked staging), the accumulators cleared
+    cudaMemcpyAsync(d_tab, ctx->h_tables, tab_off[n] * sizeof(float), cudaMemcpyHostToDevice, s);
+    cudaMemcpyAsync(d_md, ctx->h_md, n * sizeof(MeshDesc), cudaMemcpyHostToDevice, s);
+    cudaMemsetAsync(stats, 0, n * sizeof(MeshStats), s);
+    cudaMemsetAsync(bplane, 0, words * 4, s);
+    cudaMemsetAsync(toggles, 0, togg * 4, s);
+    if (stg) cudaMemsetAsync(stg, 0, stgw * 4, s);
     mark(0);
     launch_prep(bd, s);
     mark(1);
@@ -418,9 +422,9 @@ int run_batch(gpv_ctx *ctx, int n, const float *const *d_tris, const int64_t *T,
       launch_slab_offsets(wpre, wtot, (int64_t)gh[0].n[1] * gh[0].nxw, gh[0].n[2], fz, fslab,
                           d_slab, s);
     mark(4);
+    if (d_slab) cudaMemcpyAsync(ctx->h_u32 + 4, d_slab, 4 * (fslab + 1), cudaMemcpyDeviceToHost, s);
+    cudaMemcpyAsync(ctx->h_stats, stats, n * sizeof(MeshStats), cudaMemcpyDeviceToHost, s);
   }, true, &sig0));
-  if (d_slab) CK(cudaMemcpyAsync(ctx->h_u32 + 4, d_slab, 4 * (fslab + 1), cudaMemcpyDeviceToHost, s));
-  CK(cudaMemcpyAsync(ctx->h_stats, stats, n * sizeof(MeshStats), cudaMemcpyDeviceToHost, s));
   CK(cudaStreamSynchronize(s));
   ht[2] = HClock::now();
   {
@@ -494,7 +498,6 @@ int run_batch(gpv_ctx *ctx, int n, const float *const *d_tris, const int64_t *T,
     stb[m + 1] = stb[m] + nt;
   }
   std::memcpy(ctx->h_md, md.data(), n * sizeof(MeshDesc));
-  CK(cudaMemcpyAsync(d_md, ctx->h_md, n * sizeof(MeshDesc), cudaMemcpyHostToDevice, s));
 
   // ---- phase C: allocations and uploads first, then the recorded launch sequence
   const int64_t ntiles = (int64_t)st_host.size();
@@ -521,8 +524,6 @@ int run_batch(gpv_ctx *ctx, int n, const float *const *d_tris, const int64_t *T,
         if (gh[m].level2) bd.stp_words = std::max(bd.stp_words, (4 * gh[m].n2[0] * gh[m].n2[1] + 31) / 32);
       CK(ws.get(&bd.stp, (size_t)std::max<int64_t>(ub, 1) * bd.stp_words));
     }
-    CK(cudaMemcpyAsync(d_tiles, ctx->h_tiles, ntiles * sizeof(SortTile), cudaMemcpyHostToDevice, s));
-    CK(cudaMemcpyAsync(d_tb, ctx->h_tb, (n + 1) * sizeof(int64_t), cudaMemcpyHostToDevice, s));
   }
   ht[3] = HClock::now();
   // host outputs: Level1 arrays copied as soon as the expansion has written them, Level2 slab by
@@ -577,9 +578,19 @@ int run_batch(gpv_ctx *ctx, int n, const float *const *d_tris, const int64_t *T,
                      (uint64_t)(uintptr_t)(sink ? sink->prefix : nullptr),
                      (uint64_t)(uintptr_t)(sink ? sink->bindex : nullptr), (uint64_t)gh[0].N1,
                      (uint64_t)Btot, (uint64_t)(uintptr_t)set->l1, (uint64_t)(uintptr_t)set->prefix,
-                     (uint64_t)(uintptr_t)set->bindex, (uint64_t)(uintptr_t)cs, (uint64_t)l2_queue})
+                     (uint64_t)(uintptr_t)set->bindex, (uint64_t)(uintptr_t)cs, (uint64_t)l2_queue,
+                     (uint64_t)n, (uint64_t)(uintptr_t)d_md, (uint64_t)(uintptr_t)ctx->h_md,
+                     (uint64_t)(uintptr_t)ctx->h_tiles, (uint64_t)(uintptr_t)ctx->h_tb,
+                     (uint64_t)(uintptr_t)stats, (uint64_t)(uintptr_t)ctx->h_stats,
+                     (uint64_t)(uintptr_t)ctx->h_u32})
     sig1.push_back(x);
   CK(run_phase(ctx, 1, s, capturing, [&] {
+    // the descriptors with their output bases, and the sort tiles, in from page-locked staging
+    cudaMemcpyAsync(d_md, ctx->h_md, n * sizeof(MeshDesc), cudaMemcpyHostToDevice, s);
+    if (do_l2) {
+      cudaMemcpyAsync(d_tiles, ctx->h_tiles, ntiles * sizeof(SortTile), cudaMemcpyHostToDevice, s);
+      cudaMemcpyAsync(d_tb, ctx->h_tb, (n + 1) * sizeof(int64_t), cudaMemcpyHostToDevice, s);
+    }
     mark(5);
     launch_expand(bd, wpre, s);
     if (sink) {
@@ -631,9 +642,9 @@ int run_batch(gpv_ctx *ctx, int n, const float *const *d_tris, const int64_t *T,
       cudaEventRecord(ctx->cev[kMaxSlabs + 1], cs);
       cudaStreamWaitEvent(s, ctx->cev[kMaxSlabs + 1], 0);
     }
+    cudaMemcpyAsync(ctx->h_stats, stats, n * sizeof(MeshStats), cudaMemcpyDeviceToHost, s);
+    cudaMemcpyAsync(ctx->h_u32, wtot, 8, cudaMemcpyDeviceToHost, s);
   }, phase1_graph, any_hier ? nullptr : &sig1));
-  CK(cudaMemcpyAsync(ctx->h_stats, stats, n * sizeof(MeshStats), cudaMemcpyDeviceToHost, s));
-  CK(cudaMemcpyAsync(ctx->h_u32, wtot, 8, cudaMemcpyDeviceToHost, s));
   CK(cudaStreamSynchronize(s));
   ht[4] = HClock::now();
   if (ctx->timing) {
