@@ -289,7 +289,8 @@ __device__ __forceinline__ void write_block_vec(uint8_t *out, const uint32_t *sa
       nin += (unsigned)__popc(inf);
       o[k] = sf * 254u + inf * 127u;  // flags are 0/1 per byte and disjoint: no carries
     }
-    *reinterpret_cast<uint4 *>(out + byte0) = make_uint4(o[0], o[1], o[2], o[3]);
+    // streaming store: the output is not read again, so it should not displace the working set
+    __stcs(reinterpret_cast<uint4 *>(out + byte0), make_uint4(o[0], o[1], o[2], o[3]));
   }
 }
 
@@ -1043,7 +1044,8 @@ __global__ void __launch_bounds__(kWarps * 32, QUEUE ? 6 : 7) k_level2c(
       nin += (unsigned)__popc(ib);
       uint8_t *o = out + pq;
       for (int r = 0; r < n2z; ++r)
-        o[(size_t)r * ncol2] = ((sb >> r) & 1u) ? (uint8_t)254 : (((ib >> r) & 1u) ? (uint8_t)127 : (uint8_t)0);
+        __stcs(reinterpret_cast<char *>(o + (size_t)r * ncol2),
+               (char)(((sb >> r) & 1u) ? 254 : (((ib >> r) & 1u) ? 127 : 0)));
     }
     __syncwarp();
   }
