@@ -298,3 +298,47 @@ def test_gpu_stencil_batch_equals_alone(ctx):
         np.testing.assert_array_equal(l1, ref.level1_bytes())
         np.testing.assert_array_equal(l2, (ref.level2_state()[0] * 127).astype(np.uint8))
         ctx.release(r)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("slabs", [0, 3])
+def test_gpu_stencil_with_normals_and_hierarchy_to_host(ctx, slabs):
+    """Stencil fill with normals and the box hierarchy switched on, host to host (Level2 written
+    straight into page-locked memory, or copied per z slab): every output equals the oracle's."""
+    import gpview_gb300 as gpv
+    torch = pytest.importorskip("torch")
+
+    tris = gpv.gen_torus(23, 128, 64, (0.5, 0.5, 0.5), 0.3, 0.1, 0.006)
+    spec = gpv.grid_padded(*gpv.mesh_bounds(tris), 32, 4)
+    ref = orc.Run(tris, spec, fill=orc.FILL_STENCIL)
+    n1, cells = 32 ** 3, 4 ** 3
+    h_tris = torch.from_numpy(tris).pin_memory()
+    l1 = torch.empty(n1, dtype=torch.uint8).pin_memory()
+    pre = torch.empty(n1, dtype=torch.int32).pin_memory()
+    bi = torch.empty(ref.B, dtype=torch.int32).pin_memory()
+    l2 = torch.empty(ref.B * cells, dtype=torch.uint8).pin_memory()
+    ctx.set_fill(gpv.FILL_STENCIL)
+    ctx.set_normals(gpv.NORMALS_FLOAT)
+    ctx.set_hierarchy(True)
+    try:
+        rc, res = ctx.voxelize_to_host(h_tris.data_ptr(), tris.size // 9, spec, l1.data_ptr(),
+                                       pre.data_ptr(), bi.data_ptr(), l2.data_ptr(),
+                                       ref.B * cells, slabs)
+    finally:
+        ctx.set_fill(gpv.FILL_RAY)
+        ctx.set_normals(gpv.NORMALS_OFF)
+        ctx.set_hierarchy(False)
+    assert rc == 0 and res.num_boundary == ref.B
+    np.testing.assert_array_equal(l1.numpy(), ref.level1_bytes())
+    np.testing.assert_array_equal(pre.numpy(), ref.prefix())
+    np.testing.assert_array_equal(bi.numpy(), ref.boundary_index())
+    np.testing.assert_array_equal(l2.numpy(), ref.level2_bytes())
+    m1, m2 = ctx.fetch_normals(res)
+    np.testing.assert_array_equal(m1, ref.level1_normals())
+    np.testing.assert_array_equal(m2, ref.level2_normals())
+    lv, want = ref.hierarchy()
+    h = ctx.fetch_hierarchy(res)
+    assert res.hierarchy_levels == lv
+    for f in ("mid", "half", "solid", "child1", "child2", "index"):
+        np.testing.assert_array_equal(h[f], want[f], err_msg=f)
+    ctx.release(res)
