@@ -399,13 +399,16 @@ int run_batch(gpv_ctx *ctx, int n, const float *const *d_tris, const int64_t *T,
                      (uint64_t)(uintptr_t)stg, (uint64_t)stgw})
     sig0.push_back(x);
   CK(run_phase(ctx, 0, s, capturing, [&] {
-    // this call's tables and descriptors in (from page-locked staging), the accumulators cleared
-    cudaMemcpyAsync(d_tab, ctx->h_tables, tab_off[n] * sizeof(float), cudaMemcpyHostToDevice, s);
-    cudaMemcpyAsync(d_md, ctx->h_md, n * sizeof(MeshDesc), cudaMemcpyHostToDevice, s);
-    cudaMemsetAsync(stats, 0, n * sizeof(MeshStats), s);
-    cudaMemsetAsync(bplane, 0, words * 4, s);
-    cudaMemsetAsync(toggles, 0, togg * 4, s);
-    if (stg) cudaMemsetAsync(stg, 0, stgw * 4, s);
+    // this call's tables and descriptors in (read from page-locked staging), the accumulators
+    // cleared: one kernel
+    StageList in(ctx->num_sms, s);
+    in.copy(d_tab, ctx->h_tables, tab_off[n] * sizeof(float));
+    in.copy(d_md, ctx->h_md, n * sizeof(MeshDesc));
+    in.clear(stats, n * sizeof(MeshStats));
+    in.clear(bplane, words * 4);
+    in.clear(toggles, togg * 4);
+    if (stg) in.clear(stg, stgw * 4);
+    in.launch();
     mark(0);
     launch_prep(bd, s);
     mark(1);
@@ -422,8 +425,11 @@ int run_batch(gpv_ctx *ctx, int n, const float *const *d_tris, const int64_t *T,
       launch_slab_offsets(wpre, wtot, (int64_t)gh[0].n[1] * gh[0].nxw, gh[0].n[2], fz, fslab,
                           d_slab, s);
     mark(4);
-    if (d_slab) cudaMemcpyAsync(ctx->h_u32 + 4, d_slab, 4 * (fslab + 1), cudaMemcpyDeviceToHost, s);
-    cudaMemcpyAsync(ctx->h_stats, stats, n * sizeof(MeshStats), cudaMemcpyDeviceToHost, s);
+    // counts out, written straight into page-locked staging
+    StageList out(ctx->num_sms, s);
+    if (d_slab) out.copy(ctx->h_u32 + 4, d_slab, 4 * (fslab + 1));
+    out.copy(ctx->h_stats, stats, n * sizeof(MeshStats));
+    out.launch();
   }, true, &sig0));
   CK(cudaStreamSynchronize(s));
   ht[2] = HClock::now();
@@ -585,12 +591,14 @@ int run_batch(gpv_ctx *ctx, int n, const float *const *d_tris, const int64_t *T,
                      (uint64_t)(uintptr_t)ctx->h_u32})
     sig1.push_back(x);
   CK(run_phase(ctx, 1, s, capturing, [&] {
-    // the descriptors with their output bases, and the sort tiles, in from page-locked staging
-    cudaMemcpyAsync(d_md, ctx->h_md, n * sizeof(MeshDesc), cudaMemcpyHostToDevice, s);
+    // the descriptors with their output bases, and the sort tiles, read from page-locked staging
+    StageList in(ctx->num_sms, s);
+    in.copy(d_md, ctx->h_md, n * sizeof(MeshDesc));
     if (do_l2) {
-      cudaMemcpyAsync(d_tiles, ctx->h_tiles, ntiles * sizeof(SortTile), cudaMemcpyHostToDevice, s);
-      cudaMemcpyAsync(d_tb, ctx->h_tb, (n + 1) * sizeof(int64_t), cudaMemcpyHostToDevice, s);
+      in.copy(d_tiles, ctx->h_tiles, ntiles * sizeof(SortTile));
+      in.copy(d_tb, ctx->h_tb, (n + 1) * sizeof(int64_t));
     }
+    in.launch();
     mark(5);
     launch_expand(bd, wpre, s);
     if (sink) {
@@ -642,8 +650,10 @@ int run_batch(gpv_ctx *ctx, int n, const float *const *d_tris, const int64_t *T,
       cudaEventRecord(ctx->cev[kMaxSlabs + 1], cs);
       cudaStreamWaitEvent(s, ctx->cev[kMaxSlabs + 1], 0);
     }
-    cudaMemcpyAsync(ctx->h_stats, stats, n * sizeof(MeshStats), cudaMemcpyDeviceToHost, s);
-    cudaMemcpyAsync(ctx->h_u32, wtot, 8, cudaMemcpyDeviceToHost, s);
+    StageList out(ctx->num_sms, s);
+    out.copy(ctx->h_stats, stats, n * sizeof(MeshStats));
+    out.copy(ctx->h_u32, wtot, 8);
+    out.launch();
   }, phase1_graph, any_hier ? nullptr : &sig1));
   CK(cudaStreamSynchronize(s));
   ht[4] = HClock::now();

@@ -88,6 +88,35 @@ struct BatchDev {
   int stp_words;         //   column's triangles recorded only below it (stp_words words each)
 };
 
+// Small copies and clears around a phase, done by one kernel instead of copy-engine and memset
+// nodes, so a recorded phase is kernels only.  Every address must be device-accessible: device
+// memory, or page-locked host memory (cudaMallocHost), which unified addressing maps at the same
+// address.  The operations of one list run concurrently: none may read what another writes.
+// Sizes that are not a multiple of 4 bytes go to cudaMemcpyAsync / cudaMemsetAsync instead.
+struct StageOp {
+  const uint32_t *src;  // nullptr: clear dst
+  uint32_t *dst;
+  int64_t words;
+};
+struct StageOps {
+  static constexpr int kMax = 8;
+  StageOp op[kMax];
+  int n;
+};
+class StageList {
+ public:
+  StageList(int num_sms, cudaStream_t s) : sms_(num_sms), s_(s) { ops_.n = 0; }
+  void copy(void *dst, const void *src, size_t bytes) { add(dst, src, bytes); }
+  void clear(void *dst, size_t bytes) { add(dst, nullptr, bytes); }
+  void launch();  // runs the queued operations (one kernel) and empties the list
+
+ private:
+  void add(void *dst, const void *src, size_t bytes);
+  StageOps ops_;
+  int sms_;
+  cudaStream_t s_;
+};
+
 void launch_prep(const BatchDev &bd, cudaStream_t s);
 // Boundary rank at each z-slab start of a single mesh (nslab + 1 values into out).
 void launch_slab_offsets(const uint32_t *wpre, const uint32_t *wtot, int64_t words_per_layer,

@@ -634,6 +634,34 @@ __global__ void k_useg(const uint32_t *__restrict__ flags, const uint32_t *__res
   if (e == P - 1) useg[uidx[e] + flags[e]] = (uint32_t)P;
 }
 
+// Copies and clears of StageOps (see StageList): 16-byte accesses where both addresses allow,
+// 4-byte ones otherwise.  Sources are read with cache-volatile loads: page-locked host staging is
+// rewritten by the host between launches.
+__global__ void __launch_bounds__(256) k_stage(StageOps L) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  for (int k = 0; k < L.n; ++k) {
+    const uint32_t *src = L.op[k].src;
+    uint32_t *dst = L.op[k].dst;
+    const int64_t w = L.op[k].words;
+    int64_t i0 = 0;
+    if (((reinterpret_cast<uintptr_t>(src) | reinterpret_cast<uintptr_t>(dst)) & 15u) == 0) {
+      const int64_t w4 = w >> 2;
+      uint4 *d4 = reinterpret_cast<uint4 *>(dst);
+      const uint4 *s4 = reinterpret_cast<const uint4 *>(src);
+      if (src)
+        for (int64_t i = t; i < w4; i += stride) d4[i] = __ldcv(s4 + i);
+      else
+        for (int64_t i = t; i < w4; i += stride) d4[i] = make_uint4(0u, 0u, 0u, 0u);
+      i0 = w4 << 2;
+    }
+    if (src)
+      for (int64_t i = i0 + t; i < w; i += stride) dst[i] = __ldcv(src + i);
+    else
+      for (int64_t i = i0 + t; i < w; i += stride) dst[i] = 0u;
+  }
+}
+
 }  // namespace
 
 // ---- launchers --------------------------------------------------------------------------------
@@ -658,6 +686,30 @@ void launch_slab_offsets(const uint32_t *wpre, const uint32_t *wtot, int64_t wor
                          int nz, int zslab, int nslab, uint32_t *out, cudaStream_t s) {
   k_slab_offsets<<<1, 32, 0, s>>>(wpre, wtot, words_per_layer, nz, zslab, nslab, out);
   count_launch();
+}
+
+void StageList::add(void *dst, const void *src, size_t bytes) {
+  if (bytes == 0) return;
+  if (bytes & 3u) {
+    if (src)
+      cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDefault, s_);
+    else
+      cudaMemsetAsync(dst, 0, bytes, s_);
+    return;
+  }
+  if (ops_.n == StageOps::kMax) launch();
+  ops_.op[ops_.n++] = {static_cast<const uint32_t *>(src), static_cast<uint32_t *>(dst),
+                       (int64_t)(bytes / 4)};
+}
+
+void StageList::launch() {
+  if (ops_.n == 0) return;
+  int64_t w = 0;
+  for (int k = 0; k < ops_.n; ++k) w = std::max(w, ops_.op[k].words);
+  const int64_t blocks = std::min<int64_t>((w / 4 + 255) / 256 + 1, 2 * (int64_t)sms_);
+  k_stage<<<(unsigned)blocks, 256, 0, s_>>>(ops_);
+  count_launch();
+  ops_.n = 0;
 }
 
 void launch_pair_bases(const BatchDev &bd, MeshDesc *d_md, uint32_t *keys, uint32_t *vals,
