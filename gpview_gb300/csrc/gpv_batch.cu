@@ -265,13 +265,20 @@ int run_batch(gpv_ctx *ctx, int n, const float *const *d_tris, const int64_t *T,
   CK(ws.get(&ptri, 3 * (size_t)std::max<int64_t>(tris, 1)));
   CK(ws.get(&rng, (size_t)std::max<int64_t>(tris, 1)));
   CK(ws.get(&fbox, (size_t)std::max<int64_t>(tris, 1)));
-  CK(ws.get(&bplane, (size_t)words));
+  // without normals the pair lists are built by a counting sort, which ranks the voxels of the
+  // pairs through a second, column-major bit plane after the boundary plane; one popcount and one
+  // scan cover both planes
+  const bool kmark = nmode == 0 && words > 0;
+  const int64_t swords = kmark ? 2 * words : words;
+  CK(ws.get(&bplane, (size_t)swords));
   CK(ws.get(&iplane, (size_t)words));
   CK(ws.get(&toggles, (size_t)togg));
-  CK(ws.get(&wcnt, (size_t)words));
-  CK(ws.get(&wpre, (size_t)words));
+  CK(ws.get(&wcnt, (size_t)swords));
+  CK(ws.get(&wpre, (size_t)swords));
   CK(ws.get(&wtot, 4));
-  CK(ws.get(&stmp, (size_t)scan_temp_words(words)));
+  CK(ws.get(&stmp, (size_t)scan_temp_words(swords)));
+  // the boundary-voxel total: past the boundary plane's words in the prefix when both are scanned
+  const uint32_t *btot = kmark ? wpre + words : wtot;
   CK(ws.get(&queue, 16));  // [0] Level1 tickets, [1 + k] Level2 tickets of slab k
   // z slabs of the Level2 launch when the outputs go to the host (one mesh): the boundary ranks
   // at up to kMaxSlabs fine slab starts are read with the first phase's counts; the launch then
@@ -344,6 +351,7 @@ int run_batch(gpv_ctx *ctx, int n, const float *const *d_tris, const int64_t *T,
   bd.fill = ctx->fill;
   bd.stp = nullptr;
   bd.stp_words = 0;
+  bd.kmask = kmark ? bplane + words : nullptr;
   CK(ctx_ensure_host(ctx, (size_t)n));
   std::memcpy(ctx->h_md, md.data(), n * sizeof(MeshDesc));
 
@@ -405,7 +413,7 @@ int run_batch(gpv_ctx *ctx, int n, const float *const *d_tris, const int64_t *T,
     in.copy(d_tab, ctx->h_tables, tab_off[n] * sizeof(float));
     in.copy(d_md, ctx->h_md, n * sizeof(MeshDesc));
     in.clear(stats, n * sizeof(MeshStats));
-    in.clear(bplane, words * 4);
+    in.clear(bplane, swords * 4);
     in.clear(toggles, togg * 4);
     if (stg) in.clear(stg, stgw * 4);
     in.launch();
@@ -418,11 +426,11 @@ int run_batch(gpv_ctx *ctx, int n, const float *const *d_tris, const int64_t *T,
     if (stencil) launch_stencil1(bd, s);
     mark(3);
     launch_fill_finish(bd, s);
-    launch_popc(bplane, words, wcnt, s);
-    scan_u32(wcnt, wpre, words, wtot, stmp, s);
-    launch_boundary_counts(bd, wpre, wtot, s);
+    launch_popc(bplane, swords, wcnt, s);
+    scan_u32(wcnt, wpre, swords, wtot, stmp, s);
+    launch_boundary_counts(bd, wpre, btot, s);
     if (d_slab)
-      launch_slab_offsets(wpre, wtot, (int64_t)gh[0].n[1] * gh[0].nxw, gh[0].n[2], fz, fslab,
+      launch_slab_offsets(wpre, btot, (int64_t)gh[0].n[1] * gh[0].nxw, gh[0].n[2], fz, fslab,
                           d_slab, s);
     mark(4);
     // counts out, written straight into page-locked staging
@@ -508,6 +516,7 @@ int run_batch(gpv_ctx *ctx, int n, const float *const *d_tris, const int64_t *T,
   // ---- phase C: allocations and uploads first, then the recorded launch sequence
   const int64_t ntiles = (int64_t)st_host.size();
   const bool do_l2 = (any_l2 || nmode) && ntiles > 0;  // sort + lists (+ Level2, normals)
+  const bool csort = do_l2 && kmark;                   // lists by the counting sort
   SortTile *d_tiles = nullptr;
   int64_t *d_tb = nullptr;
   uint32_t *kalt = nullptr, *valt = nullptr, *flags = nullptr, *uidx = nullptr, *useg = nullptr,
@@ -520,10 +529,11 @@ int run_batch(gpv_ctx *ctx, int n, const float *const *d_tris, const int64_t *T,
     CK(ws.get(&d_tb, (size_t)n + 1));
     CK(ws.get(&kalt, (size_t)std::max<int64_t>(P2, 1)));
     CK(ws.get(&valt, (size_t)std::max<int64_t>(P2, 1)));
-    CK(ws.get(&flags, (size_t)P2));
+    CK(ws.get(&flags, (size_t)std::max<int64_t>(P2, ub)));  // the counting sort's counts too
     CK(ws.get(&uidx, (size_t)P2));
     CK(ws.get(&useg, (size_t)ub + 1));
-    CK(ws.get(&sortmp, (size_t)std::max(sort_seg_temp_words(ntiles), scan_temp_words(P2))));
+    CK(ws.get(&sortmp, (size_t)std::max({sort_seg_temp_words(ntiles), scan_temp_words(P2),
+                                         scan_temp_words(ub)})));
     CK(ws.get(&l2tmp, (size_t)level2_temp_words(ub)));
     if (stencil && any_l2) {  // per boundary voxel: the column prefix of sample coverage
       for (int m = 0; m < n; ++m)
@@ -598,6 +608,10 @@ int run_batch(gpv_ctx *ctx, int n, const float *const *d_tris, const int64_t *T,
       in.copy(d_tiles, ctx->h_tiles, ntiles * sizeof(SortTile));
       in.copy(d_tb, ctx->h_tb, (n + 1) * sizeof(int64_t));
     }
+    if (csort) {
+      in.clear(flags, ub * 4);  // the voxel counts
+      in.clear(wtot + 1, 4);    // voxels completed
+    }
     in.launch();
     mark(5);
     launch_expand(bd, wpre, s);
@@ -615,13 +629,21 @@ int run_batch(gpv_ctx *ctx, int n, const float *const *d_tris, const int64_t *T,
         launch_hierarchy(md[m].g, md[m].iplane, static_cast<gpv_box *>(set->hier) + res_hier[m], s);
     mark(6);
     if (do_l2) {
-      const bool in_alt = sort_pairs_seg(bd, d_tiles, d_tb, ntiles, keys, vals, kalt, valt, P2,
-                                         max_keybits, nmode ? val_bits : 0, sortmp, s);
-      const uint32_t *sk = in_alt ? kalt : keys;
-      const uint32_t *sv = in_alt ? valt : vals;
-      launch_heads(sk, P2, flags, bd, s);
-      scan_u32(flags, uidx, P2, wtot + 1, sortmp, s);
-      launch_useg(flags, uidx, P2, useg, s);
+      const uint32_t *sk = kalt, *sv = valt;
+      if (csort) {
+        // lists in any triangle order: counting sort by voxel rank, segment starts from its scan
+        count_sort_pairs(bd, d_tiles, ntiles, keys, vals, wpre + words, ub, P2, flags, useg, kalt,
+                         valt, wtot + 1, sortmp, s);
+      } else {
+        // normals sum in ascending triangle order: radix sort by (voxel, triangle)
+        const bool in_alt = sort_pairs_seg(bd, d_tiles, d_tb, ntiles, keys, vals, kalt, valt, P2,
+                                           max_keybits, nmode ? val_bits : 0, sortmp, s);
+        sk = in_alt ? kalt : keys;
+        sv = in_alt ? valt : vals;
+        launch_heads(sk, P2, flags, bd, s);
+        scan_u32(flags, uidx, P2, wtot + 1, sortmp, s);
+        launch_useg(flags, uidx, P2, useg, s);
+      }
       mark(7);
       if (any_l2)
         launch_level2(bd, sk, sv, useg, ub, l2tmp, warp_words, ctx->num_sms, s, [&] { mark(9); },

@@ -86,6 +86,9 @@ struct BatchDev {
   int fill;              // GPV_FILL_* of this batch
   uint32_t *stp;         // stencil fill: per boundary voxel, the sample-coverage parity of the
   int stp_words;         //   column's triangles recorded only below it (stp_words words each)
+  // Level1 marks the voxel of every pair it emits for a mesh with a Level2 grid here: one
+  // column-major bit plane per mesh (bit = pair key) at the mesh's word_base; nullptr: no marks
+  uint32_t *kmask = nullptr;
 };
 
 // Small copies and clears around a phase, done by one kernel instead of copy-engine and memset
@@ -143,6 +146,16 @@ struct SortTile { int32_t mesh, j, count, pad; };
 int64_t sort_seg_temp_words(int64_t ntiles);
 // Returns true when the sorted data ended in (kalt, valt).  tiles[] (device) lists the tiles of
 // every mesh; hist_base[m] = 256 * (tiles before mesh m) (device).
+// Counting sort of the emitted pairs by voxel, for lists whose triangle order does not matter
+// (no normals): the rank of a pair's voxel among the marked voxels in key order comes from
+// bd.kmask and its exclusive word prefix kpre (global over all meshes: kpre[0] is subtracted), so
+// one count, one scan and one scatter give the dense (kout, vout) lists and the segment starts
+// useg[0..nseg] directly.  done receives the number of voxels whose last pair was placed (nseg
+// when the marks and the pairs agree); cnt (nseg words) must be zero and is left zero.
+void count_sort_pairs(const BatchDev &bd, const SortTile *tiles, int64_t ntiles,
+                      const uint32_t *keys, const uint32_t *vals, const uint32_t *kpre,
+                      int64_t nseg, int64_t P, uint32_t *cnt, uint32_t *useg, uint32_t *kout,
+                      uint32_t *vout, uint32_t *done, uint32_t *temp, cudaStream_t s);
 bool sort_pairs_seg(const BatchDev &bd, const SortTile *tiles, const int64_t *tile_base_dev,
                     int64_t ntiles, uint32_t *keys, uint32_t *vals, uint32_t *kalt, uint32_t *valt,
                     int64_t Ptotal, int key_bits, int val_bits, uint32_t *temp, cudaStream_t s);

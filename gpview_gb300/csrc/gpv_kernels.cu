@@ -328,6 +328,7 @@ __global__ void __launch_bounds__(kL1Threads) k_level1(BatchDev bd) {
     const MeshDesc &d = bd.md[m];
     const GridDev &g = d.g;
     const int64_t t0 = (item - d.tile_base) * TILE;
+    uint32_t *const kmask = bd.kmask && d.has_l2 ? bd.kmask + d.word_base : nullptr;
     const int nt = (int)min((int64_t)TILE, d.T - t0);
 
     // ---- stage the tile with bulk async copies completing on the mbarrier
@@ -419,12 +420,14 @@ __global__ void __launch_bounds__(kL1Threads) k_level1(BatchDev bd) {
           const int dd = __ffs(mask) - 1;
           mask &= mask - 1u;
           const int r = ztop - dd;
+          const uint32_t key = (uint32_t)(((uint64_t)q * nx + p) * nz + r);
           if (pos < cap) {
-            d.keys[pos] = (uint32_t)(((uint64_t)q * nx + p) * nz + r);
+            d.keys[pos] = key;
             d.vals[pos] = tglob | (first ? 0x80000000u : 0u);
           } else {
             atomicOr(&d.stats->status, (unsigned)ST_PAIR_OVERFLOW);
           }
+          if (kmask) atomicOr(kmask + (key >> 5), 1u << (key & 31u));
           first = false;
           ++pos;
           atomicOr(&d.bplane[((size_t)r * ny + q) * g.nxw + (p >> 5)], 1u << (p & 31));

@@ -363,6 +363,63 @@ int64_t sort_seg_temp_words(int64_t ntiles) {
   return 2 * 256 * ntiles + scan_temp_words(256 * ntiles) + 4;
 }
 
+// ---- counting sort by voxel (lists without triangle order) -----------------------------------
+// Rank of a pair's voxel among the marked voxels of all meshes in key order; nseg past the end
+// when the marks do not hold the key (a broken invariant: the pair is then skipped).
+__device__ __forceinline__ uint32_t cs_rank(const BatchDev &bd, const MeshDesc &d,
+                                            const uint32_t *__restrict__ kpre, uint32_t key,
+                                            int64_t nseg) {
+  const int64_t w = d.word_base + (key >> 5);
+  const uint32_t word = bd.kmask[w], bit = 1u << (key & 31u);
+  if (!(word & bit)) return (uint32_t)nseg;
+  return kpre[w] - kpre[0] + __popc(word & (bit - 1u));
+}
+
+__global__ void __launch_bounds__(kSortThreads) k_cs_count(BatchDev bd,
+                                                           const SortTile *__restrict__ tiles,
+                                                           const uint32_t *__restrict__ keys,
+                                                           const uint32_t *__restrict__ kpre,
+                                                           int64_t nseg, uint32_t *__restrict__ cnt) {
+  const SortTile st = tiles[blockIdx.x];
+  const MeshDesc &d = bd.md[st.mesh];
+  const int64_t in0 = d.emit_base + (int64_t)st.j * kSortTile;
+  for (int i = threadIdx.x; i < st.count; i += kSortThreads) {
+    const uint32_t g = cs_rank(bd, d, kpre, keys[in0 + i], nseg);
+    if (g < nseg) atomicAdd(cnt + g, 1u);
+  }
+}
+
+// Places each pair at its voxel's segment start + (pairs of the voxel still unplaced - 1), so the
+// counts return to zero; counts the voxels whose last pair this block placed.
+__global__ void __launch_bounds__(kSortThreads) k_cs_scatter(
+    BatchDev bd, const SortTile *__restrict__ tiles, const uint32_t *__restrict__ keys,
+    const uint32_t *__restrict__ vals, const uint32_t *__restrict__ kpre, int64_t nseg, int64_t P,
+    uint32_t *__restrict__ cnt, const uint32_t *__restrict__ useg, uint32_t *__restrict__ kout,
+    uint32_t *__restrict__ vout, uint32_t *__restrict__ done) {
+  __shared__ uint32_t s_done;
+  if (threadIdx.x == 0) s_done = 0;
+  __syncthreads();
+  const SortTile st = tiles[blockIdx.x];
+  const MeshDesc &d = bd.md[st.mesh];
+  const int64_t in0 = d.emit_base + (int64_t)st.j * kSortTile;
+  uint32_t fin = 0;
+  for (int i = threadIdx.x; i < st.count; i += kSortThreads) {
+    const uint32_t key = keys[in0 + i];
+    const uint32_t g = cs_rank(bd, d, kpre, key, nseg);
+    if (g >= nseg) continue;
+    const uint32_t left = atomicSub(cnt + g, 1u);
+    const int64_t pos = (int64_t)useg[g] + left - 1;
+    if (left == 0 || pos >= P) continue;
+    kout[pos] = key;
+    vout[pos] = vals[in0 + i];
+    fin += left == 1u;
+  }
+  fin = __reduce_add_sync(0xffffffffu, fin);
+  if ((threadIdx.x & 31u) == 0 && fin) atomicAdd(&s_done, fin);
+  __syncthreads();
+  if (threadIdx.x == 0 && s_done) atomicAdd(done, s_done);
+}
+
 bool sort_pairs_seg(const BatchDev &bd, const SortTile *tiles, const int64_t *tile_base_dev,
                     int64_t ntiles, uint32_t *keys, uint32_t *vals, uint32_t *kalt, uint32_t *valt,
                     int64_t Ptotal, int key_bits, int val_bits, uint32_t *temp, cudaStream_t s) {
@@ -395,6 +452,18 @@ bool sort_pairs_seg(const BatchDev &bd, const SortTile *tiles, const int64_t *ti
     alt = !alt;
   }
   return alt;
+}
+
+void count_sort_pairs(const BatchDev &bd, const SortTile *tiles, int64_t ntiles,
+                      const uint32_t *keys, const uint32_t *vals, const uint32_t *kpre,
+                      int64_t nseg, int64_t P, uint32_t *cnt, uint32_t *useg, uint32_t *kout,
+                      uint32_t *vout, uint32_t *done, uint32_t *temp, cudaStream_t s) {
+  if (P <= 0 || ntiles <= 0 || nseg <= 0) return;
+  k_cs_count<<<(unsigned)ntiles, kSortThreads, 0, s>>>(bd, tiles, keys, kpre, nseg, cnt);
+  scan_u32(cnt, useg, nseg, useg + nseg, temp, s);
+  k_cs_scatter<<<(unsigned)ntiles, kSortThreads, 0, s>>>(bd, tiles, keys, vals, kpre, nseg, P, cnt,
+                                                          useg, kout, vout, done);
+  count_launch(2);
 }
 
 }  // namespace gpv
