@@ -264,7 +264,8 @@ class Context:
     def error(self):
         return lib().gpv_last_error(self._h).decode()
 
-    STAGES = ("prep", "level1", "fill_finish", "expand", "sort_lists", "level2", "level2_kernel")
+    STAGES = ("prep", "level1", "fill_finish", "expand", "sort_lists", "level2", "level2_kernel",
+              "pair_bases", "between_phases")
 
     def set_timing(self, on=True):
         self._check(lib().gpv_set_timing(self._h, int(bool(on))), "set_timing")

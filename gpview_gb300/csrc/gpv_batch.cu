@@ -681,9 +681,10 @@ int run_batch(gpv_ctx *ctx, int n, const float *const *d_tris, const int64_t *T,
   ht[4] = HClock::now();
   if (ctx->timing) {
     // stages: 0 prep, 1 level1, 2 fill finish + boundary scan, 3 expand, 4 sort + lists,
-    // 5 level2 (work items + kernel), 6 the Level2 kernel alone
-    const int pr[7][2] = {{0, 1}, {2, 3}, {3, 4}, {5, 6}, {6, 7}, {7, 8}, {9, 8}};
-    for (int k = 0; k < 7; ++k) {
+    // 5 level2 (work items + kernel), 6 the Level2 kernel alone, 7 per-mesh pair bases,
+    // 8 between the phases (counts out, host planning, second launch, uploads in)
+    const int pr[9][2] = {{0, 1}, {2, 3}, {3, 4}, {5, 6}, {6, 7}, {7, 8}, {9, 8}, {1, 2}, {4, 5}};
+    for (int k = 0; k < 9; ++k) {
       float ms = 0.f;
       if (cudaEventElapsedTime(&ms, ctx->ev[pr[k][0]], ctx->ev[pr[k][1]]) == cudaSuccess)
         ctx->stage_ms[k] += ms;

@@ -167,7 +167,8 @@ int gpv_autotune(gpv_ctx *ctx, int32_t n, const float *const *d_tris, const int6
                  int32_t *level2_chunk, float *ms_per_batch);
 /* Per-stage CUDA-event timing on the launching stream (off by default).  Stages:
  * 0 prep, 1 Level1 SAT+fill, 2 fill finish + boundary scan, 3 Level1 expansion,
- * 4 pair sort + lists, 5 Level2 (work items + kernel), 6 the Level2 kernel alone.
+ * 4 pair sort + lists, 5 Level2 (work items + kernel), 6 the Level2 kernel alone, 7 per-mesh pair
+ * bases, 8 between the two phases (counts copied out, host planning, second launch, uploads in).
  * gpv_stage_times returns the number of timed calls and the accumulated milliseconds per stage
  * (up to 9 slots; unused slots stay 0). */
 int gpv_set_timing(gpv_ctx *ctx, int on);
