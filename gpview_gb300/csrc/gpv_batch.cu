@@ -231,7 +231,7 @@ int run_batch(gpv_ctx *ctx, int n, const float *const *d_tris, const int64_t *T,
     d.word_base = words;
     tris += T[m];
     tiles += (T[m] + tile - 1) / tile;
-    fwarps += (int64_t)g.n[1] * g.nxw;
+    fwarps += (int64_t)g.n[1] * g.nxw * g.nzw;
     rows += (int64_t)g.n[2] * g.n[1];
     words += (int64_t)g.n[2] * g.n[1] * g.nxw;
     togg += (int64_t)g.n[0] * g.n[1] * g.nzw;

@@ -63,7 +63,7 @@ struct MeshDesc {
   int64_t T, pair_cap;
   int64_t tri_base;      // prefix over meshes of triangles
   int64_t tile_base;     // ... of Level1 tiles
-  int64_t fwarp_base;    // ... of fill-finish warps (ny * nxw)
+  int64_t fwarp_base;    // ... of fill-finish warps (ny * nxw * nzw)
   int64_t row_base;      // ... of Level1 rows (nz * ny)
   int64_t word_base;     // ... of bit-plane words (nz * ny * nxw)
   int64_t emit_base;     // ... of pair capacities (emission segments)

@@ -489,8 +489,9 @@ __global__ void __launch_bounds__(kL1Threads) k_level1(BatchDev bd) {
 }
 
 // ---------------------------------------------------------------------------------------------
-// One warp per (mesh, row j, 32-column group): suffix XOR of each column's toggles gives the
-// parity of every voxel; 32 ballots per word transpose it into the linear inside plane.
+// One warp per (mesh, row j, 32-column group, 32-layer word w): suffix XOR of each column's
+// toggles gives the parity of every voxel (the toggles of the words above w give the carry); 32
+// ballots transpose the word into the linear inside plane.
 // Stencil fill: the parity of each of the voxel column's four sample columns is the prefix XOR
 // of its slice toggles (lowest slice first), and a voxel is inside where at least three of the
 // four are odd.
@@ -503,55 +504,60 @@ __global__ void __launch_bounds__(256) k_fill_finish(BatchDev bd) {
   const GridDev &g = d.g;
   const int64_t lw = gw - d.fwarp_base;
   const int nx = g.n[0], ny = g.n[1], nz = g.n[2];
-  const int j = (int)(lw / g.nxw), ig = (int)(lw % g.nxw);
+  const int w = (int)(lw % g.nzw);
+  const int64_t cgrp = lw / g.nzw;
+  const int j = (int)(cgrp / g.nxw), ig = (int)(cgrp % g.nxw);
   const int i = ig * 32 + (int)lane;
   const bool valid = i < nx;
   const size_t col = (size_t)j * nx + i;
   const bool stencil = bd.fill == GPV_FILL_STENCIL;
   const uint32_t *sc[4] = {nullptr, nullptr, nullptr, nullptr};
-  uint32_t tot = 0, above = 0;  // bit a: toggle parity of sample column a, in all / higher words
-  if (stencil && valid) {
-    const size_t SW = 2 * (size_t)nx;
-    sc[0] = d.stg + ((size_t)(2 * j) * SW + 2 * (size_t)i) * g.nzw;
-    sc[1] = sc[0] + g.nzw;
-    sc[2] = sc[0] + SW * g.nzw;
-    sc[3] = sc[2] + g.nzw;
-    for (int w = 0; w < g.nzw; ++w)
+  uint32_t s;
+  if (stencil) {
+    // bit a: toggle parity of sample column a in all words / in the words above w
+    uint32_t tot = 0, above = 0;
+    if (valid) {
+      const size_t SW = 2 * (size_t)nx;
+      sc[0] = d.stg + ((size_t)(2 * j) * SW + 2 * (size_t)i) * g.nzw;
+      sc[1] = sc[0] + g.nzw;
+      sc[2] = sc[0] + SW * g.nzw;
+      sc[3] = sc[2] + g.nzw;
+      for (int v = 0; v < g.nzw; ++v)
 #pragma unroll
-      for (int a = 0; a < 4; ++a) tot ^= (uint32_t)(__popc(sc[a][w]) & 1) << a;
-  }
-  uint32_t carry = 0;
-  for (int w = g.nzw - 1; w >= 0; --w) {
-    uint32_t s;
-    if (stencil) {
-      uint32_t x[4];
-#pragma unroll
-      for (int a = 0; a < 4; ++a) {
-        const uint32_t D = valid ? sc[a][w] : 0u;
-        const uint32_t pd = (uint32_t)(__popc(D) & 1);
-        uint32_t y = D;  // prefix XOR from the lowest slice of the word
-        y ^= y << 1; y ^= y << 2; y ^= y << 4; y ^= y << 8; y ^= y << 16;
-        if ((((tot ^ above) >> a) & 1u) ^ pd) y = ~y;  // odd toggles in the words below
-        above ^= pd << a;
-        x[a] = y;
-      }
-      s = (x[0] & x[1] & (x[2] | x[3])) | (x[2] & x[3] & (x[0] | x[1]));
-    } else {
-      const uint32_t D = valid ? d.toggles[col * g.nzw + w] : 0u;
-      s = D;
-      s ^= s >> 1; s ^= s >> 2; s ^= s >> 4; s ^= s >> 8; s ^= s >> 16;
-      if (carry) s = ~s;
-      carry ^= (uint32_t)(__popc(D) & 1);
+        for (int a = 0; a < 4; ++a) {
+          const uint32_t pv = (uint32_t)(__popc(sc[a][v]) & 1) << a;
+          tot ^= pv;
+          if (v > w) above ^= pv;
+        }
     }
-    uint32_t mine = 0;
+    uint32_t x[4];
 #pragma unroll
-    for (int bb = 0; bb < 32; ++bb) {
-      const uint32_t mm = __ballot_sync(FULL, (s >> bb) & 1u);
-      if ((int)lane == bb) mine = mm;
+    for (int a = 0; a < 4; ++a) {
+      const uint32_t D = valid ? sc[a][w] : 0u;
+      const uint32_t pd = (uint32_t)(__popc(D) & 1);
+      uint32_t y = D;  // prefix XOR from the lowest slice of the word
+      y ^= y << 1; y ^= y << 2; y ^= y << 4; y ^= y << 8; y ^= y << 16;
+      if ((((tot ^ above) >> a) & 1u) ^ pd) y = ~y;  // odd toggles in the words below
+      x[a] = y;
     }
-    const int k = w * 32 + (int)lane;
-    if (k < nz) d.iplane[((size_t)k * ny + j) * g.nxw + ig] = mine;
+    s = (x[0] & x[1] & (x[2] | x[3])) | (x[2] & x[3] & (x[0] | x[1]));
+  } else {
+    uint32_t carry = 0;  // toggle parity of the column in the words above w
+    if (valid)
+      for (int v = w + 1; v < g.nzw; ++v) carry ^= (uint32_t)(__popc(d.toggles[col * g.nzw + v]) & 1);
+    const uint32_t D = valid ? d.toggles[col * g.nzw + w] : 0u;
+    s = D;
+    s ^= s >> 1; s ^= s >> 2; s ^= s >> 4; s ^= s >> 8; s ^= s >> 16;
+    if (carry) s = ~s;
   }
+  uint32_t mine = 0;
+#pragma unroll
+  for (int bb = 0; bb < 32; ++bb) {
+    const uint32_t mm = __ballot_sync(FULL, (s >> bb) & 1u);
+    if ((int)lane == bb) mine = mm;
+  }
+  const int k = w * 32 + (int)lane;
+  if (k < nz) d.iplane[((size_t)k * ny + j) * g.nxw + ig] = mine;
 }
 
 __global__ void k_popc(const uint32_t *__restrict__ plane, int64_t nw, uint32_t *__restrict__ cnt) {
@@ -569,9 +575,14 @@ __global__ void k_boundary_counts(BatchDev bd, const uint32_t *__restrict__ wpre
   bd.md[m].stats->boundary = e - s;
 }
 
-// One block per (mesh, Level1 row (k, j)): state bytes, boundaryPrefixSum, boundaryIndex.
-__global__ void __launch_bounds__(128) k_expand(BatchDev bd, const uint32_t *__restrict__ wpre) {
-  const int64_t grow = blockIdx.x;
+// One warp per (mesh, Level1 row (k, j)), kExpandWarps rows per block: state bytes,
+// boundaryPrefixSum, boundaryIndex.
+constexpr int kExpandWarps = 8;
+__global__ void __launch_bounds__(kExpandWarps * 32) k_expand(BatchDev bd,
+                                                            const uint32_t *__restrict__ wpre) {
+  const int64_t grow = (int64_t)blockIdx.x * kExpandWarps + (threadIdx.x >> 5);
+  if (grow >= bd.total_rows) return;  // warp-uniform
+  const unsigned lane = threadIdx.x & 31u;
   const int m = find_mesh<&MeshDesc::row_base>(bd.md, bd.nmesh, grow);
   const MeshDesc &d = bd.md[m];
   const GridDev &g = d.g;
@@ -582,7 +593,7 @@ __global__ void __launch_bounds__(128) k_expand(BatchDev bd, const uint32_t *__r
   const int nx = g.n[0];
   const bool vec = (nx & 3) == 0;
   unsigned long long nin = 0;
-  for (int x4 = threadIdx.x * 4; x4 < nx; x4 += blockDim.x * 4) {
+  for (int x4 = (int)lane * 4; x4 < nx; x4 += 128) {
     uint32_t bytes = 0;
     int32_t pre[4];
 #pragma unroll
@@ -613,7 +624,7 @@ __global__ void __launch_bounds__(128) k_expand(BatchDev bd, const uint32_t *__r
     }
   }
   nin = warp_sum(nin);
-  if ((threadIdx.x & 31u) == 0 && nin) atomicAdd(&d.stats->l1_inside, nin);
+  if (lane == 0 && nin) atomicAdd(&d.stats->l1_inside, nin);
 }
 
 __global__ void k_heads(const uint32_t *__restrict__ keys, int64_t P, uint32_t *__restrict__ flags) {
@@ -754,7 +765,8 @@ void launch_boundary_counts(const BatchDev &bd, const uint32_t *wpre, const uint
 
 void launch_expand(const BatchDev &bd, const uint32_t *wpre, cudaStream_t s) {
   if (bd.total_rows <= 0) return;
-  k_expand<<<(unsigned)bd.total_rows, 128, 0, s>>>(bd, wpre);
+  k_expand<<<(unsigned)((bd.total_rows + kExpandWarps - 1) / kExpandWarps), kExpandWarps * 32, 0,
+             s>>>(bd, wpre);
   count_launch();
 }
 

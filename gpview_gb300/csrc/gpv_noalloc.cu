@@ -225,7 +225,7 @@ extern "C" int gpv_voxelize_level1_noalloc(const float *d_tris, int64_t num_tria
   bd.nmesh = 1;
   bd.tile = 128;
   bd.total_tris = T;
-  bd.total_fwarps = (int64_t)g.n[1] * g.nxw;
+  bd.total_fwarps = (int64_t)g.n[1] * g.nxw * g.nzw;
   bd.total_rows = (int64_t)g.n[2] * g.n[1];
   bd.total_words = N1w;
 
