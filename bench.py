@@ -360,9 +360,9 @@ def run_reference(args):
 # Warp instructions one launch of the Level2 kernel executes on each single-mesh workload, from
 # `ncu --metrics smsp__inst_executed.sum` on the current kernel (profiles/k_level2c_*.md give the
 # commands).  The count is a property of the kernel's code and the input, not of the clock.
-LEVEL2_INST_PER_LAUNCH = {"torus262k": 384583248, "sphere16k": 27545565}
+LEVEL2_INST_PER_LAUNCH = {"torus262k": 383936298, "sphere16k": 27523672}
 # DRAM bytes read + written by one launch of the Level2 kernel (same captures)
-LEVEL2_TRAFFIC = {"torus262k": 30674603 + 6144341, "sphere16k": 2841685}
+LEVEL2_TRAFFIC = {"torus262k": 30715392 + 4094208, "sphere16k": 2840747}
 
 
 def max_over_ranks(seconds, dist, device):
