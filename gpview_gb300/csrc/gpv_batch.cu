@@ -1,13 +1,16 @@
 // gpv_batch.cu -- host orchestration of a batch of meshes (the plain path is a batch of one).
 //
-// Three phases, one host synchronisation after each, independent of the number of meshes:
-//   A  prep over every triangle of every mesh            -> per-mesh candidate counts (pair caps)
-//   B  persistent Level1 (tiles of all meshes), fill finish, boundary scan
-//                                                        -> per-mesh pair and boundary counts
-//   C  Level1 expansion, segmented radix sort, segment heads, persistent Level2 over the column
-//      chunks of all meshes                              -> per-mesh statistics
-// Phase B and C launch sequences are recorded into CUDA graphs when graphs are enabled
-// (gpv_set_graphs); their launch shapes are fixed by the counts read at the phase boundary.
+// Two phases, one host synchronisation after each, independent of the number of meshes:
+//   1  prep over every triangle of every mesh, the per-mesh pair segments from its candidate
+//      counts (on the device), persistent Level1 (tiles of all meshes), fill finish, boundary
+//      scan                                              -> per-mesh pair and boundary counts
+//   2  Level1 expansion, the per-voxel pair lists (a counting sort by voxel rank; a segmented
+//      radix sort when normals need triangle order), persistent Level2 over the column chunks of
+//      all meshes                                        -> per-mesh statistics
+// Each phase is recorded into a CUDA graph when graphs are enabled (gpv_set_graphs) and replayed
+// while its launch arguments repeat; its launch shapes are fixed by the counts read at the phase
+// boundary.  A staging kernel at each end of a phase moves the small per-call data between
+// page-locked host staging and the device.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -373,7 +376,7 @@ int run_batch(gpv_ctx *ctx, int n, const float *const *d_tris, const int64_t *T,
     return ctx_fail(ctx, code, msg);
   };
 
-  // ---- phase A+B (one recording): prep, per-mesh pair bases on the device (no host round trip:
+  // ---- phase 1 (one recording): prep, per-mesh pair bases on the device (no host round trip:
   // the pair buffer has the context's capacity hint; a mesh that does not fit raises
   // ST_PAIR_OVERFLOW and the call re-runs with the exact capacity), Level1, fill finish,
   // boundary scan.
@@ -513,7 +516,7 @@ int run_batch(gpv_ctx *ctx, int n, const float *const *d_tris, const int64_t *T,
   }
   std::memcpy(ctx->h_md, md.data(), n * sizeof(MeshDesc));
 
-  // ---- phase C: allocations and uploads first, then the recorded launch sequence
+  // ---- phase 2: allocations and staging first, then the recorded launch sequence
   const int64_t ntiles = (int64_t)st_host.size();
   const bool do_l2 = (any_l2 || nmode) && ntiles > 0;  // sort + lists (+ Level2, normals)
   const bool csort = do_l2 && kmark;                   // lists by the counting sort

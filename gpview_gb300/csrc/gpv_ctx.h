@@ -40,11 +40,11 @@ struct gpv_ctx {
   std::string err;
   int tile = 0;                        // Level1 triangles per tile (autotuned; 0: by mesh size)
   int l2_chunk_cap = 8;                // Level2 boundary voxels per chunk, upper bound (autotuned)
-  bool graphs = true;                  // record phases B and C as CUDA graphs
+  bool graphs = true;                  // record the two phases as CUDA graphs
   int normals = 0;                     // GPV_NORMALS_* for the next voxelizations
   bool hierarchy = false;              // build the voxel box hierarchy
   int fill = GPV_FILL_RAY;             // inside fill of both levels
-  cudaGraphExec_t gexec[2] = {};       // cached executable graphs of phases B and C
+  cudaGraphExec_t gexec[2] = {};       // cached executable graphs of the two phases
   // Launch signature of each cached graph (every value its kernels and copies take as
   // arguments: workspace pointers, sizes, flags) and its kernel count: a call whose signature
   // matches replays the graph without recording it again.
