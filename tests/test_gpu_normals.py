@@ -159,3 +159,31 @@ def test_hierarchy_absent_for_non_power_of_two(ctx):
     with pytest.raises(gpv.GpvError):
         ctx.fetch_hierarchy(res)
     ctx.release(res)
+
+
+@pytest.mark.parametrize("fill", ["ray", "stencil"])
+def test_lists_with_and_without_normals_give_the_same_voxels(ctx, fill):
+    """Without normals the pair lists come from a counting sort by voxel (a voxel's triangles in
+    any order); with normals, from the radix sort (ascending triangle order).  Every Level1 and
+    Level2 output and every work count is the same either way."""
+    import gpview_gb300 as gpv
+
+    tris, spec = W.make(W.C2)
+    ctx.set_fill(gpv.FILL_STENCIL if fill == "stencil" else gpv.FILL_RAY)
+    try:
+        out = []
+        for mode in (gpv.NORMALS_OFF, gpv.NORMALS_BYTES):
+            ctx.set_normals(mode)
+            try:
+                res = ctx.voxelize_host(tris, spec)
+            finally:
+                ctx.set_normals(gpv.NORMALS_OFF)
+            out.append((ctx.fetch(res), (res.num_pairs, res.num_boundary, res.work.sat1,
+                                         res.work.sat2, res.work.ray1, res.work.ray2)))
+            ctx.release(res)
+    finally:
+        ctx.set_fill(gpv.FILL_RAY)
+    (a, wa), (b, wb) = out
+    for x, y in zip(a, b):
+        np.testing.assert_array_equal(x, y)
+    assert wa == wb
