@@ -170,7 +170,8 @@ int gpv_autotune(gpv_ctx *ctx, int32_t n, const float *const *d_tris, const int6
  * 4 pair sort + lists, 5 Level2 (work items + kernel), 6 the Level2 kernel alone, 7 per-mesh pair
  * bases, 8 between the two phases (counts copied out, host planning, second launch, uploads in).
  * gpv_stage_times returns the number of timed calls and the accumulated milliseconds per stage
- * (up to 9 slots; unused slots stay 0). */
+ * (up to 9 slots; unused slots stay 0).  The events are recorded inside the phases' CUDA graphs
+ * and cost ~0.01-0.05 ms per call, so time the calls themselves with timing off. */
 int gpv_set_timing(gpv_ctx *ctx, int on);
 int gpv_stage_times(gpv_ctx *ctx, double *ms, int n);
 /* Host-side milliseconds per call segment, accumulated while timing is on: 0 setup up to the
