@@ -578,11 +578,11 @@ __global__ void k_boundary_counts(BatchDev bd, const uint32_t *__restrict__ wpre
 // One warp per (mesh, Level1 row (k, j)), kExpandWarps rows per block: state bytes,
 // boundaryPrefixSum, boundaryIndex.
 constexpr int kExpandWarps = 8;
-__global__ void __launch_bounds__(kExpandWarps * 32) k_expand(BatchDev bd,
-                                                            const uint32_t *__restrict__ wpre) {
-  const int64_t grow = (int64_t)blockIdx.x * kExpandWarps + (threadIdx.x >> 5);
-  if (grow >= bd.total_rows) return;  // warp-uniform
-  const unsigned lane = threadIdx.x & 31u;
+// One row by one warp; returns the lane's inside-voxel count and the row's mesh statistics.
+__device__ __forceinline__ unsigned long long expand_row(const BatchDev &bd,
+                                                         const uint32_t *__restrict__ wpre,
+                                                         int64_t grow, unsigned lane,
+                                                         MeshStats *&st) {
   const int m = find_mesh<&MeshDesc::row_base>(bd.md, bd.nmesh, grow);
   const MeshDesc &d = bd.md[m];
   const GridDev &g = d.g;
@@ -623,8 +623,40 @@ __global__ void __launch_bounds__(kExpandWarps * 32) k_expand(BatchDev bd,
       *reinterpret_cast<int4 *>(d.prefix + v) = make_int4(pre[0], pre[1], pre[2], pre[3]);
     }
   }
+  st = d.stats;
+  return nin;
+}
+
+// The inside counts of the block's rows go to the statistics with one atomic per mesh run of
+// rows rather than one per row (all rows of a mesh add to one counter).
+__global__ void __launch_bounds__(kExpandWarps * 32) k_expand(BatchDev bd,
+                                                            const uint32_t *__restrict__ wpre) {
+  __shared__ unsigned long long s_nin[kExpandWarps];
+  __shared__ MeshStats *s_st[kExpandWarps];
+  const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+  const int64_t grow = (int64_t)blockIdx.x * kExpandWarps + warp;
+  MeshStats *st = nullptr;
+  unsigned long long nin = 0;
+  if (grow < bd.total_rows) nin = expand_row(bd, wpre, grow, lane, st);  // warp-uniform
   nin = warp_sum(nin);
-  if (lane == 0 && nin) atomicAdd(&d.stats->l1_inside, nin);
+  if (lane == 0) {
+    s_nin[warp] = nin;
+    s_st[warp] = st;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    MeshStats *cur = nullptr;
+    unsigned long long acc = 0;
+    for (int w = 0; w < kExpandWarps; ++w) {
+      if (s_st[w] != cur) {
+        if (cur && acc) atomicAdd(&cur->l1_inside, acc);
+        cur = s_st[w];
+        acc = 0;
+      }
+      acc += s_nin[w];
+    }
+    if (cur && acc) atomicAdd(&cur->l1_inside, acc);
+  }
 }
 
 __global__ void k_heads(const uint32_t *__restrict__ keys, int64_t P, uint32_t *__restrict__ flags) {
