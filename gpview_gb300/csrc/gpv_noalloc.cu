@@ -1,27 +1,30 @@
 // gpv_noalloc.cu -- Level1 voxelization that allocates nothing.
 //
 // Some callers cannot call cudaMalloc: code that runs inside another allocator's or memory
-// pool's hooks, host paths that must not take the implicit device synchronisation that
-// cudaMalloc/cudaFree can cause, and plugin hosts that hand a library its buffers and forbid it
-// to acquire device memory of its own.  gpv_voxelize_level1_noalloc serves them: the caller
-// passes the triangles and the three Level1 outputs, and every intermediate lives in
-// g_noalloc_scratch, a file-scope __device__ array of fixed size (kScratchBytes, 32 MiB) that
-// every GPU loading this library holds until the process exits.
+// pool's hooks (a call back into the allocator would recurse or deadlock), host paths that must
+// not take the implicit device synchronisation that cudaMalloc/cudaFree can cause, and plugin
+// hosts that hand a library its buffers and forbid it to acquire device memory of its own.
+// gpv_voxelize_level1_noalloc serves them: the caller passes the triangles and the three Level1
+// outputs, and every intermediate lives in g_noalloc_scratch, a file-scope __device__ array of
+// fixed size (kScratchBytes, 32 MiB) that every GPU loading this library holds until the
+// process exits.
 //
 // Rules of use:
-//   * The first call on a device resolves the array's device address with
-//     cudaGetSymbolAddress (with that device current) and caches it; make that first call before
-//     any stream capture.
+//   * Host code cannot use the array's name as a device address.  Every call looks the address
+//     up with cudaGetSymbolAddress while the caller's device is current and checks the result
+//     (a lookup costs far less than the call's own stream synchronisation, and it stays right
+//     after a device reset, which loads the module -- and the array -- again).  The first call
+//     on a device also loads this library's device code there; make that first call before any
+//     stream capture.
 //   * All calls share the one array, which keeps the previous call's contents.  Each call clears
 //     the regions that must start at zero.  Calls whose GPU work overlaps -- on different
 //     streams or host threads -- race on the array; serialise them.
 //   * Sizes whose intermediates do not fit the array are rejected with GPV_ERR_INVALID and a
-//     message from gpv_noalloc_last_error(); nothing is launched then.
+//     message from gpv_noalloc_last_error() (kept per host thread); nothing is launched then.
 //   * No cudaMalloc, cudaFree, host heap or library allocation is made.
 #include <cmath>
 #include <cstdio>
 #include <cstring>
-#include <mutex>
 
 #include "gpv_internal.h"
 
@@ -29,26 +32,30 @@ namespace gpv {
 namespace {
 
 constexpr size_t kScratchBytes = size_t(32) << 20;
-constexpr int kMaxDevices = 64;
 constexpr int kMaxTableFloats = 12288;  // nx + ny + nz
+// Scratch bytes per triangle (packed vertices 48, SAT box 16, ray box 16).  Triangle counts are
+// checked against the array with this before any size is formed, so no size can wrap.
+constexpr size_t kBytesPerTriangle = 80;
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
 
-std::mutex g_setup_mutex;
-void *g_scratch_ptr[kMaxDevices] = {};
-char g_err[256] = "";
+thread_local char g_err[256] = "";
 
 void set_err(const char *msg) {
   std::snprintf(g_err, sizeof(g_err), "%s", msg);
 }
 
-// Variant of the Level1 kernel without the (voxel, triangle) records: one thread per triangle
-// runs its SAT candidate box (boundary bits) and its fill columns (parity toggles).  Inputs are
-// the packed triangles written by the prep kernel.
+// Variant of the Level1 kernel without the (voxel, triangle) records: one warp per triangle,
+// whose lanes share its SAT candidate columns (boundary bits) and its fill columns (parity
+// toggles).  Inputs are the packed triangles written by the prep kernel.  A triangle's work is
+// its candidate box plus its fill columns times nz, spread over 32 lanes: a triangle whose box
+// spans the whole grid (or an ill-conditioned one, whose fill box is the whole grid) costs about
+// nx*ny*nz/32 tests per lane.
 __global__ void k_level1_nopairs(const MeshDesc *__restrict__ md) {
   const MeshDesc &b = *md;
   const GridDev &g = b.g;
-  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int lane = threadIdx.x & 31;
+  const int64_t t = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;  // warp-uniform
   if (t >= b.T) return;
   const float4 a0 = b.ptri[3 * t], a1 = b.ptri[3 * t + 1], a2 = b.ptri[3 * t + 2];
   const float V[9] = {a0.x, a0.y, a0.z, a1.x, a1.y, a1.z, a2.x, a2.y, a2.z};
@@ -57,36 +64,38 @@ __global__ void k_level1_nopairs(const MeshDesc *__restrict__ md) {
   const int x0 = (int)(rg.x & 0xffff), x1 = (int)((unsigned)rg.x >> 16);
   const int y0 = (int)(rg.y & 0xffff), y1 = (int)((unsigned)rg.y >> 16);
   const int z0 = (int)(rg.z & 0xffff), z1 = (int)((unsigned)rg.z >> 16);
-  for (int p = x0; p <= x1; ++p)
-    for (int q = y0; q <= y1; ++q) {
-      SatCol sc;
-      if (!sat_col(V, g.c1[0][p], g.c1[1][q], g.e1, sc)) continue;
-      for (int r = z0; r <= z1; ++r)
-        if (sat_z(sc, V, g.c1[2][r], g.e1))
-          atomicOr(&b.bplane[((size_t)r * ny + q) * g.nxw + (p >> 5)], 1u << (p & 31));
-    }
+  const int sx = max(x1 - x0 + 1, 0), sy = max(y1 - y0 + 1, 0);
+  for (int c = lane; c < sx * sy; c += 32) {
+    const int p = x0 + c % sx, q = y0 + c / sx;
+    SatCol sc;
+    if (!sat_col(V, g.c1[0][p], g.c1[1][q], g.e1, sc)) continue;
+    for (int r = z0; r <= z1; ++r)
+      if (sat_z(sc, V, g.c1[2][r], g.e1))
+        atomicOr(&b.bplane[((size_t)r * ny + q) * g.nxw + (p >> 5)], 1u << (p & 31));
+  }
   const uint32_t fxr = __float_as_uint(a0.w), fyr = __float_as_uint(a1.w);
   const int fx0 = (int)(fxr & 0xffff), fx1 = (int)(fxr >> 16);
   const int fy0 = (int)(fyr & 0xffff), fy1 = (int)(fyr >> 16);
+  const int fsx = max(fx1 - fx0 + 1, 0), fsy = max(fy1 - fy0 + 1, 0);
   RayTri rt;
   ray_tri_pre(V, a2.w, rt);
-  for (int j = fy0; j <= fy1; ++j)
-    for (int i = fx0; i <= fx1; ++i) {
-      RayCol rc;
-      if (!ray_col(rt, g.c1[0][i], g.c1[1][j], rc)) continue;
-      const size_t col = (size_t)j * nx + i;
-      uint32_t carry = 0;
-      for (int w = g.nzw - 1; w >= 0; --w) {
-        uint32_t h = 0;
-        for (int bb = 0; bb < 32; ++bb) {
-          const int k = 32 * w + bb;
-          if (k < nz && ray_t(rt, rc, g.c1[2][k], g.thr)) h |= 1u << bb;
-        }
-        const uint32_t d = h ^ ((h >> 1) | (carry << 31));
-        carry = h & 1u;
-        if (d) atomicXor(&b.toggles[col * g.nzw + w], d);
+  for (int c = lane; c < fsx * fsy; c += 32) {
+    const int i = fx0 + c % fsx, j = fy0 + c / fsx;
+    RayCol rc;
+    if (!ray_col(rt, g.c1[0][i], g.c1[1][j], rc)) continue;
+    const size_t col = (size_t)j * nx + i;
+    uint32_t carry = 0;
+    for (int w = g.nzw - 1; w >= 0; --w) {
+      uint32_t h = 0;
+      for (int bb = 0; bb < 32; ++bb) {
+        const int k = 32 * w + bb;
+        if (k < nz && ray_t(rt, rc, g.c1[2][k], g.thr)) h |= 1u << bb;
       }
+      const uint32_t d = h ^ ((h >> 1) | (carry << 31));
+      carry = h & 1u;
+      if (d) atomicXor(&b.toggles[col * g.nzw + w], d);
     }
+  }
 }
 
 size_t align256(size_t v) { return (v + 255) & ~size_t(255); }
@@ -110,6 +119,25 @@ extern "C" int gpv_voxelize_level1_noalloc(const float *d_tris, int64_t num_tria
   if (num_triangles > 0 && (reinterpret_cast<uintptr_t>(d_tris) & 15u)) {
     set_err("triangle buffer must be 16-byte aligned");
     return GPV_ERR_INVALID;
+  }
+  if (num_triangles > (int64_t)(kScratchBytes / kBytesPerTriangle)) {
+    char msg[160];
+    std::snprintf(msg, sizeof(msg),
+                  "%lld triangles exceed the fixed no-alloc scratch (%zu bytes, %zu per triangle)",
+                  (long long)num_triangles, kScratchBytes, kBytesPerTriangle);
+    set_err(msg);
+    return GPV_ERR_INVALID;
+  }
+  // Level2 divisions are not used here, but a specification gpv_voxelize would reject is
+  // rejected here too: each in 0..32, all zero or all positive.
+  {
+    const int32_t *n2 = spec->ndiv2;
+    const bool any2 = n2[0] || n2[1] || n2[2], all2 = n2[0] && n2[1] && n2[2];
+    if (n2[0] < 0 || n2[1] < 0 || n2[2] < 0 || n2[0] > 32 || n2[1] > 32 || n2[2] > 32 ||
+        (any2 && !all2)) {
+      set_err("invalid grid specification (Level2 divisions)");
+      return GPV_ERR_INVALID;
+    }
   }
   // ---- grid, derived exactly as the plain path does (no host heap: tables on the stack)
   GridDev g;
@@ -176,25 +204,17 @@ extern "C" int gpv_voxelize_level1_noalloc(const float *d_tris, int64_t num_tria
     return GPV_ERR_INVALID;
   }
 
-  // ---- once per device: the array's device address
-  int dev = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) {
-    set_err("no current CUDA device");
-    return GPV_ERR_CUDA;
-  }
-  unsigned char *base;
+  // ---- the array's device address on the current device (looked up on every call)
+  unsigned char *base = nullptr;
   {
-    std::lock_guard<std::mutex> lk(g_setup_mutex);
-    if (!g_scratch_ptr[dev]) {
-      void *p = nullptr;
-      const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-      if (e != cudaSuccess || !p) {
-        set_err("cudaGetSymbolAddress failed for the no-alloc scratch array");
-        return GPV_ERR_CUDA;
-      }
-      g_scratch_ptr[dev] = p;
+    void *p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess || !p) {
+      cudaGetLastError();
+      set_err("cudaGetSymbolAddress failed for the no-alloc scratch array (no usable device?)");
+      return GPV_ERR_CUDA;
     }
-    base = static_cast<unsigned char *>(g_scratch_ptr[dev]);
+    base = static_cast<unsigned char *>(p);
   }
 
   float *d_tab = reinterpret_cast<float *>(base + o_tab);
@@ -243,7 +263,7 @@ extern "C" int gpv_voxelize_level1_noalloc(const float *d_tris, int64_t num_tria
   }
   launch_prep(bd, stream);
   if (T > 0) {
-    k_level1_nopairs<<<(unsigned)((T + 127) / 128), 128, 0, stream>>>(d_md);
+    k_level1_nopairs<<<(unsigned)((T + 3) / 4), 128, 0, stream>>>(d_md);  // a warp per triangle
     count_launch();
   }
   launch_fill_finish(bd, stream);

@@ -11,6 +11,7 @@ import numpy as np
 import pytest
 
 import workloads as W
+from oracle import oracle as orc
 
 pytestmark = pytest.mark.gpu
 
@@ -48,7 +49,27 @@ def test_noalloc_two_calls_match_plain_path(built):
         np.testing.assert_array_equal(a1, l1)
         np.testing.assert_array_equal(apre, pre)
         np.testing.assert_array_equal(abi, bi)
+        # and directly against the oracle (the reference's CPU composition)
+        ref = orc.Run(tris, spec, fill=orc.FILL_CAND)
+        assert nb == ref.B
+        np.testing.assert_array_equal(a1, ref.level1_bytes())
+        np.testing.assert_array_equal(apre, ref.prefix())
+        np.testing.assert_array_equal(abi, ref.boundary_index())
     ctx.close()
+
+
+def test_noalloc_rejects_bad_level2_divisions(built):
+    """A spec gpv_voxelize rejects (Level2 divisions partly zero) is rejected here too."""
+    gpv = built
+    L = gpv.lib()
+    spec = gpv.grid_padded((0, 0, 0), (1, 1, 1), 16, 0)
+    spec.ndiv2[:] = (4, 0, 4)
+    nb = C.c_int64(-1)
+    dummy = C.c_void_p(256)  # never dereferenced: the spec check fails first
+    rc = L.gpv_voxelize_level1_noalloc(dummy, 10, C.byref(spec), dummy, dummy, dummy,
+                                       C.byref(nb), None)
+    assert rc == -1
+    assert b"Level2" in L.gpv_noalloc_last_error()
 
 
 def test_noalloc_rejects_oversize(built):
