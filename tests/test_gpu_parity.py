@@ -50,26 +50,6 @@ def test_torus262k_full(ctx):
     _check_full(ctx, tris, spec)
 
 
-def test_star1310k_level1_full_level2_sampled(ctx):
-    """Level1 outputs in full; Level2 on three seeded ranges of boundary voxels."""
-    tris, spec = W.make(W.C3)
-    res = ctx.voxelize_host(tris, spec)
-    l1, pre, bi, l2 = ctx.fetch(res)
-    ref = orc.Run(tris, spec, fill=orc.FILL_CAND)
-    assert res.num_boundary == ref.B
-    np.testing.assert_array_equal(l1, ref.level1_bytes())
-    np.testing.assert_array_equal(pre, ref.prefix())
-    np.testing.assert_array_equal(bi, ref.boundary_index())
-    assert res.num_pairs == ref.num_pairs()
-    cells = ref.cells
-    rng = np.random.default_rng(1234)
-    for b0 in sorted(rng.integers(0, max(ref.B - 3000, 1), size=3)):
-        b1 = min(int(b0) + 3000, ref.B)
-        exp = ref.level2_bytes(int(b0), b1)
-        np.testing.assert_array_equal(l2[int(b0) * cells:b1 * cells], exp)
-    ctx.release(res)
-
-
 def _pad_spec(tris, n, n2):
     import gpview_gb300 as gpv
 

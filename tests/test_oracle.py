@@ -71,6 +71,116 @@ def test_fill_modes_agree_on_sphere16k():
     assert a.B == b.B > 0
 
 
+@pytest.mark.parametrize("name", ["torus262k", "star1310k"])
+def test_candidate_fill_equals_unfiltered_fill_in_full(name):
+    """The large plain configurations in full: the candidate-list fill (the mode the GPU parity
+    tests compare against) equals the unfiltered per-column fill, which tests every triangle
+    against every column with the reference predicate's float operations.  Level2 has no
+    prefilter in either mode (its candidate set is the reference's column union)."""
+    import workloads as W
+
+    cfg = {"torus262k": W.C2, "star1310k": W.C3}[name]
+    tris, grid = W.make(cfg, cpu=True)
+    a = orc.Run(tris, grid, fill=orc.FILL_COLUMN)
+    b = orc.Run(tris, grid, fill=orc.FILL_CAND)
+    assert a.B == b.B > 0
+    np.testing.assert_array_equal(a.level1_state(), b.level1_state())
+    np.testing.assert_array_equal(a.prefix(), b.prefix())
+
+
+@pytest.mark.parametrize("k", range(4))
+def test_adversarial_soups_candidate_fill_equals_brute_force(k):
+    """On the triangles aimed at the certified bounds (tests/adversarial.py), the oracle's
+    candidate-list fill equals ClassifyInOutCPU's brute force, and the soups really sit at the
+    bounds: slivers on both sides of the rel = 1/8 cutoff, and +z ray tests whose float t lies
+    within a few ulps of 1e-6 on both sides."""
+    import adversarial as A
+
+    g = A.GRIDS[k]
+    tab = orc.grid_tables(g)
+    tris = A.soup(g, tab, seed=100 + k)
+    a = orc.Run(tris, g, fill=orc.FILL_VOXEL)
+    b = orc.Run(tris, g, fill=orc.FILL_CAND)
+    assert a.B == b.B > 0
+    np.testing.assert_array_equal(a.level1_state(), b.level1_state())
+    V = tris.reshape(-1, 9)
+    rel, adet = A.sliver_rel(V)
+    live = adet > 1e-6
+    assert ((rel > 0.11) & (rel <= 0.125) & live).sum() >= 3
+    assert ((rel > 0.125) & (rel < 0.14) & live).sum() >= 3
+    # the t ~ 1e-6 family: re-find each triangle's nearest threshold crossing over the grid's
+    # Level1 centres and Level2 origins directly below its centroid
+    n, n2 = [int(x) for x in g[2]], [int(x) for x in g[3]]
+    (cx, cy, cz), (ox, oy, oz), _ = A._tables(tab, n, n2)
+    ulp = float(np.spacing(np.float32(1e-6)))
+    near_hit = near_miss = 0
+    for xs, ys, zs in ((cx, cy, cz), (ox, oy, oz)):
+        cen = V.reshape(-1, 3, 3).mean(1)
+        i = np.clip(np.searchsorted(xs, cen[:, 0]) - 1, 0, len(xs) - 1)
+        j = np.clip(np.searchsorted(ys, cen[:, 1]) - 1, 0, len(ys) - 1)
+        for di in (0, 1):
+            for dj in (0, 1):
+                ii = np.clip(i + di, 0, len(xs) - 1)
+                jj = np.clip(j + dj, 0, len(ys) - 1)
+                kz = np.clip(np.searchsorted(zs, cen[:, 2]) - 1, 0, len(zs) - 1)
+                O = np.stack([xs[ii], ys[jj], zs[kz]], 1)
+                ins, t, hit = A.ray_z(V, O)
+                close = ins & (np.abs(t.astype(np.float64) - 1e-6) <= 8 * ulp)
+                near_hit += int((close & hit).sum())
+                near_miss += int((close & ~hit).sum())
+    assert near_hit >= 10 and near_miss >= 10, (near_hit, near_miss)
+
+
+def test_as_written_fill_equals_oracle_on_sampled_columns():
+    """ClassifyInOutCPU as the reference writes it (every voxel centre against every triangle
+    with the general-direction ray test), on seeded columns of sphere16k, gives the oracle's
+    inside states wherever no boundary state overrides them."""
+    import workloads as W
+
+    tris, grid = W.make(W.C1, cpu=True)
+    run = orc.Run(tris, grid, fill=orc.FILL_CAND)
+    nx, ny, nz = (int(v) for v in run.spec.n)
+    st = run.level1_state().reshape(nz, ny, nx)
+    cols = np.random.default_rng(3).choice(nx * ny, 48, replace=False)
+    cols = np.concatenate([cols, [(ny // 2) * nx + nx // 2]])  # one column through the middle
+    par = run.voxel_fill_columns(cols)
+    for c, p in zip(cols, par):
+        s = st[:, c // nx, c % nx]
+        keep = s != 2
+        np.testing.assert_array_equal(p[keep], s[keep])
+    assert par.any()
+
+
+def test_level2_counts_and_list_sampling():
+    """The count-only pass and the list form of Level2 agree with the range form."""
+    import workloads as W
+
+    tris, grid = W.make(W.C1, cpu=True)
+    run = orc.Run(tris, grid)
+    st, s2, r2 = run.level2_state()
+    assert run.level2_work() == (s2, r2)
+    pick = np.array([0, 5, 17, run.B // 2, run.B - 1], np.int64)
+    got, _, _ = run.level2_list(pick)
+    exp = np.concatenate([st[b * run.cells:(b + 1) * run.cells] for b in pick])
+    np.testing.assert_array_equal(got, exp)
+
+
+@pytest.mark.parametrize("name", ["sphere16k", "torus262k", "star1310k"])
+def test_cpu_workload_generation_is_bit_identical(name, built):
+    """The benchmark's reference arm makes its mesh and grid with the oracle library's build of
+    the generator source; they equal the GPU library's, bit for bit."""
+    import workloads as W
+
+    cfg = {"sphere16k": W.C1, "torus262k": W.C2, "star1310k": W.C3}[name]
+    a, spec = W.make(cfg)
+    b, grid = W.make(cfg, cpu=True)
+    np.testing.assert_array_equal(a.view(np.uint32), b.view(np.uint32))
+    for x, y in ((spec.bbox_min, grid[0]), (spec.bbox_max, grid[1])):
+        np.testing.assert_array_equal(np.array(list(x), np.float32).view(np.uint32),
+                                      np.asarray(y, np.float32).view(np.uint32))
+    assert list(spec.ndiv) == list(grid[2]) and list(spec.ndiv2) == list(grid[3])
+
+
 def test_reference_sizing_formula():
     # maxModelSize/voxelCount and GetNextDiv4 (src/Object.cpp:3094-3107)
     assert orc.reference_divisions((0, 0, 0), (1.0, 0.5, 0.26), 1.0, 8) == (8, 4, 4)
