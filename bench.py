@@ -1,21 +1,27 @@
 #!/usr/bin/env python3
 """Benchmark of the two-level voxelizer (prints one JSON line on rank 0).
 
-Default workload (one step = one voxelization of one mesh through the plain path):
-  torus262k -- torus R=0.35 r=0.12, 512x256 segments (262,144 triangles), 4-octave value-noise
-               displacement of amplitude 0.01, Level1 128^3 over the mesh box padded by one cell,
-               Level2 8^3 per boundary voxel.  Seeded synthetic data.
+Default workload (one step = one voxelization of one mesh through the plain path): the largest
+plain configuration,
+  star1310k -- star surface r = 0.3(1 + 0.2 sum a_lm Y_lm), l <= 6, on an icosphere subdivided 8
+               times (1,310,720 triangles), scaled 1:1:6 in z; Level1 256^3 over the mesh box
+               padded by one cell, Level2 16^3 per boundary voxel.  Seeded synthetic data.
+(--workload sphere16k / torus262k run the two smaller plain configurations.)
 
-value    tri-voxel tests/s on device-resident triangles (results stay on the device), timed with
-         CUDA events on the launching stream; L2 is flushed (256 MiB write) between steps,
-         outside the timed spans.
+value    reference-equivalent tri-voxel tests/s on device-resident triangles (results stay on the
+         device), timed with CUDA events on the launching stream; L2 is flushed (256 MiB write)
+         between steps, outside the timed spans.
 e2e      the same metric through the public host API (gpv_voxelize_to_host): H2D of the step's
          triangles from pinned memory, voxelization, D2H of every result array into pinned
-         buffers (overlapped with the Level2 slabs), timed on the host around each step.
-tests    = sat1 + sat2 + ray1 + ray2 counted from the reference algorithm (see include/gpview.h).
+         buffers, timed on the host around each step.
+tests    = sat1 + sat2 + ray1 + ray2: the tests the reference's algorithm performs on the mesh,
+         counted by its definitions (include/gpview.h, gpv_work).  The kernels decide many of them
+         in groups without evaluating each, so this is a reference-equivalent rate, not the
+         number of predicate evaluations the GPU executes.
 
 --impl reference times the reference's CPU path (the oracle restatement, all host threads) on a
-bounded sample of the same workload and reports the same metric.
+bounded sample of the same workload and reports the same metric and config.  It generates the
+mesh with the oracle library's build of the same generator source and never loads the GPU library.
 Multi-GPU: replicas only (each rank voxelizes its own copy; the path has no exchange step).
 """
 import argparse
@@ -39,7 +45,7 @@ def parse():
     p.add_argument("--steps", type=int, default=10)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="gpv", choices=["gpv", "reference"])
-    p.add_argument("--workload", default="torus262k", choices=["sphere16k", "torus262k", "star1310k"])
+    p.add_argument("--workload", default="star1310k", choices=["sphere16k", "torus262k", "star1310k"])
     p.add_argument("--tile", type=int, default=0)
     p.add_argument("--level2", type=int, default=0, help="override the workload's Level2 divisions")
     p.add_argument("--chunk", type=int, default=0, help="Level2 chunk of the plain path (0: default)")
@@ -48,7 +54,16 @@ def parse():
                    help="z slabs of the e2e path's Level2 launch (0: by the Level2 output size)")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-stencil", action="store_true", help="skip the stencil-fill section")
-    p.add_argument("--cpu-seconds", type=float, default=15.0)
+    p.add_argument("--no-shims", action="store_true", help="skip the reference-named shim section")
+    p.add_argument("--cpu-seconds", type=float, default=15.0,
+                   help="CPU-baseline budget of the GPU arm (the reference arm uses --ref-step-seconds)")
+    p.add_argument("--ref-step-seconds", type=float, default=3.0,
+                   help="CPU seconds per step of the reference arm's bounded sample")
+    p.add_argument("--no-as-written", action="store_true",
+                   help="skip the one-thread reference-as-written CPU estimate")
+    p.add_argument("--as-written-seconds", type=float, default=12.0)
+    p.add_argument("--stencil-cpu", action="store_true",
+                   help="also time the oracle's stencil-fill restatement on the host")
     p.add_argument("--batch", type=int, default=4096, help="meshes of the batched workload (0: skip)")
     p.add_argument("--batch-reps", type=int, default=3)
     p.add_argument("--batch-tile", type=int, default=0, help="fixed Level1 tile (0: autotune)")
@@ -130,32 +145,104 @@ def load_peaks():
         return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "sm_max_mhz": 2070.0}, "fallback"
 
 
-def cpu_baseline(tris, spec, work_total, seconds, threads):
-    """The oracle (port of the reference CPU path) on a bounded sample: Level1 in full, Level2 on
-    a contiguous range of boundary voxels sized to the time budget; extrapolated to the mesh."""
+METRIC = "tri-voxel tests/s (reference-equivalent)"
+L2_FLUSH = ("GPU arm: a 256 MiB write between steps, outside the timed spans; "
+            "the CPU reference arm has no flush")
+
+
+def workload_config(cfg, T):
+    """The config dict both arms print (identical for the same workload)."""
+    return {"workload": cfg["name"], "desc": cfg["desc"], "triangles": int(T),
+            "level1": cfg["level1"], "level2": cfg["level2"], "parallelism": "replicas",
+            "l2_flush": L2_FLUSH}
+
+
+def cpu_work(tris, grid, threads):
+    """(oracle run, tests per mesh): the reference algorithm's sat1 + ray1 + sat2 + ray2 on the
+    mesh, by the oracle's counts (the same definitions the library's gpv_work uses)."""
+    from oracle import oracle as orc
+
+    run = orc.Run(tris, grid, fill=orc.FILL_CAND, threads=threads)
+    s2, r2 = run.level2_work(threads)
+    return run, run.sat1_tests() + run.ray1_candidates() + s2 + r2
+
+
+def _level2_sample(run, seconds, threads):
+    """Level2 of the oracle on an evenly strided sample of the boundary voxels (every part of the
+    mesh represented), in one parallel pass per round: a first round of 64 voxels per thread
+    measures the cost per voxel, a second round fills the rest of the budget.  Returns (seconds,
+    voxels done)."""
+    import numpy as np
+
+    B = run.B
+    if B == 0:
+        return 0.0, 0
+    spent, done = 0.0, 0
+    n = min(B, 64 * max(threads, 1))
+    for rnd in range(2):
+        if n <= 0:
+            break
+        # offset the second round by half a stride so that the two samples interleave
+        pick = ((np.arange(n, dtype=np.int64) * B) // n + (rnd * B) // (2 * n)) % B
+        pick = np.unique(pick)
+        t0 = time.perf_counter()
+        run.level2_list(pick, threads)
+        spent += time.perf_counter() - t0
+        done += pick.size
+        per = spent / done
+        n = min(B - done, int(max(seconds - spent, 0.0) / per))
+    return spent, done
+
+
+def cpu_sample(tris, grid, work_total, seconds, threads, run=None):
+    """One bounded sample of the reference's CPU path as the oracle port restates it, on all
+    host threads: Level1 in full (ClassifyTessellation + the candidate-list parity fill) and
+    Level2 on an evenly strided sample of the boundary voxels sized to the budget, extrapolated
+    to the whole mesh."""
     from oracle import oracle as orc
 
     t0 = time.perf_counter()
-    run = orc.Run(tris, spec, fill=orc.FILL_CAND, threads=threads)
+    run = orc.Run(tris, grid, fill=orc.FILL_CAND, threads=threads)
     t_l1 = time.perf_counter() - t0
-    B = run.B
-    nb = min(B, 256)
-    t_l2 = 0.0
-    done = 0
-    while done < B:
-        t1 = time.perf_counter()
-        run.level2_state(done, done + nb, threads)
-        dt = time.perf_counter() - t1
-        t_l2 += dt
-        done += nb
-        if t_l1 + t_l2 > seconds:
-            break
-        nb = min(B - done, nb * 2)
-    t_full = t_l1 + (t_l2 * B / done if done else 0.0)
+    t_l2, done = _level2_sample(run, max(seconds - t_l1, 0.2), threads)
+    t_full = t_l1 + (t_l2 * run.B / done if done else 0.0)
     return {"value": work_total / t_full, "unit": "tests/s", "cores": threads, "kind": "port",
-            "sample": f"Level1 in full + Level2 on {done}/{B} boundary voxels, extrapolated "
-                      f"({t_l1 + t_l2:.1f} s of CPU work, est. {t_full:.2f} s per mesh)",
+            "sample": f"Level1 in full + Level2 on an evenly strided sample of {done}/{run.B} "
+                      f"boundary voxels, extrapolated ({t_l1 + t_l2:.1f} s of CPU work, "
+                      f"est. {t_full:.2f} s per mesh)",
             "sec_per_mesh": t_full}
+
+
+def cpu_as_written(tris, grid, work_total, seconds, seed=7):
+    """The reference's CPU path as it is written, on ONE thread (SURVEY: 'reference-as-written'):
+    ClassifyTessellation and the compaction (timed in full), ClassifyInOutCPU's brute force --
+    every voxel centre against every triangle -- on a seeded sample of Level1 columns, and the
+    Level2 passes on an evenly strided sample of boundary voxels; the two sampled parts are extrapolated
+    to the whole mesh."""
+    import numpy as np
+    from oracle import oracle as orc
+
+    t0 = time.perf_counter()
+    run = orc.Run(tris, grid, fill=orc.FILL_CAND, threads=1)
+    t_l1 = time.perf_counter() - t0
+    nx, ny = int(run.spec.n[0]), int(run.spec.n[1])
+    rng = np.random.default_rng(seed)
+    order = rng.permutation(nx * ny)
+    t_fill, ncol, k = 0.0, 0, 1
+    while t_fill < seconds / 2 and ncol < order.size:
+        cols = order[ncol:ncol + k]
+        t1 = time.perf_counter()
+        run.voxel_fill_columns(cols)
+        t_fill += time.perf_counter() - t1
+        ncol += cols.size
+        k *= 2
+    t_l2, done = _level2_sample(run, seconds / 2, 1)
+    t_full = t_l1 + t_fill * (nx * ny) / ncol + (t_l2 * run.B / done if done else 0.0)
+    return {"value": work_total / t_full, "unit": "tests/s", "cores": 1, "kind": "port",
+            "sec_per_mesh": t_full,
+            "sample": f"one thread: Level1 SAT + compaction in full ({t_l1:.1f} s), the brute-force "
+                      f"parity fill on {ncol}/{nx * ny} seeded columns ({t_fill:.1f} s), Level2 on "
+                      f"{done}/{run.B} boundary voxels ({t_l2:.1f} s); extrapolated"}
 
 
 def batch_bench(gpv, ctx, torch, stream, local, args):
@@ -321,6 +408,9 @@ def served_bench(gpv, torch, local, args, tuned):
 
 
 def run_reference(args):
+    """The reference arm: the reference's CPU path (oracle port, all host threads), rank 0 only.
+    Each step is one bounded sample (Level1 in full, Level2 on an evenly strided sample of
+    boundary voxels), extrapolated to the mesh; value = tests per mesh / mean extrapolated seconds."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
@@ -329,40 +419,41 @@ def run_reference(args):
     cfg = WORKLOADS[args.workload]
     if args.level2:
         cfg = dict(cfg, level2=args.level2)
-    tris, spec = W.make(cfg)
-    from oracle import oracle as orc
-
+    tris, grid = W.make(cfg, cpu=True)  # the oracle's generator build: no GPU library loaded
     threads = os.cpu_count() or 1
-    # per-mesh work counts from the oracle (Level1 exact; Level2 counted on the sample)
+    _, work_total = cpu_work(tris, grid, threads)
     times = []
-    work_total = None
+    base = None
     for step in range(args.warmup + args.steps):
-        base = cpu_baseline(tris, spec, 1.0, max(args.cpu_seconds / 3, 3.0), threads)
-        if work_total is None:
-            run = orc.Run(tris, spec, fill=orc.FILL_CAND, threads=threads)
-            _, s2, r2 = run.level2_state(0, run.B, threads)
-            work_total = run.sat1_tests() + run.ray1_candidates() + s2 + r2
+        base = cpu_sample(tris, grid, work_total, args.ref_step_seconds, threads)
         if step >= args.warmup:
             times.append(base["sec_per_mesh"])
     t = sum(times) / len(times)
     value = work_total / t
-    line = {"metric": "tri-voxel tests/s", "value": value, "unit": "tests/s", "n_gpus": args.gpus,
+    line = {"metric": METRIC, "value": value, "unit": "tests/s", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic", "impl": "reference",
-            "config": {"workload": cfg["name"], "desc": cfg["desc"], "l2_flush": "n/a (CPU)"},
+            "config": workload_config(cfg, tris.size // 9),
+            "tests_per_mesh": work_total,
             "cpu_baseline": {"value": value, "unit": "tests/s", "cores": threads, "kind": "port",
-                             "sample": base["sample"]},
+                             "sample": "per step: " + base["sample"]},
             "e2e": {"value": value, "unit": "tests/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    if not args.no_as_written:
+        aw = cpu_as_written(tris, grid, work_total, args.as_written_seconds)
+        line["cpu_as_written"] = {k: v for k, v in aw.items()}
     print(json.dumps(line))
 
 
 # Warp instructions one launch of the Level2 kernel executes on each single-mesh workload, from
-# `ncu --metrics smsp__inst_executed.sum` on the current kernel (profiles/k_level2c_*.md give the
-# commands).  The count is a property of the kernel's code and the input, not of the clock.
-LEVEL2_INST_PER_LAUNCH = {"torus262k": 383936298, "sphere16k": 27523672}
+# a one-launch capture `ncu --metrics smsp__inst_executed.sum,dram__bytes_read.sum,
+# dram__bytes_write.sum -k regex:k_level2c -c 1` of this bench on that workload.  The count is a
+# property of the kernel's code and the input, not of the clock; it is re-captured whenever the
+# kernel changes.
+LEVEL2_INST_PER_LAUNCH = {"star1310k": 3487153763, "torus262k": 383936298, "sphere16k": 27523672}
 # DRAM bytes read + written by one launch of the Level2 kernel (same captures)
-LEVEL2_TRAFFIC = {"torus262k": 30715392 + 4094208, "sphere16k": 2840747}
+LEVEL2_TRAFFIC = {"star1310k": 129920000 + 1140515584, "torus262k": 30715392 + 4094208,
+                  "sphere16k": 2840747}
 
 
 def max_over_ranks(seconds, dist, device):
@@ -481,6 +572,134 @@ def stencil_bench(gpv, ctx, torch, stream, step_device, flush, args, tris, spec,
         out["cpu_oracle_s_per_mesh"] = time.perf_counter() - t0
         out["cpu_oracle_cores"] = os.cpu_count() or 1
     return out
+
+
+def shim_bench(gpv, torch, local, args):
+    """The reference-named shims driven as GPView's Object drives them, on the mid-size mesh
+    (torus262k): CUDAClassifyTessellation into per-voxel id buffers sized to the largest count
+    (src/Object.cpp:2116-2183), the host building the flat and column lists (:2146-2180,
+    :2560-2577), then CUDAClassifyInOutLevel2 and CUDAClassifyTessellationLevel2 (:2603, :2606).
+    Device time of each shim call (CUDA events on the legacy stream, warm), against the native
+    call on the same mesh."""
+    import ctypes as C
+
+    import numpy as np
+
+    import workloads as W
+    from oracle import oracle as orc
+
+    class F3(C.Structure):
+        _fields_ = [("x", C.c_float), ("y", C.c_float), ("z", C.c_float)]
+
+    class I3(C.Structure):
+        _fields_ = [("x", C.c_int), ("y", C.c_int), ("z", C.c_int)]
+
+    L = gpv.lib()
+    vp = C.c_void_p
+    L.CUDAClassifyTessellation.argtypes = [vp, C.c_int, vp, vp, vp, F3, F3, F3, I3, C.c_int]
+    L.CUDAClassifyTessellationLevel2.argtypes = [vp, vp, vp, vp, vp, vp, vp, vp, C.c_int, I3, F3, F3]
+    L.CUDAClassifyInOutLevel2.argtypes = [vp, vp, vp, vp, vp, vp, vp, C.c_int, I3, I3, F3, F3]
+    dev = f"cuda:{local}"
+    tris, spec = W.make(W.C2)
+    T = tris.size // 9
+    tab = orc.grid_tables(spec)  # the caller's float grid values (boxExtents, midpoints)
+    nd = [int(v) for v in spec.ndiv]
+    n2 = [int(v) for v in spec.ndiv2]
+    N1 = int(np.prod(nd))
+    cells = int(np.prod(n2))
+    e1 = F3(*[float(v) for v in tab["e1"]])
+    e2 = F3(*[float(v) for v in tab["e2"]])
+    d_tris = torch.from_numpy(tris).to(dev)
+    s0 = torch.cuda.default_stream(local)
+
+    def timed(fn, reps=5):
+        ms = []
+        for k in range(reps + 1):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(s0)
+            fn()
+            b.record(s0)
+            torch.cuda.synchronize()
+            if k:
+                ms.append(a.elapsed_time(b))
+        return sum(ms) / len(ms)
+
+    with torch.cuda.stream(s0):
+        inout = torch.zeros(N1, dtype=torch.float32, device=dev)
+        cnt = torch.zeros(N1, dtype=torch.int32, device=dev)
+        one = torch.zeros(N1, dtype=torch.int32, device=dev)
+        L.CUDAClassifyTessellation(d_tris.data_ptr(), T, inout.data_ptr(), cnt.data_ptr(),
+                                   one.data_ptr(), F3(*spec.bbox_min), F3(*spec.bbox_max), e1,
+                                   I3(*nd), 1)
+        buf = int(cnt.max().item())
+        idx = torch.zeros(N1 * buf, dtype=torch.int32, device=dev)
+
+        def level1():
+            inout.zero_()
+            cnt.zero_()
+            L.CUDAClassifyTessellation(d_tris.data_ptr(), T, inout.data_ptr(), cnt.data_ptr(),
+                                       idx.data_ptr(), F3(*spec.bbox_min), F3(*spec.bbox_max), e1,
+                                       I3(*nd), buf)
+
+        l1_ms = timed(level1)
+        # the host lists the reference builds between the two levels
+        c = cnt.cpu().numpy()
+        ids = idx.cpu().numpy().reshape(N1, buf)
+        keep = np.arange(buf)[None, :] < c[:, None]
+        flat = ids[keep].astype(np.int32)
+        flat_index = np.zeros(N1, np.int32)
+        flat_index[1:] = np.cumsum(c)[:-1]
+        bidx = np.nonzero(inout.cpu().numpy() == 2)[0].astype(np.int32)
+        B = bidx.size
+        col = (np.repeat(np.arange(N1), c) % (nd[0] * nd[1])).astype(np.int64)
+        u = np.unique(col * T + flat)
+        ucol, utri = u // T, (u % T).astype(np.int32)
+        xcnt = np.bincount(ucol, minlength=nd[0] * nd[1]).astype(np.int32)
+        xidx = np.zeros(nd[0] * nd[1], np.int32)
+        xidx[1:] = np.cumsum(xcnt)[:-1]
+        c1 = tab["c1"]
+        ks, rem = np.divmod(bidx, nd[0] * nd[1])
+        js, is_ = np.divmod(rem, nd[0])
+        mid = np.stack([c1[is_], c1[nd[0] + js], c1[nd[0] + nd[1] + ks]], 1).astype(np.float32)
+        t_mid, t_bi = torch.from_numpy(mid.reshape(-1)).to(dev), torch.from_numpy(bidx).to(dev)
+        t_cnt, t_fi, t_fl = (torch.from_numpy(x).to(dev) for x in (c.astype(np.int32), flat_index, flat))
+        t_xc, t_xi, t_xf = (torch.from_numpy(x).to(dev) for x in (xcnt, xidx, utri))
+        l2 = torch.zeros(B * cells, dtype=torch.float32, device=dev)
+        nrm = torch.zeros(B * cells * 4, dtype=torch.float32, device=dev)
+
+        def level2_fill():
+            l2.zero_()
+            L.CUDAClassifyInOutLevel2(d_tris.data_ptr(), l2.data_ptr(), t_mid.data_ptr(), t_bi.data_ptr(),
+                                      t_xc.data_ptr(), t_xi.data_ptr(), t_xf.data_ptr(), B, I3(*nd),
+                                      I3(*n2), e1, e2)
+
+        def level2_sat():
+            nrm.zero_()
+            L.CUDAClassifyTessellationLevel2(d_tris.data_ptr(), l2.data_ptr(), nrm.data_ptr(),
+                                             t_mid.data_ptr(), t_bi.data_ptr(), t_cnt.data_ptr(),
+                                             t_fi.data_ptr(), t_fl.data_ptr(), B, I3(*n2), e1, e2)
+
+        fill_ms = timed(level2_fill, 3)
+        sat_ms = timed(level2_sat, 3)
+        ctx = gpv.Context(local)
+        ref_boundary = None
+
+        def native():
+            nonlocal ref_boundary
+            r = ctx.voxelize_device(d_tris.data_ptr(), T, spec, s0.cuda_stream)
+            ref_boundary = r.num_boundary
+            ctx.release(r)
+
+        native_ms = timed(native)
+        ctx.close()
+    return {"workload": "torus262k", "level1_buffer": buf, "boundary": int(B),
+            "boundary_matches_native": int(B) == int(ref_boundary),
+            "ms": {"CUDAClassifyTessellation": l1_ms, "CUDAClassifyInOutLevel2": fill_ms,
+                   "CUDAClassifyTessellationLevel2": sat_ms},
+            "shim_total_ms": l1_ms + fill_ms + sat_ms, "native_ms": native_ms,
+            "note": "device time per shim call (legacy stream, CUDA events); the host list "
+                    "building between the levels is not included; the native call computes "
+                    "both levels' states, prefix, index and Level2 bytes without normals"}
 
 
 def progress(msg):
@@ -634,15 +853,11 @@ def main():
     N1, B = stats["level1"], stats["boundary"]
     roof = roofline(rname, per_call, work, stats, spec, T, peaks, peak_kind, clk)
 
-    line = {"metric": "tri-voxel tests/s", "value": value, "unit": "tests/s", "n_gpus": world,
+    line = {"metric": METRIC, "value": value, "unit": "tests/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_total * 1e3 / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-            "data": "synthetic",
-            "config": {"workload": cfg["name"], "desc": cfg["desc"], "triangles": T,
-                       "level1": cfg["level1"], "level2": cfg["level2"], "parallelism": "replicas",
-                       "l2_flush": "256 MiB write between steps (outside the timed spans)",
-                       "work_per_step": dict(zip(("sat1", "sat2", "ray1", "ray2"), work)),
-                       "stats": stats},
+            "data": "synthetic", "config": workload_config(cfg, T),
+            "work_per_step": dict(zip(("sat1", "sat2", "ray1", "ray2"), work)), "stats": stats,
             "meshes_per_s": args.steps * world / t_total,
             "voxels_per_s": (N1 + B * cells) * args.steps * world / t_total,
             "e2e": {"value": e2e_value, "unit": "tests/s", "h2d_bytes_per_step": h2d,
@@ -655,19 +870,30 @@ def main():
     if not args.no_stencil:
         progress("stencil fill section")
         line["stencil_fill"] = stencil_bench(gpv, ctx, torch, stream, step_device, flush, args,
-                                             tris, spec, rank == 0 and not args.no_cpu_baseline)
+                                             tris, spec, rank == 0 and args.stencil_cpu)
     if args.batch > 0:
         progress("batched section")
         line["batched"] = batch_bench(gpv, ctx, torch, stream, local, args)
         tuned = (line["batched"]["tile"], line["batched"]["level2_chunk"])
+    if not args.no_shims:
+        progress("shim section")
+        line["shims"] = shim_bench(gpv, torch, local, args)
     if args.serve_seconds > 0:
         progress("served section")
         line["served"] = served_bench(gpv, torch, local, args, tuned)
     if rank == 0 and not args.no_cpu_baseline:
         progress("cpu baseline")
-        line["cpu_baseline"] = cpu_baseline(tris, spec, tests_per_step, args.cpu_seconds,
-                                            os.cpu_count() or 1)
+        threads = os.cpu_count() or 1
+        # the GPU's work counts are the reference algorithm's: the oracle counts the same
+        _, work_cpu = cpu_work(tris, spec, threads)
+        line["cpu_baseline"] = cpu_sample(tris, spec, tests_per_step, args.cpu_seconds, threads)
         line["cpu_baseline"].pop("sec_per_mesh", None)
+        line["cpu_baseline"]["tests_per_mesh_oracle"] = work_cpu
+        line["cpu_baseline"]["tests_per_mesh_match"] = work_cpu == tests_per_step
+        if not args.no_as_written:
+            aw = cpu_as_written(tris, spec, tests_per_step, args.as_written_seconds)
+            aw.pop("sec_per_mesh", None)
+            line["cpu_baseline"]["as_written"] = aw
     if rank == 0:
         print(json.dumps(line))
     ctx.close()

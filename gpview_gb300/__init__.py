@@ -67,6 +67,8 @@ NORMALS_OFF, NORMALS_BYTES, NORMALS_FLOAT = 0, 1, 2
 # inside fill: +z ray parity (ClassifyInOutCPU / ClassifyInOutLevel2CPU) or the rasterised
 # stencil parity (ClassifyInOut2x / ClassifyInOut2xLevel2)
 FILL_RAY, FILL_STENCIL = 0, 1
+# Level2 SAT organisation (identical results): chosen per launch, queued records, or per lane
+LEVEL2_AUTO, LEVEL2_QUEUED, LEVEL2_INLINE = 0, 1, 2
 
 
 class VoxelConfig(C.Structure):
@@ -144,6 +146,10 @@ def lib():
                                               C.POINTER(C.c_int64), C.c_void_p]
     L.gpv_noalloc_last_error.restype = C.c_char_p
     L.gpv_set_level2_chunk.argtypes = [C.c_void_p, C.c_int]
+    L.gpv_set_level2_mode.argtypes = [C.c_void_p, C.c_int]
+    L.gpv_set_debug.argtypes = [C.c_void_p, C.c_int, C.c_int64]
+    L.gpv_get_debug.argtypes = [C.c_void_p, C.c_int]
+    L.gpv_get_debug.restype = C.c_int64
     L.gpv_set_graphs.argtypes = [C.c_void_p, C.c_int]
     L.gpv_autotune.argtypes = [C.c_void_p, C.c_int32, C.POINTER(C.c_void_p), C.POINTER(C.c_int64),
                                C.POINTER(GridSpec), C.c_void_p, C.POINTER(C.c_int32),
@@ -295,6 +301,20 @@ class Context:
     def set_level2_chunk(self, max_voxels):
         """Largest number of boundary voxels of one Level1 column per Level2 work item."""
         self._check(lib().gpv_set_level2_chunk(self._h, int(max_voxels)), "set_level2_chunk")
+
+    def set_level2_mode(self, mode):
+        """LEVEL2_AUTO (default), LEVEL2_QUEUED or LEVEL2_INLINE: the Level2 SAT organisation."""
+        self._check(lib().gpv_set_level2_mode(self._h, int(mode)), "set_level2_mode")
+
+    DEBUG = {"wait_limit": 1, "fail_wait": 2, "pair_capacity": 3, "fail_allocs": 4, "replans": 5}
+
+    def set_debug(self, what, value):
+        """Failure-detection hooks (gpv_set_debug): 'wait_limit', 'fail_wait', 'pair_capacity',
+        'fail_allocs'."""
+        self._check(lib().gpv_set_debug(self._h, self.DEBUG[what], int(value)), "set_debug")
+
+    def get_debug(self, what):
+        return int(lib().gpv_get_debug(self._h, self.DEBUG[what]))
 
     def _check(self, rc, what):
         if rc:

@@ -288,6 +288,38 @@ int gpv_set_level2_chunk(gpv_ctx *ctx, int cap) {
   return GPV_OK;
 }
 
+int gpv_set_debug(gpv_ctx *ctx, int what, int64_t value) {
+  if (!ctx || value < 0) return GPV_ERR_INVALID;
+  switch (what) {
+    case GPV_DEBUG_WAIT_LIMIT:
+      if (value > 0xffffffffll) return GPV_ERR_INVALID;
+      ctx->wait_limit = (uint32_t)value;
+      return GPV_OK;
+    case GPV_DEBUG_FAIL_WAIT: ctx->fail_wait = value != 0; return GPV_OK;
+    case GPV_DEBUG_PAIR_CAPACITY: ctx->debug_pair_cap = value; return GPV_OK;
+    case GPV_DEBUG_FAIL_ALLOCS: ctx->fail_allocs = value; return GPV_OK;
+    default: return GPV_ERR_INVALID;
+  }
+}
+
+int64_t gpv_get_debug(gpv_ctx *ctx, int what) {
+  if (!ctx) return GPV_ERR_INVALID;
+  switch (what) {
+    case GPV_DEBUG_WAIT_LIMIT: return ctx->wait_limit;
+    case GPV_DEBUG_FAIL_WAIT: return ctx->fail_wait;
+    case GPV_DEBUG_PAIR_CAPACITY: return ctx->debug_pair_cap;
+    case GPV_DEBUG_FAIL_ALLOCS: return ctx->fail_allocs;
+    case GPV_DEBUG_REPLANS: return ctx->replans;
+    default: return GPV_ERR_INVALID;
+  }
+}
+
+int gpv_set_level2_mode(gpv_ctx *ctx, int mode) {
+  if (!ctx || mode < GPV_LEVEL2_AUTO || mode > GPV_LEVEL2_INLINE) return GPV_ERR_INVALID;
+  ctx->l2_mode = mode;
+  return GPV_OK;
+}
+
 int gpv_autotune(gpv_ctx *ctx, int32_t n, const float *const *d_tris, const int64_t *num_triangles,
                  const gpv_grid_spec *specs, cudaStream_t stream, int32_t *tile,
                  int32_t *level2_chunk, float *ms_per_batch) {

@@ -67,7 +67,7 @@ struct Arena {
     }
     off += bytes;
     void *q = nullptr;
-    cudaError_t e = cudaMallocAsync(&q, bytes, s);
+    cudaError_t e = ctx_malloc_async(ctx, &q, bytes, s);
     if (e == cudaSuccess) extra.push_back(q);
     *p = (T *)q;
     return e;
@@ -304,12 +304,12 @@ int run_batch(gpv_ctx *ctx, int n, const float *const *d_tris, const int64_t *T,
   // result arenas (shared by the batch's results, freed when the last one is released)
   auto set = std::make_shared<ResultSet>();
   set->stream = s;
-  CK(cudaMallocAsync(&set->l1, std::max<int64_t>(res_l1[n], 16), s));
-  CK(cudaMallocAsync(&set->prefix, 4 * std::max<int64_t>(res_pre[n], 16), s));
-  if (res_hier[n] > 0) CK(cudaMallocAsync(&set->hier, sizeof(gpv_box) * res_hier[n], s));
+  CK(ctx_malloc_async(ctx, &set->l1, std::max<int64_t>(res_l1[n], 16), s));
+  CK(ctx_malloc_async(ctx, &set->prefix, 4 * std::max<int64_t>(res_pre[n], 16), s));
+  if (res_hier[n] > 0) CK(ctx_malloc_async(ctx, &set->hier, sizeof(gpv_box) * res_hier[n], s));
   if (nmode) {
     // voxels without recorded triangles keep the zero normal: 0.0f, or byte 127 (0 * scale + 127)
-    CK(cudaMallocAsync(&set->l1n, std::max<int64_t>(res_l1n[n], 16), s));
+    CK(ctx_malloc_async(ctx, &set->l1n, std::max<int64_t>(res_l1n[n], 16), s));
     CK(cudaMemsetAsync(set->l1n, nmode == GPV_NORMALS_FLOAT ? 0 : 127, res_l1n[n], s));
   }
 
@@ -355,6 +355,8 @@ int run_batch(gpv_ctx *ctx, int n, const float *const *d_tris, const int64_t *T,
   bd.stp = nullptr;
   bd.stp_words = 0;
   bd.kmask = kmark ? bplane + words : nullptr;
+  bd.wait_limit = ctx->wait_limit;
+  bd.fail_wait = ctx->fail_wait;
   CK(ctx_ensure_host(ctx, (size_t)n));
   std::memcpy(ctx->h_md, md.data(), n * sizeof(MeshDesc));
 
@@ -380,7 +382,11 @@ int run_batch(gpv_ctx *ctx, int n, const float *const *d_tris, const int64_t *T,
   // the pair buffer has the context's capacity hint; a mesh that does not fit raises
   // ST_PAIR_OVERFLOW and the call re-runs with the exact capacity), Level1, fill finish,
   // boundary scan.
-  const int64_t pair_cap = std::max<int64_t>(ctx->pair_hint, std::max<int64_t>(16 * tris, 1 << 16));
+  int64_t pair_cap = std::max<int64_t>(ctx->pair_hint, std::max<int64_t>(16 * tris, 1 << 16));
+  if (ctx->debug_pair_cap > 0) {  // failure-detection hook: a first capacity that overflows
+    pair_cap = ctx->debug_pair_cap;
+    ctx->debug_pair_cap = 0;
+  }
   uint32_t *keys, *vals;
   CK(ws.get(&keys, (size_t)pair_cap));
   CK(ws.get(&vals, (size_t)pair_cap));
@@ -392,7 +398,8 @@ int run_batch(gpv_ctx *ctx, int n, const float *const *d_tris, const int64_t *T,
                        (uint64_t)bd.total_rows, (uint64_t)bd.total_words,
                        (uint64_t)(uintptr_t)bd.queue, (uint64_t)bd.normals, (uint64_t)bd.fill,
                        (uint64_t)(uintptr_t)bd.stp, (uint64_t)bd.stp_words,
-                       (uint64_t)ctx->timing, (uint64_t)ctx->num_sms})
+                       (uint64_t)ctx->timing, (uint64_t)ctx->num_sms, (uint64_t)bd.wait_limit,
+                       (uint64_t)bd.fail_wait})
       v.push_back(x);
   };
   std::vector<uint64_t> sig0;
@@ -463,6 +470,7 @@ int run_batch(gpv_ctx *ctx, int n, const float *const *d_tris, const int64_t *T,
     if (overflow) {
       if (ctx->pair_hint >= need) return fail_all(GPV_ERR_DEVICE, "pair buffer overflow");
       ctx->pair_hint = need + need / 8;
+      ctx->replans++;
       fail_all(GPV_OK, "");
       ctx->err.clear();
       return run_batch(ctx, n, d_tris, T, specs, out, s);
@@ -489,15 +497,15 @@ int run_batch(gpv_ctx *ctx, int n, const float *const *d_tris, const int64_t *T,
   // host outputs into pinned memory: the Level2 kernel writes its bytes there itself (over the
   // CPU-GPU link while it computes) instead of into device memory followed by copies
   const bool l2_direct = sink && sink->l2_dev && gh[0].level2 && sink->l2_cap >= l2bytes;
-  CK(cudaMallocAsync(&set->bindex, 4 * std::max<int64_t>(Btot, 4), s));
+  CK(ctx_malloc_async(ctx, &set->bindex, 4 * std::max<int64_t>(Btot, 4), s));
   if (l2_direct) {
     set->l2 = sink->l2_dev;
     set->l2_external = true;
   } else {
-    CK(cudaMallocAsync(&set->l2, std::max<int64_t>(l2bytes, 16), s));
+    CK(ctx_malloc_async(ctx, &set->l2, std::max<int64_t>(l2bytes, 16), s));
   }
   if (nmode) {
-    CK(cudaMallocAsync(&set->l2n, std::max<int64_t>(3 * l2bytes * (int64_t)nsz, 16), s));
+    CK(ctx_malloc_async(ctx, &set->l2n, std::max<int64_t>(3 * l2bytes * (int64_t)nsz, 16), s));
     for (int m = 0; m < n; ++m) md[m].l2n = static_cast<uint8_t *>(set->l2n) + 3 * l2off[m] * nsz;
   }
   for (int m = 0; m < n; ++m) {
@@ -579,7 +587,9 @@ int run_batch(gpv_ctx *ctx, int n, const float *const *d_tris, const int64_t *T,
   {
     std::unique_ptr<bool[]> has_l2(new bool[n]);
     for (int m = 0; m < n; ++m) has_l2[m] = gh[m].level2;
-    l2_queue = level2_queue_pays(ctx->h_stats, has_l2.get(), n);
+    l2_queue = ctx->l2_mode == GPV_LEVEL2_QUEUED   ? true
+               : ctx->l2_mode == GPV_LEVEL2_INLINE ? false
+                                                   : level2_queue_pays(ctx->h_stats, has_l2.get(), n);
   }
   std::vector<uint64_t> sig1;
   bool any_hier = false;

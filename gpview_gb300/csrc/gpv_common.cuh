@@ -3,7 +3,7 @@
 //
 // Every predicate is written with __fadd_rn/__fsub_rn/__fmul_rn so that no multiply-add is
 // contracted whatever the compiler flags, and follows the operation order of the reference's
-// CPU code (src/TriBoxIntersection.cpp:64-210, src/TriRayIntersection.cpp:289-342).  The two
+// CPU code (src/TriBoxIntersection.cpp:64-210, src/TriRayIntersection.cpp:78-131).  The two
 // double-precision comparisons of the ray test (det against +-1e-6, t > 1e-6) are evaluated
 // exactly in float against `thr`, the largest float below 1e-6:  for a float x,
 // (double)x < 1e-6  <=>  x <= thr,  and  (double)x > 1e-6  <=>  x > thr.

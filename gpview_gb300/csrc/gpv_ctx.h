@@ -40,6 +40,13 @@ struct gpv_ctx {
   std::string err;
   int tile = 0;                        // Level1 triangles per tile (autotuned; 0: by mesh size)
   int l2_chunk_cap = 8;                // Level2 boundary voxels per chunk, upper bound (autotuned)
+  int l2_mode = GPV_LEVEL2_AUTO;       // Level2 SAT organisation (GPV_LEVEL2_*)
+  // failure-detection hooks (gpv_set_debug) and what they caused (gpv_get_debug)
+  uint32_t wait_limit = 0;             // Level1 tile wait polls (0: built-in)
+  int fail_wait = 0;                   // Level1's tile wait gives up at once
+  int64_t debug_pair_cap = 0;          // next call's first pair capacity (one-shot)
+  int64_t fail_allocs = 0;             // refuse this many of the next device allocations
+  int64_t replans = 0;                 // calls re-run after a pair-buffer overflow
   bool graphs = true;                  // record the two phases as CUDA graphs
   int normals = 0;                     // GPV_NORMALS_* for the next voxelizations
   bool hierarchy = false;              // build the voxel box hierarchy
@@ -86,7 +93,18 @@ inline int ctx_fail(gpv_ctx *ctx, int code, const char *what) {
 
 inline int ctx_cuda_fail(gpv_ctx *ctx, cudaError_t e, const char *where) {
   if (ctx) ctx->err = std::string(where) + ": " + cudaGetErrorString(e);
-  return GPV_ERR_CUDA;
+  return e == cudaErrorMemoryAllocation ? GPV_ERR_OOM : GPV_ERR_CUDA;
+}
+
+// Stream-ordered device allocation of the context; refused while the failure-detection hook
+// GPV_DEBUG_FAIL_ALLOCS has refusals left.
+inline cudaError_t ctx_malloc_async(gpv_ctx *ctx, void **p, size_t bytes, cudaStream_t s) {
+  if (ctx->fail_allocs > 0) {
+    ctx->fail_allocs--;
+    *p = nullptr;
+    return cudaErrorMemoryAllocation;
+  }
+  return cudaMallocAsync(p, bytes, s);
 }
 
 inline cudaError_t ctx_ensure_tables(gpv_ctx *ctx, size_t n) {

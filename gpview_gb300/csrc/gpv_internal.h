@@ -76,6 +76,10 @@ struct MeshDesc {
   uint32_t *stg;         // stencil fill: Level1 sample-column toggles, (2nx * 2ny) x nzw words
 };
 
+// BatchDev::fill value for Level1 SAT units only (no parity fill): the reference-named Level1
+// shim, whose ClassifyTessellation marks boundary voxels and records their triangles.
+constexpr int kFillNone = -1;
+
 struct BatchDev {
   const MeshDesc *md;
   int nmesh;
@@ -89,6 +93,10 @@ struct BatchDev {
   // Level1 marks the voxel of every pair it emits for a mesh with a Level2 grid here: one
   // column-major bit plane per mesh (bit = pair key) at the mesh's word_base; nullptr: no marks
   uint32_t *kmask = nullptr;
+  // Level1's bounded wait for its staged tile: polls before giving up (0: the built-in limit);
+  // fail_wait != 0 gives up at once (GPV_DEBUG_FAIL_WAIT, failure-detection tests)
+  uint32_t wait_limit = 0;
+  int fail_wait = 0;
 };
 
 // Small copies and clears around a phase, done by one kernel instead of copy-engine and memset

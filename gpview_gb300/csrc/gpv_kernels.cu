@@ -222,12 +222,12 @@ __global__ void __launch_bounds__(256) k_prep(BatchDev bd) {
     }
     if (fx0 <= fx1 && fy0 <= fy1) fu = (unsigned long long)(fx1 - fx0 + 1) * (fy1 - fy0 + 1);
     else { fx0 = 1; fx1 = 0; fy0 = 1; fy1 = 0; }
-    if (bd.fill == GPV_FILL_STENCIL) {  // the stencil kernel fills instead of the ray units
+    if (bd.fill != GPV_FILL_RAY) {  // the stencil kernel fills instead (or nothing fills)
       fx0 = 1; fx1 = 0; fy0 = 1; fy1 = 0;
       fu = 0;
       r1 = 0;
     }
-    // 1/det of the +z ray test (src/TriRayIntersection.cpp:310), shared by every column
+    // 1/det of the +z ray test (src/TriRayIntersection.cpp:99), shared by every column
     const float det = fa(fm(fs(V[3], V[0]), -fs(V[7], V[1])), fm(fs(V[4], V[1]), fs(V[6], V[0])));
     d.ptri[3 * t + 0] = make_float4(V[0], V[1], V[2], __uint_as_float(pack2(fx0, fx1)));
     d.ptri[3 * t + 1] = make_float4(V[3], V[4], V[5], __uint_as_float(pack2(fy0, fy1)));
@@ -338,7 +338,11 @@ __global__ void __launch_bounds__(kL1Threads) k_level1(BatchDev bd) {
       bulk_g2s(s_tri, d.ptri + 3 * t0, bt, &s_bar);
       bulk_g2s(s_rng, d.rng + t0, br, &s_bar);
     }
-    const bool ok = mbar_wait_bounded(&s_bar, iter & 1u, kWaitLimit);
+    // bounded wait (bd.wait_limit polls, kWaitLimit when 0); bd.fail_wait makes it give up at
+    // once (failure-detection tests).  On giving up, the status word is raised and thread 0
+    // waits, bounded again, for the copies in flight to land before the block returns.
+    const bool ok = !bd.fail_wait &&
+                    mbar_wait_bounded(&s_bar, iter & 1u, bd.wait_limit ? bd.wait_limit : kWaitLimit);
     if (__syncthreads_or(!ok)) {
       if (threadIdx.x == 0) {
         atomicOr(&d.stats->status, (unsigned)ST_WAIT_TIMEOUT);

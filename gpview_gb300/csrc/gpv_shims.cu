@@ -1,6 +1,13 @@
-// gpv_shims.cu -- the reference-named C entry points GPView's Object class binds
-// (includes/CUDAUtilities.h:63-64, :87-89), with the same signatures, caller-owned device
-// buffers, legacy default stream and "return 1" convention.
+// gpv_shims.cu -- the reference-named C entry points of GPView's CUDA library (GPViewCUDA, built
+// from cuda/CUDAClassifyTessellation.cu and cuda/THRUSTUtilities.cu), with the same signatures,
+// caller-owned device buffers, legacy default stream and return conventions, so that GPView
+// relinks against libgpview.so in place of GPViewCUDA:
+//   CUDAClassifyTessellation, CUDAClassifyTessellationLevel2, CUDAClassifyInOutLevel2
+//     (includes/CUDAUtilities.h:87-89);
+//   THRUSTDeviceFindMax, THRUSTDeviceFindMaxFloat4, THRUSTDeviceMinMaxSort
+//     (includes/CUDAUtilities.h:72-74; src/CUDAUtilities.cpp:121-132 calls the first).
+// InitializeCUDA and CUDACheckErrors are not here: the reference declares them with C++ linkage
+// (includes/CUDAUtilities.h:63-64) and defines them in the application (src/CUDAUtilities.cpp).
 //
 // Arithmetic follows the reference's CPU code, not its CUDA-8 kernels: box centres are the CPU's
 // double-then-float expressions, predicates run without contraction (the reference kernels let
@@ -8,8 +15,15 @@
 // inputs do not carry what the CPU formula needs (the Level2 ray origins of
 // CUDAClassifyInOutLevel2), the reference kernel's own FP32 formula is used, evaluated without
 // contraction.
+//
+// CUDAClassifyTessellation runs on the library's Level1 engine (the prep kernel, the persistent
+// TMA-staged Level1 kernel's SAT units, then a scatter of its (voxel, triangle) records into the
+// caller's arrays).  All shims share one grow-only device workspace kept for the process, so a
+// call allocates only when it needs more room than any earlier call.
+#include <algorithm>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <vector>
 
 #include "gpv_internal.h"
@@ -17,8 +31,92 @@
 namespace gpv {
 namespace {
 
-// CUDAClassifyTessellationKernel (cuda/CUDAClassifyTessellation.cu:320-401), one thread per
-// triangle over its candidate box; the per-voxel list never writes past triBufferLen.
+// Grow-only workspace of the shims (process-wide; the reference's callers are single-threaded,
+// and a mutex serialises calls from several threads).  Growth frees the old block after a
+// device synchronisation, so work still queued on it has finished.
+struct ShimSpace {
+  std::mutex mu;
+  void *dev = nullptr;
+  size_t cap = 0;
+  MeshStats *h_stats = nullptr;  // page-locked
+  float *h_tab = nullptr;        // page-locked staging of tables
+  size_t h_tab_cap = 0;
+  int device = -1, num_sms = 0;
+};
+ShimSpace g_shim;
+
+size_t al256(size_t v) { return (v + 255) & ~size_t(255); }
+
+// Room for `bytes` in the workspace; false if it cannot be had.
+bool shim_reserve(size_t bytes) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return false;
+  if (dev != g_shim.device) {  // another device: start over there
+    g_shim.dev = nullptr;
+    g_shim.cap = 0;
+    g_shim.device = dev;
+    cudaDeviceGetAttribute(&g_shim.num_sms, cudaDevAttrMultiProcessorCount, dev);
+  }
+  if (!g_shim.h_stats && cudaMallocHost(&g_shim.h_stats, sizeof(MeshStats)) != cudaSuccess) {
+    g_shim.h_stats = nullptr;
+    return false;
+  }
+  if (bytes <= g_shim.cap) return true;
+  if (g_shim.dev) {
+    cudaDeviceSynchronize();
+    cudaFree(g_shim.dev);
+  }
+  g_shim.dev = nullptr;
+  g_shim.cap = 0;
+  const size_t want = std::max(bytes + bytes / 4, size_t(1) << 20);
+  if (cudaMalloc(&g_shim.dev, want) != cudaSuccess) {
+    cudaGetLastError();
+    g_shim.dev = nullptr;
+    return false;
+  }
+  g_shim.cap = want;
+  return true;
+}
+
+bool shim_tables(size_t floats) {
+  if (floats <= g_shim.h_tab_cap) return true;
+  if (g_shim.h_tab) cudaFreeHost(g_shim.h_tab);
+  g_shim.h_tab = nullptr;
+  g_shim.h_tab_cap = 0;
+  if (cudaMallocHost(&g_shim.h_tab, std::max<size_t>(floats, 4096) * sizeof(float)) != cudaSuccess) {
+    g_shim.h_tab = nullptr;
+    return false;
+  }
+  g_shim.h_tab_cap = std::max<size_t>(floats, 4096);
+  return true;
+}
+
+// The Level1 engine's (voxel, triangle) records into the reference's arrays: inOut[v] = 2,
+// voxelTriCount[v] += 1 and the triangle id in the next free slot of voxelTriIndex[v * buf ..]
+// (never past buf; the count keeps the true number).  keys are column-major voxel keys
+// ((y * nx + x) * nz + z); the top bit of a value flags a column's topmost record.
+__global__ void k_shim_scatter(const uint32_t *__restrict__ keys, const uint32_t *__restrict__ vals,
+                               const MeshStats *__restrict__ st, int nx, int ny, int nz,
+                               float *__restrict__ inOut, int *__restrict__ cnt,
+                               int *__restrict__ idx, int buf) {
+  const uint64_t P = st->pairs < st->pair_cap ? st->pairs : st->pair_cap;
+  for (uint64_t e = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; e < P;
+       e += (uint64_t)gridDim.x * blockDim.x) {
+    const uint32_t key = keys[e];
+    const int r = (int)(key % (uint32_t)nz);
+    const uint32_t col = key / (uint32_t)nz;
+    const int p = (int)(col % (uint32_t)nx), q = (int)(col / (uint32_t)nx);
+    const size_t v = ((size_t)r * ny + q) * nx + p;
+    inOut[v] = 2.0f;
+    const int slot = atomicAdd(&cnt[v], 1);
+    if (slot >= 0 && slot < buf) idx[v * (size_t)buf + slot] = (int)(vals[e] & 0x7fffffffu);
+  }
+}
+
+// CUDAClassifyTessellationKernel's launch shape (cuda/CUDAClassifyTessellation.cu:320-401): one
+// thread per triangle over its candidate box; the per-voxel list never writes past
+// triBufferLen.  Used only for triangle buffers that are not 16-byte aligned (the engine's
+// prep kernel reads them as such).
 __global__ void k_shim_level1(const float *__restrict__ tris, int T, float *__restrict__ inOut,
                               int *__restrict__ cnt, int *__restrict__ idx, GridDev g, int buf) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -45,6 +143,80 @@ __global__ void k_shim_level1(const float *__restrict__ tris, int T, float *__re
         if (slot >= 0 && slot < buf) idx[v * (size_t)buf + slot] = t;
       }
     }
+}
+
+// ---- the THRUSTUtilities entry points, without Thrust --------------------------------------
+// thrust::max_element's answer, the first index of the largest value under operator<, for a
+// sequence read from the start: the first element stays the answer while nothing compares
+// greater, so a NaN first element is the answer and later NaNs never are; -0 and +0 compare
+// equal.  One 64-bit key per element orders by value, then by lower index.
+__device__ unsigned long long g_thrust_max_key;
+
+__device__ __forceinline__ unsigned long long max_key(float v, uint64_t i, bool first_nan) {
+  if (first_nan) return ~0ull;  // element 0 is NaN: it is the answer
+  if (v != v) return 0ull;      // later NaNs never are
+  uint32_t b = __float_as_uint(v == 0.0f ? 0.0f : v);
+  b = (b & 0x80000000u) ? ~b : (b | 0x80000000u);
+  return ((unsigned long long)b << 32) | (0xffffffffull - (uint32_t)i);
+}
+
+// Values at x[i * stride] (stride 1: floats; stride 4 with x pointing at .w: float4's w).
+__global__ void k_thrust_max(const float *__restrict__ x, int64_t n, int stride) {
+  unsigned long long best = 0ull;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const float v = x[i * stride];
+    const unsigned long long k = max_key(v, (uint64_t)i, i == 0 && v != v);
+    best = k > best ? k : best;
+  }
+#pragma unroll
+  for (int d = 16; d > 0; d >>= 1) {
+    const unsigned long long o = __shfl_xor_sync(0xffffffffu, best, d);
+    best = o > best ? o : best;
+  }
+  if ((threadIdx.x & 31) == 0 && best) atomicMax(&g_thrust_max_key, best);
+}
+
+// Index of the answer of k_thrust_max over n values, or -1 (n <= 0 or failure).
+int64_t thrust_argmax(const float *x, int64_t n, int stride, int num_sms) {
+  if (n <= 0 || n > 0xffffffffll) return -1;
+  const unsigned long long zero = 0ull;
+  if (cudaMemcpyToSymbolAsync(g_thrust_max_key, &zero, sizeof(zero), 0, cudaMemcpyHostToDevice, 0) !=
+      cudaSuccess)
+    return -1;
+  const int64_t blocks = std::min<int64_t>((n + 255) / 256, (int64_t)std::max(num_sms, 1) * 8);
+  k_thrust_max<<<(unsigned)blocks, 256>>>(x, n, stride);
+  count_launch();
+  unsigned long long key = 0ull;
+  if (cudaMemcpyFromSymbol(&key, g_thrust_max_key, sizeof(key)) != cudaSuccess) return -1;
+  if (key == ~0ull) return 0;
+  if (key == 0ull) return 0;  // every value NaN after a non-NaN first: the first stays
+  return (int64_t)(0xffffffffull - (key & 0xffffffffull));
+}
+
+int shim_num_sms() {
+  int dev = 0, sms = 1;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  return sms;
+}
+
+// THRUSTDeviceMinMaxSort's keys: rows >= 0 by value, then every negative row, in input order
+// (the reference's comparator -- a < b when a.row >= 0 and a.row < b.row -- leaves the negative
+// rows unordered; stable placement after the others is this library's choice).
+__global__ void k_minmax_keys(const int *__restrict__ row, int64_t n, uint32_t *__restrict__ keys,
+                              uint32_t *__restrict__ vals) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int r = row[i];
+  keys[i] = r >= 0 ? (uint32_t)r : 0xffffffffu;
+  vals[i] = (uint32_t)i;
+}
+
+__global__ void k_minmax_gather(const int *__restrict__ row, const uint32_t *__restrict__ order,
+                                int64_t n, int *__restrict__ out) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = row[order[i]];
 }
 
 // Unit face normal as the loaders compute it (VectorCrossProduct then VectorNormalize,
@@ -138,34 +310,6 @@ using namespace gpv;
 
 extern "C" {
 
-void InitializeCUDA(void) {
-  // CUTGetMaxGflopsDeviceID (includes/CUDAUtilities.h:32-61): most SMs x clock.
-  int n = 0;
-  cudaGetDeviceCount(&n);
-  int best = 0;
-  long long best_score = -1;
-  for (int d = 0; d < n; ++d) {
-    int sms = 0, clk = 0;
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, d);
-    cudaDeviceGetAttribute(&clk, cudaDevAttrClockRate, d);
-    if ((long long)sms * clk > best_score) {
-      best_score = (long long)sms * clk;
-      best = d;
-    }
-  }
-  cudaSetDevice(best);
-  cudaDeviceProp prop;
-  if (cudaGetDeviceProperties(&prop, best) == cudaSuccess) std::printf("Device in use : %s\n", prop.name);
-  CUDACheckErrors(" Init ");
-}
-
-void CUDACheckErrors(char const *label) {
-  // src/CUDAUtilities.cpp:33-49: synchronise, read the last error, print it, continue.
-  cudaError_t e = cudaDeviceSynchronize();
-  if (e == cudaSuccess) e = cudaGetLastError();
-  if (e != cudaSuccess) std::printf("CUDA Error: %s %s\n", label ? label : "", cudaGetErrorString(e));
-}
-
 int CUDAClassifyTessellation(float *trianglesCUDAData, int numTriangles, float *inOutCUDAData,
                              int *voxelTriCountCUDAData, int *voxelTriIndexCUDAData,
                              float3 objBoxMin, float3 objBoxMax, float3 boxExtents, int3 numDiv,
@@ -178,27 +322,119 @@ int CUDAClassifyTessellation(float *trianglesCUDAData, int numTriangles, float *
   const float ext[3] = {boxExtents.x, boxExtents.y, boxExtents.z};
   GridHost gh;
   if (grid_derive(spec, gh, ext) != GPV_OK || numTriangles <= 0) return 1;
-  std::vector<float> tab;
-  for (int a = 0; a < 3; ++a) tab.insert(tab.end(), gh.c1[a].begin(), gh.c1[a].end());
-  float *d_tab = nullptr;
-  if (cudaMalloc(&d_tab, tab.size() * sizeof(float)) != cudaSuccess) return 1;
-  cudaMemcpy(d_tab, tab.data(), tab.size() * sizeof(float), cudaMemcpyHostToDevice);
-  GridDev g;
-  std::memset(&g, 0, sizeof(g));
-  for (int a = 0; a < 3; ++a) {
-    g.bmin[a] = spec.bbox_min[a];
-    g.bmax[a] = spec.bbox_max[a];
-    g.n[a] = gh.n[a];
-    g.e1[a] = gh.e1[a];
+  std::lock_guard<std::mutex> lk(g_shim.mu);
+  const int64_t T = numTriangles;
+  const int64_t N1w = (int64_t)gh.n[2] * gh.n[1] * gh.nxw;
+  const int64_t tog = (int64_t)gh.n[0] * gh.n[1] * gh.nzw;
+  const int64_t ntab = table_floats(gh);
+  // workspace: tables, packed triangles, SAT ranges, ray boxes, planes, toggles, stats,
+  // descriptor, queue, then the records (sized after the prep kernel has counted them)
+  size_t off = 0;
+  auto take = [&](size_t bytes) { const size_t at = off; off = al256(off + bytes); return at; };
+  const size_t o_tab = take(4 * (size_t)ntab), o_ptri = take(48 * (size_t)T),
+               o_rng = take(16 * (size_t)T), o_fbox = take(16 * (size_t)T),
+               o_bp = take(4 * (size_t)N1w), o_ip = take(4 * (size_t)N1w),
+               o_tg = take(4 * (size_t)tog), o_st = take(sizeof(MeshStats)),
+               o_md = take(sizeof(MeshDesc)), o_q = take(64);
+  const size_t fixed = off;
+  const bool aligned = (reinterpret_cast<uintptr_t>(trianglesCUDAData) & 15u) == 0;
+  if (!shim_reserve(fixed) || !shim_tables((size_t)ntab)) return 1;
+  char *base = static_cast<char *>(g_shim.dev);
+  pack_tables(gh, g_shim.h_tab);
+  float *d_tab = reinterpret_cast<float *>(base + o_tab);
+  cudaMemcpyAsync(d_tab, g_shim.h_tab, 4 * (size_t)ntab, cudaMemcpyHostToDevice, 0);
+  GridDev g = make_griddev(gh, d_tab);
+  if (!aligned) {
+    k_shim_level1<<<(numTriangles + 127) / 128, 128>>>(trianglesCUDAData, numTriangles,
+                                                        inOutCUDAData, voxelTriCountCUDAData,
+                                                        voxelTriIndexCUDAData, g, triBufferLen);
+    count_launch();
+    cudaStreamSynchronize(0);  // the staged tables may be rewritten by the next call
+    return 1;
   }
-  g.c1[0] = d_tab;
-  g.c1[1] = d_tab + gh.n[0];
-  g.c1[2] = d_tab + gh.n[0] + gh.n[1];
-  k_shim_level1<<<(numTriangles + 127) / 128, 128>>>(trianglesCUDAData, numTriangles,
-                                                      inOutCUDAData, voxelTriCountCUDAData,
-                                                      voxelTriIndexCUDAData, g, triBufferLen);
+  MeshDesc md;
+  std::memset(&md, 0, sizeof(md));
+  md.g = g;
+  md.tris = trianglesCUDAData;
+  md.T = T;
+  md.ptri = reinterpret_cast<float4 *>(base + o_ptri);
+  md.rng = reinterpret_cast<int4 *>(base + o_rng);
+  md.fbox = reinterpret_cast<float4 *>(base + o_fbox);
+  md.bplane = reinterpret_cast<uint32_t *>(base + o_bp);
+  md.iplane = reinterpret_cast<uint32_t *>(base + o_ip);
+  md.toggles = reinterpret_cast<uint32_t *>(base + o_tg);
+  md.stats = reinterpret_cast<MeshStats *>(base + o_st);
+  md.ch = 1;
+  MeshDesc *d_md = reinterpret_cast<MeshDesc *>(base + o_md);
+  int tile = 256;
+  while (tile > 32 && T < (int64_t)tile * 3 * g_shim.num_sms) tile >>= 1;
+  BatchDev bd;
+  std::memset(&bd, 0, sizeof(bd));
+  bd.md = d_md;
+  bd.nmesh = 1;
+  bd.tile = tile;
+  bd.total_tris = T;
+  bd.total_tiles = (T + tile - 1) / tile;
+  bd.total_fwarps = (int64_t)gh.n[1] * gh.nxw * gh.nzw;
+  bd.total_rows = (int64_t)gh.n[2] * gh.n[1];
+  bd.total_words = N1w;
+  bd.queue = reinterpret_cast<uint32_t *>(base + o_q);
+  bd.fill = kFillNone;  // SAT units only: ClassifyTessellation marks boundaries, nothing fills
+  cudaMemsetAsync(md.stats, 0, sizeof(MeshStats), 0);
+  cudaMemsetAsync(md.bplane, 0, 4 * (size_t)N1w, 0);
+  cudaMemcpyAsync(d_md, &md, sizeof(md), cudaMemcpyHostToDevice, 0);
+  launch_prep(bd, 0);
+  // the records' room: one per candidate-box test at most (sat1), read back once
+  cudaMemcpyAsync(g_shim.h_stats, md.stats, sizeof(MeshStats), cudaMemcpyDeviceToHost, 0);
+  if (cudaStreamSynchronize(0) != cudaSuccess) return 1;
+  const int64_t cap = std::max<int64_t>((int64_t)g_shim.h_stats->sat1, 1);
+  const size_t o_keys = al256(fixed), o_vals = al256(o_keys + 4 * (size_t)cap);
+  const size_t need = al256(o_vals + 4 * (size_t)cap);
+  if (need > g_shim.cap) {
+    // growing frees the block: copy what the prep kernel produced to the new one
+    void *old = g_shim.dev;
+    g_shim.dev = nullptr;
+    g_shim.cap = 0;
+    if (!shim_reserve(need)) {
+      g_shim.dev = old;  // keep the old block; give up on this call
+      return 1;
+    }
+    cudaMemcpy(g_shim.dev, old, fixed, cudaMemcpyDeviceToDevice);
+    cudaFree(old);
+    base = static_cast<char *>(g_shim.dev);
+    md.g = make_griddev(gh, reinterpret_cast<float *>(base + o_tab));
+    md.ptri = reinterpret_cast<float4 *>(base + o_ptri);
+    md.rng = reinterpret_cast<int4 *>(base + o_rng);
+    md.fbox = reinterpret_cast<float4 *>(base + o_fbox);
+    md.bplane = reinterpret_cast<uint32_t *>(base + o_bp);
+    md.iplane = reinterpret_cast<uint32_t *>(base + o_ip);
+    md.toggles = reinterpret_cast<uint32_t *>(base + o_tg);
+    md.stats = reinterpret_cast<MeshStats *>(base + o_st);
+    d_md = reinterpret_cast<MeshDesc *>(base + o_md);
+    bd.md = d_md;
+    bd.queue = reinterpret_cast<uint32_t *>(base + o_q);
+  }
+  uint32_t *keys = reinterpret_cast<uint32_t *>(base + o_keys);
+  uint32_t *vals = reinterpret_cast<uint32_t *>(base + o_vals);
+  md.keys = keys;
+  md.vals = vals;
+  md.pair_cap = cap;
+  md.emit_base = 0;
+  cudaMemcpyAsync(d_md, &md, sizeof(md), cudaMemcpyHostToDevice, 0);
+  {
+    // the pair capacity the Level1 kernel checks its records against
+    const unsigned long long c = (unsigned long long)cap;
+    cudaMemcpyAsync(&md.stats->pair_cap, &c, sizeof(c), cudaMemcpyHostToDevice, 0);
+  }
+  launch_level1(bd, g_shim.num_sms, 0);
+  const int64_t blocks = std::min<int64_t>((cap + 255) / 256, (int64_t)g_shim.num_sms * 8);
+  k_shim_scatter<<<(unsigned)std::max<int64_t>(blocks, 1), 256>>>(
+      keys, vals, md.stats, gh.n[0], gh.n[1], gh.n[2], inOutCUDAData, voxelTriCountCUDAData,
+      voxelTriIndexCUDAData, triBufferLen);
   count_launch();
-  cudaFree(d_tab);  // ordered after the kernel on the legacy stream
+  // the workspace is reused by the next call: let this one finish first (the reference's
+  // caller synchronises right after anyway, src/Object.cpp:2116-2120)
+  cudaStreamSynchronize(0);
   return 1;
 }
 
@@ -210,11 +446,15 @@ int CUDAClassifyTessellationLevel2(float *trianglesCUDAData, float *level2InOutC
                                    float3 boxExtentsLevel2) {
   const int cells = numDiv2.x * numDiv2.y * numDiv2.z;
   if (numBoundary <= 0 || cells <= 0) return 1;
-  // Midpoints are device data: bring them over, form the centre table in double on the host.
+  std::lock_guard<std::mutex> lk(g_shim.mu);
+  // Midpoints are device data: bring them over (page-locked staging) and form the centre table
+  // in double on the host, as the CPU path does; the table goes to the shared workspace.
   const int nn = numDiv2.x + numDiv2.y + numDiv2.z;
-  std::vector<float> mid((size_t)numBoundary * 3), cen((size_t)numBoundary * nn);
-  if (cudaMemcpy(mid.data(), level1MidPointCUDAData, mid.size() * sizeof(float),
-                 cudaMemcpyDeviceToHost) != cudaSuccess)
+  const size_t nmid = (size_t)numBoundary * 3, ncen = (size_t)numBoundary * nn;
+  if (!shim_reserve(4 * ncen) || !shim_tables(nmid + ncen)) return 1;
+  float *mid = g_shim.h_tab, *cen = g_shim.h_tab + nmid;
+  if (cudaMemcpy(mid, level1MidPointCUDAData, nmid * sizeof(float), cudaMemcpyDeviceToHost) !=
+      cudaSuccess)
     return 1;
   const float e1[3] = {boxExtentsLevel1.x, boxExtentsLevel1.y, boxExtentsLevel1.z};
   const float e2[3] = {boxExtentsLevel2.x, boxExtentsLevel2.y, boxExtentsLevel2.z};
@@ -225,16 +465,15 @@ int CUDAClassifyTessellationLevel2(float *trianglesCUDAData, float *level2InOutC
       for (int p = 0; p < n2[a]; ++p)
         cen[(size_t)b * nn + o + p] = (float)((p + 0.5) * g2 + (double)mid[3 * (size_t)b + a] - e1[a]);
     }
-  float *d_cen = nullptr;
-  if (cudaMalloc(&d_cen, cen.size() * sizeof(float)) != cudaSuccess) return 1;
-  cudaMemcpy(d_cen, cen.data(), cen.size() * sizeof(float), cudaMemcpyHostToDevice);
+  float *d_cen = static_cast<float *>(g_shim.dev);
+  cudaMemcpyAsync(d_cen, cen, ncen * sizeof(float), cudaMemcpyHostToDevice, 0);
   const int64_t n = (int64_t)numBoundary * cells;
   k_shim_level2_sat<<<(unsigned)((n + 127) / 128), 128>>>(
       trianglesCUDAData, level2InOutCUDAData, level2NormalCUDAData, d_cen, level2IndexCUDAData,
       voxelTriCountCUDAData, level1TriFlatIndexCUDAData, level1TriFlatCUDAData, numBoundary,
       numDiv2, boxExtentsLevel2);
   count_launch();
-  cudaFree(d_cen);
+  cudaStreamSynchronize(0);  // the staging and the workspace are reused by the next call
   return 1;
 }
 
@@ -252,6 +491,53 @@ int CUDAClassifyInOutLevel2(float *trianglesCUDAData, float *level2InOutCUDAData
       boxExtentsLevel1, boxExtentsLevel2, eps_threshold());
   count_launch();
   return 1;
+}
+
+// cuda/THRUSTUtilities.cu:44-60: the largest of w*h device floats (thrust::max_element's answer,
+// first index on ties), copied to the host.  0 when w*h <= 0 (the reference then reads one past
+// the end).
+float THRUSTDeviceFindMax(float *dataCUDAPointer, int w, int h) {
+  const int64_t n = (int64_t)w * h;
+  const int64_t i = thrust_argmax(dataCUDAPointer, n, 1, shim_num_sms());
+  float v = 0.0f;
+  if (i >= 0) cudaMemcpy(&v, dataCUDAPointer + i, sizeof(v), cudaMemcpyDeviceToHost);
+  return v;
+}
+
+// cuda/THRUSTUtilities.cu:82-102: the float4 with the largest w (first on ties); its x, y, z and
+// w = 1 into *maxVal, its index into *maxLoc (host pointers), its w returned.  With
+// numValues <= 0: *maxLoc = 0, *maxVal = (0, 0, 0, 1), 0 returned.
+float THRUSTDeviceFindMaxFloat4(float4 *dataCUDAPointer, int numValues, float4 *maxVal, int *maxLoc) {
+  const int64_t i = thrust_argmax(reinterpret_cast<const float *>(dataCUDAPointer) + 3, numValues, 4,
+                                  shim_num_sms());
+  float4 e = make_float4(0.f, 0.f, 0.f, 0.f);
+  if (i >= 0) cudaMemcpy(&e, dataCUDAPointer + i, sizeof(e), cudaMemcpyDeviceToHost);
+  if (maxLoc) *maxLoc = i >= 0 ? (int)i : 0;
+  if (maxVal) *maxVal = make_float4(e.x, e.y, e.z, 1.0f);
+  return e.w;
+}
+
+// cuda/THRUSTUtilities.cu:128-160: sorts copies of the (row, min, max) triples by row and copies
+// the sorted rows to the host array rowNumbers (n ints); the device inputs are not changed and,
+// as in the reference, minData / maxData are not written.  Rows >= 0 come first in ascending
+// order, then the negative rows in input order.
+void THRUSTDeviceMinMaxSort(float *minDataCUDAPointer, float *maxDataCUDAPointer,
+                            int *rowDataCUDAPointer, int n, float *minData, float *maxData,
+                            int *rowNumbers) {
+  (void)minDataCUDAPointer; (void)maxDataCUDAPointer; (void)minData; (void)maxData;
+  if (n <= 0 || !rowNumbers) return;
+  std::lock_guard<std::mutex> lk(g_shim.mu);
+  const size_t w = al256(4 * (size_t)n) / 4;
+  const size_t words = 5 * w + (size_t)sort_temp_words(n);
+  if (!shim_reserve(4 * words)) return;
+  uint32_t *keys = static_cast<uint32_t *>(g_shim.dev), *vals = keys + w, *kalt = vals + w,
+           *valt = kalt + w, *out = valt + w, *temp = out + w;
+  const unsigned nb = (unsigned)((n + 255) / 256);
+  k_minmax_keys<<<nb, 256>>>(rowDataCUDAPointer, n, keys, vals);
+  const bool alt = sort_pairs(keys, vals, kalt, valt, n, 32, temp, 0);
+  k_minmax_gather<<<nb, 256>>>(rowDataCUDAPointer, alt ? valt : vals, n, reinterpret_cast<int *>(out));
+  count_launch(2);
+  cudaMemcpy(rowNumbers, out, 4 * (size_t)n, cudaMemcpyDeviceToHost);
 }
 
 }  // extern "C"

@@ -123,6 +123,14 @@ const char *gpv_last_error(gpv_ctx *ctx);
  * of boundary voxels of one Level1 column that one Level2 work item takes (1..32). */
 int gpv_set_tile(gpv_ctx *ctx, int tris_per_tile);
 int gpv_set_level2_chunk(gpv_ctx *ctx, int max_voxels);
+/* Organisation of the Level2 kernel's SAT stage (results are identical; only speed differs):
+ * GPV_LEVEL2_AUTO (default) picks per launch from the item density the prep kernel measures;
+ * GPV_LEVEL2_QUEUED queues the (triangle, sub-column) items that pass the z-invariant axes and
+ * finishes them 32 at a time; GPV_LEVEL2_INLINE lets each item's lane finish its own item. */
+#define GPV_LEVEL2_AUTO 0
+#define GPV_LEVEL2_QUEUED 1
+#define GPV_LEVEL2_INLINE 2
+int gpv_set_level2_mode(gpv_ctx *ctx, int mode);
 /* Voxel normals (default off), the reference's Level1 and Level2 normal passes
  * (src/Object.cpp:3219-3253, :2402-2424, :2715-2719): GPV_NORMALS_OFF, GPV_NORMALS_BYTES (the
  * .raw encoding) or GPV_NORMALS_FLOAT.  With normals on, each voxel's triangles are also ordered
@@ -181,6 +189,25 @@ int gpv_stage_times(gpv_ctx *ctx, double *ms, int n);
 int gpv_host_times(gpv_ctx *ctx, double *ms, int n);
 /* Number of kernels this library has launched in this process. */
 uint64_t gpv_kernel_launches(void);
+/* Failure-detection hooks (no counterpart in the reference).  They make the failure paths run
+ * on demand, without faulting or hanging the GPU:
+ *   GPV_DEBUG_WAIT_LIMIT    polls of the Level1 kernel's bounded wait for a staged tile before it
+ *                           gives up (0: the built-in limit);
+ *   GPV_DEBUG_FAIL_WAIT     non-zero: that wait gives up at once.  The kernel raises its status
+ *                           word, lets the copies in flight land and returns; the call returns
+ *                           GPV_ERR_DEVICE and the context stays usable;
+ *   GPV_DEBUG_PAIR_CAPACITY the next call starts with this (voxel, triangle) record capacity
+ *                           (one-shot): an overflow re-runs the call with the exact capacity;
+ *   GPV_DEBUG_FAIL_ALLOCS   the next this-many device allocations of the context are refused
+ *                           (the call returns GPV_ERR_OOM).
+ * gpv_get_debug reads GPV_DEBUG_REPLANS: calls re-run after a record-buffer overflow. */
+#define GPV_DEBUG_WAIT_LIMIT 1
+#define GPV_DEBUG_FAIL_WAIT 2
+#define GPV_DEBUG_PAIR_CAPACITY 3
+#define GPV_DEBUG_FAIL_ALLOCS 4
+#define GPV_DEBUG_REPLANS 5
+int gpv_set_debug(gpv_ctx *ctx, int what, int64_t value);
+int64_t gpv_get_debug(gpv_ctx *ctx, int what);
 
 /* ---- grids --------------------------------------------------------------------------------- */
 /* Explicit grid: n^3 cells over the mesh box grown by one cell on every side. */
@@ -237,17 +264,22 @@ int gpv_voxelize_batch(gpv_ctx *ctx, int32_t n, const float *const *d_tris,
                        gpv_result *results, cudaStream_t stream);
 
 /* Level1 voxelization that allocates nothing (no counterpart in the reference).  For callers
- * that cannot call cudaMalloc -- code running inside another allocator's or memory pool's
- * hooks, host paths that must not take the device synchronisation cudaMalloc/cudaFree can cause,
- * plugin hosts that forbid a library its own device memory.  The caller passes device triangles
- * (16-byte aligned) and three device outputs: level1_inout (nx*ny*nz bytes), level1_prefix
- * (nx*ny*nz int32) and boundary_index (room for nx*ny*nz int32); the boundary count is returned
- * in *num_boundary and the call waits for `stream`.  Results equal gpv_voxelize's Level1 outputs.
- * All intermediates live in one file-scope device array of 32 MiB that every GPU loading the
- * library holds until exit; larger inputs are rejected with GPV_ERR_INVALID (reason in
- * gpv_noalloc_last_error()).  The first call on each device looks up that array's address
- * (cudaGetSymbolAddress); make it before any stream capture.  Calls share the array and clear
- * it themselves; calls whose GPU work overlaps race on it and must be serialised. */
+ * that cannot call cudaMalloc -- code running inside another allocator's or memory pool's hooks
+ * (calling back into an allocator from there recurses or deadlocks), host paths that must not
+ * take the device synchronisation cudaMalloc/cudaFree can cause, plugin hosts that forbid a
+ * library its own device memory.  The caller passes device triangles (16-byte aligned) and three
+ * device outputs: level1_inout (nx*ny*nz bytes), level1_prefix (nx*ny*nz int32) and
+ * boundary_index (room for nx*ny*nz int32); the boundary count is returned in *num_boundary and
+ * the call waits for `stream`.  Results equal gpv_voxelize's Level1 outputs; the Level2 divisions
+ * of the spec are checked as gpv_voxelize checks them and otherwise ignored.  All intermediates
+ * live in one file-scope device array of 32 MiB that every GPU loading the library holds until
+ * exit; inputs whose intermediates do not fit (about 400k triangles at most, fewer on large
+ * grids) are rejected with GPV_ERR_INVALID and a reason in gpv_noalloc_last_error() (per host
+ * thread).  Every call looks up the array's device address (cudaGetSymbolAddress) with the
+ * caller's device current; the first call on a device also loads the library's device code
+ * there, so make that first call before any stream capture.  Calls share the array and clear
+ * what must start at zero themselves; calls whose GPU work overlaps race on it and must be
+ * serialised. */
 int gpv_voxelize_level1_noalloc(const float *d_tris, int64_t num_triangles,
                                 const gpv_grid_spec *spec, uint8_t *d_level1_inout,
                                 int32_t *d_level1_prefix, int32_t *d_boundary_index,
@@ -328,9 +360,10 @@ int64_t gpv_gen_superellipsoid(uint64_t seed, int32_t nlon, int32_t nlat, const 
                                const float semi[3], float e1, float e2, const float rot[9],
                                float *tris);
 
-/* ---- reference-named shims (includes/CUDAUtilities.h:63-64, :87-89) --------------------------- */
-void InitializeCUDA(void);                 /* src/CUDAUtilities.cpp:51-55 */
-void CUDACheckErrors(char const *label);   /* src/CUDAUtilities.cpp:33-49 */
+/* ---- reference-named shims: the C entry points of GPView's GPViewCUDA library ------------------
+ * (includes/CUDAUtilities.h:72-74, :87-89).  InitializeCUDA and CUDACheckErrors are not among
+ * them: the reference declares those with C++ linkage (includes/CUDAUtilities.h:63-64) and
+ * defines them in the application (src/CUDAUtilities.cpp:33-55), which keeps them. */
 /* cuda/CUDAClassifyTessellation.cu:507-515.  Marks inOut[v]=2 for every voxel whose SAT test
  * passes inside each triangle's candidate box, counts triangles per voxel in voxelTriCount and
  * stores up to triBufferLen ids per voxel in voxelTriIndex[v*triBufferLen..] (never beyond;
@@ -356,6 +389,19 @@ int CUDAClassifyInOutLevel2(float *trianglesCUDAData, float *level2InOutCUDAData
                             int *xyTriCountCUDAData, int *xyTriFlatIndexCUDAData,
                             int *xyTriFlatCUDAData, int numBoundary, int3 numDiv, int3 numDiv2,
                             float3 boxExtentsLevel1, float3 boxExtentsLevel2);
+/* cuda/THRUSTUtilities.cu:44-60 (called by src/CUDAUtilities.cpp:121-132 under the default
+ * `#define THRUST`, includes/Includes.h:49): the largest of w*h device floats, first index on ties
+ * (thrust::max_element), returned to the host; 0 for an empty range. */
+float THRUSTDeviceFindMax(float *dataCUDAPointer, int w, int h);
+/* cuda/THRUSTUtilities.cu:82-102: the float4 with the largest w; x, y, z and w = 1 into the host
+ * *maxVal, its index into the host *maxLoc, its w returned. */
+float THRUSTDeviceFindMaxFloat4(float4 *dataCUDAPointer, int numValues, float4 *maxVal, int *maxLoc);
+/* cuda/THRUSTUtilities.cu:128-160: the rows of n (row, min, max) triples sorted by row into the
+ * host array rowNumbers (rows >= 0 ascending, then negative rows in input order); the device
+ * inputs are unchanged and minData / maxData are not written, as in the reference. */
+void THRUSTDeviceMinMaxSort(float *minDataCUDAPointer, float *maxDataCUDAPointer,
+                            int *rowDataCUDAPointer, int n, float *minData, float *maxData,
+                            int *rowNumbers);
 
 #ifdef __cplusplus
 }

@@ -1,6 +1,9 @@
 """Builds the CPU oracle (test infrastructure, never part of the product).
 
-  oracle/liboracle.so          the C restatement (gpv_oracle.c), always built
+  oracle/liboracle.so          the C restatement (gpv_oracle.c), always built, plus the seeded
+                               mesh generators of the workloads (orc_gen_*), compiled from the
+                               library's own gpv_meshgen.cpp so that a CPU-only process makes
+                               bit-identical inputs without loading the GPU library
   oracle/_ref/liboracle_ref.so the same composition linked against the reference's own
                                TriBoxIntersection.cpp / TriRayIntersection.cpp, built only where
                                the reference sources are present (they are compiled where they
@@ -32,11 +35,17 @@ def _stale(out, deps):
     return any(os.path.getmtime(d) > t for d in deps if os.path.exists(d))
 
 
+MESHGEN = os.path.join(os.path.dirname(HERE), "gpview_gb300", "csrc", "gpv_meshgen.cpp")
+
+
 def build(force=False):
     src = os.path.join(HERE, "gpv_oracle.c")
     out = os.path.join(HERE, "liboracle.so")
-    if force or _stale(out, [src]):
-        _run(["gcc", *FLAGS, "-fopenmp", "-shared", "-o", out, src, "-lm"])
+    if force or _stale(out, [src, MESHGEN]):
+        obj = os.path.join(HERE, "_meshgen.o")
+        _run(["g++", *FLAGS, "-std=c++17", "-DGPV_MESHGEN_ORACLE", "-c", MESHGEN, "-o", obj])
+        _run(["gcc", *FLAGS, "-fopenmp", "-shared", "-o", out, src, obj, "-lm", "-lstdc++"])
+        os.unlink(obj)
     ref_files = [os.path.join(REF_SRC, f) for f in ("TriBoxIntersection.cpp", "TriRayIntersection.cpp")]
     ref_hdr = os.path.join(REF_INC, "FloatVector.h")
     if all(os.path.exists(f) for f in ref_files + [ref_hdr]):

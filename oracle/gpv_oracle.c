@@ -7,7 +7,7 @@
  * It restates, in plain C with the reference's exact float/double promotions and operation
  * order, the CPU composition of the reference (GPView, idealab-isu):
  *   - predicates:   src/TriBoxIntersection.cpp:64-210 (planeBoxOverlap, TriBoxOverlap)
- *                   src/TriRayIntersection.cpp:289-342 (triangle_ray_intersection)
+ *                   src/TriRayIntersection.cpp:78-131 (triangle_ray_intersection)
  *   - grid sizing:  src/Object.cpp:3094-3136 (reference mode) and the explicit-grid mode
  *   - Level1 fill:  src/Object.cpp:716-779   (ClassifyInOutCPU, +z ray parity over all triangles)
  *   - Level1 SAT:   src/Object.cpp:2256-2342 (ClassifyTessellation) + :2681-2748 (TestTriBox,
@@ -185,7 +185,7 @@ static int orc_tri_box_own(const float c[3], const float h[3], const float *tv, 
 }
 
 /* Moller-Trumbore ray/triangle test with a general direction, as src/TriRayIntersection.cpp:
- * 289-342: edges from V1, P = D x e2, det compared against 1e-6 IN DOUBLE, u/v bounds in
+ * 78-131: edges from V1, P = D x e2, det compared against 1e-6 IN DOUBLE, u/v bounds in
  * float, t > 1e-6 IN DOUBLE.  Returns 1 on a hit and writes t. */
 int orc_tri_ray(const float V1[3], const float V2[3], const float V3[3], const float O[3],
                 const float D[3], float *out)
@@ -879,16 +879,84 @@ static void orc_fill_stencil2(const orc_run *r, int i, int j, int k, uint8_t *bl
     free(par);
 }
 
-/* Level2 of boundary voxels [b0, b1): ClassifyInOutLevel2CPU then ClassifyTessellationLevel2.
- * out receives (b1-b0)*n2x*n2y*n2z states (0/1/2) in the reference's block layout.
- * Also accumulates the algorithmic Level2 test counts. */
-void orc_level2(const orc_run *r, int64_t b0, int64_t b1, uint8_t *out, int nthreads,
-                int64_t *sat2_tests, int64_t *ray2_tests)
+/* Level2 of one boundary voxel b into blk (n2x*n2y*n2z states 0/1/2): ClassifyInOutLevel2CPU
+ * then ClassifyTessellationLevel2.  uni/ucap/mark/par are the calling thread's scratch (mark all
+ * zero on entry and exit); the algorithmic Level2 test counts are added to *s2 and *r2. */
+static void orc_level2_voxel(const orc_run *r, int64_t b, uint8_t *blk, int32_t **uni_p,
+                             int64_t *ucap_p, uint8_t *mark, uint8_t *par, int64_t *s2, int64_t *r2)
 {
-    int nth = orc_threads(nthreads);
     const int nx = r->s.n[0], ny = r->s.n[1], nz = r->s.n[2];
     const int n2x = r->s.n2[0], n2y = r->s.n2[1], n2z = r->s.n2[2];
     const int64_t cells = (int64_t)n2x * n2y * n2z;
+    int32_t *uni = *uni_p;
+    int64_t ucap = *ucap_p;
+    memset(blk, 0, (size_t)cells);
+    int64_t v = r->bindex[b];
+    int k = (int)(v / ((int64_t)nx * ny));
+    int64_t ij = v - (int64_t)k * nx * ny;
+    int j = (int)(ij / nx), i = (int)(ij % nx);
+    /* Union of the triangles of Level1 voxels (i,j,z>=k), each once (:1162-1193). */
+    int64_t nu = 0;
+    for (int z = k; z < nz; ++z) {
+        int64_t w = (int64_t)z * nx * ny + ij;
+        for (int64_t e = r->vstart[w]; e < r->vstart[w + 1]; ++e) {
+            int32_t t = r->vtris[e];
+            if (mark[t]) continue;
+            mark[t] = 1;
+            if (nu == ucap) {
+                ucap = ucap ? 2 * ucap : 256;
+                uni = (int32_t *)realloc(uni, sizeof(int32_t) * (size_t)ucap);
+            }
+            uni[nu++] = t;
+        }
+    }
+    for (int64_t e = 0; e < nu; ++e) mark[uni[e]] = 0;
+    *uni_p = uni;
+    *ucap_p = ucap;
+    if (r->fill == ORC_FILL_STENCIL) {
+        orc_fill_stencil2(r, i, j, k, blk);
+    } else {
+        *r2 += nu * cells;
+        const float *ox = r->t.o2[0] + (size_t)i * n2x;
+        const float *oy = r->t.o2[1] + (size_t)j * n2y;
+        const float *oz = r->t.o2[2] + (size_t)k * n2z;
+        for (int q = 0; q < n2y; ++q)
+            for (int p = 0; p < n2x; ++p) {
+                memset(par, 0, (size_t)n2z);
+                for (int64_t e = 0; e < nu; ++e) {
+                    orc_colhit s;
+                    if (!orc_ray_column(r->tris + 9 * (int64_t)uni[e], ox[p], oy[q], &s)) continue;
+                    for (int rr = 0; rr < n2z; ++rr) par[rr] ^= (uint8_t)orc_ray_t(&s, oz[rr]);
+                }
+                for (int rr = 0; rr < n2z; ++rr)
+                    if (par[rr]) blk[((int64_t)rr * n2y + q) * n2x + p] = 1;
+            }
+    }
+    /* Level2 SAT over every sub-cell for every triangle of the voxel (:2374-2398). */
+    const float *sx = r->t.c2s[0] + (size_t)i * n2x;
+    const float *sy = r->t.c2s[1] + (size_t)j * n2y;
+    const float *sz = r->t.c2s[2] + (size_t)k * n2z;
+    int64_t nt = r->vstart[v + 1] - r->vstart[v];
+    *s2 += nt * cells;
+    for (int64_t e = r->vstart[v]; e < r->vstart[v + 1]; ++e) {
+        const float *tv = r->tris + 9 * (int64_t)r->vtris[e];
+        for (int p = 0; p < n2x; ++p)
+            for (int q = 0; q < n2y; ++q)
+                for (int rr = 0; rr < n2z; ++rr) {
+                    float c3[3] = {sx[p], sy[q], sz[rr]};
+                    if (orc_tri_box(c3, r->t.e2, tv)) blk[((int64_t)rr * n2y + q) * n2x + p] = 2;
+                }
+    }
+}
+
+/* Level2 of the boundary voxels list[0..n) (list == NULL: voxels b0 + 0..n) in one parallel
+ * region; out receives n blocks of n2x*n2y*n2z states in list order. */
+static void orc_level2_many(const orc_run *r, int64_t b0, int64_t n, const int64_t *list,
+                            uint8_t *out, int nthreads, int64_t *sat2_tests, int64_t *ray2_tests)
+{
+    int nth = orc_threads(nthreads);
+    const int n2z = r->s.n2[2];
+    const int64_t cells = (int64_t)r->s.n2[0] * r->s.n2[1] * n2z;
     int64_t s2 = 0, r2 = 0;
 #pragma omp parallel num_threads(nth) reduction(+ : s2, r2)
     {
@@ -896,70 +964,90 @@ void orc_level2(const orc_run *r, int64_t b0, int64_t b1, uint8_t *out, int nthr
         int64_t ucap = 0;
         uint8_t *mark = (uint8_t *)calloc((size_t)r->T + 1, 1);
         uint8_t *par = (uint8_t *)malloc((size_t)(n2z > 0 ? n2z : 1));
-#pragma omp for schedule(dynamic, 16)
-        for (int64_t b = b0; b < b1; ++b) {
-            uint8_t *blk = out + (b - b0) * cells;
-            memset(blk, 0, (size_t)cells);
-            int64_t v = r->bindex[b];
-            int k = (int)(v / ((int64_t)nx * ny));
-            int64_t ij = v - (int64_t)k * nx * ny;
-            int j = (int)(ij / nx), i = (int)(ij % nx);
-            /* Union of the triangles of Level1 voxels (i,j,z>=k), each once (:1162-1193). */
-            int64_t nu = 0;
-            for (int z = k; z < nz; ++z) {
-                int64_t w = (int64_t)z * nx * ny + ij;
-                for (int64_t e = r->vstart[w]; e < r->vstart[w + 1]; ++e) {
-                    int32_t t = r->vtris[e];
-                    if (mark[t]) continue;
-                    mark[t] = 1;
-                    if (nu == ucap) {
-                        ucap = ucap ? 2 * ucap : 256;
-                        uni = (int32_t *)realloc(uni, sizeof(int32_t) * (size_t)ucap);
-                    }
-                    uni[nu++] = t;
-                }
-            }
-            for (int64_t e = 0; e < nu; ++e) mark[uni[e]] = 0;
-            if (r->fill == ORC_FILL_STENCIL) {
-                orc_fill_stencil2(r, i, j, k, blk);
-                goto level2_sat;
-            }
-            r2 += nu * cells;
-            const float *ox = r->t.o2[0] + (size_t)i * n2x;
-            const float *oy = r->t.o2[1] + (size_t)j * n2y;
-            const float *oz = r->t.o2[2] + (size_t)k * n2z;
-            for (int q = 0; q < n2y; ++q)
-                for (int p = 0; p < n2x; ++p) {
-                    memset(par, 0, (size_t)n2z);
-                    for (int64_t e = 0; e < nu; ++e) {
-                        orc_colhit s;
-                        if (!orc_ray_column(r->tris + 9 * (int64_t)uni[e], ox[p], oy[q], &s)) continue;
-                        for (int rr = 0; rr < n2z; ++rr) par[rr] ^= (uint8_t)orc_ray_t(&s, oz[rr]);
-                    }
-                    for (int rr = 0; rr < n2z; ++rr)
-                        if (par[rr]) blk[((int64_t)rr * n2y + q) * n2x + p] = 1;
-                }
-        level2_sat:
-            /* Level2 SAT over every sub-cell for every triangle of the voxel (:2374-2398). */
-            const float *sx = r->t.c2s[0] + (size_t)i * n2x;
-            const float *sy = r->t.c2s[1] + (size_t)j * n2y;
-            const float *sz = r->t.c2s[2] + (size_t)k * n2z;
-            int64_t nt = r->vstart[v + 1] - r->vstart[v];
-            s2 += nt * cells;
-            for (int64_t e = r->vstart[v]; e < r->vstart[v + 1]; ++e) {
-                const float *tv = r->tris + 9 * (int64_t)r->vtris[e];
-                for (int p = 0; p < n2x; ++p)
-                    for (int q = 0; q < n2y; ++q)
-                        for (int rr = 0; rr < n2z; ++rr) {
-                            float c3[3] = {sx[p], sy[q], sz[rr]};
-                            if (orc_tri_box(c3, r->t.e2, tv)) blk[((int64_t)rr * n2y + q) * n2x + p] = 2;
-                        }
-            }
-        }
+#pragma omp for schedule(dynamic, 1)
+        for (int64_t e = 0; e < n; ++e)
+            orc_level2_voxel(r, list ? list[e] : b0 + e, out + e * cells, &uni, &ucap, mark, par,
+                             &s2, &r2);
         free(uni); free(mark); free(par);
     }
     if (sat2_tests) *sat2_tests = s2;
     if (ray2_tests) *ray2_tests = r2;
+}
+
+/* Level2 of boundary voxels [b0, b1): ClassifyInOutLevel2CPU then ClassifyTessellationLevel2.
+ * out receives (b1-b0)*n2x*n2y*n2z states (0/1/2) in the reference's block layout.
+ * Also accumulates the algorithmic Level2 test counts. */
+void orc_level2(const orc_run *r, int64_t b0, int64_t b1, uint8_t *out, int nthreads,
+                int64_t *sat2_tests, int64_t *ray2_tests)
+{
+    orc_level2_many(r, b0, b1 > b0 ? b1 - b0 : 0, NULL, out, nthreads, sat2_tests, ray2_tests);
+}
+
+/* Level2 of the listed boundary voxels (any order, e.g. a strided sample), one block each. */
+void orc_level2_list(const orc_run *r, int64_t n, const int64_t *list, uint8_t *out,
+                     int nthreads, int64_t *sat2_tests, int64_t *ray2_tests)
+{
+    orc_level2_many(r, 0, n, list, out, nthreads, sat2_tests, ray2_tests);
+}
+
+/* ClassifyInOutCPU as the reference writes it (src/Object.cpp:716-779), on a sample of Level1
+ * columns, on the calling thread: every voxel centre of column cols[c] = j*nx + i against every
+ * triangle with the general-direction ray test (D = +z), parity into out[c*nz + k] (1 = odd).
+ * Timing it gives the reference's single-threaded brute-force fill cost per column. */
+void orc_voxel_fill_columns(const orc_run *r, int64_t ncols, const int64_t *cols, uint8_t *out)
+{
+    const int nx = r->s.n[0], nz = r->s.n[2];
+    const float D[3] = {0.f, 0.f, 1.f};
+    for (int64_t c = 0; c < ncols; ++c) {
+        const int i = (int)(cols[c] % nx), j = (int)(cols[c] / nx);
+        for (int k = 0; k < nz; ++k) {
+            float O[3] = {r->t.c1[0][i], r->t.c1[1][j], r->t.c1[2][k]};
+            int cnt = 0;
+            for (int64_t t = 0; t < r->T; ++t) {
+                const float *tv = r->tris + 9 * t;
+                float tt;
+                if (orc_tri_ray(tv, tv + 3, tv + 6, O, D, &tt)) cnt++;
+            }
+            out[c * nz + k] = (uint8_t)(cnt & 1);
+        }
+    }
+}
+
+/* The algorithmic Level2 test counts of orc_level2 over every boundary voxel, without running
+ * the predicates: sat2 = sum of |tris(b)| * n2^3, ray2 = sum of |column union(b)| * n2^3, the
+ * union being the triangles of Level1 voxels (i,j,z>=k) counted once (src/Object.cpp:1162-1193).
+ * Used to state a sampled CPU timing per whole mesh. */
+void orc_level2_work(const orc_run *r, int nthreads, int64_t *sat2_tests, int64_t *ray2_tests)
+{
+    int nth = orc_threads(nthreads);
+    const int nx = r->s.n[0], ny = r->s.n[1], nz = r->s.n[2];
+    const int64_t cells = (int64_t)r->s.n2[0] * r->s.n2[1] * r->s.n2[2];
+    int64_t s2 = 0, r2 = 0;
+#pragma omp parallel num_threads(nth) reduction(+ : s2, r2)
+    {
+        uint8_t *mark = (uint8_t *)calloc((size_t)r->T + 1, 1);
+#pragma omp for schedule(dynamic, 64)
+        for (int64_t b = 0; b < r->B; ++b) {
+            int64_t v = r->bindex[b];
+            int k = (int)(v / ((int64_t)nx * ny));
+            int64_t ij = v - (int64_t)k * nx * ny;
+            int64_t nu = 0;
+            for (int z = k; z < nz; ++z) {
+                int64_t w = (int64_t)z * nx * ny + ij;
+                for (int64_t e = r->vstart[w]; e < r->vstart[w + 1]; ++e)
+                    if (!mark[r->vtris[e]]) { mark[r->vtris[e]] = 1; ++nu; }
+            }
+            for (int z = k; z < nz; ++z) {
+                int64_t w = (int64_t)z * nx * ny + ij;
+                for (int64_t e = r->vstart[w]; e < r->vstart[w + 1]; ++e) mark[r->vtris[e]] = 0;
+            }
+            if (r->fill != ORC_FILL_STENCIL) r2 += nu * cells;
+            s2 += (r->vstart[v + 1] - r->vstart[v]) * cells;
+        }
+        free(mark);
+    }
+    *sat2_tests = s2;
+    *ray2_tests = r2;
 }
 
 /* Algorithmic FP32 work of the reference predicates over the tests the work counts define,

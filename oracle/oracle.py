@@ -52,7 +52,10 @@ def _load(ref=False):
     L.orc_voxel_tris.argtypes = [vp, i64, vp, i64]
     L.orc_voxel_tris.restype = i64
     L.orc_level2.argtypes = [vp, i64, i64, vp, C.c_int, C.POINTER(i64), C.POINTER(i64)]
+    L.orc_level2_list.argtypes = [vp, i64, vp, vp, C.c_int, C.POINTER(i64), C.POINTER(i64)]
     L.orc_count_ops.argtypes = [vp, i64, i64, C.c_int, vp]
+    L.orc_level2_work.argtypes = [vp, C.c_int, C.POINTER(i64), C.POINTER(i64)]
+    L.orc_voxel_fill_columns.argtypes = [vp, i64, vp, vp]
     L.orc_face_normal.argtypes = [vp, vp]
     L.orc_build_hierarchy.argtypes = [vp, vp]
     L.orc_build_hierarchy.restype = C.c_int
@@ -63,6 +66,14 @@ def _load(ref=False):
     L.orc_tri_ray_z.argtypes = [vp, vp]
     L.orc_grid_tables.argtypes = [C.POINTER(Spec), vp, vp, vp, vp, vp, vp, vp]
     L.orc_reference_divisions.argtypes = [vp, vp, C.c_float, C.c_int, vp]
+    if hasattr(L, "orc_gen_star"):
+        f3 = C.POINTER(C.c_float)
+        for name, extra in (("orc_gen_uvsphere", [C.c_int32, C.c_int32, f3, C.c_float, C.c_float]),
+                            ("orc_gen_torus", [C.c_int32, C.c_int32, f3, C.c_float, C.c_float, C.c_float]),
+                            ("orc_gen_star", [C.c_int32, f3, C.c_float, C.c_float, f3])):
+            fn = getattr(L, name)
+            fn.argtypes = [C.c_uint64, *extra, vp]
+            fn.restype = C.c_int64
     _libs[ref] = L
     return L
 
@@ -144,6 +155,33 @@ class Run:
         if b1 > b0:
             self.L.orc_level2(self.h, int(b0), int(b1), _p(out), int(threads), C.byref(s2), C.byref(r2))
         return out, int(s2.value), int(r2.value)
+
+    def voxel_fill_columns(self, cols):
+        """ClassifyInOutCPU as written (every voxel centre against every triangle, one thread)
+        on the given columns (j*nx + i): parity uint8 [len(cols), nz]."""
+        cols = np.ascontiguousarray(cols, np.int64)
+        nz = int(self.spec.n[2])
+        out = np.zeros(cols.size * nz, np.uint8)
+        self.L.orc_voxel_fill_columns(self.h, cols.size, _p(cols), _p(out))
+        return out.reshape(cols.size, nz)
+
+    def level2_list(self, blist, threads=0):
+        """States of the listed boundary voxels (one block each, list order) in one parallel
+        pass, plus their (sat2, ray2) work counts."""
+        blist = np.ascontiguousarray(blist, np.int64)
+        out = np.empty(blist.size * self.cells, np.uint8)
+        s2, r2 = C.c_int64(), C.c_int64()
+        if blist.size:
+            self.L.orc_level2_list(self.h, blist.size, _p(blist), _p(out), int(threads),
+                                   C.byref(s2), C.byref(r2))
+        return out, int(s2.value), int(r2.value)
+
+    def level2_work(self, threads=0):
+        """(sat2, ray2): the algorithmic Level2 test counts of the whole mesh, without running
+        the predicates (equal to the counts level2_state reports over every boundary voxel)."""
+        s2, r2 = C.c_int64(), C.c_int64()
+        self.L.orc_level2_work(self.h, int(threads), C.byref(s2), C.byref(r2))
+        return int(s2.value), int(r2.value)
 
     def count_ops(self, b0=0, b1=None, threads=0):
         """Executed FP32 operations of the reference predicates over the algorithmic tests
@@ -238,3 +276,43 @@ def grid_tables(grid):
     o2 = np.empty_like(c2s)
     L.orc_grid_tables(C.byref(s), _p(g), _p(e1), _p(g2), _p(e2), _p(c1), _p(c2s), _p(o2))
     return dict(g=g, e1=e1, g2=g2, e2=e2, c1=c1, c2s=c2s, o2=o2)
+
+
+# ---- seeded workload meshes, without the GPU library --------------------------------------------
+# The same generator source as gpview_gb300's gpv_gen_* (gpv_meshgen.cpp), built into this library:
+# a CPU-only process (the benchmark's reference arm) makes bit-identical inputs with these.
+def _f3(v):
+    return (C.c_float * 3)(*[float(x) for x in v])
+
+
+def _gen(name, seed, *args):
+    fn = getattr(_load(False), name)
+    n = fn(C.c_uint64(seed), *args, None)
+    out = np.empty(9 * n, dtype=np.float32)
+    assert fn(C.c_uint64(seed), *args, out.ctypes.data_as(C.c_void_p)) == n
+    return out
+
+
+def gen_uvsphere(seed, nlon=128, nlat=64, center=(0.5, 0.5, 0.5), radius=0.4, jitter=0.002):
+    return _gen("orc_gen_uvsphere", seed, int(nlon), int(nlat), _f3(center), float(radius), float(jitter))
+
+
+def gen_torus(seed, nu=512, nv=256, center=(0.5, 0.5, 0.5), R=0.35, r=0.12, noise=0.01):
+    return _gen("orc_gen_torus", seed, int(nu), int(nv), _f3(center), float(R), float(r), float(noise))
+
+
+def gen_star(seed, subdiv=8, center=(0.5, 0.5, 0.5), radius=0.3, amp=0.2, scale=(1, 1, 6)):
+    return _gen("orc_gen_star", seed, int(subdiv), _f3(center), float(radius), float(amp), _f3(scale))
+
+
+def grid_padded(mesh_min, mesh_max, n, n2):
+    """gpv_grid_padded in float32 arithmetic: n cells over the mesh box grown by one cell of size
+    extent/(n-2) on each side (returns a (bmin, bmax, ndiv, ndiv2) tuple for Run)."""
+    mn = np.asarray(mesh_min, np.float32)
+    mx = np.asarray(mesh_max, np.float32)
+    n3 = np.array([n] * 3 if np.isscalar(n) else n, np.int32)
+    n23 = np.array([n2] * 3 if np.isscalar(n2) else n2, np.int32)
+    ext = (mx - mn).astype(np.float32)
+    ext = np.where(ext > 0, ext, np.float32(1e-3)).astype(np.float32)
+    cell = (ext / (n3 - 2).astype(np.float32)).astype(np.float32)
+    return ((mn - cell).astype(np.float32), (mx + cell).astype(np.float32), n3, n23)

@@ -1,6 +1,7 @@
 """The reference-named shims (includes/CUDAUtilities.h:63-64, :87-89) driven the way
 Object::ClassifyTessellationCUDA / ClassifyInOutTessellationLevel2CUDA drive them."""
 import ctypes as C
+import os
 
 import numpy as np
 import pytest
@@ -23,7 +24,11 @@ def _setup(gpv, L):
     L.CUDAClassifyTessellation.argtypes = [vp, C.c_int, vp, vp, vp, F3, F3, F3, I3, C.c_int]
     L.CUDAClassifyTessellationLevel2.argtypes = [vp, vp, vp, vp, vp, vp, vp, vp, C.c_int, I3, F3, F3]
     L.CUDAClassifyInOutLevel2.argtypes = [vp, vp, vp, vp, vp, vp, vp, C.c_int, I3, I3, F3, F3]
-    L.CUDACheckErrors.argtypes = [C.c_char_p]
+    L.THRUSTDeviceFindMax.argtypes = [vp, C.c_int, C.c_int]
+    L.THRUSTDeviceFindMax.restype = C.c_float
+    L.THRUSTDeviceFindMaxFloat4.argtypes = [vp, C.c_int, vp, C.POINTER(C.c_int)]
+    L.THRUSTDeviceFindMaxFloat4.restype = C.c_float
+    L.THRUSTDeviceMinMaxSort.argtypes = [vp, vp, vp, C.c_int, vp, vp, vp]
 
 
 def test_shims_follow_reference(built):
@@ -31,7 +36,6 @@ def test_shims_follow_reference(built):
     gpv = built
     L = gpv.lib()
     _setup(gpv, L)
-    L.InitializeCUDA()
     tris = gpv.gen_uvsphere(31, 24, 12, (0.5, 0.5, 0.5), 0.4, 0.002)
     spec = gpv.grid_padded(*gpv.mesh_bounds(tris), 14, 2)
     ref = orc.Run(tris, spec, fill=orc.FILL_VOXEL)
@@ -53,7 +57,7 @@ def test_shims_follow_reference(built):
         rc = L.CUDAClassifyTessellation(d_tris.data_ptr(), T, inout.data_ptr(), cnt.data_ptr(),
                                         idx.data_ptr(), F3(*spec.bbox_min), F3(*spec.bbox_max), e1,
                                         I3(*nd), buf)
-        L.CUDACheckErrors(b"shim level1")
+        torch.cuda.synchronize()
         assert rc == 1
         np.testing.assert_array_equal(inout.cpu().numpy() == 2, st1 == 2)
         np.testing.assert_array_equal(cnt.cpu().numpy(), counts)
@@ -137,3 +141,114 @@ def test_shims_follow_reference(built):
             if hits % 2:
                 exp[b * cells + c] = 1.0
     np.testing.assert_array_equal(got, exp)
+
+
+def _first_max_index(x):
+    """thrust::max_element's answer read from the start: the first element stays while nothing
+    compares greater (a NaN first element stays; later NaNs never win; -0 == +0)."""
+    best = 0
+    for i in range(1, len(x)):
+        if x[best] < x[i]:
+            best = i
+    return best
+
+
+def test_thrust_entry_points(built):
+    torch = pytest.importorskip("torch")
+    gpv = built
+    L = gpv.lib()
+    _setup(gpv, L)
+    rng = np.random.default_rng(5)
+    cases = [rng.normal(size=100003).astype(np.float32),
+             np.array([-3.0, 7.0, 7.0, -0.0, 7.0], np.float32),          # ties: first
+             np.array([np.nan, 1.0, 5.0], np.float32),                   # NaN first stays
+             np.array([1.0, np.nan, 5.0, np.nan], np.float32),           # later NaNs ignored
+             np.array([-0.0, 0.0, -1.0], np.float32),                    # -0 == +0
+             -np.abs(rng.normal(size=4097)).astype(np.float32)]
+    for x in cases:
+        d = torch.from_numpy(x).cuda()
+        got = L.THRUSTDeviceFindMax(d.data_ptr(), x.size, 1)
+        exp = x[_first_max_index(x)]
+        assert np.float32(got).view(np.uint32) == exp.view(np.uint32) or (np.isnan(got) and np.isnan(exp))
+    assert L.THRUSTDeviceFindMax(d.data_ptr(), 0, 5) == 0.0
+    # float4: the element with the largest w, first on ties; x, y, z copied, w = 1
+    v4 = rng.normal(size=(5000, 4)).astype(np.float32)
+    v4[4000, 3] = v4[:, 3].max() + 1
+    v4[4500, 3] = v4[4000, 3]
+    d4 = torch.from_numpy(v4).cuda()
+    out = (C.c_float * 4)()
+    loc = C.c_int(-1)
+    w = L.THRUSTDeviceFindMaxFloat4(d4.data_ptr(), 5000, out, C.byref(loc))
+    assert loc.value == 4000 and w == v4[4000, 3]
+    assert list(out) == [float(v4[4000, 0]), float(v4[4000, 1]), float(v4[4000, 2]), 1.0]
+    # rows sorted (non-negative ascending, then negative rows in input order); inputs unchanged
+    rows = rng.integers(-5, 1000, 20000).astype(np.int32)
+    dr = torch.from_numpy(rows.copy()).cuda()
+    dmin = torch.zeros(20000, device="cuda")
+    res = np.zeros(20000, np.int32)
+    L.THRUSTDeviceMinMaxSort(dmin.data_ptr(), dmin.data_ptr(), dr.data_ptr(), 20000, None, None,
+                             res.ctypes.data_as(C.c_void_p))
+    exp = np.concatenate([np.sort(rows[rows >= 0], kind="stable"), rows[rows < 0]])
+    np.testing.assert_array_equal(res, exp)
+    np.testing.assert_array_equal(dr.cpu().numpy(), rows)
+
+
+def test_level1_shim_on_torus262k(built):
+    """CUDAClassifyTessellation on the mid-size configuration through the engine: boundary flags,
+    per-voxel counts and stored ids against the oracle's records."""
+    torch = pytest.importorskip("torch")
+    import workloads as W
+
+    gpv = built
+    L = gpv.lib()
+    _setup(gpv, L)
+    tris, spec = W.make(W.C2)
+    ref = orc.Run(tris, spec)
+    tab = orc.grid_tables(spec)
+    nd = list(spec.ndiv)
+    N1 = int(np.prod(nd))
+    d_tris = torch.from_numpy(tris).cuda()
+    buf = 64
+    inout = torch.zeros(N1, dtype=torch.float32, device="cuda")
+    cnt = torch.zeros(N1, dtype=torch.int32, device="cuda")
+    idx = torch.full((N1 * buf,), -1, dtype=torch.int32, device="cuda")
+    rc = L.CUDAClassifyTessellation(d_tris.data_ptr(), tris.size // 9, inout.data_ptr(), cnt.data_ptr(),
+                                    idx.data_ptr(), F3(*spec.bbox_min), F3(*spec.bbox_max),
+                                    F3(*[float(v) for v in tab["e1"]]), I3(*nd), buf)
+    torch.cuda.synchronize()
+    assert rc == 1
+    st1 = ref.level1_state()
+    np.testing.assert_array_equal(inout.cpu().numpy() == 2, st1 == 2)
+    c = cnt.cpu().numpy()
+    assert c.sum() == ref.num_pairs()
+    got = idx.cpu().numpy().reshape(N1, buf)
+    rs = np.random.default_rng(0)
+    for v in rs.choice(np.nonzero(c)[0], 2000, replace=False):
+        lst = np.sort(ref.voxel_tris(v))
+        assert c[v] == lst.size
+        stored = got[v][:min(c[v], buf)]
+        if c[v] <= buf:
+            np.testing.assert_array_equal(np.sort(stored), lst)
+        else:  # a full buffer holds distinct ids of the voxel's list
+            assert set(stored.tolist()) <= set(lst.tolist()) and len(set(stored.tolist())) == buf
+
+
+def test_reference_caller_runs_on_gpu(built, tmp_path):
+    """The C++ caller of tests/test_link.py, linked against libgpview.so, run with its GPU calls."""
+    import subprocess
+
+    import test_link as TL
+
+    inc, cudalib = TL._cuda_dirs()
+    if not inc or not cudalib:
+        pytest.skip("no CUDA toolkit")
+    src = tmp_path / "caller.cpp"
+    src.write_text(TL.CALLER)
+    exe = tmp_path / "caller"
+    libdir = os.path.join(TL.ROOT, "gpview_gb300")
+    r = subprocess.run(["g++", "-std=c++17", "-I", inc, str(src), "-L", libdir, "-lgpview", "-L",
+                        cudalib, "-lcudart", f"-Wl,-rpath,{libdir}:{cudalib}", "-o", str(exe)],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    r = subprocess.run([str(exe), "run"], capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0 and "rc=1" in r.stdout and "CUDA Error" not in r.stdout, r.stdout + r.stderr

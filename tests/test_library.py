@@ -15,13 +15,15 @@ def test_exports_every_header_symbol(built):
     text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
     names = set(re.findall(r"\b([A-Za-z_][A-Za-z0-9_]*)\s*\(", text))
     names -= {"if", "sizeof", "defined"}
-    decl = [n for n in names if n.startswith("gpv_") or n in (
-        "InitializeCUDA", "CUDACheckErrors", "CUDAClassifyTessellation",
-        "CUDAClassifyTessellationLevel2", "CUDAClassifyInOutLevel2")]
+    decl = [n for n in names if n.startswith("gpv_") or n.startswith("THRUSTDevice") or n in (
+        "CUDAClassifyTessellation", "CUDAClassifyTessellationLevel2", "CUDAClassifyInOutLevel2")]
     assert len(decl) >= 20
+    assert {"THRUSTDeviceFindMax", "THRUSTDeviceFindMaxFloat4", "THRUSTDeviceMinMaxSort"} <= set(decl)
     L = built.lib()
     missing = [n for n in decl if not hasattr(L, n)]
     assert not missing, missing
+    # the application's C++-linkage helpers are not exported under C names
+    assert not hasattr(L, "InitializeCUDA") and not hasattr(L, "CUDACheckErrors")
 
 
 def test_generator_counts_and_determinism(built):
@@ -104,11 +106,11 @@ def test_off_loader_and_errors(built, tmp_path):
     assert e.value.code == -4
 
 
-@pytest.mark.skipif(not os.path.exists("/root/reference/files/cessna.obj"), reason="reference fixture absent")
 def test_cessna_fixture(built):
+    """The reference's only mesh file (files/cessna.obj, committed as tests/golden/cessna.obj)."""
     gpv = built
     o = gpv.Object()
-    o.ReadObject("/root/reference/files/cessna.obj")
+    o.ReadObject(os.path.join(ROOT, "tests", "golden", "cessna.obj"))
     o.CreateFlatTriangleData()
     assert o.totalNumTriangles == 7446
     assert _edges_shared_twice(o.flatCPUTriangleData)  # closed and manifold

@@ -1,7 +1,22 @@
-"""Seeded synthetic workloads with the shapes and sizes of the benchmark configurations."""
+"""Seeded synthetic workloads with the shapes and sizes of the benchmark configurations.
+
+make(cfg) uses the library's generators (gpview_gb300.gen_*); make(cfg, cpu=True) makes the same
+mesh and grid bit for bit from the CPU oracle's copy of the same generator source, without loading
+the GPU library (the benchmark's reference arm runs that way)."""
 import numpy as np
 
-import gpview_gb300 as gpv
+
+class _LazyGpv:
+    """gpview_gb300, imported on first use (a CPU-only caller of make(cfg, cpu=True) never
+    imports it)."""
+
+    def __getattr__(self, name):
+        import gpview_gb300
+
+        return getattr(gpview_gb300, name)
+
+
+gpv = _LazyGpv()
 
 # name -> (generator, Level1 divisions, Level2 divisions)
 C1 = dict(name="sphere16k", level1=64, level2=4)
@@ -25,12 +40,31 @@ def star1310k(seed=3):
 
 
 GENS = {"sphere16k": sphere16k, "torus262k": torus262k, "star1310k": star1310k}
+# the same meshes from the oracle library's build of the generator source
+CPU_GENS = {"sphere16k": lambda seed=1: _orc().gen_uvsphere(seed, 128, 64, (0.5, 0.5, 0.5), 0.4, 0.002),
+            "torus262k": lambda seed=2: _orc().gen_torus(seed, 512, 256, (0.5, 0.5, 0.5), 0.35, 0.12, 0.01),
+            "star1310k": lambda seed=3: _orc().gen_star(seed, 8, (0.5, 0.5, 0.5), 0.3, 0.2, (1.0, 1.0, 6.0))}
 
 
-def make(cfg, seed=None):
-    gen = GENS[cfg["name"]]
+def _orc():
+    from oracle import oracle
+
+    return oracle
+
+
+def mesh_bounds(tris):
+    v = np.asarray(tris, dtype=np.float32).reshape(-1, 3)
+    return v.min(axis=0), v.max(axis=0)
+
+
+def make(cfg, seed=None, cpu=False):
+    """(triangles, grid) of a named workload.  cpu=True: generated by the oracle library and the
+    grid returned as a (bmin, bmax, ndiv, ndiv2) tuple, with no GPU library loaded."""
+    gen = (CPU_GENS if cpu else GENS)[cfg["name"]]
     tris = gen() if seed is None else gen(seed)
-    mn, mx = gpv.mesh_bounds(tris)
+    mn, mx = mesh_bounds(tris)
+    if cpu:
+        return tris, _orc().grid_padded(mn, mx, cfg["level1"], cfg["level2"])
     spec = gpv.grid_padded(mn, mx, cfg["level1"], cfg["level2"])
     return tris, spec
 
