@@ -49,6 +49,8 @@ def parse():
     p.add_argument("--tile", type=int, default=0)
     p.add_argument("--level2", type=int, default=0, help="override the workload's Level2 divisions")
     p.add_argument("--chunk", type=int, default=0, help="Level2 chunk of the plain path (0: default)")
+    p.add_argument("--level2-mode", default="auto", choices=["auto", "queued", "inline"],
+                   help="Level2 SAT organisation of the plain path (default: chosen per launch)")
     p.add_argument("--no-graphs", action="store_true")
     p.add_argument("--slabs", type=int, default=0,
                    help="z slabs of the e2e path's Level2 launch (0: by the Level2 output size)")
@@ -71,6 +73,9 @@ def parse():
     p.add_argument("--serve-seconds", type=float, default=60.0, help="served stream length (0: skip)")
     p.add_argument("--serve-pool", type=int, default=256)
     p.add_argument("--serve-rate", type=float, nargs=2, default=(100.0, 5000.0))
+    p.add_argument("--serve-tight-seconds", type=float, default=15.0,
+                   help="length of the stream under a binding budget (0: skip)")
+    p.add_argument("--serve-tight-gb", type=float, default=2.0)
     return p.parse_args()
 
 
@@ -320,40 +325,35 @@ def batch_bench(gpv, ctx, torch, stream, local, args):
             "batched_host_ms_per_call": {k: v / max(hcalls, 1) for k, v in host_ms.items()}}
 
 
-def served_bench(gpv, torch, local, args, tuned):
-    """Open-loop Poisson stream (rate ramped linearly over the run) against the continuous-
-    batching server with a 150 GB HBM budget; latency = submit to results on the device."""
-    import threading
-    from collections import deque
-
+def poisson_schedule(D, r0, r1, seed):
+    """Arrival times of an open-loop Poisson stream whose rate ramps linearly from r0 to r1 over
+    D seconds (thinning of a rate-r1 process)."""
     import numpy as np
 
-    import workloads as W
-
-    pool = W.served_pool(args.serve_pool)
-    pinned = [torch.from_numpy(t).pin_memory() for t, _ in pool]
-    specs = [s for _, s in pool]
-    D = args.serve_seconds
-    r0, r1 = args.serve_rate
-    rng = np.random.default_rng(77)
+    rng = np.random.default_rng(seed)
     sched, t = [], 0.0
-    while True:  # thinning of a Poisson process with rate r(t) = r0 + (r1 - r0) t / D
+    while True:
         t += rng.exponential(1.0 / r1)
         if t >= D:
             break
         if rng.random() < (r0 + (r1 - r0) * t / D) / r1:
             sched.append(t)
-    picks = rng.integers(0, len(pool), len(sched))
-    srv = gpv.Server(local, budget_bytes=150 << 30, workers=2, max_batch=256)
-    srv.set_tunables(*tuned)
-    for i in range(8):  # warm-up
-        tk = srv.submit(pinned[i % len(pool)], specs[i % len(pool)])
-        srv.poll(tk, -1)
-        srv.release(tk)
-    shed_limit = 2000
+    return sched, rng
+
+
+def serve_stream(srv, submit, n_pool, D, r0, r1, seed, shed_limit=2000):
+    """Drives one stream against a server: submit(k) enqueues pool mesh k.  A collector thread
+    polls and releases results in submission order.  Returns the per-request records and the
+    stream's wall time; requests are shed (not submitted) while more than shed_limit wait."""
+    import threading
+    from collections import deque
+
+    sched, rng = poisson_schedule(D, r0, r1, seed)
+    picks = rng.integers(0, n_pool, len(sched))
     q = deque()
     done = []
     shed = [0]
+    peak = [0]
     finished = threading.Event()
 
     def collector():
@@ -375,36 +375,111 @@ def served_bench(gpv, torch, local, args, tuned):
         now = time.perf_counter() - start
         if ts > now:
             time.sleep(ts - now)
-        if srv.stats()["pending"] > shed_limit:
+        st = srv.stats()
+        peak[0] = max(peak[0], st["in_use_bytes"])
+        if st["pending"] > shed_limit:
             shed[0] += 1
             continue
-        q.append((srv.submit(pinned[k], specs[k]), ts))
+        tk = submit(int(k))
+        if tk is not None:
+            q.append((tk, ts))
     finished.set()
     col.join()
-    wall = time.perf_counter() - start
-    st = srv.stats()
-    srv.close()
+    return done, time.perf_counter() - start, len(sched), shed[0], peak[0]
+
+
+def stream_summary(done, wall, offered, shed, D, r0, r1, nbins=6):
+    import numpy as np
+
     lat = np.array([d[1] for d in done if d[3] == 0])
     ts = np.array([d[0] for d in done if d[3] == 0])
+    pct = lambda x, p: float(np.percentile(x, p)) if len(x) else None  # noqa: E731
     bins = []
-    for b in range(6):
-        lo, hi = b * D / 6, (b + 1) * D / 6
+    for b in range(nbins):
+        lo, hi = b * D / nbins, (b + 1) * D / nbins
         m = (ts >= lo) & (ts < hi)
         if m.any():
             bins.append({"rate_req_s": round(r0 + (r1 - r0) * (lo + hi) / 2 / D),
-                         "completed": int(m.sum()), "p50_ms": float(np.percentile(lat[m], 50)),
-                         "p99_ms": float(np.percentile(lat[m], 99))})
-    return {"workload": "served", "duration_s": D, "rate_req_s": [r0, r1],
-            "desc": "Poisson stream, rate ramped linearly; pool of %d meshes (3 families, T log-uniform "
-                    "1e3-1e6, Level1 {64,128,256}^3, Level2 {4,8}^3); 150 GB budget; 2 workers" % len(pool),
-            "offered": len(sched), "shed": shed[0], "completed": int(len(lat)),
-            "failed": int(sum(1 for d in done if d[3] != 0)),
-            "meshes_per_s": len(lat) / wall, "batches": st["batches"],
-            "p50_ms": float(np.percentile(lat, 50)) if len(lat) else None,
-            "p95_ms": float(np.percentile(lat, 95)) if len(lat) else None,
-            "p99_ms": float(np.percentile(lat, 99)) if len(lat) else None,
-            "queue_p50_ms": float(np.percentile([d[2] for d in done], 50)) if done else None,
-            "by_rate": bins}
+                         "completed": int(m.sum()), "p50_ms": pct(lat[m], 50),
+                         "p95_ms": pct(lat[m], 95), "p99_ms": pct(lat[m], 99)})
+    return {"offered": offered, "shed": shed, "completed": int(len(lat)),
+            "failed": int(sum(1 for d in done if d[3] != 0)), "meshes_per_s": len(lat) / wall,
+            "p50_ms": pct(lat, 50), "p95_ms": pct(lat, 95), "p99_ms": pct(lat, 99),
+            "queue_p50_ms": pct([d[2] for d in done], 50), "by_rate": bins}
+
+
+def served_bench(gpv, torch, local, args, tuned):
+    """Open-loop Poisson streams against the continuous-batching server; latency = submit to
+    results on the device.
+      main stream  -- rate ramped 100 -> 5,000 req/s over 60 s, 150 GB budget, the pool's meshes
+                      resident on the device (uploaded once, requested by id);
+      plain        -- the same pool voxelized one call per mesh on one context (the comparator);
+      tight budget -- a shorter stream of host-triangle requests (copied in per request) under a
+                      2 GB budget, where admission by predicted footprint binds."""
+    import workloads as W
+
+    pool = W.served_pool(args.serve_pool)
+    specs = [s for _, s in pool]
+    D = args.serve_seconds
+    r0, r1 = args.serve_rate
+    out = {"workload": "served", "duration_s": D, "rate_req_s": [r0, r1],
+           "desc": "Poisson stream, rate ramped linearly; pool of %d meshes (3 families, T log-uniform "
+                   "1e3-1e6, Level1 {64,128,256}^3, Level2 {4,8}^3); 150 GB budget; 2 workers; meshes "
+                   "resident in the server's device pool" % len(pool)}
+    # the comparator: one plain call per pool mesh, device-resident triangles
+    dev = [torch.from_numpy(t).to(f"cuda:{local}") for t, _ in pool]
+    ctx = gpv.Context(local)
+    for d, (t, s) in list(zip(dev, pool))[:8]:
+        ctx.release(ctx.voxelize_device(d.data_ptr(), t.size // 9, s))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for d, (t, s) in zip(dev, pool):
+        ctx.release(ctx.voxelize_device(d.data_ptr(), t.size // 9, s))
+    torch.cuda.synchronize()
+    out["plain_meshes_per_s"] = len(pool) / (time.perf_counter() - t0)
+    ctx.close()
+    del dev
+    # main stream, resident meshes
+    srv = gpv.Server(local, budget_bytes=150 << 30, workers=2, max_batch=256)
+    srv.set_tunables(*tuned)
+    ids = [srv.add_mesh(t) for t, _ in pool]
+    out["pool_bytes"] = int(sum(t.size * 4 for t, _ in pool))
+    for i in range(8):  # warm-up
+        tk = srv.submit_mesh(ids[i], specs[i])
+        srv.poll(tk, -1)
+        srv.release(tk)
+    done, wall, offered, shed, peak = serve_stream(srv, lambda k: srv.submit_mesh(ids[k], specs[k]),
+                                                  len(pool), D, r0, r1, 77)
+    out["batches"] = srv.stats()["batches"]
+    srv.close()
+    out.update(stream_summary(done, wall, offered, shed, D, r0, r1))
+    out["peak_in_use_gb"] = peak / 2**30
+    out["served_vs_plain"] = out["meshes_per_s"] / out["plain_meshes_per_s"]
+    # a budget that binds: admission by predicted footprint, host triangles copied per request
+    if args.serve_tight_seconds > 0:
+        pinned = [torch.from_numpy(t).pin_memory() for t, _ in pool]
+        budget = int(args.serve_tight_gb * 2**30)
+        srv = gpv.Server(local, budget_bytes=budget, workers=2, max_batch=256)
+        srv.set_tunables(*tuned)
+        Dt = args.serve_tight_seconds
+        refused = [0]
+
+        def submit(k):
+            # a request whose predicted footprint exceeds the whole budget is refused at submit
+            try:
+                return srv.submit(pinned[k], specs[k])
+            except gpv.GpvError:
+                refused[0] += 1
+                return None
+
+        done, wall, offered, shed, peak = serve_stream(srv, submit, len(pool), Dt, 500.0, 500.0, 78)
+        tight = stream_summary(done, wall, offered, shed, Dt, 500.0, 500.0, nbins=3)
+        tight.update({"budget_gb": budget / 2**30, "duration_s": Dt, "rate_req_s": 500.0,
+                      "peak_in_use_gb": peak / 2**30, "batches": srv.stats()["batches"],
+                      "refused_as_oversize": refused[0]})
+        srv.close()
+        out["tight_budget"] = tight
+    return out
 
 
 def run_reference(args):
@@ -742,6 +817,8 @@ def main():
         ctx.set_tile(args.tile)
     if args.chunk:
         ctx.set_level2_chunk(args.chunk)
+    ctx.set_level2_mode({"auto": gpv.LEVEL2_AUTO, "queued": gpv.LEVEL2_QUEUED,
+                         "inline": gpv.LEVEL2_INLINE}[args.level2_mode])
     ctx.set_graphs(not args.no_graphs)
     stream = torch.cuda.Stream(device=local)
     sp = stream.cuda_stream

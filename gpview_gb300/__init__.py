@@ -161,6 +161,10 @@ def lib():
     L.gpv_server_poll.argtypes = [C.c_void_p, C.c_uint64, C.c_int32, C.POINTER(Result),
                                   C.POINTER(C.c_double), C.POINTER(C.c_double)]
     L.gpv_server_release.argtypes = [C.c_void_p, C.c_uint64]
+    L.gpv_server_add_mesh.argtypes = [C.c_void_p, C.c_void_p, C.c_int64, C.POINTER(C.c_uint64)]
+    L.gpv_server_submit_mesh.argtypes = [C.c_void_p, C.c_uint64, C.POINTER(GridSpec),
+                                         C.POINTER(C.c_uint64)]
+    L.gpv_server_remove_mesh.argtypes = [C.c_void_p, C.c_uint64]
     L.gpv_server_stats.argtypes = [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int64),
                                    C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]
     L.gpv_server_destroy.argtypes = [C.c_void_p]
@@ -627,6 +631,27 @@ class Server:
             raise GpvError(rc, "submit")
         self._keep[t.value] = tris
         return t.value
+
+    def add_mesh(self, tris):
+        """Uploads a mesh once into the server's device pool; returns its id."""
+        tris = np.ascontiguousarray(tris, np.float32).reshape(-1)
+        mid = C.c_uint64()
+        rc = lib().gpv_server_add_mesh(self._h, tris.ctypes.data_as(C.c_void_p), tris.size // 9,
+                                       C.byref(mid))
+        if rc:
+            raise GpvError(rc, "add_mesh")
+        return mid.value
+
+    def submit_mesh(self, mesh_id, spec):
+        """A voxelization of a resident mesh (no host-to-device copy)."""
+        t = C.c_uint64()
+        rc = lib().gpv_server_submit_mesh(self._h, C.c_uint64(mesh_id), C.byref(spec), C.byref(t))
+        if rc:
+            raise GpvError(rc, "submit_mesh")
+        return t.value
+
+    def remove_mesh(self, mesh_id):
+        return lib().gpv_server_remove_mesh(self._h, C.c_uint64(mesh_id))
 
     def poll(self, ticket, timeout_ms=0):
         """(status, result, latency_ms, queue_ms); status GPV_ERR_PENDING (-8) while running."""

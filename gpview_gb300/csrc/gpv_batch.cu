@@ -468,8 +468,9 @@ int run_batch(gpv_ctx *ctx, int n, const float *const *d_tris, const int64_t *T,
       need += want;
     }
     if (overflow) {
-      if (ctx->pair_hint >= need) return fail_all(GPV_ERR_DEVICE, "pair buffer overflow");
-      ctx->pair_hint = need + need / 8;
+      // a buffer that held every candidate test cannot overflow: something else is wrong
+      if (pair_cap >= need) return fail_all(GPV_ERR_DEVICE, "pair buffer overflow");
+      ctx->pair_hint = std::max(ctx->pair_hint, need + need / 8);
       ctx->replans++;
       fail_all(GPV_OK, "");
       ctx->err.clear();

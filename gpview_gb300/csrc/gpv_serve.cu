@@ -8,6 +8,10 @@
 // into the next batch as soon as a worker and budget free up; with two workers, two batches are
 // in flight on the device at once.  Results stay on the device until the client releases them,
 // and their bytes count against the budget until then.
+//
+// Meshes can also be made resident: gpv_server_add_mesh uploads a mesh once into the server's
+// device pool (its bytes count against the budget while it stays), and gpv_server_submit_mesh
+// requests it by id, so a batch reads it in place with no host-to-device copy.
 #include <algorithm>
 #include <chrono>
 #include <condition_variable>
@@ -29,6 +33,8 @@ using Clock = std::chrono::steady_clock;
 struct Request {
   uint64_t ticket = 0;
   const float *h_tris = nullptr;
+  const float *d_tris = nullptr;  // a resident mesh's device triangles (no copy), else null
+  uint64_t mesh_id = 0;           // the resident mesh, 0 for host triangles
   int64_t T = 0;
   gpv_grid_spec spec{};
   Clock::time_point t_submit, t_start, t_done;
@@ -49,10 +55,17 @@ void predict(Request &r) {
   const int64_t cells = (int64_t)r.spec.ndiv2[0] * r.spec.ndiv2[1] * r.spec.ndiv2[2];
   const int64_t B = std::min(N1, 2 * surf);
   const int64_t pairs = 8 * r.T + 4 * B;
-  const int64_t work = 36 * r.T + 80 * r.T + N1 / 2 + 40 * pairs + 24 * B;
+  const int64_t work = (r.d_tris ? 0 : 36 * r.T) + 80 * r.T + N1 / 2 + 40 * pairs + 24 * B;
   r.res_bytes = 5 * N1 + B * (4 + cells);
   r.pred = work + r.res_bytes + (1 << 20);
 }
+
+// A mesh kept in the server's device pool (gpv_server_add_mesh).
+struct ResidentMesh {
+  float *d_tris = nullptr;
+  int64_t T = 0, bytes = 0;
+  int64_t refs = 0;  // pending or running requests that read it
+};
 
 }  // namespace
 }  // namespace gpv
@@ -60,6 +73,8 @@ void predict(Request &r) {
 using namespace gpv;
 
 struct gpv_server {
+  std::unordered_map<uint64_t, ResidentMesh> meshes;
+  uint64_t next_mesh = 1;
   std::mutex mu;
   std::condition_variable cv_work, cv_done;
   std::deque<Request *> pending;
@@ -119,15 +134,21 @@ void worker_loop(gpv_server *srv, int w) {
     for (int i = 0; i < n; ++i) {
       T[i] = batch[i]->T;
       specs[i] = batch[i]->spec;
-      off[i + 1] = off[i] + ((T[i] * 9 + 3) / 4) * 4;  // 16-byte aligned slots
+      // host triangles get 16-byte aligned slots of one device buffer; resident ones none
+      off[i + 1] = off[i] + (batch[i]->d_tris ? 0 : ((T[i] * 9 + 3) / 4) * 4);
       batch[i]->t_start = t0;
       batch[i]->worker = w;
     }
     float *d = nullptr;
-    int rc = (cudaMallocAsync((void **)&d, std::max<int64_t>(off[n], 4) * sizeof(float), s) == cudaSuccess)
-                 ? GPV_OK : GPV_ERR_OOM;
+    int rc = GPV_OK;
+    if (off[n] > 0)
+      rc = (cudaMallocAsync((void **)&d, off[n] * sizeof(float), s) == cudaSuccess) ? GPV_OK : GPV_ERR_OOM;
     std::vector<const float *> ptrs(n);
     for (int i = 0; i < n && rc == GPV_OK; ++i) {
+      if (batch[i]->d_tris) {  // resident: read in place
+        ptrs[i] = batch[i]->d_tris;
+        continue;
+      }
       ptrs[i] = d + off[i];
       if (T[i] > 0 &&
           cudaMemcpyAsync(d + off[i], batch[i]->h_tris, T[i] * 9 * sizeof(float),
@@ -145,6 +166,10 @@ void worker_loop(gpv_server *srv, int w) {
         Request *r = batch[i];
         r->t_done = t1;
         r->status = rc;
+        if (r->mesh_id) {
+          auto mt = srv->meshes.find(r->mesh_id);
+          if (mt != srv->meshes.end()) mt->second.refs--;
+        }
         if (rc == GPV_OK) {
           r->res = res[i];
           srv->in_use -= r->pred - r->res_bytes;  // workspace returns now, results on release
@@ -229,6 +254,90 @@ int gpv_server_submit(gpv_server *srv, const float *h_tris, int64_t num_triangle
   return GPV_OK;
 }
 
+int gpv_server_add_mesh(gpv_server *srv, const float *h_tris, int64_t num_triangles,
+                        uint64_t *mesh_id) {
+  if (!srv || !mesh_id || num_triangles <= 0 || !h_tris || num_triangles >= ((int64_t)1 << 31))
+    return GPV_ERR_INVALID;
+  const int64_t bytes = num_triangles * 9 * (int64_t)sizeof(float);
+  {
+    std::lock_guard<std::mutex> lk(srv->mu);
+    if (srv->in_use + bytes > srv->budget) return GPV_ERR_BUDGET;
+    srv->in_use += bytes;  // reserved while the upload runs
+  }
+  int prev = 0;
+  cudaGetDevice(&prev);
+  cudaSetDevice(srv->device);
+  float *d = nullptr;
+  int rc = GPV_OK;
+  if (cudaMalloc(&d, bytes) != cudaSuccess) {
+    cudaGetLastError();
+    rc = GPV_ERR_OOM;
+  } else if (cudaMemcpy(d, h_tris, bytes, cudaMemcpyHostToDevice) != cudaSuccess) {
+    cudaFree(d);
+    rc = GPV_ERR_CUDA;
+  }
+  cudaSetDevice(prev);
+  std::lock_guard<std::mutex> lk(srv->mu);
+  if (rc != GPV_OK) {
+    srv->in_use -= bytes;
+    return rc;
+  }
+  ResidentMesh m;
+  m.d_tris = d;
+  m.T = num_triangles;
+  m.bytes = bytes;
+  *mesh_id = srv->next_mesh++;
+  srv->meshes.emplace(*mesh_id, m);
+  return GPV_OK;
+}
+
+int gpv_server_submit_mesh(gpv_server *srv, uint64_t mesh_id, const gpv_grid_spec *spec,
+                           uint64_t *ticket) {
+  if (!srv || !spec || !ticket) return GPV_ERR_INVALID;
+  auto r = std::make_unique<Request>();
+  r->spec = *spec;
+  r->t_submit = Clock::now();
+  {
+    std::lock_guard<std::mutex> lk(srv->mu);
+    auto mt = srv->meshes.find(mesh_id);
+    if (mt == srv->meshes.end()) return GPV_ERR_NOTFOUND;
+    r->d_tris = mt->second.d_tris;
+    r->T = mt->second.T;
+    r->mesh_id = mesh_id;
+    predict(*r);
+    if (r->pred > srv->budget || (int64_t)srv->pending.size() >= srv->max_pending)
+      return GPV_ERR_BUDGET;
+    mt->second.refs++;
+    r->ticket = srv->next++;
+    *ticket = r->ticket;
+    srv->pending.push_back(r.get());
+    srv->all.emplace(r->ticket, std::move(r));
+  }
+  srv->cv_work.notify_one();
+  return GPV_OK;
+}
+
+int gpv_server_remove_mesh(gpv_server *srv, uint64_t mesh_id) {
+  if (!srv) return GPV_ERR_INVALID;
+  ResidentMesh m;
+  {
+    std::lock_guard<std::mutex> lk(srv->mu);
+    auto mt = srv->meshes.find(mesh_id);
+    if (mt == srv->meshes.end()) return GPV_ERR_NOTFOUND;
+    if (mt->second.refs > 0) return GPV_ERR_PENDING;  // requests still read it
+    m = mt->second;
+    srv->meshes.erase(mt);
+    srv->in_use -= m.bytes;
+  }
+  int prev = 0;
+  cudaGetDevice(&prev);
+  cudaSetDevice(srv->device);
+  cudaFree(m.d_tris);  // waits for any work still reading it
+  cudaSetDevice(prev);
+  srv->cv_work.notify_all();
+  return GPV_OK;
+}
+
 // Waits up to timeout_ms (0: do not wait, <0: forever) for a request; on completion fills the
 // result (device arrays owned by the server until gpv_server_release) and the latency.
 int gpv_server_poll(gpv_server *srv, uint64_t ticket, int32_t timeout_ms, gpv_result *out,
@@ -292,6 +401,13 @@ void gpv_server_destroy(gpv_server *srv) {
     cudaStreamSynchronize(srv->streams[k]);
     gpv_destroy(srv->ctxs[k]);
     cudaStreamDestroy(srv->streams[k]);
+  }
+  if (!srv->meshes.empty()) {
+    int prev = 0;
+    cudaGetDevice(&prev);
+    cudaSetDevice(srv->device);
+    for (auto &kv : srv->meshes) cudaFree(kv.second.d_tris);
+    cudaSetDevice(prev);
   }
   delete srv;
 }

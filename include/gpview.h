@@ -305,6 +305,15 @@ int gpv_server_submit(gpv_server *srv, const float *h_tris, int64_t num_triangle
 int gpv_server_poll(gpv_server *srv, uint64_t ticket, int32_t timeout_ms, gpv_result *out,
                     double *latency_ms, double *queue_ms);
 int gpv_server_release(gpv_server *srv, uint64_t ticket);
+/* Resident meshes: gpv_server_add_mesh uploads a mesh once into the server's device pool (its
+ * bytes count against the budget until removed) and returns its id; gpv_server_submit_mesh
+ * requests a voxelization of it by id (no host-to-device copy per request);
+ * gpv_server_remove_mesh frees it (GPV_ERR_PENDING while requests still read it). */
+int gpv_server_add_mesh(gpv_server *srv, const float *h_tris, int64_t num_triangles,
+                        uint64_t *mesh_id);
+int gpv_server_submit_mesh(gpv_server *srv, uint64_t mesh_id, const gpv_grid_spec *spec,
+                           uint64_t *ticket);
+int gpv_server_remove_mesh(gpv_server *srv, uint64_t mesh_id);
 int gpv_server_stats(gpv_server *srv, int64_t *in_use_bytes, int64_t *pending, uint64_t *batches,
                      uint64_t *served);
 void gpv_server_destroy(gpv_server *srv);

@@ -8,7 +8,8 @@ and src/TriRayIntersection.cpp) and writes:
   pred_ray.npz   ray/triangle cases and triangle_ray_intersection's answers (hit, t)
   normal_face.npz  face normals of the SAT-case triangles from the reference's own vector code
                  (includes/FloatVector.h: VectorCrossProduct, VectorNormalize)
-  mesh_*.npz     small meshes + grids and the full two-level outputs of the reference's CPU
+  mesh_*.npz     small meshes (and the reference's cessna.obj at voxelCount 8 and 32) + grids
+                 and the full two-level outputs of the reference's CPU
                  composition (E3) evaluated with the reference's predicates, voxel by voxel
                  (ClassifyInOutCPU semantics: every voxel centre against every triangle), plus
                  the Level1 and Level2 normals with the reference's vector arithmetic
@@ -116,7 +117,26 @@ def mesh_cases():
     return cases
 
 
+def cessna_cases():
+    """The reference's only mesh file (files/cessna.obj, committed here as cessna.obj), loaded with
+    the reference's OBJ semantics and sized by its own rule (GLParameters::voxelCount ->
+    GetNextDiv4, src/Object.cpp:3094-3107) at voxelCount 8 and 32, voxelCount2 4."""
+    import gpview_gb300 as gpv
+
+    obj = gpv.Object()
+    obj.ReadObject(os.path.join(HERE, "cessna.obj"))
+    obj.CreateFlatTriangleData()
+    out = {}
+    for vc in (8, 32):
+        spec = gpv.grid_reference(obj.bBoxMin, obj.bBoxMax, obj.maxModelSize, vc, 4)
+        out[f"cessna_v{vc}"] = (obj.flatCPUTriangleData, spec)
+    return out
+
+
 def main():
+    if "--only-cessna" in sys.argv:
+        write_meshes(cessna_cases())
+        return
     L = _ref_pred()
     rng = np.random.default_rng(20261203)
     n = 8000
@@ -142,9 +162,16 @@ def main():
     np.savez_compressed(os.path.join(HERE, "pred_ray.npz"), tri=v, origin=o, direction=d, hit=hit, t=tt)
     print("pred_ray: hit rate", hit.mean())
 
+    write_meshes(mesh_cases())
+    write_meshes(cessna_cases())
+
+
+def write_meshes(cases):
+    """Full two-level outputs and normals of the reference's CPU composition on the reference's
+    own predicates (oracle/_ref), brute-force Level1 fill."""
     from oracle import oracle as orc
 
-    for name, (tris, spec) in mesh_cases().items():
+    for name, (tris, spec) in cases.items():
         run = orc.Run(tris, spec, fill=orc.FILL_VOXEL, ref=True)
         st2, s2, r2 = run.level2_state()
         np.savez_compressed(
