@@ -16,7 +16,7 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libgpview.so")
 SOURCES = ["gpv_api.cu", "gpv_kernels.cu", "gpv_level2.cu", "gpv_sort.cu", "gpv_batch.cu", "gpv_shims.cu",
            "gpv_serve.cu", "gpv_noalloc.cu", "gpv_normals.cu", "gpv_hierarchy.cu", "gpv_stencil.cu",
-           "gpv_meshgen.cpp",
+           "gpv_meshgen.cpp", "gpv_hostio.cpp",
            "gpv_mesh.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-fmad=false", "-prec-div=true",

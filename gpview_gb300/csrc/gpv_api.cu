@@ -206,6 +206,8 @@ void gpv_destroy(gpv_ctx *ctx) {
   if (ctx->slab_aux.fork) cudaEventDestroy(ctx->slab_aux.fork);
   for (cudaEvent_t &e : ctx->slab_aux.join)
     if (e) cudaEventDestroy(e);
+  ctx->pool.reset();
+  if (ctx->h_codes) cudaFreeHost(ctx->h_codes);
   if (ctx->slab) cudaFree(ctx->slab);
   if (ctx->h_stats) cudaFreeHost(ctx->h_stats);
   if (ctx->h_md) cudaFreeHost(ctx->h_md);
@@ -285,6 +287,15 @@ int gpv_set_normals(gpv_ctx *ctx, int mode) {
 int gpv_set_level2_chunk(gpv_ctx *ctx, int cap) {
   if (!ctx || cap < 1 || cap > 32) return GPV_ERR_INVALID;
   ctx->l2_chunk_cap = cap;
+  return GPV_OK;
+}
+
+int gpv_set_host_expand(gpv_ctx *ctx, int threads, uint32_t slab_mask, int64_t min_level2_bytes) {
+  if (!ctx || threads < -1 || threads > 256 || min_level2_bytes < 0) return GPV_ERR_INVALID;
+  if (threads != ctx->host_threads) ctx->pool.reset();  // made again with the new count
+  ctx->host_threads = threads;
+  ctx->packed_slabs = slab_mask;
+  ctx->packed_min_bytes = min_level2_bytes;
   return GPV_OK;
 }
 

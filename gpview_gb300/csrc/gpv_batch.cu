@@ -399,7 +399,7 @@ int run_batch(gpv_ctx *ctx, int n, const float *const *d_tris, const int64_t *T,
                        (uint64_t)(uintptr_t)bd.queue, (uint64_t)bd.normals, (uint64_t)bd.fill,
                        (uint64_t)(uintptr_t)bd.stp, (uint64_t)bd.stp_words,
                        (uint64_t)ctx->timing, (uint64_t)ctx->num_sms, (uint64_t)bd.wait_limit,
-                       (uint64_t)bd.fail_wait})
+                       (uint64_t)bd.fail_wait, (uint64_t)bd.packed_slabs})
       v.push_back(x);
   };
   std::vector<uint64_t> sig0;
@@ -498,6 +498,35 @@ int run_batch(gpv_ctx *ctx, int n, const float *const *d_tris, const int64_t *T,
   // host outputs into pinned memory: the Level2 kernel writes its bytes there itself (over the
   // CPU-GPU link while it computes) instead of into device memory followed by copies
   const bool l2_direct = sink && sink->l2_dev && gh[0].level2 && sink->l2_cap >= l2bytes;
+  // packed Level2 host output (gpv_set_host_expand): the slabs in the context's mask send 2-bit
+  // codes into page-locked staging, a quarter of the bytes over the link, and host threads
+  // expand each finished slab into the caller's buffer while later slabs compute.  It needs the
+  // 16-cell output layout (n2z 8 or 16, a multiple of 16 sub-columns per layer, an aligned
+  // buffer) and pays only for large outputs.
+  bool packed = l2_direct && ctx->host_threads != 0 && ctx->host_threads != 1 &&
+                ctx->packed_slabs != 0 && (gh[0].n2[2] == 8 || gh[0].n2[2] == 16) &&
+                ((gh[0].n2[0] * gh[0].n2[1]) & 15) == 0 && l2bytes >= ctx->packed_min_bytes &&
+                sink->nslab == 0 && (reinterpret_cast<uintptr_t>(sink->l2_dev) & 15) == 0;
+  if (packed) {
+    const size_t words = (size_t)(l2bytes / 16);
+    if (ctx->h_codes_cap < words) {
+      if (ctx->h_codes) cudaFreeHost(ctx->h_codes);
+      ctx->h_codes = nullptr;
+      ctx->h_codes_cap = 0;
+      if (cudaMallocHost(&ctx->h_codes, words * sizeof(uint32_t)) == cudaSuccess) ctx->h_codes_cap = words;
+      else cudaGetLastError();
+    }
+    if (!ctx->pool && ctx->h_codes_cap >= words) {
+      const int hw = (int)std::max(1u, std::thread::hardware_concurrency());
+      ctx->pool.reset(new ExpandPool(ctx->host_threads > 1 ? ctx->host_threads : std::min(hw, 16)));
+    }
+    uint32_t *dcodes = nullptr;
+    packed = ctx->h_codes_cap >= words && ctx->pool &&
+             cudaHostGetDevicePointer((void **)&dcodes, ctx->h_codes, 0) == cudaSuccess && dcodes;
+    if (!packed) cudaGetLastError();  // the Level2 kernel writes bytes instead
+    md[0].l2codes = packed ? dcodes : nullptr;
+  }
+  bd.packed_slabs = packed ? ctx->packed_slabs : 0u;
   CK(ctx_malloc_async(ctx, &set->bindex, 4 * std::max<int64_t>(Btot, 4), s));
   if (l2_direct) {
     set->l2 = sink->l2_dev;
@@ -574,6 +603,7 @@ int run_batch(gpv_ctx *ctx, int n, const float *const *d_tris, const int64_t *T,
     // slab count: the caller's, or one per 12 MB of Level2 output (the copy of each slab then
     // overlaps the computation of the next; smaller slabs cost more than they hide)
     int want = sink->nslab > 0 ? sink->nslab
+               : packed        ? kMaxSlabs
                : l2_direct     ? 1
                                : (int)std::min<int64_t>(kMaxSlabs, l2bytes / (12ll << 20));
     want = std::max(1, std::min(want, fslab));
@@ -583,7 +613,7 @@ int run_batch(gpv_ctx *ctx, int n, const float *const *d_tris, const int64_t *T,
     for (int k = 0; k <= nslab; ++k) slab_off[k] = ctx->h_u32[4 + std::min(k * gsz, fslab)];
   }
   // host outputs: recorded too when only page-locked Level1 copies ride along (direct Level2)
-  const bool phase1_graph = !sink || (l2_direct && sink->l1_pinned);
+  const bool phase1_graph = !sink || (l2_direct && sink->l1_pinned && !packed);
   bool l2_queue = true;
   {
     std::unique_ptr<bool[]> has_l2(new bool[n]);
@@ -662,6 +692,10 @@ int run_batch(gpv_ctx *ctx, int n, const float *const *d_tris, const int64_t *T,
       if (any_l2)
         launch_level2(bd, sk, sv, useg, ub, l2tmp, warp_words, ctx->num_sms, s, [&] { mark(9); },
                       zslab, nslab, [&](int k, cudaStream_t ls) {
+                        if (packed) {  // the host expands this slab's codes once it is done
+                          cudaEventRecord(ctx->cev[1 + k], ls);
+                          return;
+                        }
                         if (!sink || !l2_copied || l2_direct) return;
                         cudaEventRecord(ctx->cev[1 + k], ls);
                         cudaStreamWaitEvent(cs, ctx->cev[1 + k], 0);
@@ -691,6 +725,15 @@ int run_batch(gpv_ctx *ctx, int n, const float *const *d_tris, const int64_t *T,
     out.copy(ctx->h_u32, wtot, 8);
     out.launch();
   }, phase1_graph, any_hier ? nullptr : &sig1));
+  if (packed) {
+    // each finished slab's codes -> the caller's bytes, while later slabs compute
+    for (int k = 0; k < nslab; ++k) {
+      if (!((bd.packed_slabs >> k) & 1u)) continue;
+      CK(cudaEventSynchronize(ctx->cev[1 + k]));
+      const int64_t a = (int64_t)slab_off[k] * gh[0].cells, b = (int64_t)slab_off[k + 1] * gh[0].cells;
+      if (b > a) ctx->pool->run(ctx->h_codes + a / 16, sink->l2 + a, (size_t)((b - a) / 16));
+    }
+  }
   CK(cudaStreamSynchronize(s));
   ht[4] = HClock::now();
   if (ctx->timing) {

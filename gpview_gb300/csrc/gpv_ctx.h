@@ -7,6 +7,7 @@
 #include <unordered_map>
 #include <vector>
 
+#include "gpv_hostio.h"
 #include "gpv_internal.h"
 
 namespace gpv {
@@ -47,6 +48,14 @@ struct gpv_ctx {
   int64_t debug_pair_cap = 0;          // next call's first pair capacity (one-shot)
   int64_t fail_allocs = 0;             // refuse this many of the next device allocations
   int64_t replans = 0;                 // calls re-run after a pair-buffer overflow
+  // gpv_voxelize_to_host's packed Level2 output (gpv_set_host_expand): host threads expanding
+  // 2-bit codes from page-locked staging, and which of the 8 z slabs send codes
+  int host_threads = -1;               // -1: by the machine (up to 16); 0 or 1: off
+  uint32_t packed_slabs = 0xff;        // slab k sends codes when bit k is set
+  int64_t packed_min_bytes = 64ll << 20;  // smaller Level2 outputs go as bytes
+  std::unique_ptr<gpv::ExpandPool> pool;
+  uint32_t *h_codes = nullptr;         // page-locked staging of the codes (device-mapped)
+  size_t h_codes_cap = 0;              // words
   bool graphs = true;                  // record the two phases as CUDA graphs
   int normals = 0;                     // GPV_NORMALS_* for the next voxelizations
   bool hierarchy = false;              // build the voxel box hierarchy

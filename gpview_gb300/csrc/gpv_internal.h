@@ -74,6 +74,11 @@ struct MeshDesc {
   float4 *fnorm;         // normals on: normalised face normal per triangle
   void *l1n, *l2n;       // normals on: Level1 / Level2 normal outputs (bytes or floats)
   uint32_t *stg;         // stencil fill: Level1 sample-column toggles, (2nx * 2ny) x nzw words
+  // host outputs through packed codes (one mesh): the Level2 states as 2-bit codes (0 outside,
+  // 1 inside, 2 boundary), 16 cells per word in output byte order, written here (device-mapped
+  // page-locked staging) by the z slabs whose bit is set in BatchDev::packed_slabs; the host
+  // expands them into the caller's bytes while later slabs compute
+  uint32_t *l2codes;
 };
 
 // BatchDev::fill value for Level1 SAT units only (no parity fill): the reference-named Level1
@@ -97,6 +102,8 @@ struct BatchDev {
   // fail_wait != 0 gives up at once (GPV_DEBUG_FAIL_WAIT, failure-detection tests)
   uint32_t wait_limit = 0;
   int fail_wait = 0;
+  // z slabs of the Level2 launch (bit k: slab k) that write MeshDesc::l2codes instead of bytes
+  uint32_t packed_slabs = 0;
 };
 
 // Small copies and clears around a phase, done by one kernel instead of copy-engine and memset

@@ -257,18 +257,20 @@ __device__ __forceinline__ uint32_t byte_flags4(uint32_t x) { return (x * 0x0020
 // Output bytes of one boundary voxel when n2z is 8 or 16 and a z layer holds a multiple of 16
 // sub-columns: each lane builds 16 consecutive bytes (16 sub-columns of one layer) from the mask
 // words, where layer r of a sub-column is bit r of its n2z-bit field, and writes them with one
-// 16-byte store (a warp covers 512 contiguous bytes per instruction).
+// 16-byte store (a warp covers 512 contiguous bytes per instruction).  With `codes`, the same 16
+// cells go out as one word of 2-bit codes (cell k of the 16 at bits 2k: 0 outside, 1 inside,
+// 2 boundary) for the host to expand, a quarter of the bytes over the CPU-GPU link.
 template <int NZ>
-__device__ __forceinline__ void write_block_vec(uint8_t *out, const uint32_t *satj,
-                                                const uint32_t *parj, const uint32_t *ftacc,
-                                                int ncol2, unsigned lane, unsigned long long &nbd,
-                                                unsigned long long &nin) {
+__device__ __forceinline__ void write_block_vec(uint8_t *out, uint32_t *codes,
+                                                const uint32_t *satj, const uint32_t *parj,
+                                                const uint32_t *ftacc, int ncol2, unsigned lane,
+                                                unsigned long long &nbd, unsigned long long &nin) {
   const int chunks = NZ * ncol2 / 16;
   for (int c = (int)lane; c < chunks; c += 32) {
     const int byte0 = c * 16;
     const int r = byte0 / ncol2, pq0 = byte0 - r * ncol2;
     const uint32_t f16 = (ftacc[pq0 >> 5] >> (pq0 & 31)) & 0xffffu;
-    uint32_t o[4];
+    uint32_t o[4], code = 0;
 #pragma unroll
     for (int k = 0; k < 4; ++k) {  // sub-columns pq0 + 4k .. pq0 + 4k + 3
       uint32_t sf, pf;
@@ -288,9 +290,15 @@ __device__ __forceinline__ void write_block_vec(uint8_t *out, const uint32_t *sa
       nbd += (unsigned)__popc(sf);
       nin += (unsigned)__popc(inf);
       o[k] = sf * 254u + inf * 127u;  // flags are 0/1 per byte and disjoint: no carries
+      if (codes) {
+        // bytes holding 0..2 -> four 2-bit fields
+        const uint32_t c4 = sf * 2u + inf;
+        code |= ((c4 & 3u) | ((c4 >> 6) & 0xcu) | ((c4 >> 12) & 0x30u) | ((c4 >> 18) & 0xc0u)) << (8 * k);
+      }
     }
-    // streaming store: the output is not read again, so it should not displace the working set
-    __stcs(reinterpret_cast<uint4 *>(out + byte0), make_uint4(o[0], o[1], o[2], o[3]));
+    // streaming stores: the output is not read again, so it should not displace the working set
+    if (codes) __stcs(codes + c, code);
+    else __stcs(reinterpret_cast<uint4 *>(out + byte0), make_uint4(o[0], o[1], o[2], o[3]));
   }
 }
 
@@ -1016,17 +1024,21 @@ __global__ void __launch_bounds__(kWarps * 32, QUEUE ? 6 : 7) k_level2c(
   // 16-byte stores where the layout allows them (also the fast pattern into pinned host memory);
   // measured faster with the queued organisation (torus262k: -6%) and slower with the per-lane
   // one on the mixed batch (+3%), so only the former uses them
-  const bool vec = QUEUE && (n2z == 8 || n2z == 16) && (ncol2 & 15) == 0 &&
+  // packed codes for the host: this launch's slab is one of BatchDev::packed_slabs (the host
+  // enables it only where the 16-byte layout below applies)
+  const bool packed = d.l2codes && ((bd.packed_slabs >> slab) & 1u);
+  const bool vec = (QUEUE || packed) && (n2z == 8 || n2z == 16) && (ncol2 & 15) == 0 &&
                    (reinterpret_cast<uintptr_t>(d.l2) & 15) == 0;
   for (int jv = m - 1; jv >= 0; --jv) {
     for (int w = lane; w < FW; w += 32) ftacc[w] ^= ft[jv * FW + w];
     __syncwarp();
     const int64_t vlin = ((int64_t)kz[jv] * ny + cj) * nx + ci;
     uint8_t *out = d.l2 + (size_t)d.prefix[vlin] * cells;
+    uint32_t *codes = packed ? d.l2codes + (size_t)d.prefix[vlin] * (cells >> 4) : nullptr;
     const uint32_t *satj = sat + jv * W, *parj = par + jv * W;
     if (vec) {
-      if (n2z == 8) write_block_vec<8>(out, satj, parj, ftacc, ncol2, lane, nbd, nin);
-      else write_block_vec<16>(out, satj, parj, ftacc, ncol2, lane, nbd, nin);
+      if (n2z == 8) write_block_vec<8>(out, codes, satj, parj, ftacc, ncol2, lane, nbd, nin);
+      else write_block_vec<16>(out, codes, satj, parj, ftacc, ncol2, lane, nbd, nin);
       __syncwarp();
       continue;
     }

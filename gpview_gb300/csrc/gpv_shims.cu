@@ -235,59 +235,73 @@ __device__ __forceinline__ void face_normal(const float *V, float n[3]) {
   }
 }
 
-// CUDAClassifyTessellationLevel2Kernel (.cu:403-448): one thread per (boundary voxel, cell).
-// Centres come from `cen` ([b][n2x | n2y | n2z] floats, formed on the host as the CPU does:
-// float(((p+0.5)*gridSize2 + mid) - ext1) in double, src/Object.cpp:2389-2391); the CPU's unit
-// face normals are summed in list order.
+// CUDAClassifyTessellationLevel2Kernel (.cu:403-448), one thread per (boundary voxel,
+// sub-column) instead of per cell: the SAT's z-invariant axes run once per (triangle,
+// sub-column) and the z-dependent part per cell (the split is exact: the test is the conjunction
+// of its axes).  Centres come from `cen` ([b][n2x | n2y | n2z] floats, formed on the host as the
+// CPU does: float(((p+0.5)*gridSize2 + mid) - ext1) in double, src/Object.cpp:2389-2391); each
+// cell sums the CPU's unit face normals in list order, as a per-cell thread would.
 __global__ void k_shim_level2_sat(const float *__restrict__ tris, float *__restrict__ l2,
                                   float *__restrict__ nrm, const float *__restrict__ cen,
                                   const int *__restrict__ l2index, const int *__restrict__ cnt,
                                   const int *__restrict__ flatIndex, const int *__restrict__ flat,
                                   int B, int3 n2, float3 e2) {
   const int64_t gid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  const int cells = n2.x * n2.y * n2.z;
-  if (gid >= (int64_t)B * cells) return;
-  const int b = (int)(gid / cells), c = (int)(gid % cells);
-  const int r = c / (n2.x * n2.y), q = (c / n2.x) % n2.y, p = c % n2.x;
+  const int ncol2 = n2.x * n2.y, cells = ncol2 * n2.z;
+  if (gid >= (int64_t)B * ncol2) return;
+  const int b = (int)(gid / ncol2), pq = (int)(gid % ncol2);
+  const int q = pq / n2.x, p = pq - q * n2.x;
   const int v = l2index[b];
   const float *cb = cen + (size_t)b * (n2.x + n2.y + n2.z);
-  const float cc[3] = {cb[p], cb[n2.x + q], cb[n2.x + n2.y + r]};
+  const float *cz = cb + n2.x + n2.y;
+  const float cx = cb[p], cy = cb[n2.x + q];
   const float h[3] = {e2.x, e2.y, e2.z};
   const int n = cnt[v], f0 = flatIndex[v];
   for (int k = 0; k < n; ++k) {
     const int t = flat[f0 + k];
     float V[9];
     for (int j = 0; j < 9; ++j) V[j] = tris[9 * (size_t)t + j];
-    if (!tri_box(V, cc, h)) continue;
+    SatCol sc;
+    if (!sat_col(V, cx, cy, h, sc)) continue;
+    bool have_fn = false;
     float fn[3];
-    face_normal(V, fn);
-    const size_t o = (size_t)b * cells + c;
-    l2[o] = 2.0f;
-    nrm[4 * o + 0] = fa(nrm[4 * o + 0], fn[0]);
-    nrm[4 * o + 1] = fa(nrm[4 * o + 1], fn[1]);
-    nrm[4 * o + 2] = fa(nrm[4 * o + 2], fn[2]);
-    nrm[4 * o + 3] = fa(nrm[4 * o + 3], 1.0f);
+    for (int r = 0; r < n2.z; ++r) {
+      if (!sat_z(sc, V, cz[r], h)) continue;
+      if (!have_fn) {
+        face_normal(V, fn);
+        have_fn = true;
+      }
+      const size_t o = (size_t)b * cells + (size_t)r * ncol2 + pq;
+      l2[o] = 2.0f;
+      nrm[4 * o + 0] = fa(nrm[4 * o + 0], fn[0]);
+      nrm[4 * o + 1] = fa(nrm[4 * o + 1], fn[1]);
+      nrm[4 * o + 2] = fa(nrm[4 * o + 2], fn[2]);
+      nrm[4 * o + 3] = fa(nrm[4 * o + 3], 1.0f);
+    }
   }
 }
 
-// CUDAClassifyInOutLevel2Kernel (.cu:450-504): one thread per (boundary voxel, cell), +z parity
-// against the x/y-column list.  Origin: (2p+1)*ext2 + mid - ext1 in float, left to right.
+// CUDAClassifyInOutLevel2Kernel (.cu:450-504), one thread per (boundary voxel, sub-column)
+// instead of per cell: the ray test's u/v part depends only on the origin's x and y, so it runs
+// once per (triangle, sub-column), and t per cell; the +z parity of every cell of the sub-column
+// against the x/y-column list is kept in one bit each.  Origins: (2p+1)*ext2 + mid - ext1 in
+// float, left to right, as the reference kernel forms them.
 __global__ void k_shim_level2_fill(const float *__restrict__ tris, float *__restrict__ l2,
                                    const float *__restrict__ mid, const int *__restrict__ l2index,
                                    const int *__restrict__ xycnt, const int *__restrict__ xyIndex,
                                    const int *__restrict__ xyflat, int B, int3 nd, int3 n2,
                                    float3 e1, float3 e2, float thr) {
   const int64_t gid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  const int cells = n2.x * n2.y * n2.z;
-  if (gid >= (int64_t)B * cells) return;
-  const int b = (int)(gid / cells), c = (int)(gid % cells);
-  const int r = c / (n2.x * n2.y), q = (c / n2.x) % n2.y, p = c % n2.x;
+  const int ncol2 = n2.x * n2.y, cells = ncol2 * n2.z;
+  if (gid >= (int64_t)B * ncol2) return;
+  const int b = (int)(gid / ncol2), pq = (int)(gid % ncol2);
+  const int q = pq / n2.x, p = pq - q * n2.x;
   const int v = l2index[b];
   const int xy = v % (nd.x * nd.y);
   const float ox = fs(fa(fm((float)(2 * p + 1), e2.x), mid[3 * b + 0]), e1.x);
   const float oy = fs(fa(fm((float)(2 * q + 1), e2.y), mid[3 * b + 1]), e1.y);
-  const float oz = fs(fa(fm((float)(2 * r + 1), e2.z), mid[3 * b + 2]), e1.z);
-  int hits = 0;
+  const float mz = mid[3 * b + 2];
+  uint32_t par = 0;  // one bit per cell (n2z <= 32)
   const int n = xycnt[xy], f0 = xyIndex[xy];
   for (int k = 0; k < n; ++k) {
     const int t = xyflat[f0 + k];
@@ -298,9 +312,13 @@ __global__ void k_shim_level2_fill(const float *__restrict__ tris, float *__rest
     if (!rt.ok) continue;
     RayCol rc;
     if (!ray_col(rt, ox, oy, rc)) continue;
-    hits += ray_t(rt, rc, oz, thr) ? 1 : 0;
+    for (int r = 0; r < n2.z; ++r) {
+      const float oz = fs(fa(fm((float)(2 * r + 1), e2.z), mz), e1.z);
+      if (ray_t(rt, rc, oz, thr)) par ^= 1u << r;
+    }
   }
-  if (hits % 2 == 1) l2[(size_t)b * cells + c] = 1.0f;
+  for (int r = 0; r < n2.z; ++r)
+    if ((par >> r) & 1u) l2[(size_t)b * cells + (size_t)r * ncol2 + pq] = 1.0f;
 }
 
 }  // namespace
@@ -467,7 +485,7 @@ int CUDAClassifyTessellationLevel2(float *trianglesCUDAData, float *level2InOutC
     }
   float *d_cen = static_cast<float *>(g_shim.dev);
   cudaMemcpyAsync(d_cen, cen, ncen * sizeof(float), cudaMemcpyHostToDevice, 0);
-  const int64_t n = (int64_t)numBoundary * cells;
+  const int64_t n = (int64_t)numBoundary * numDiv2.x * numDiv2.y;  // a thread per sub-column
   k_shim_level2_sat<<<(unsigned)((n + 127) / 128), 128>>>(
       trianglesCUDAData, level2InOutCUDAData, level2NormalCUDAData, d_cen, level2IndexCUDAData,
       voxelTriCountCUDAData, level1TriFlatIndexCUDAData, level1TriFlatCUDAData, numBoundary,
@@ -484,7 +502,8 @@ int CUDAClassifyInOutLevel2(float *trianglesCUDAData, float *level2InOutCUDAData
                             float3 boxExtentsLevel1, float3 boxExtentsLevel2) {
   const int cells = numDiv2.x * numDiv2.y * numDiv2.z;
   if (numBoundary <= 0 || cells <= 0) return 1;
-  const int64_t n = (int64_t)numBoundary * cells;
+  if (numDiv2.z > 32) return 1;  // one parity bit per cell of a sub-column
+  const int64_t n = (int64_t)numBoundary * numDiv2.x * numDiv2.y;  // a thread per sub-column
   k_shim_level2_fill<<<(unsigned)((n + 127) / 128), 128>>>(
       trianglesCUDAData, level2InOutCUDAData, level1MidPointCUDAData, level2IndexCUDAData,
       xyTriCountCUDAData, xyTriFlatIndexCUDAData, xyTriFlatCUDAData, numBoundary, numDiv, numDiv2,

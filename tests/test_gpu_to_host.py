@@ -125,3 +125,44 @@ def test_to_host_level1_only(ctx):
     assert rc == 0
     np.testing.assert_array_equal(l1, orc.Run(tris, spec).level1_bytes())
     ctx.release(res)
+
+
+@pytest.mark.parametrize("mask", [0xff, 0x0f, 0x55, 0x80])
+def test_packed_transfer_equals_plain_torus262k(ctx, mask):
+    """The packed Level2 transfer (2-bit codes expanded by host threads) gives the bytes the
+    kernel writes directly, whichever slabs send codes; the size threshold is lowered so that
+    this 56 MB output takes it."""
+    tris, spec = W.make(W.C2)
+    plain = ctx.voxelize_host(tris, spec)
+    p = ctx.fetch(plain)
+    ctx.release(plain)
+    ctx.set_host_expand(-1, mask, 0)
+    try:
+        rc, res, l1, pre, bi, l2 = _to_host(ctx, tris, spec, 0)
+    finally:
+        ctx.set_host_expand()
+    assert rc == 0
+    for a, b in zip((l1, pre, bi, l2), p):
+        np.testing.assert_array_equal(a, b)
+    assert res.num_level2_inside == int((l2 == 127).sum())
+    ctx.release(res)
+
+
+def test_packed_transfer_star1310k_and_threads(ctx):
+    """The largest plain configuration through the default packed transfer, then with 3 host
+    threads and part of the slabs, then with it off: identical bytes each time, equal to the
+    device result."""
+    tris, spec = W.make(W.C3)
+    plain = ctx.voxelize_host(tris, spec)
+    p = ctx.fetch(plain)
+    ctx.release(plain)
+    try:
+        for threads, mask in ((-1, 0xff), (3, 0x3f), (0, 0xff)):
+            ctx.set_host_expand(threads, mask)
+            rc, res, l1, pre, bi, l2 = _to_host(ctx, tris, spec, 0)
+            assert rc == 0
+            ctx.release(res)
+            for a, b in zip((l1, pre, bi, l2), p):
+                np.testing.assert_array_equal(a, b)
+    finally:
+        ctx.set_host_expand()
