@@ -311,7 +311,7 @@ class Context:
         """LEVEL2_AUTO (default), LEVEL2_QUEUED or LEVEL2_INLINE: the Level2 SAT organisation."""
         self._check(lib().gpv_set_level2_mode(self._h, int(mode)), "set_level2_mode")
 
-    def set_host_expand(self, threads=-1, slab_mask=0xff, min_level2_bytes=64 << 20):
+    def set_host_expand(self, threads=-1, slab_mask=0x0f, min_level2_bytes=64 << 20):
         """Packed Level2 transfer of voxelize_to_host (gpv_set_host_expand): host threads (-1 by
         the machine, 0 off), the z slabs (bit mask of 8) that send 2-bit codes, and the Level2
         output size from which it applies."""

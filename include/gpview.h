@@ -239,8 +239,8 @@ int gpv_voxelize_host(gpv_ctx *ctx, const float *h_tris, int64_t num_triangles,
  * also returned (device arrays valid until gpv_result_release).  If h_l2_bytes < num_boundary *
  * n2^3 nothing is written to h_l2 and GPV_ERR_BUDGET is returned with the result complete
  * (release it; num_boundary gives the size needed). */
-/* Packed Level2 transfer of gpv_voxelize_to_host (default: on, threads by the machine, all 8
- * slabs, outputs of 64 MiB and more).  When the Level2 kernel writes page-locked host memory
+/* Packed Level2 transfer of gpv_voxelize_to_host (default: on, threads by the machine, slabs
+ * 0-3 of 8, outputs of 64 MiB and more).  When the Level2 kernel writes page-locked host memory
  * directly (slabs == 0), the link carries one byte per Level2 cell.  With this on, the z slabs
  * in slab_mask (bit k: slab k of 8) send 2-bit codes into page-locked staging instead, a quarter
  * of the bytes.  `threads` host threads (the calling thread among them; -1: up to 16 by the
