@@ -219,7 +219,7 @@ def cpu_sample(tris, grid, work_total, seconds, threads, run=None):
 
 
 def cpu_as_written(tris, grid, work_total, seconds, seed=7):
-    """The reference's CPU path as it is written, on ONE thread (SURVEY: 'reference-as-written'):
+    """The reference's CPU path as it is written, on ONE thread (the reference-as-written baseline):
     ClassifyTessellation and the compaction (timed in full), ClassifyInOutCPU's brute force --
     every voxel centre against every triangle -- on a seeded sample of Level1 columns, and the
     Level2 passes on an evenly strided sample of boundary voxels; the two sampled parts are extrapolated
