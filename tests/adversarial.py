@@ -19,6 +19,9 @@ as a flipped state against the oracle:
                        binning's cell boundaries, moved by -3..+3 ulps;
   corner_planes     -- triangles whose plane passes within rounding of a Level2 cell corner (the
                        SAT plane test at its tie), moved by -2..+2 ulps in z;
+  edge_corners      -- edges through two Level2 sub-column corners, moved by -2..+2 ulps in x
+                       (the x/y edge axes of the z-invariant SAT part at their ties);
+  x_parallel        -- edges nearly parallel to x (their ends' y 0..8 ulps apart);
   near_vertical     -- tall faces whose normal has a tiny z component (wide plane slabs);
   degenerate        -- zero-area, collinear and sub-ulp triangles.
 The soup is not closed; the outputs are still fully defined by the reference's algorithm, and the
@@ -216,6 +219,52 @@ def corner_planes(rng, centres, half, count):
     return np.array(out, F).reshape(-1, 9)
 
 
+def edge_corners(rng, centres, half, zrange, count):
+    """Triangles with an edge through two Level2 sub-column corners (the x/y edge-axis test of
+    the SAT at its tie, decided once per sub-column by the Level2 kernel), each repeated with
+    the edge's ends moved by -2..+2 ulps in x."""
+    sx, sy = centres
+    out = []
+    for _ in range(count):
+        a = np.array([F(rng.choice(sx)) + F(half[0]) * F(rng.choice([-1.0, 1.0])),
+                      F(rng.choice(sy)) + F(half[1]) * F(rng.choice([-1.0, 1.0]))], F)
+        # the other end a few sub-columns away (or far away, for long edges)
+        reach = float(half[0]) * 2 * rng.choice([1, 2, 3, 7, 40])
+        b = (a.astype(np.float64) + reach * rng.choice([-1.0, 1.0], 2) *
+             np.array([rng.integers(0, 4), rng.integers(1, 4)])).astype(F)
+        b = (np.round((b.astype(np.float64) - a) / (2 * np.asarray(half[:2], np.float64))) *
+             (2 * np.asarray(half[:2], np.float64)) + a).astype(F)
+        c = (a.astype(np.float64) + rng.normal(size=2) * reach).astype(F)
+        z = rng.uniform(zrange[0], zrange[1], 3).astype(F)
+        if (a == b).all():
+            continue
+        V = np.array([[a[0], a[1], z[0]], [b[0], b[1], z[1]], [c[0], c[1], z[2]]], F)
+        if (V <= 0).any():
+            continue
+        for k in (-2, -1, 0, 1, 2):
+            W = V.copy()
+            W[:2, 0] = ulp_shift(W[:2, 0], k)
+            out.append(W.reshape(9))
+    return np.array(out, F).reshape(-1, 9)
+
+
+def x_parallel(rng, bmin, bmax, count):
+    """Triangles with an edge nearly parallel to x: its ends' y differ by 0..8 ulps, so its
+    x/y edge axis is ill-conditioned (the float test is decided by rounding)."""
+    bmin = np.asarray(bmin, np.float64)
+    span = np.asarray(bmax, np.float64) - bmin
+    out = []
+    for k in range(count):
+        p = (bmin + span * rng.uniform(0.2, 0.8, 3)).astype(F)
+        q = (bmin + span * rng.uniform(0.2, 0.8, 3)).astype(F)
+        if p[1] <= 0:
+            continue
+        q[1] = ulp_shift(np.array([p[1]], F), int(k % 9))[0]
+        r = (bmin + span * rng.uniform(0.2, 0.8, 3)).astype(F)
+        out.append(np.stack([p, q, r]).astype(F).reshape(9))
+    return np.array(out, F).reshape(-1, 9)
+
+
 def near_vertical(rng, bmin, bmax, count):
     """Tall faces whose normal's z component is tiny (1e-7 .. 1e-3 of its length)."""
     bmin = np.asarray(bmin, np.float64)
@@ -283,6 +332,9 @@ def soup(spec_tuple, tab, seed=0, scale=1.0):
     parts.append(face_snapped(rng, f2, cell / max(n2), k(160)))
     parts.append(face_snapped(rng, fb, cell, k(80)))
     parts.append(corner_planes(rng, (sx, sy, sz), np.asarray(e2, np.float64), k(50)))
+    zr = (bmin[2] + 0.1 * (bmax[2] - bmin[2]), bmax[2] - 0.1 * (bmax[2] - bmin[2]))
+    parts.append(edge_corners(rng, (sx, sy), np.asarray(e2, np.float64), zr, k(40)))
+    parts.append(x_parallel(rng, bmin, bmax, k(30)))
     parts.append(near_vertical(rng, bmin, bmax, k(60)))
     parts.append(degenerate(rng, bmin, bmax, k(24)))
     tris = np.concatenate([p.reshape(-1, 9) for p in parts if p.size]).astype(F)
