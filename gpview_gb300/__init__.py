@@ -148,7 +148,7 @@ def lib():
     L.gpv_set_level2_chunk.argtypes = [C.c_void_p, C.c_int]
     L.gpv_set_level2_mode.argtypes = [C.c_void_p, C.c_int]
     L.gpv_set_debug.argtypes = [C.c_void_p, C.c_int, C.c_int64]
-    L.gpv_set_host_expand.argtypes = [C.c_void_p, C.c_int, C.c_uint32, C.c_int64]
+    L.gpv_set_host_expand.argtypes = [C.c_void_p, C.c_int, C.c_uint32, C.c_int32, C.c_int64]
     L.gpv_get_debug.argtypes = [C.c_void_p, C.c_int]
     L.gpv_get_debug.restype = C.c_int64
     L.gpv_set_graphs.argtypes = [C.c_void_p, C.c_int]
@@ -311,11 +311,12 @@ class Context:
         """LEVEL2_AUTO (default), LEVEL2_QUEUED or LEVEL2_INLINE: the Level2 SAT organisation."""
         self._check(lib().gpv_set_level2_mode(self._h, int(mode)), "set_level2_mode")
 
-    def set_host_expand(self, threads=-1, slab_mask=0x0f, min_level2_bytes=64 << 20):
+    def set_host_expand(self, threads=-1, slab_mask=0xff, share=45, min_level2_bytes=64 << 20):
         """Packed Level2 transfer of voxelize_to_host (gpv_set_host_expand): host threads (-1 by
-        the machine, 0 off), the z slabs (bit mask of 8) that send 2-bit codes, and the Level2
-        output size from which it applies."""
-        self._check(lib().gpv_set_host_expand(self._h, int(threads), int(slab_mask),
+        the machine, 0 off), the z slabs (bit mask of 8) that send 2-bit codes for the first
+        `share` percent of their boundary voxels, and the Level2 output size from which it
+        applies."""
+        self._check(lib().gpv_set_host_expand(self._h, int(threads), int(slab_mask), int(share),
                                               int(min_level2_bytes)), "set_host_expand")
 
     DEBUG = {"wait_limit": 1, "fail_wait": 2, "pair_capacity": 3, "fail_allocs": 4, "replans": 5}

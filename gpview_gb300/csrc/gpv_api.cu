@@ -290,11 +290,15 @@ int gpv_set_level2_chunk(gpv_ctx *ctx, int cap) {
   return GPV_OK;
 }
 
-int gpv_set_host_expand(gpv_ctx *ctx, int threads, uint32_t slab_mask, int64_t min_level2_bytes) {
-  if (!ctx || threads < -1 || threads > 256 || min_level2_bytes < 0) return GPV_ERR_INVALID;
+int gpv_set_host_expand(gpv_ctx *ctx, int threads, uint32_t slab_mask, int32_t share_percent,
+                        int64_t min_level2_bytes) {
+  if (!ctx || threads < -1 || threads > 256 || min_level2_bytes < 0 || share_percent < 0 ||
+      share_percent > 100)
+    return GPV_ERR_INVALID;
   if (threads != ctx->host_threads) ctx->pool.reset();  // made again with the new count
   ctx->host_threads = threads;
   ctx->packed_slabs = slab_mask;
+  ctx->packed_share = share_percent;
   ctx->packed_min_bytes = min_level2_bytes;
   return GPV_OK;
 }

@@ -399,7 +399,7 @@ int run_batch(gpv_ctx *ctx, int n, const float *const *d_tris, const int64_t *T,
                        (uint64_t)(uintptr_t)bd.queue, (uint64_t)bd.normals, (uint64_t)bd.fill,
                        (uint64_t)(uintptr_t)bd.stp, (uint64_t)bd.stp_words,
                        (uint64_t)ctx->timing, (uint64_t)ctx->num_sms, (uint64_t)bd.wait_limit,
-                       (uint64_t)bd.fail_wait, (uint64_t)bd.packed_slabs})
+                       (uint64_t)bd.fail_wait})
       v.push_back(x);
   };
   std::vector<uint64_t> sig0;
@@ -504,7 +504,8 @@ int run_batch(gpv_ctx *ctx, int n, const float *const *d_tris, const int64_t *T,
   // 16-cell output layout (n2z 8 or 16, a multiple of 16 sub-columns per layer, an aligned
   // buffer) and pays only for large outputs.
   bool packed = l2_direct && ctx->host_threads != 0 && ctx->host_threads != 1 &&
-                ctx->packed_slabs != 0 && (gh[0].n2[2] == 8 || gh[0].n2[2] == 16) &&
+                ctx->packed_slabs != 0 && ctx->packed_share > 0 &&
+                (gh[0].n2[2] == 8 || gh[0].n2[2] == 16) &&
                 ((gh[0].n2[0] * gh[0].n2[1]) & 15) == 0 && l2bytes >= ctx->packed_min_bytes &&
                 sink->nslab == 0 && (reinterpret_cast<uintptr_t>(sink->l2_dev) & 15) == 0;
   if (packed) {
@@ -526,7 +527,6 @@ int run_batch(gpv_ctx *ctx, int n, const float *const *d_tris, const int64_t *T,
     if (!packed) cudaGetLastError();  // the Level2 kernel writes bytes instead
     md[0].l2codes = packed ? dcodes : nullptr;
   }
-  bd.packed_slabs = packed ? ctx->packed_slabs : 0u;
   CK(ctx_malloc_async(ctx, &set->bindex, 4 * std::max<int64_t>(Btot, 4), s));
   if (l2_direct) {
     set->l2 = sink->l2_dev;
@@ -611,6 +611,13 @@ int run_batch(gpv_ctx *ctx, int n, const float *const *d_tris, const int64_t *T,
     zslab = gsz * fz;
     nslab = (fslab + gsz - 1) / gsz;
     for (int k = 0; k <= nslab; ++k) slab_off[k] = ctx->h_u32[4 + std::min(k * gsz, fslab)];
+  }
+  // packed output: the first share of each masked slab's boundary voxels (output order)
+  for (int k = 0; k < kMaxSlabs; ++k) {
+    bd.pk_end[k] = 0;
+    if (!packed || k >= std::max(nslab, 1) || !((ctx->packed_slabs >> k) & 1u)) continue;
+    const uint32_t lo = d_slab ? slab_off[k] : 0u, hi = d_slab ? slab_off[k + 1] : (uint32_t)Btot;
+    bd.pk_end[k] = lo + (uint32_t)(((uint64_t)(hi - lo) * (uint64_t)ctx->packed_share + 99) / 100);
   }
   // host outputs: recorded too when only page-locked Level1 copies ride along (direct Level2)
   const bool phase1_graph = !sink || (l2_direct && sink->l1_pinned && !packed);
@@ -728,9 +735,10 @@ int run_batch(gpv_ctx *ctx, int n, const float *const *d_tris, const int64_t *T,
   if (packed) {
     // each finished slab's codes -> the caller's bytes, while later slabs compute
     for (int k = 0; k < nslab; ++k) {
-      if (!((bd.packed_slabs >> k) & 1u)) continue;
+      const uint32_t lo = d_slab ? slab_off[k] : 0u;
+      if (bd.pk_end[k] <= lo) continue;
       CK(cudaEventSynchronize(ctx->cev[1 + k]));
-      const int64_t a = (int64_t)slab_off[k] * gh[0].cells, b = (int64_t)slab_off[k + 1] * gh[0].cells;
+      const int64_t a = (int64_t)lo * gh[0].cells, b = (int64_t)bd.pk_end[k] * gh[0].cells;
       if (b > a) ctx->pool->run(ctx->h_codes + a / 16, sink->l2 + a, (size_t)((b - a) / 16));
     }
   }

@@ -51,11 +51,13 @@ struct gpv_ctx {
   // gpv_voxelize_to_host's packed Level2 output (gpv_set_host_expand): host threads expanding
   // 2-bit codes from page-locked staging, and which of the 8 z slabs send codes
   int host_threads = -1;               // -1: by the machine (up to 16); 0 or 1: off
-  // slab k sends codes when bit k is set.  The first four: their codes are expanded by the host
-  // while the GPU computes the last four, whose bytes it writes over the link itself (star1310k
-  // host to host: 7.32 ms all bytes, 7.72 all codes, 6.70 the first four as codes, 7.46 the
-  // last four, 6.93 every other one)
-  uint32_t packed_slabs = 0x0f;
+  // slab k sends codes for the first packed_share percent of its boundary voxels when bit k is
+  // set, and bytes for the rest.  Sharing every slab keeps the link and the host threads busy
+  // together from the first slab to the last (star1310k host to host, ms: all bytes 7.30; the
+  // first four slabs as codes 6.70; every slab 20% codes 6.78, 40% 6.48, 45% 6.41, 50% 6.56,
+  // 60% 6.79, 100% 8.28)
+  uint32_t packed_slabs = 0xff;
+  int packed_share = 45;
   int64_t packed_min_bytes = 64ll << 20;  // smaller Level2 outputs go as bytes
   std::unique_ptr<gpv::ExpandPool> pool;
   uint32_t *h_codes = nullptr;         // page-locked staging of the codes (device-mapped)

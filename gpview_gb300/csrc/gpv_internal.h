@@ -102,8 +102,9 @@ struct BatchDev {
   // fail_wait != 0 gives up at once (GPV_DEBUG_FAIL_WAIT, failure-detection tests)
   uint32_t wait_limit = 0;
   int fail_wait = 0;
-  // z slabs of the Level2 launch (bit k: slab k) that write MeshDesc::l2codes instead of bytes
-  uint32_t packed_slabs = 0;
+  // packed Level2 host output: in z slab k of the Level2 launch, the boundary voxels whose output
+  // index is below pk_end[k] write MeshDesc::l2codes instead of bytes (the slab's first share)
+  uint32_t pk_end[8] = {};
 };
 
 // Small copies and clears around a phase, done by one kernel instead of copy-engine and memset

@@ -1024,17 +1024,18 @@ __global__ void __launch_bounds__(kWarps * 32, QUEUE ? 6 : 7) k_level2c(
   // 16-byte stores where the layout allows them (also the fast pattern into pinned host memory);
   // measured faster with the queued organisation (torus262k: -6%) and slower with the per-lane
   // one on the mixed batch (+3%), so only the former uses them
-  // packed codes for the host: this launch's slab is one of BatchDev::packed_slabs (the host
+  // packed codes for the host: the voxels of this launch's slab below BatchDev::pk_end (the host
   // enables it only where the 16-byte layout below applies)
-  const bool packed = d.l2codes && ((bd.packed_slabs >> slab) & 1u);
-  const bool vec = (QUEUE || packed) && (n2z == 8 || n2z == 16) && (ncol2 & 15) == 0 &&
+  const uint32_t pkend = d.l2codes ? bd.pk_end[slab] : 0u;
+  const bool vec = (QUEUE || pkend) && (n2z == 8 || n2z == 16) && (ncol2 & 15) == 0 &&
                    (reinterpret_cast<uintptr_t>(d.l2) & 15) == 0;
   for (int jv = m - 1; jv >= 0; --jv) {
     for (int w = lane; w < FW; w += 32) ftacc[w] ^= ft[jv * FW + w];
     __syncwarp();
     const int64_t vlin = ((int64_t)kz[jv] * ny + cj) * nx + ci;
     uint8_t *out = d.l2 + (size_t)d.prefix[vlin] * cells;
-    uint32_t *codes = packed ? d.l2codes + (size_t)d.prefix[vlin] * (cells >> 4) : nullptr;
+    const uint32_t vidx = (uint32_t)d.prefix[vlin];
+    uint32_t *codes = vidx < pkend ? d.l2codes + (size_t)vidx * (cells >> 4) : nullptr;
     const uint32_t *satj = sat + jv * W, *parj = par + jv * W;
     if (vec) {
       if (n2z == 8) write_block_vec<8>(out, codes, satj, parj, ftacc, ncol2, lane, nbd, nin);

@@ -239,17 +239,19 @@ int gpv_voxelize_host(gpv_ctx *ctx, const float *h_tris, int64_t num_triangles,
  * also returned (device arrays valid until gpv_result_release).  If h_l2_bytes < num_boundary *
  * n2^3 nothing is written to h_l2 and GPV_ERR_BUDGET is returned with the result complete
  * (release it; num_boundary gives the size needed). */
-/* Packed Level2 transfer of gpv_voxelize_to_host (default: on, threads by the machine, slabs
- * 0-3 of 8, outputs of 64 MiB and more).  When the Level2 kernel writes page-locked host memory
+/* Packed Level2 transfer of gpv_voxelize_to_host (default: on, threads by the machine, every
+ * slab with a share of 45 percent, outputs of 64 MiB and more).  When the Level2 kernel writes page-locked host memory
  * directly (slabs == 0), the link carries one byte per Level2 cell.  With this on, the z slabs
  * in slab_mask (bit k: slab k of 8) send 2-bit codes into page-locked staging instead, a quarter
- * of the bytes.  `threads` host threads (the calling thread among them; -1: up to 16 by the
- * machine; 0 or 1: off) turn each finished slab's codes into the same bytes in
+ * of the bytes, for the first share_percent percent of their boundary voxels (output order; the
+ * rest keep the direct byte writes).  `threads` host threads (the calling thread among them; -1:
+ * up to 16 by the machine; 0 or 1: off) turn each finished slab's codes into the same bytes in
  * h_level2_inout, while later slabs compute.  It applies to Level2 grids with n2z of 8 or 16 and
  * a multiple of 16 sub-columns per layer, to 16-byte aligned Level2 buffers and to outputs of at
- * least min_level2_bytes.  Slabs left out of the mask keep the direct byte writes, so the link
- * and the host threads share the output. */
-int gpv_set_host_expand(gpv_ctx *ctx, int threads, uint32_t slab_mask, int64_t min_level2_bytes);
+ * least min_level2_bytes.  The link carries the direct bytes and the codes while the host
+ * threads expand, so the two share the output.  share_percent 0..100 (0: off). */
+int gpv_set_host_expand(gpv_ctx *ctx, int threads, uint32_t slab_mask, int32_t share_percent,
+                        int64_t min_level2_bytes);
 int gpv_voxelize_to_host(gpv_ctx *ctx, const float *h_tris, int64_t num_triangles,
                          const gpv_grid_spec *spec, uint8_t *h_level1_inout,
                          int32_t *h_level1_prefix, int32_t *h_boundary_index, uint8_t *h_level2_inout,

@@ -127,16 +127,17 @@ def test_to_host_level1_only(ctx):
     ctx.release(res)
 
 
-@pytest.mark.parametrize("mask", [0xff, 0x0f, 0x55, 0x80])
-def test_packed_transfer_equals_plain_torus262k(ctx, mask):
+@pytest.mark.parametrize("mask,share", [(0xff, 100), (0x0f, 100), (0x55, 100), (0x80, 100),
+                                        (0xff, 50), (0xff, 1), (0x3c, 37)])
+def test_packed_transfer_equals_plain_torus262k(ctx, mask, share):
     """The packed Level2 transfer (2-bit codes expanded by host threads) gives the bytes the
-    kernel writes directly, whichever slabs send codes; the size threshold is lowered so that
-    this 56 MB output takes it."""
+    kernel writes directly, whichever slabs and whichever share of their voxels send codes; the
+    size threshold is lowered so that this 56 MB output takes it."""
     tris, spec = W.make(W.C2)
     plain = ctx.voxelize_host(tris, spec)
     p = ctx.fetch(plain)
     ctx.release(plain)
-    ctx.set_host_expand(-1, mask, 0)
+    ctx.set_host_expand(-1, mask, share=share, min_level2_bytes=0)
     try:
         rc, res, l1, pre, bi, l2 = _to_host(ctx, tris, spec, 0)
     finally:
@@ -157,8 +158,8 @@ def test_packed_transfer_star1310k_and_threads(ctx):
     p = ctx.fetch(plain)
     ctx.release(plain)
     try:
-        for threads, mask in ((-1, 0xff), (3, 0x3f), (0, 0xff)):
-            ctx.set_host_expand(threads, mask)
+        for threads, mask, share in ((-1, 0xff, 100), (3, 0x3f, 60), (-1, 0xff, 50), (0, 0xff, 100)):
+            ctx.set_host_expand(threads, mask, share=share)
             rc, res, l1, pre, bi, l2 = _to_host(ctx, tris, spec, 0)
             assert rc == 0
             ctx.release(res)
