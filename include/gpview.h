@@ -120,7 +120,7 @@ void gpv_destroy(gpv_ctx *ctx);
 const char *gpv_last_error(gpv_ctx *ctx);
 /* Tunables (autotuner output): triangles per Level1 tile (32..256, power of two; 0, the default,
  * picks per call the largest tile that still gives every SM three tiles) and the largest number
- * of boundary voxels of one Level1 column that one Level2 work item takes (1..32). */
+ * of boundary voxels of one Level1 column that one Level2 work item takes (1..32, default 16). */
 int gpv_set_tile(gpv_ctx *ctx, int tris_per_tile);
 int gpv_set_level2_chunk(gpv_ctx *ctx, int max_voxels);
 /* Organisation of the Level2 kernel's SAT stage (results are identical; only speed differs):
