@@ -167,7 +167,7 @@ int gpv_init(int device, gpv_ctx **out) {
     uint64_t thr = UINT64_MAX;
     cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
   }
-  if (ctx_ensure_host(ctx, 16) != cudaSuccess || cudaMallocHost(&ctx->h_u32, 64) != cudaSuccess) {
+  if (ctx_ensure_host(ctx, 16) != cudaSuccess || cudaMallocHost(&ctx->h_u32, 256) != cudaSuccess) {
     delete ctx;
     return GPV_ERR_CUDA;
   }

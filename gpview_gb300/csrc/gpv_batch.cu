@@ -282,7 +282,7 @@ int run_batch(gpv_ctx *ctx, int n, const float *const *d_tris, const int64_t *T,
   CK(ws.get(&stmp, (size_t)scan_temp_words(swords)));
   // the boundary-voxel total: past the boundary plane's words in the prefix when both are scanned
   const uint32_t *btot = kmark ? wpre + words : wtot;
-  CK(ws.get(&queue, 16));  // [0] Level1 tickets, [1 + k] Level2 tickets of slab k
+  CK(ws.get(&queue, 1 + kMaxSlabs));  // [0] Level1 tickets, [1 + k] Level2 tickets of slab k
   // z slabs of the Level2 launch when the outputs go to the host (one mesh): the boundary ranks
   // at up to kMaxSlabs fine slab starts are read with the first phase's counts; the launch then
   // groups fine slabs into as many slabs as the Level2 output size calls for
@@ -292,7 +292,7 @@ int run_batch(gpv_ctx *ctx, int n, const float *const *d_tris, const int64_t *T,
     fslab = std::min(kMaxSlabs, gh[0].n[2]);
     fz = (gh[0].n[2] + fslab - 1) / fslab;
     fslab = (gh[0].n[2] + fz - 1) / fz;
-    CK(ws.get(&d_slab, 16));
+    CK(ws.get(&d_slab, kMaxSlabs + 1));
   }
   CK(ws.get(&stats, (size_t)n));
   CK(ws.get(&d_md, (size_t)n));
@@ -605,7 +605,7 @@ int run_batch(gpv_ctx *ctx, int n, const float *const *d_tris, const int64_t *T,
     int want = sink->nslab > 0 ? sink->nslab
                : packed        ? kMaxSlabs
                : l2_direct     ? 1
-                               : (int)std::min<int64_t>(kMaxSlabs, l2bytes / (12ll << 20));
+                               : (int)std::min<int64_t>(kCopySlabs, l2bytes / (12ll << 20));
     want = std::max(1, std::min(want, fslab));
     const int gsz = (fslab + want - 1) / want;
     zslab = gsz * fz;

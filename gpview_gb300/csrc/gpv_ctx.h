@@ -12,7 +12,8 @@
 
 namespace gpv {
 
-constexpr int kMaxSlabs = 8;  // z slabs of gpv_voxelize_to_host's Level2 launch, at most
+constexpr int kMaxSlabs = kSlabsMax;  // z slabs of gpv_voxelize_to_host's Level2 launch, at most
+constexpr int kCopySlabs = 8;         // ... when its slabs are copied (pageable or slab outputs)
 
 // Result arrays of one batch; every result of the batch holds a reference.
 struct ResultSet {

@@ -85,6 +85,11 @@ struct MeshDesc {
 // shim, whose ClassifyTessellation marks boundary voxels and records their triangles.
 constexpr int kFillNone = -1;
 
+// z slabs of one Level2 launch sequence, at most (gpv_voxelize_to_host).  16 measured slower
+// than 8 for the packed host transfer (star1310k host to host 6.58 against 6.43 ms): each slab
+// launch adds its ramp and tail
+constexpr int kSlabsMax = 8;
+
 struct BatchDev {
   const MeshDesc *md;
   int nmesh;
@@ -104,7 +109,7 @@ struct BatchDev {
   int fail_wait = 0;
   // packed Level2 host output: in z slab k of the Level2 launch, the boundary voxels whose output
   // index is below pk_end[k] write MeshDesc::l2codes instead of bytes (the slab's first share)
-  uint32_t pk_end[8] = {};
+  uint32_t pk_end[kSlabsMax] = {};
 };
 
 // Small copies and clears around a phase, done by one kernel instead of copy-engine and memset

@@ -1111,7 +1111,7 @@ bool level2_queue_pays(const MeshStats *stats, const bool *has_l2, int n) {
 
 size_t level2_smem_bytes(int warp_words) { return (size_t)warp_words * 4 * kWarps; }
 
-int64_t level2_temp_words(int64_t B) { return 7 * B + 32 + scan_temp_words(B); }
+int64_t level2_temp_words(int64_t B) { return 7 * B + 8 + 2 * (kSlabsMax + 4) + scan_temp_words(B); }
 
 // Builds the chunk items from the sorted pair lists and runs the persistent Level2 kernel.
 void launch_level2(const BatchDev &bd, const uint32_t *keys, const uint32_t *vals,
@@ -1122,7 +1122,7 @@ void launch_level2(const BatchDev &bd, const uint32_t *keys, const uint32_t *val
   if (B <= 0) return;
   uint32_t *cflag = tmp, *cord = cflag + B, *colhead = cord + B, *iflag = colhead + B + 1,
            *iord = iflag + B, *istart = iord + B, *nitems = istart + B + 1,
-           *slabcnt = nitems + 4, *ioff = slabcnt + 12, *ilist = ioff + 12,
+           *slabcnt = nitems + 4, *ioff = slabcnt + (kSlabsMax + 4), *ilist = ioff + (kSlabsMax + 4),
            *stmp = ilist + B;
   if (nslab <= 1) zslab = 0;
   const unsigned nb = (unsigned)((B + 255) / 256);
@@ -1155,7 +1155,7 @@ void launch_level2(const BatchDev &bd, const uint32_t *keys, const uint32_t *val
   const int nz = slab_nz;
   if (zslab > 0) {
     // single mesh: order the items by slab so that each launch takes only its own
-    cudaMemsetAsync(slabcnt, 0, 12 * sizeof(uint32_t), s);
+    cudaMemsetAsync(slabcnt, 0, (kSlabsMax + 4) * sizeof(uint32_t), s);
     k_item_slab_count<<<nb, 256, 0, s>>>(istart, nitems, keys, useg, nz, zslab, slabcnt);
     k_item_slab_offsets<<<1, 32, 0, s>>>(slabcnt, nslab, ioff);
     k_item_slab_place<<<nb, 256, 0, s>>>(istart, nitems, keys, useg, nz, zslab, slabcnt, ilist);
