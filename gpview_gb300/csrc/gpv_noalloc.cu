@@ -13,9 +13,9 @@
 //   * Host code cannot use the array's name as a device address.  Every call looks the address
 //     up with cudaGetSymbolAddress while the caller's device is current and checks the result
 //     (a lookup costs far less than the call's own stream synchronisation, and it stays right
-//     after a device reset, which loads the module -- and the array -- again).  The first call
-//     on a device also loads this library's device code there; make that first call before any
-//     stream capture.
+//     after a device reset, which loads the module -- and the array -- again).
+//   * A call copies its tables from host memory and waits for its stream, so it cannot be
+//     recorded into a graph: a call on a stream that is capturing is refused.
 //   * All calls share the one array, which keeps the previous call's contents.  Each call clears
 //     the regions that must start at zero.  Calls whose GPU work overlaps -- on different
 //     streams or host threads -- race on the array; serialise them.
@@ -119,6 +119,14 @@ extern "C" int gpv_voxelize_level1_noalloc(const float *d_tris, int64_t num_tria
   if (num_triangles > 0 && (reinterpret_cast<uintptr_t>(d_tris) & 15u)) {
     set_err("triangle buffer must be 16-byte aligned");
     return GPV_ERR_INVALID;
+  }
+  {
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(stream, &cap) != cudaSuccess || cap != cudaStreamCaptureStatusNone) {
+      cudaGetLastError();
+      set_err("stream is capturing (the call copies from host memory and waits for the stream)");
+      return GPV_ERR_INVALID;
+    }
   }
   if (num_triangles > (int64_t)(kScratchBytes / kBytesPerTriangle)) {
     char msg[160];

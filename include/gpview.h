@@ -289,8 +289,8 @@ int gpv_voxelize_batch(gpv_ctx *ctx, int32_t n, const float *const *d_tris,
  * exit; inputs whose intermediates do not fit (about 400k triangles at most, fewer on large
  * grids) are rejected with GPV_ERR_INVALID and a reason in gpv_noalloc_last_error() (per host
  * thread).  Every call looks up the array's device address (cudaGetSymbolAddress) with the
- * caller's device current; the first call on a device also loads the library's device code
- * there, so make that first call before any stream capture.  Calls share the array and clear
+ * caller's device current.  A call copies its tables from host memory and waits for `stream`,
+ * so it is refused (GPV_ERR_INVALID) on a stream that is capturing.  Calls share the array and clear
  * what must start at zero themselves; calls whose GPU work overlaps race on it and must be
  * serialised. */
 int gpv_voxelize_level1_noalloc(const float *d_tris, int64_t num_triangles,

@@ -82,3 +82,33 @@ def test_noalloc_rejects_oversize(built):
                                        C.byref(nb), None)
     assert rc == -1
     assert b"scratch" in L.gpv_noalloc_last_error()
+
+
+def test_noalloc_refuses_a_capturing_stream(built):
+    """A call copies its tables from host memory and waits for its stream, so it cannot be
+    recorded into a graph: on a capturing stream it is refused before any work is enqueued, and
+    the caller's capture stays usable."""
+    torch = pytest.importorskip("torch")
+    gpv = built
+    L = gpv.lib()
+    tris, spec = W.make(W.C1)
+    n1 = int(np.prod(list(spec.ndiv)))
+    d_tris = torch.from_numpy(np.ascontiguousarray(tris, np.float32)).cuda()
+    l1 = torch.empty((n1,), dtype=torch.uint8, device="cuda")
+    pre = torch.empty((n1,), dtype=torch.int32, device="cuda")
+    bi = torch.empty((n1,), dtype=torch.int32, device="cuda")
+    nb = C.c_int64(-1)
+    x = torch.zeros(4, device="cuda")
+    s = torch.cuda.Stream()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g, stream=s):
+        rc = L.gpv_voxelize_level1_noalloc(C.c_void_p(d_tris.data_ptr()), tris.size // 9, C.byref(spec),
+                                           C.c_void_p(l1.data_ptr()), C.c_void_p(pre.data_ptr()),
+                                           C.c_void_p(bi.data_ptr()), C.byref(nb),
+                                           C.c_void_p(s.cuda_stream))
+        x.add_(1.0)  # the capture goes on
+    g.replay()
+    torch.cuda.synchronize()
+    assert rc == -1
+    assert b"capturing" in L.gpv_noalloc_last_error()
+    assert x.tolist() == [1.0, 1.0, 1.0, 1.0]
