@@ -166,3 +166,25 @@ def test_graph_replay_with_other_mesh_data(ctx):
         refs.append((res.num_pairs, res.num_boundary))
         ctx.release(res)
     assert refs[0] == refs[1] == refs[2]  # identical sizes: the graphs were replayed
+
+
+@pytest.mark.parametrize("n,n2", [(16, (32, 32, 32)), (20, (32, 32, 1)), (20, (1, 1, 32)),
+                                  (24, (1, 1, 1)), (18, (31, 7, 17))])
+def test_extreme_level2_shapes(ctx, n, n2):
+    """The largest Level2 grid the API admits (32^3: one boundary voxel per work item, n2z = 32
+    columns filling whole mask words), flat and needle-shaped sub-grids, a single sub-cell and odd
+    divisions, each against the oracle byte for byte."""
+    import gpview_gb300 as gpv
+
+    tris = gpv.gen_uvsphere(21, 40, 20, (0.5, 0.5, 0.5), 0.4, 0.002)
+    _check_full(ctx, tris, _pad_spec(tris, n, n2))
+
+
+def test_large_level1_grid(ctx):
+    """A 1536 x 1536 x 32 Level1 grid (75.5 M voxels, 24 words per bit-plane row) around a small
+    torus: the bit planes, the column-major pair keys, the boundary scan and the prefix sums at
+    large N1, against the oracle."""
+    import gpview_gb300 as gpv
+
+    tris = gpv.gen_torus(13, 96, 48, (0.5, 0.5, 0.5), 0.35, 0.12, 0.01)
+    _check_full(ctx, tris, _pad_spec(tris, (1536, 1536, 32), (2, 2, 2)))
