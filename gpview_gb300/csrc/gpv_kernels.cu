@@ -307,6 +307,7 @@ __global__ void __launch_bounds__(kL1Threads) k_level1(BatchDev bd) {
   __shared__ uint32_t s_foff[TILE + 1];
   __shared__ uint32_t s_q[kL1Warps][32];
   __shared__ uint32_t s_ws[kL1Warps], s_wf[kL1Warps];
+  __shared__ uint32_t s_next;  // next 32-unit chunk of the tile (SAT chunks, then fill chunks)
   __shared__ __align__(8) uint64_t s_bar;
   __shared__ int64_t s_item;
 
@@ -376,14 +377,26 @@ __global__ void __launch_bounds__(kL1Threads) k_level1(BatchDev bd) {
         s_soff[TILE] = bs + is;
         s_foff[TILE] = bf + iff;
       }
+      if (threadIdx.x == 0) s_next = 0;
       __syncthreads();
     }
     const uint32_t Us = s_soff[TILE], Uf = s_foff[TILE];
     const int nx = g.n[0], ny = g.n[1], nz = g.n[2];
     const uint64_t cap = (uint64_t)d.pair_cap;
 
+    // Warps take 32-unit chunks from a counter, the SAT chunks first and then the fill chunks,
+    // so that a warp whose z runs or hits were short takes more chunks instead of waiting at the
+    // tile's closing barrier for the others.
+    const uint32_t nsc = (Us + 31u) >> 5;
+    auto next_chunk = [&]() {
+      uint32_t c = 0;
+      if (lane == 0) c = atomicAdd(&s_next, 1u);
+      return __shfl_sync(FULL, c, 0);
+    };
+    uint32_t chunk = next_chunk();
     // ---- (a) SAT units
-    for (uint32_t base = warp * 32u; base < Us; base += kL1Warps * 32u) {
+    for (; chunk < nsc; chunk = next_chunk()) {
+      const uint32_t base = chunk * 32u;
       const uint32_t u = base + lane;
       int lt = 0, p = 0, q = 0, z0 = 0, zc = -1;
       float V[9];
@@ -440,7 +453,8 @@ __global__ void __launch_bounds__(kL1Threads) k_level1(BatchDev bd) {
     }
 
     // ---- (b) fill units
-    for (uint32_t base = warp * 32u; base < Uf; base += kL1Warps * 32u) {
+    for (; (chunk - nsc) * 32u < Uf; chunk = next_chunk()) {
+      const uint32_t base = (chunk - nsc) * 32u;
       const uint32_t u = base + lane;
       bool pass = false;
       if (u < Uf) {
