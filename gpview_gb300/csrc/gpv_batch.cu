@@ -218,7 +218,7 @@ int run_batch(gpv_ctx *ctx, int n, const float *const *d_tris, const int64_t *T,
   std::vector<int64_t> tab_off(n + 1, 0), res_l1(n + 1, 0), res_pre(n + 1, 0), res_l1n(n + 1, 0),
       res_hier(n + 1, 0);
   std::vector<MeshDesc> md(n);
-  int64_t tris = 0, tiles = 0, fwarps = 0, rows = 0, words = 0, togg = 0, stgw = 0;
+  int64_t tris = 0, tiles = 0, fwarps = 0, rows = 0, xchunks = 0, words = 0, togg = 0, stgw = 0;
   int max_keybits = 1, warp_words = 0;
   int64_t max_T = 1;
   bool any_l2 = false;
@@ -231,11 +231,13 @@ int run_batch(gpv_ctx *ctx, int n, const float *const *d_tris, const int64_t *T,
     d.tile_base = tiles;
     d.fwarp_base = fwarps;
     d.row_base = rows;
+    d.xc_base = xchunks;
     d.word_base = words;
     tris += T[m];
     tiles += (T[m] + tile - 1) / tile;
     fwarps += (int64_t)g.n[1] * g.nxw * g.nzw;
     rows += (int64_t)g.n[2] * g.n[1];
+    xchunks += ((int64_t)g.n[0] * g.n[1] * g.n[2] + 127) / 128;
     words += (int64_t)g.n[2] * g.n[1] * g.nxw;
     togg += (int64_t)g.n[0] * g.n[1] * g.nzw;
     if (stencil) stgw += 4 * (int64_t)g.n[0] * g.n[1] * g.nzw;
@@ -348,6 +350,7 @@ int run_batch(gpv_ctx *ctx, int n, const float *const *d_tris, const int64_t *T,
   bd.total_tiles = tiles;
   bd.total_fwarps = fwarps;
   bd.total_rows = rows;
+  bd.total_xchunks = xchunks;
   bd.total_words = words;
   bd.queue = queue;
   bd.normals = nmode;
@@ -395,7 +398,7 @@ int run_batch(gpv_ctx *ctx, int n, const float *const *d_tris, const int64_t *T,
   auto bd_sig = [&](std::vector<uint64_t> &v) {
     for (uint64_t x : {(uint64_t)(uintptr_t)bd.md, (uint64_t)bd.nmesh, (uint64_t)bd.tile,
                        (uint64_t)bd.total_tris, (uint64_t)bd.total_tiles, (uint64_t)bd.total_fwarps,
-                       (uint64_t)bd.total_rows, (uint64_t)bd.total_words,
+                       (uint64_t)bd.total_rows, (uint64_t)bd.total_words, (uint64_t)bd.total_xchunks,
                        (uint64_t)(uintptr_t)bd.queue, (uint64_t)bd.normals, (uint64_t)bd.fill,
                        (uint64_t)(uintptr_t)bd.stp, (uint64_t)bd.stp_words,
                        (uint64_t)ctx->timing, (uint64_t)ctx->num_sms, (uint64_t)bd.wait_limit,

@@ -65,6 +65,7 @@ struct MeshDesc {
   int64_t tile_base;     // ... of Level1 tiles
   int64_t fwarp_base;    // ... of fill-finish warps (ny * nxw * nzw)
   int64_t row_base;      // ... of Level1 rows (nz * ny)
+  int64_t xc_base;       // ... of 128-voxel expansion chunks (ceil(N1 / 128))
   int64_t word_base;     // ... of bit-plane words (nz * ny * nxw)
   int64_t emit_base;     // ... of pair capacities (emission segments)
   int64_t pair_base;     // ... of pairs (dense layout after the sort)
@@ -95,6 +96,7 @@ struct BatchDev {
   int nmesh;
   int tile;              // Level1 triangles per tile (32, 64, 128, 256)
   int64_t total_tris, total_tiles, total_fwarps, total_rows, total_words;
+  int64_t total_xchunks;  // 128-voxel expansion chunks of all meshes
   uint32_t *queue;       // work-queue tickets, zeroed before each persistent launch
   int normals;           // GPV_NORMALS_* of this batch
   int fill;              // GPV_FILL_* of this batch

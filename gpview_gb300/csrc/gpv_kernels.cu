@@ -593,87 +593,125 @@ __global__ void k_boundary_counts(BatchDev bd, const uint32_t *__restrict__ wpre
   bd.md[m].stats->boundary = e - s;
 }
 
-// One warp per (mesh, Level1 row (k, j)), kExpandWarps rows per block: state bytes,
-// boundaryPrefixSum, boundaryIndex.
+// One warp per chunk of 128 consecutive voxels of one mesh's linear index (x fastest),
+// kExpandWarps chunks per block: state bytes, boundaryPrefixSum, boundaryIndex.  Every lane of a
+// chunk works whatever the row length (a warp per row left three quarters of the lanes idle on a
+// 32-voxel row), and a block whose chunks lie in one mesh looks the mesh up once.
 constexpr int kExpandWarps = 8;
-// One row by one warp; returns the lane's inside-voxel count and the row's mesh statistics.
-__device__ __forceinline__ unsigned long long expand_row(const BatchDev &bd,
-                                                         const uint32_t *__restrict__ wpre,
-                                                         int64_t grow, unsigned lane,
-                                                         MeshStats *&st) {
-  const int m = find_mesh<&MeshDesc::row_base>(bd.md, bd.nmesh, grow);
+constexpr int kExpandVox = 128;
+// One chunk by one warp; returns the lane's inside-voxel count and the chunk's mesh statistics.
+__device__ __forceinline__ unsigned long long expand_chunk(const BatchDev &bd,
+                                                           const uint32_t *__restrict__ wpre, int m,
+                                                           int64_t gc, unsigned lane,
+                                                           MeshStats *&st) {
   const MeshDesc &d = bd.md[m];
   const GridDev &g = d.g;
-  const int64_t row = grow - d.row_base;
+  st = d.stats;
+  const int nx = g.n[0];
+  const int64_t N1 = (int64_t)nx * g.n[1] * g.n[2];
+  const int64_t v0 = (gc - d.xc_base) * kExpandVox + (int64_t)lane * 4;
+  if (v0 >= N1) return 0;
   const uint32_t pbase = wpre[d.word_base];
   const uint32_t *bplane = d.bplane, *iplane = d.iplane;
   const uint32_t *wp = wpre + d.word_base;
-  const int nx = g.n[0];
-  const bool vec = (nx & 3) == 0;
   unsigned long long nin = 0;
-  for (int x4 = (int)lane * 4; x4 < nx; x4 += 128) {
+  // (the 4- and 16-byte stores need aligned outputs: the batch's arenas are, a no-alloc caller's
+  // buffers may not be)
+  if ((nx & 3) == 0 && (reinterpret_cast<uintptr_t>(d.l1) & 3u) == 0 &&
+      (reinterpret_cast<uintptr_t>(d.prefix) & 15u) == 0) {
+    // the lane's four voxels share a row and a plane word (nx and v0 are multiples of 4), and
+    // N1 is a multiple of 4 too
+    const int64_t row = v0 / nx;
+    const int x0 = (int)(v0 - row * nx);
+    const size_t w = (size_t)row * g.nxw + (x0 >> 5);
+    const int b0 = x0 & 31;
+    const uint32_t bw = bplane[w], iw = iplane[w];
+    uint32_t p = wp[w] - pbase + __popc(bw & ((1u << b0) - 1u));
     uint32_t bytes = 0;
     int32_t pre[4];
 #pragma unroll
     for (int e = 0; e < 4; ++e) {
-      const int x = x4 + e;
-      pre[e] = 0;
-      if (x >= nx) break;
+      const bool isb = (bw >> (b0 + e)) & 1u, isi = (iw >> (b0 + e)) & 1u;
+      pre[e] = (int32_t)p;
+      if (isb) {
+        d.bindex[p] = (int32_t)(v0 + e);
+        ++p;
+      }
+      nin += (!isb && isi);
+      bytes |= (isb ? 254u : (isi ? 127u : 0u)) << (8 * e);
+    }
+    *reinterpret_cast<uint32_t *>(d.l1 + v0) = bytes;
+    *reinterpret_cast<int4 *>(d.prefix + v0) = make_int4(pre[0], pre[1], pre[2], pre[3]);
+  } else {
+    for (int e = 0; e < 4; ++e) {
+      const int64_t v = v0 + e;
+      if (v >= N1) break;
+      const int64_t row = v / nx;
+      const int x = (int)(v - row * nx);
       const size_t w = (size_t)row * g.nxw + (x >> 5);
       const int bit = x & 31;
       const uint32_t bw = bplane[w], iw = iplane[w];
       const uint32_t p = wp[w] - pbase + __popc(bw & ((1u << bit) - 1u));
       const bool isb = (bw >> bit) & 1u, isi = (iw >> bit) & 1u;
-      const uint32_t s = isb ? 254u : (isi ? 127u : 0u);
       nin += (!isb && isi);
-      pre[e] = (int32_t)p;
-      const int64_t v = row * nx + x;
       if (isb) d.bindex[p] = (int32_t)v;
-      if (!vec) {
-        d.l1[v] = (uint8_t)s;
-        d.prefix[v] = (int32_t)p;
-      }
-      bytes |= s << (8 * e);
-    }
-    if (vec) {
-      const int64_t v = row * nx + x4;
-      *reinterpret_cast<uint32_t *>(d.l1 + v) = bytes;
-      *reinterpret_cast<int4 *>(d.prefix + v) = make_int4(pre[0], pre[1], pre[2], pre[3]);
+      d.l1[v] = (uint8_t)(isb ? 254u : (isi ? 127u : 0u));
+      d.prefix[v] = (int32_t)p;
     }
   }
-  st = d.stats;
   return nin;
 }
 
-// The inside counts of the block's rows go to the statistics with one atomic per mesh run of
-// rows rather than one per row (all rows of a mesh add to one counter).
+// A block takes `iters` x kExpandWarps consecutive chunks; warp w the chunks c0 + w + k x
+// kExpandWarps.  Thread 0 looks up the mesh of the block's first chunk once (a binary search over
+// the descriptors), and each warp walks forward from it as its chunks pass mesh boundaries, so
+// the search is not repeated per chunk.  A warp adds its inside count to the statistics when it
+// leaves a mesh; the block adds the warps' last runs with one atomic per mesh.
 __global__ void __launch_bounds__(kExpandWarps * 32) k_expand(BatchDev bd,
-                                                            const uint32_t *__restrict__ wpre) {
+                                                            const uint32_t *__restrict__ wpre,
+                                                            int iters) {
+  __shared__ int s_mesh;
+  __shared__ int s_m[kExpandWarps];
   __shared__ unsigned long long s_nin[kExpandWarps];
-  __shared__ MeshStats *s_st[kExpandWarps];
   const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
-  const int64_t grow = (int64_t)blockIdx.x * kExpandWarps + warp;
-  MeshStats *st = nullptr;
+  const int64_t c0 = (int64_t)blockIdx.x * kExpandWarps * iters;
+  if (threadIdx.x == 0) s_mesh = find_mesh<&MeshDesc::xc_base>(bd.md, bd.nmesh, c0);
+  __syncthreads();
+  int m = s_mesh;
   unsigned long long nin = 0;
-  if (grow < bd.total_rows) nin = expand_row(bd, wpre, grow, lane, st);  // warp-uniform
-  nin = warp_sum(nin);
+  for (int k = 0; k < iters; ++k) {
+    const int64_t gc = c0 + (int64_t)k * kExpandWarps + warp;
+    if (gc >= bd.total_xchunks) break;  // warp-uniform
+    int mn = m;
+    while (mn + 1 < bd.nmesh && bd.md[mn + 1].xc_base <= gc) ++mn;
+    if (mn != m) {
+      const unsigned long long t = warp_sum(nin);
+      if (lane == 0 && t) atomicAdd(&bd.md[m].stats->l1_inside, t);
+      nin = 0;
+      m = mn;
+    }
+    MeshStats *st = nullptr;
+    nin += expand_chunk(bd, wpre, m, gc, lane, st);
+  }
+  // the warps' last mesh runs: one atomic per mesh of the block
+  const unsigned long long t = warp_sum(nin);
   if (lane == 0) {
-    s_nin[warp] = nin;
-    s_st[warp] = st;
+    s_m[warp] = m;
+    s_nin[warp] = t;
   }
   __syncthreads();
   if (threadIdx.x == 0) {
-    MeshStats *cur = nullptr;
+    int cur = s_m[0];
     unsigned long long acc = 0;
     for (int w = 0; w < kExpandWarps; ++w) {
-      if (s_st[w] != cur) {
-        if (cur && acc) atomicAdd(&cur->l1_inside, acc);
-        cur = s_st[w];
+      if (s_m[w] != cur) {
+        if (acc) atomicAdd(&bd.md[cur].stats->l1_inside, acc);
+        cur = s_m[w];
         acc = 0;
       }
       acc += s_nin[w];
     }
-    if (cur && acc) atomicAdd(&cur->l1_inside, acc);
+    if (acc) atomicAdd(&bd.md[cur].stats->l1_inside, acc);
   }
 }
 
@@ -814,9 +852,14 @@ void launch_boundary_counts(const BatchDev &bd, const uint32_t *wpre, const uint
 }
 
 void launch_expand(const BatchDev &bd, const uint32_t *wpre, cudaStream_t s) {
-  if (bd.total_rows <= 0) return;
-  k_expand<<<(unsigned)((bd.total_rows + kExpandWarps - 1) / kExpandWarps), kExpandWarps * 32, 0,
-             s>>>(bd, wpre);
+  if (bd.total_xchunks <= 0) return;
+  // up to 8 chunks per warp where the chunks are many enough to give each of the 152 SMs 64
+  // warps anyway
+  const int64_t spread = bd.total_xchunks / (152 * 64);
+  const int iters = (int)(spread < 1 ? 1 : spread > 8 ? 8 : spread);
+  const int64_t per_block = (int64_t)kExpandWarps * iters;
+  k_expand<<<(unsigned)((bd.total_xchunks + per_block - 1) / per_block), kExpandWarps * 32, 0, s>>>(
+      bd, wpre, iters);
   count_launch();
 }
 

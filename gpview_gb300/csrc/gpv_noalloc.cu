@@ -255,6 +255,7 @@ extern "C" int gpv_voxelize_level1_noalloc(const float *d_tris, int64_t num_tria
   bd.total_tris = T;
   bd.total_fwarps = (int64_t)g.n[1] * g.nxw * g.nzw;
   bd.total_rows = (int64_t)g.n[2] * g.n[1];
+  bd.total_xchunks = (N1 + 127) / 128;
   bd.total_words = N1w;
 
   // The array keeps the last call's data: clear everything that must start at zero.  The

@@ -112,3 +112,29 @@ def test_noalloc_refuses_a_capturing_stream(built):
     assert rc == -1
     assert b"capturing" in L.gpv_noalloc_last_error()
     assert x.tolist() == [1.0, 1.0, 1.0, 1.0]
+
+
+def test_noalloc_unaligned_outputs(built):
+    """Output buffers off the 4- and 16-byte boundaries (a caller's sub-array) take the per-voxel
+    stores of the expansion and give the same outputs."""
+    torch = pytest.importorskip("torch")
+    gpv = built
+    L = gpv.lib()
+    tris, spec = W.make(W.C1)
+    n1 = int(np.prod(list(spec.ndiv)))
+    ref = orc.Run(tris, spec, fill=orc.FILL_CAND)
+    d_tris = torch.from_numpy(np.ascontiguousarray(tris, np.float32)).cuda()
+    l1 = torch.zeros((n1 + 16,), dtype=torch.uint8, device="cuda")
+    pre = torch.zeros((n1 + 4,), dtype=torch.int32, device="cuda")
+    bi = torch.zeros((n1 + 4,), dtype=torch.int32, device="cuda")
+    nb = C.c_int64(-1)
+    stream = torch.cuda.current_stream().cuda_stream
+    rc = L.gpv_voxelize_level1_noalloc(C.c_void_p(d_tris.data_ptr()), tris.size // 9, C.byref(spec),
+                                       C.c_void_p(l1.data_ptr() + 1), C.c_void_p(pre.data_ptr() + 4),
+                                       C.c_void_p(bi.data_ptr() + 4), C.byref(nb), C.c_void_p(stream))
+    assert rc == 0, L.gpv_noalloc_last_error()
+    torch.cuda.synchronize()
+    assert nb.value == ref.B
+    np.testing.assert_array_equal(l1.cpu().numpy()[1:1 + n1], ref.level1_bytes())
+    np.testing.assert_array_equal(pre.cpu().numpy()[1:1 + n1], ref.prefix())
+    np.testing.assert_array_equal(bi.cpu().numpy()[1:1 + nb.value], ref.boundary_index())
