@@ -293,19 +293,30 @@ def batch_bench(gpv, ctx, torch, stream, local, args):
         torch.cuda.synchronize()
         plain_s = time.perf_counter() - tp
         progress(f"plain loop {plain_s:.2f} s")
-        # batched path
-        times = []
-        for k in range(args.batch_reps + 1):
-            torch.cuda.synchronize()
-            tb = time.perf_counter()
-            res = ctx.voxelize_batch(ptrs, counts, specs, sp)
-            torch.cuda.synchronize()
-            dt = time.perf_counter() - tb
-            bwork = sum(r.work.total() for r in res)
-            for r in res:
-                ctx.release(r)
-            if k > 0:
-                times.append(dt)
+        # batched path: the first call runs as two graphs and records the sizes; the repeated
+        # calls are one graph each (and the same calls as two graphs, for comparison)
+        def batched_calls():
+            ts, w = [], 0
+            for k in range(args.batch_reps + 1):
+                torch.cuda.synchronize()
+                tb = time.perf_counter()
+                res = ctx.voxelize_batch(ptrs, counts, specs, sp)
+                torch.cuda.synchronize()
+                dt = time.perf_counter() - tb
+                w = sum(r.work.total() for r in res)
+                for r in res:
+                    ctx.release(r)
+                if k > 0:
+                    ts.append(dt)
+            return ts, w
+
+        og0 = ctx.get_debug("one_graph_calls")
+        times, bwork = batched_calls()
+        og_calls = ctx.get_debug("one_graph_calls") - og0
+        ctx.set_graphs(ctx.GRAPHS_TWO)
+        times2, bwork2 = batched_calls()
+        ctx.set_graphs(True)
+        assert bwork2 == bwork, (bwork2, bwork)
         # one more call with host timing on: where the host time of a batch call goes
         ctx.set_timing(True)
         for r in ctx.voxelize_batch(ptrs, counts, specs, sp):
@@ -320,6 +331,9 @@ def batch_bench(gpv, ctx, torch, stream, local, args):
             "desc": "sphere/noisy torus/superellipsoid, T log-uniform 500-200000, Level1 {32..128}^3, Level2 {2,4,8}^3",
             "tile": tile, "level2_chunk": chunk, "autotune_sample_ms": tune_ms,
             "plain_meshes_per_s": n / plain_s, "batched_meshes_per_s": n / batch_s,
+            "batched_graphs": f"one CUDA graph per call ({og_calls} of {args.batch_reps + 1} calls; "
+                              "the first records the sizes as two graphs)",
+            "batched_two_graph_meshes_per_s": n / (sum(times2) / len(times2)),
             "batched_vs_plain": plain_s / batch_s, "batched_tests_per_s": work / batch_s,
             "plain_s": plain_s, "batched_s": batch_s, "generate_s": gen_s,
             "batched_host_ms_per_call": {k: v / max(hcalls, 1) for k, v in host_ms.items()}}

@@ -295,8 +295,13 @@ class Context:
         calls = lib().gpv_host_times(self._h, ms, 5)
         return calls, {k: ms[i] for i, k in enumerate(self.HOST_SEGMENTS)}
 
-    def set_graphs(self, on=True):
-        self._check(lib().gpv_set_graphs(self._h, int(bool(on))), "set_graphs")
+    GRAPHS_ONE, GRAPHS_TWO = 1, 2
+
+    def set_graphs(self, mode=True):
+        """True / GRAPHS_ONE (default): CUDA graphs, a call repeating the previous call's meshes
+        and grids as one graph; GRAPHS_TWO: two graphs per call; False / 0: direct launches."""
+        m = self.GRAPHS_ONE if mode is True else (0 if mode is False else int(mode))
+        self._check(lib().gpv_set_graphs(self._h, m), "set_graphs")
 
     def set_tile(self, t):
         rc = lib().gpv_set_tile(self._h, int(t))
@@ -319,7 +324,8 @@ class Context:
         self._check(lib().gpv_set_host_expand(self._h, int(threads), int(slab_mask), int(share),
                                               int(min_level2_bytes)), "set_host_expand")
 
-    DEBUG = {"wait_limit": 1, "fail_wait": 2, "pair_capacity": 3, "fail_allocs": 4, "replans": 5}
+    DEBUG = {"wait_limit": 1, "fail_wait": 2, "pair_capacity": 3, "fail_allocs": 4, "replans": 5,
+             "one_graph_capacity": 6, "one_graph_calls": 7, "one_graph_replans": 8}
 
     def set_debug(self, what, value):
         """Failure-detection hooks (gpv_set_debug): 'wait_limit', 'fail_wait', 'pair_capacity',

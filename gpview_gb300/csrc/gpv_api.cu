@@ -247,9 +247,10 @@ int gpv_host_times(gpv_ctx *ctx, double *ms, int n) {
 
 uint64_t gpv_kernel_launches(void) { return gpv::launch_count(); }
 
-int gpv_set_graphs(gpv_ctx *ctx, int on) {
+int gpv_set_graphs(gpv_ctx *ctx, int mode) {
   if (!ctx) return GPV_ERR_INVALID;
-  ctx->graphs = on != 0;
+  ctx->graphs = mode != 0;
+  ctx->one_graph = mode != 0 && mode != GPV_GRAPHS_TWO;
   return GPV_OK;
 }
 
@@ -313,6 +314,7 @@ int gpv_set_debug(gpv_ctx *ctx, int what, int64_t value) {
     case GPV_DEBUG_FAIL_WAIT: ctx->fail_wait = value != 0; return GPV_OK;
     case GPV_DEBUG_PAIR_CAPACITY: ctx->debug_pair_cap = value; return GPV_OK;
     case GPV_DEBUG_FAIL_ALLOCS: ctx->fail_allocs = value; return GPV_OK;
+    case GPV_DEBUG_ONE_GRAPH_CAPACITY: ctx->debug_og_cap = value; return GPV_OK;
     default: return GPV_ERR_INVALID;
   }
 }
@@ -325,6 +327,9 @@ int64_t gpv_get_debug(gpv_ctx *ctx, int what) {
     case GPV_DEBUG_PAIR_CAPACITY: return ctx->debug_pair_cap;
     case GPV_DEBUG_FAIL_ALLOCS: return ctx->fail_allocs;
     case GPV_DEBUG_REPLANS: return ctx->replans;
+    case GPV_DEBUG_ONE_GRAPH_CAPACITY: return ctx->debug_og_cap;
+    case GPV_DEBUG_ONE_GRAPH_CALLS: return ctx->og_calls;
+    case GPV_DEBUG_ONE_GRAPH_REPLANS: return ctx->og_replans;
     default: return GPV_ERR_INVALID;
   }
 }

@@ -11,6 +11,11 @@
 // while its launch arguments repeat; its launch shapes are fixed by the counts read at the phase
 // boundary.  A staging kernel at each end of a phase moves the small per-call data between
 // page-locked host staging and the device.
+// One graph: a call whose meshes and grids repeat the previous call's (device triangles, no
+// normals, ray fill, no hierarchy) records both phases as one graph.  The result arrays and the
+// second phase's launches take that call's sizes as capacities, a planning kernel (k_plan) puts
+// the per-mesh bases and sizes in device memory between the phases, and the second phase's
+// kernels read them; a size above its capacity re-runs the call as two phases.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -99,6 +104,23 @@ cudaError_t grow_slab(gpv_ctx *ctx, cudaStream_t s) {
 }
 
 size_t al16(size_t v) { return (v + 15) & ~size_t(15); }
+
+// Identity of a call's meshes for the one-graph form: the triangle counts and grids (FNV-1a over
+// their bytes).  Equal keys give equal result sizes unless the triangles themselves moved.
+uint64_t call_key(int n, const int64_t *T, const gpv_grid_spec *specs) {
+  uint64_t h = 1469598103934665603ull;
+  auto mix = [&](const void *p, size_t bytes) {
+    const unsigned char *c = static_cast<const unsigned char *>(p);
+    for (size_t i = 0; i < bytes; ++i) h = (h ^ c[i]) * 1099511628211ull;
+  };
+  mix(&n, sizeof(n));
+  mix(T, sizeof(int64_t) * (size_t)n);
+  mix(specs, sizeof(gpv_grid_spec) * (size_t)n);
+  return h;
+}
+
+// Word of the page-locked scratch (gpv_ctx::h_u32) where a one-graph call's DevPlan lands.
+constexpr int kPlanWord = 32;
 
 // Runs `launches` on stream s, recorded as a CUDA graph when the context asks for graphs.  The
 // executable graph of each phase is cached in the context and updated in place when the new
@@ -419,7 +441,9 @@ int run_batch(gpv_ctx *ctx, int n, const float *const *d_tris, const int64_t *T,
                      (uint64_t)(uintptr_t)stats, (uint64_t)(uintptr_t)toggles, (uint64_t)togg,
                      (uint64_t)(uintptr_t)stg, (uint64_t)stgw})
     sig0.push_back(x);
-  CK(run_phase(ctx, 0, s, capturing, [&] {
+  // the first half: prep, pair segments, Level1, fill finish, boundary scan (one-graph calls
+  // also clear the second half's voxel counts, clr_words words, and its completed-voxel counter)
+  auto phase1_launches = [&](uint32_t *clr, int64_t clr_words) {
     // this call's tables and descriptors in (read from page-locked staging), the accumulators
     // cleared: one kernel
     StageList in(ctx->num_sms, s);
@@ -429,6 +453,10 @@ int run_batch(gpv_ctx *ctx, int n, const float *const *d_tris, const int64_t *T,
     in.clear(bplane, swords * 4);
     in.clear(toggles, togg * 4);
     if (stg) in.clear(stg, stgw * 4);
+    if (clr) {
+      in.clear(clr, clr_words * 4);
+      in.clear(wtot + 1, 4);
+    }
     in.launch();
     mark(0);
     launch_prep(bd, s);
@@ -446,6 +474,189 @@ int run_batch(gpv_ctx *ctx, int n, const float *const *d_tris, const int64_t *T,
       launch_slab_offsets(wpre, btot, (int64_t)gh[0].n[1] * gh[0].nxw, gh[0].n[2], fz, fslab,
                           d_slab, s);
     mark(4);
+  };
+  // the ray fill's u/v-passing items queued before their per-voxel work: measured faster with
+  // Level2 grids of up to 8^3 cells (the Level2 kernel on torus262k 0.596 -> 0.550 ms, on a 16k
+  // sphere at 4^3 0.146 -> 0.129 ms, on 512 meshes of the batched workload 36.6 -> 36.0 ms) and
+  // slower at 16^3 (star1310k 3.94 -> 4.21 ms)
+  bool l2_fillq = !stencil && any_l2;
+  for (int m = 0; m < n; ++m)
+    if (gh[m].level2 && gh[m].cells > kFillQueueCells) l2_fillq = false;
+  // per-stage event times of this call (timing on)
+  auto take_stage_times = [&] {
+    if (!ctx->timing) return;
+    // stages: 0 prep, 1 level1, 2 fill finish + boundary scan, 3 expand, 4 sort + lists,
+    // 5 level2 (work items + kernel), 6 the Level2 kernel alone, 7 per-mesh pair bases,
+    // 8 between the halves (counts out, host planning, second launch, uploads in; one-graph
+    // calls: the planning kernel)
+    const int pr[9][2] = {{0, 1}, {2, 3}, {3, 4}, {5, 6}, {6, 7}, {7, 8}, {9, 8}, {1, 2}, {4, 5}};
+    for (int k = 0; k < 9; ++k) {
+      float ms = 0.f;
+      if (cudaEventElapsedTime(&ms, ctx->ev[pr[k][0]], ctx->ev[pr[k][1]]) == cudaSuccess)
+        ctx->stage_ms[k] += ms;
+    }
+    ctx->stage_calls++;
+  };
+  // results: per-mesh slices of the result arrays, given the boundary-index and Level2 offsets
+  auto assemble = [&](const std::vector<int64_t> &boff, const std::vector<int64_t> &l2off) {
+    uint64_t handle;
+    {
+      std::lock_guard<std::mutex> lk(ctx->owned_mu);
+      handle = ctx->next_handle++;
+      set->refs = n;
+      ctx->owned[handle] = set;
+    }
+    for (int m = 0; m < n; ++m) {
+      const MeshStats &st = ctx->h_stats[m];
+      gpv_result &r = out[m];
+      std::memset(&r, 0, sizeof(r));
+      r.spec = specs[m];
+      for (int a = 0; a < 3; ++a) {
+        r.grid_size[a] = gh[m].g[a];
+        r.grid_size2[a] = gh[m].level2 ? gh[m].g2[a] : 0.f;
+      }
+      r.num_level1 = gh[m].N1;
+      r.num_boundary = (int64_t)st.boundary;
+      r.num_level1_inside = (int64_t)st.l1_inside;
+      r.num_level2_inside = (int64_t)st.l2_inside;
+      r.num_level2_boundary = (int64_t)st.l2_boundary;
+      r.num_pairs = (int64_t)st.pairs;
+      r.work.sat1 = (int64_t)st.sat1;
+      r.work.sat2 = gh[m].level2 ? (int64_t)st.pairs * gh[m].cells : 0;
+      r.work.ray1 = (int64_t)st.ray1;
+      r.work.ray2 = (int64_t)st.ray2;
+      r.level1_inout = static_cast<uint8_t *>(set->l1) + res_l1[m];
+      r.level1_prefix = static_cast<int32_t *>(set->prefix) + res_pre[m];
+      r.boundary_index = static_cast<int32_t *>(set->bindex) + boff[m];
+      r.level2_inout = static_cast<uint8_t *>(set->l2) + l2off[m];
+      r.handle = handle;
+      r.normal_mode = nmode;
+      if (res_hier[m + 1] > res_hier[m]) {
+        r.hierarchy = static_cast<gpv_box *>(set->hier) + res_hier[m];
+        r.hierarchy_levels = hierarchy_levels(gh[m].N1);
+      }
+      if (nmode) {
+        r.level1_normal = static_cast<uint8_t *>(set->l1n) + res_l1n[m];
+        r.level2_normal = static_cast<uint8_t *>(set->l2n) + 3 * l2off[m] * nsz;
+      }
+    }
+  };
+  auto take_host_times = [&] {
+    if (!ctx->timing) return;
+    ht[5] = HClock::now();
+    for (int k = 0; k < 5; ++k)
+      ctx->host_ms[k] += std::chrono::duration<double, std::milli>(ht[k + 1] - ht[k]).count();
+  };
+
+  // ---- one graph for the whole call, when the meshes and grids repeat the previous call's
+  const uint64_t key = call_key(n, T, specs);
+  const bool og_path = ctx->graphs && ctx->one_graph && !sink && nmode == 0 && !stencil &&
+                       res_hier[n] == 0;
+  if (og_path && ctx->og_key == key && ctx->og_caps.B > 0) {
+    PlanCaps cap = ctx->og_caps;
+    cap.P = pair_cap;
+    if (ctx->debug_og_cap > 0) {  // failure-detection hook: a boundary capacity that overflows
+      cap.B = ctx->debug_og_cap;
+      ctx->debug_og_cap = 0;
+    }
+    DevPlan *d_plan;
+    uint32_t *kalt = nullptr, *valt = nullptr, *cnt = nullptr, *useg = nullptr, *sortmp = nullptr,
+             *l2tmp = nullptr;
+    CK(ws.get(&d_plan, 1));
+    if (any_l2) {
+      CK(ws.get(&kalt, (size_t)pair_cap));
+      CK(ws.get(&valt, (size_t)pair_cap));
+      CK(ws.get(&cnt, (size_t)cap.U + 1));
+      CK(ws.get(&useg, (size_t)cap.U + 1));
+      CK(ws.get(&sortmp, (size_t)scan_temp_words(cap.U + 1)));
+      CK(ws.get(&l2tmp, (size_t)level2_temp_words(cap.U)));
+    }
+    CK(ctx_malloc_async(ctx, &set->bindex, 4 * std::max<int64_t>(cap.B, 4), s));
+    CK(ctx_malloc_async(ctx, &set->l2, std::max<int64_t>(cap.l2bytes, 16), s));
+    BatchDev bdp = bd;
+    bdp.plan = d_plan;
+    std::vector<uint64_t> sig2 = sig0;
+    for (uint64_t x : {(uint64_t)cap.B, (uint64_t)cap.U, (uint64_t)cap.l2bytes, (uint64_t)cap.tiles,
+                       (uint64_t)(uintptr_t)d_plan, (uint64_t)(uintptr_t)kalt,
+                       (uint64_t)(uintptr_t)valt, (uint64_t)(uintptr_t)cnt, (uint64_t)(uintptr_t)useg,
+                       (uint64_t)(uintptr_t)sortmp, (uint64_t)(uintptr_t)l2tmp,
+                       (uint64_t)(uintptr_t)set->l1, (uint64_t)(uintptr_t)set->prefix,
+                       (uint64_t)(uintptr_t)set->bindex, (uint64_t)(uintptr_t)set->l2,
+                       (uint64_t)warp_words, (uint64_t)l2_fillq, (uint64_t)ctx->l2_mode,
+                       (uint64_t)any_l2})
+      sig2.push_back(x);
+    CK(run_phase(ctx, 2, s, capturing, [&] {
+      phase1_launches(cnt, any_l2 ? cap.U + 1 : 0);
+      // the second half's bases and sizes, on the device
+      launch_plan(bdp, d_md, static_cast<int32_t *>(set->bindex), static_cast<uint8_t *>(set->l2),
+                  cap, ctx->l2_mode, d_plan, s);
+      mark(5);
+      launch_expand(bdp, wpre, s);
+      mark(6);
+      if (any_l2) {
+        count_sort_pairs(bdp, nullptr, cap.tiles, keys, vals, wpre + words, cap.U, pair_cap, cnt,
+                         useg, kalt, valt, wtot + 1, sortmp, s);
+        mark(7);
+        launch_level2(bdp, kalt, valt, useg, cap.U, l2tmp, warp_words, ctx->num_sms, s,
+                      [&] { mark(9); }, 0, 1, {}, 0, nullptr, true, l2_fillq);
+      } else {
+        mark(7);
+        mark(9);
+      }
+      mark(8);
+      StageList out(ctx->num_sms, s);
+      out.copy(ctx->h_stats, stats, n * sizeof(MeshStats));
+      out.copy(ctx->h_u32, wtot, 8);
+      out.copy(ctx->h_u32 + kPlanWord, d_plan, sizeof(DevPlan));
+      out.launch();
+    }, true, &sig2));
+    CK(cudaStreamSynchronize(s));
+    ht[2] = ht[3] = ht[4] = HClock::now();
+    DevPlan pl;
+    std::memcpy(&pl, ctx->h_u32 + kPlanWord, sizeof(DevPlan));
+    bool overflow = false, raised = false;
+    int64_t need = 0;
+    for (int m = 0; m < n; ++m) {
+      const MeshStats &st = ctx->h_stats[m];
+      if (st.status & ST_BAD_INPUT) return fail_all(GPV_ERR_INVALID, "non-finite vertex");
+      overflow = overflow || (st.status & ST_PAIR_OVERFLOW);
+      raised = raised || st.status;
+      need += (int64_t)st.sat1;
+    }
+    if (overflow || !pl.ok) {
+      // a record buffer or a recorded capacity too small: the call runs again with exact sizes
+      // (two halves), which also records this call's sizes for the next one-graph call
+      if (overflow) {
+        if (pair_cap >= need) return fail_all(GPV_ERR_DEVICE, "pair buffer overflow");
+        ctx->pair_hint = std::max(ctx->pair_hint, need + need / 8);
+        ctx->replans++;
+      } else {
+        if (raised) return fail_all(GPV_ERR_DEVICE, "device status raised in Level1");
+        ctx->og_replans++;
+      }
+      ctx->og_key = 0;
+      fail_all(GPV_OK, "");
+      ctx->err.clear();
+      return run_batch(ctx, n, d_tris, T, specs, out, s);
+    }
+    take_stage_times();
+    if (any_l2 && (int64_t)ctx->h_u32[1] != (int64_t)pl.ub)
+      return fail_all(GPV_ERR_DEVICE, "boundary plane and pair lists disagree");
+    // the offsets the planning kernel gave each mesh
+    std::vector<int64_t> l2off(n + 1, 0), boff(n + 1, 0);
+    for (int m = 0; m < n; ++m) {
+      const MeshStats &st = ctx->h_stats[m];
+      boff[m + 1] = boff[m] + (int64_t)st.boundary;
+      l2off[m + 1] = l2off[m] + (gh[m].level2 ? (int64_t)st.boundary * gh[m].cells : 0);
+    }
+    assemble(boff, l2off);
+    ctx->og_calls++;
+    take_host_times();
+    return GPV_OK;
+  }
+
+  CK(run_phase(ctx, 0, s, capturing, [&] {
+    phase1_launches(nullptr, 0);
     // counts out, written straight into page-locked staging
     StageList out(ctx->num_sms, s);
     if (d_slab) out.copy(ctx->h_u32 + 4, d_slab, 4 * (fslab + 1));
@@ -649,6 +860,7 @@ int run_batch(gpv_ctx *ctx, int n, const float *const *d_tris, const int64_t *T,
                      (uint64_t)(uintptr_t)(sink ? sink->bindex : nullptr), (uint64_t)gh[0].N1,
                      (uint64_t)Btot, (uint64_t)(uintptr_t)set->l1, (uint64_t)(uintptr_t)set->prefix,
                      (uint64_t)(uintptr_t)set->bindex, (uint64_t)(uintptr_t)cs, (uint64_t)l2_queue,
+                     (uint64_t)l2_fillq,
                      (uint64_t)n, (uint64_t)(uintptr_t)d_md, (uint64_t)(uintptr_t)ctx->h_md,
                      (uint64_t)(uintptr_t)ctx->h_tiles, (uint64_t)(uintptr_t)ctx->h_tb,
                      (uint64_t)(uintptr_t)stats, (uint64_t)(uintptr_t)ctx->h_stats,
@@ -714,7 +926,7 @@ int run_batch(gpv_ctx *ctx, int n, const float *const *d_tris, const int64_t *T,
                         if (b > a)
                           cudaMemcpyAsync(sink->l2 + a, static_cast<uint8_t *>(set->l2) + a, b - a,
                                           cudaMemcpyDeviceToHost, cs);
-                      }, gh[0].n[2], sink ? &ctx->slab_aux : nullptr, l2_queue);
+                      }, gh[0].n[2], sink ? &ctx->slab_aux : nullptr, l2_queue, l2_fillq);
       else
         mark(9);
       if (nmode) {
@@ -747,75 +959,28 @@ int run_batch(gpv_ctx *ctx, int n, const float *const *d_tris, const int64_t *T,
   }
   CK(cudaStreamSynchronize(s));
   ht[4] = HClock::now();
-  if (ctx->timing) {
-    // stages: 0 prep, 1 level1, 2 fill finish + boundary scan, 3 expand, 4 sort + lists,
-    // 5 level2 (work items + kernel), 6 the Level2 kernel alone, 7 per-mesh pair bases,
-    // 8 between the phases (counts out, host planning, second launch, uploads in)
-    const int pr[9][2] = {{0, 1}, {2, 3}, {3, 4}, {5, 6}, {6, 7}, {7, 8}, {9, 8}, {1, 2}, {4, 5}};
-    for (int k = 0; k < 9; ++k) {
-      float ms = 0.f;
-      if (cudaEventElapsedTime(&ms, ctx->ev[pr[k][0]], ctx->ev[pr[k][1]]) == cudaSuccess)
-        ctx->stage_ms[k] += ms;
-    }
-    ctx->stage_calls++;
-  }
+  take_stage_times();
   for (int m = 0; m < n; ++m)
     if (ctx->h_stats[m].status) return fail_all(GPV_ERR_DEVICE, "device status raised in Level2");
   if (do_l2) {
     if ((int64_t)ctx->h_u32[1] != ub)
       return fail_all(GPV_ERR_DEVICE, "boundary plane and pair lists disagree");
   }
-
-  uint64_t handle;
-  {
-    std::lock_guard<std::mutex> lk(ctx->owned_mu);
-    handle = ctx->next_handle++;
-    set->refs = n;
-    ctx->owned[handle] = set;
-  }
-  for (int m = 0; m < n; ++m) {
-    const MeshStats &st = ctx->h_stats[m];
-    gpv_result &r = out[m];
-    std::memset(&r, 0, sizeof(r));
-    r.spec = specs[m];
-    for (int a = 0; a < 3; ++a) {
-      r.grid_size[a] = gh[m].g[a];
-      r.grid_size2[a] = gh[m].level2 ? gh[m].g2[a] : 0.f;
-    }
-    r.num_level1 = gh[m].N1;
-    r.num_boundary = (int64_t)st.boundary;
-    r.num_level1_inside = (int64_t)st.l1_inside;
-    r.num_level2_inside = (int64_t)st.l2_inside;
-    r.num_level2_boundary = (int64_t)st.l2_boundary;
-    r.num_pairs = (int64_t)st.pairs;
-    r.work.sat1 = (int64_t)st.sat1;
-    r.work.sat2 = gh[m].level2 ? (int64_t)st.pairs * gh[m].cells : 0;
-    r.work.ray1 = (int64_t)st.ray1;
-    r.work.ray2 = (int64_t)st.ray2;
-    r.level1_inout = static_cast<uint8_t *>(set->l1) + res_l1[m];
-    r.level1_prefix = static_cast<int32_t *>(set->prefix) + res_pre[m];
-    r.boundary_index = static_cast<int32_t *>(set->bindex) + boff[m];
-    r.level2_inout = static_cast<uint8_t *>(set->l2) + l2off[m];
-    r.handle = handle;
-    r.normal_mode = nmode;
-    if (res_hier[m + 1] > res_hier[m]) {
-      r.hierarchy = static_cast<gpv_box *>(set->hier) + res_hier[m];
-      r.hierarchy_levels = hierarchy_levels(gh[m].N1);
-    }
-    if (nmode) {
-      r.level1_normal = static_cast<uint8_t *>(set->l1n) + res_l1n[m];
-      r.level2_normal = static_cast<uint8_t *>(set->l2n) + 3 * l2off[m] * nsz;
-    }
-  }
+  assemble(boff, l2off);
   if (!l2_copied) {
     ctx_fail(ctx, GPV_ERR_BUDGET, "host Level2 buffer too small: nothing copied there (result kept)");
     return GPV_ERR_BUDGET;
   }
-  if (ctx->timing) {
-    ht[5] = HClock::now();
-    for (int k = 0; k < 5; ++k)
-      ctx->host_ms[k] += std::chrono::duration<double, std::milli>(ht[k + 1] - ht[k]).count();
+  if (og_path) {
+    // this call's sizes, for a next call with the same meshes and grids as one graph (a little
+    // room for triangles that move between calls)
+    ctx->og_key = key;
+    ctx->og_caps.B = Btot + Btot / 64 + 64;
+    ctx->og_caps.U = ub + ub / 64 + 64;
+    ctx->og_caps.l2bytes = l2bytes + l2bytes / 64 + 4096;
+    ctx->og_caps.tiles = ntiles + ntiles / 64 + 4;
   }
+  take_host_times();
   return GPV_OK;
 #undef CK
 }

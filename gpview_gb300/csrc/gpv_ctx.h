@@ -66,16 +66,24 @@ struct gpv_ctx {
   std::unique_ptr<gpv::ExpandPool> pool;
   uint32_t *h_codes = nullptr;         // page-locked staging of the codes (device-mapped)
   size_t h_codes_cap = 0;              // words
-  bool graphs = true;                  // record the two phases as CUDA graphs
+  bool graphs = true;                  // record the launch sequences as CUDA graphs
+  // One-graph calls (gpv_set_graphs): a call whose meshes (triangle counts) and grids repeat the
+  // previous call on this path (og_key) is recorded as one graph whose result arrays and
+  // second-half launches are sized by that call's counts (og_caps).
+  bool one_graph = true;
+  uint64_t og_key = 0;
+  gpv::PlanCaps og_caps = {};
+  int64_t og_calls = 0, og_replans = 0;
+  int64_t debug_og_cap = 0;            // the next one-graph call's boundary capacity (one-shot)
   int normals = 0;                     // GPV_NORMALS_* for the next voxelizations
   bool hierarchy = false;              // build the voxel box hierarchy
   int fill = GPV_FILL_RAY;             // inside fill of both levels
-  cudaGraphExec_t gexec[2] = {};       // cached executable graphs of the two phases
+  cudaGraphExec_t gexec[3] = {};       // cached executable graphs: the two phases, one-graph calls
   // Launch signature of each cached graph (every value its kernels and copies take as
   // arguments: workspace pointers, sizes, flags) and its kernel count: a call whose signature
   // matches replays the graph without recording it again.
-  std::vector<uint64_t> gsig[2];
-  uint64_t glaunch[2] = {};
+  std::vector<uint64_t> gsig[3];
+  uint64_t glaunch[3] = {};
   uint64_t graph_launches = 0, graph_instantiations = 0;
   gpv::MeshStats *h_stats = nullptr;   // pinned, h_cap entries
   gpv::MeshDesc *h_md = nullptr;       // pinned, h_cap entries

@@ -70,6 +70,7 @@ struct MeshDesc {
   int64_t emit_base;     // ... of pair capacities (emission segments)
   int64_t pair_base;     // ... of pairs (dense layout after the sort)
   int64_t u_base;        // ... of boundary voxels
+  int64_t stile_base;    // ... of pair-sort tiles (one-graph calls: set on the device by k_plan)
   int32_t ch;            // Level2 chunk length
   int32_t has_l2;        // the mesh has a Level2 grid
   float4 *fnorm;         // normals on: normalised face normal per triangle
@@ -80,6 +81,21 @@ struct MeshDesc {
   // page-locked staging) by the z slabs whose bit is set in BatchDev::packed_slabs; the host
   // expands them into the caller's bytes while later slabs compute
   uint32_t *l2codes;
+};
+
+// Sizes of the second half of a one-graph call (the whole voxelization recorded as one CUDA
+// graph), computed on the device by k_plan from the first half's counts.  The second half's
+// kernels are launched for capacities known when the graph is recorded and read these sizes;
+// with ok = 0 (a size above its capacity, or a mesh status raised) they do nothing and the host
+// re-runs the call with the exact sizes.
+struct DevPlan {
+  uint32_t ok;
+  uint32_t qsel;     // Level2 SAT organisation: 1 queued records, 0 per lane
+  uint32_t ub;       // boundary voxels of the meshes with a Level2 grid (the sorted segments)
+  uint32_t ntiles;   // pair-sort tiles of those meshes
+  unsigned long long P2;       // pairs of those meshes
+  unsigned long long Btot;     // boundary voxels of all meshes
+  unsigned long long l2bytes;  // Level2 output bytes
 };
 
 // BatchDev::fill value for Level1 SAT units only (no parity fill): the reference-named Level1
@@ -112,7 +128,21 @@ struct BatchDev {
   // packed Level2 host output: in z slab k of the Level2 launch, the boundary voxels whose output
   // index is below pk_end[k] write MeshDesc::l2codes instead of bytes (the slab's first share)
   uint32_t pk_end[kSlabsMax] = {};
+  // one-graph calls: the device-computed sizes of the second half (nullptr: sizes from the host)
+  const DevPlan *plan = nullptr;
 };
+
+// Mesh owning work index idx: last m with md[m].*F <= idx (meshes with no work of this kind
+// share their successor's base and are skipped).
+template <int64_t MeshDesc::*F>
+__device__ __forceinline__ int find_mesh(const MeshDesc *md, int nmesh, int64_t idx) {
+  int lo = 0, hi = nmesh - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (md[mid].*F <= idx) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
 
 // Small copies and clears around a phase, done by one kernel instead of copy-engine and memset
 // nodes, so a recorded phase is kernels only.  Every address must be device-accessible: device
@@ -147,6 +177,13 @@ void launch_prep(const BatchDev &bd, cudaStream_t s);
 // Boundary rank at each z-slab start of a single mesh (nslab + 1 values into out).
 void launch_slab_offsets(const uint32_t *wpre, const uint32_t *wtot, int64_t words_per_layer,
                          int nz, int zslab, int nslab, uint32_t *out, cudaStream_t s);
+// One-graph calls: from the first half's per-mesh counts, the per-mesh bases of the second half
+// (u_base, pair_base, stile_base, and the bindex and l2 slices of the given result arenas) and
+// the DevPlan, checked against the capacities the second half was recorded with.  level2_mode is
+// GPV_LEVEL2_*; the automatic choice is the host's level2_queue_pays, evaluated on the device.
+struct PlanCaps { int64_t B, U, l2bytes, tiles, P; };
+void launch_plan(const BatchDev &bd, MeshDesc *d_md, int32_t *bindex, uint8_t *l2,
+                 const PlanCaps &caps, int level2_mode, DevPlan *plan, cudaStream_t s);
 // Device-side per-mesh pair segments (emit_base, pair_cap, keys, vals) from prep's sat1 counts.
 void launch_pair_bases(const BatchDev &bd, MeshDesc *d_md, uint32_t *keys, uint32_t *vals,
                        int64_t cap, cudaStream_t s);
@@ -175,6 +212,8 @@ int64_t sort_seg_temp_words(int64_t ntiles);
 // one count, one scan and one scatter give the dense (kout, vout) lists and the segment starts
 // useg[0..nseg] directly.  done receives the number of voxels whose last pair was placed (nseg
 // when the marks and the pairs agree); cnt (nseg words) must be zero and is left zero.
+// One-graph calls (tiles == nullptr, bd.plan set): the tiles and sizes come from the device
+// plan; ntiles and nseg are capacities, and cnt holds nseg + 1 zero words.
 void count_sort_pairs(const BatchDev &bd, const SortTile *tiles, int64_t ntiles,
                       const uint32_t *keys, const uint32_t *vals, const uint32_t *kpre,
                       int64_t nseg, int64_t P, uint32_t *cnt, uint32_t *useg, uint32_t *kout,
@@ -201,10 +240,14 @@ void launch_level2(const BatchDev &bd, const uint32_t *keys, const uint32_t *val
                    const uint32_t *useg, int64_t Btot, uint32_t *tmp, int warp_words, int num_sms,
                    cudaStream_t s, const std::function<void()> &before_kernel = {}, int zslab = 0,
                    int nslab = 1, const std::function<void(int, cudaStream_t)> &after_slab = {},
-                   int slab_nz = 0, const SlabStreams *aux = nullptr, bool queue = true);
+                   int slab_nz = 0, const SlabStreams *aux = nullptr, bool queue = true,
+                   bool fillq = false);
 // Level2 SAT organisation for a batch (see k_level2c): queued records when most of the pair work
 // belongs to meshes whose pairs carry many (triangle, sub-column) items.
 bool level2_queue_pays(const MeshStats *stats, const bool *has_l2, int n);
+// Level2 ray-fill organisation: the u/v-passing items queued before their per-voxel work when
+// every Level2 grid of the launch has at most kFillQueueCells cells.
+constexpr int kFillQueueCells = 512;
 
 // ---- normals (gpv_normals.cu) ----------------------------------------------------------------
 void launch_face_normals(const BatchDev &bd, cudaStream_t s);

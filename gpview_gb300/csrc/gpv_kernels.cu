@@ -32,18 +32,6 @@ __device__ __forceinline__ uint32_t pack2(int lo, int hi) {
 __device__ __forceinline__ int lo16(uint32_t v) { return (int)(v & 0xffffu); }
 __device__ __forceinline__ int hi16(uint32_t v) { return (int)(v >> 16); }
 
-// Mesh owning work index idx: last m with md[m].*F <= idx (meshes with no work of this kind
-// share their successor's base and are skipped).
-template <int64_t MeshDesc::*F>
-__device__ __forceinline__ int find_mesh(const MeshDesc *md, int nmesh, int64_t idx) {
-  int lo = 0, hi = nmesh - 1;
-  while (lo < hi) {
-    const int mid = (lo + hi + 1) >> 1;
-    if (md[mid].*F <= idx) lo = mid; else hi = mid - 1;
-  }
-  return lo;
-}
-
 // smallest i in [0,n] with tab[i] >= x (tab nondecreasing); approximate start then adjust.
 __device__ __forceinline__ int first_ge(const float *tab, int n, float x, float c0, float g) {
   float f = (x - c0) / g;
@@ -281,6 +269,98 @@ __global__ void __launch_bounds__(1024) k_pair_bases(int nmesh, MeshDesc *md, ui
     __syncthreads();
     if (threadIdx.x == 1023) s_carry = base + v;
     __syncthreads();
+  }
+}
+
+// One-graph calls: the second half's per-mesh bases and sizes from the first half's counts (one
+// block; meshes in rounds of 1024, seven running sums scanned together).  The sums, per mesh:
+// 0 boundary voxels (boundaryIndex slices), 1 the same for meshes with a Level2 grid (sorted
+// segments), 2 their Level2 bytes, 3 their pair-sort tiles, 4 their pairs, 5 the pairs of those
+// whose pairs carry many Level2 SAT items (the queued organisation's measure, as
+// level2_queue_pays computes it on the host), 6 meshes with a raised status.
+constexpr int kPlanSums = 7;
+__global__ void __launch_bounds__(1024) k_plan(int nmesh, MeshDesc *md, int32_t *bindex,
+                                               uint8_t *l2, PlanCaps caps, int mode,
+                                               DevPlan *plan) {
+  __shared__ unsigned long long s_w[32][kPlanSums];
+  __shared__ unsigned long long s_carry[kPlanSums];
+  const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+  if (threadIdx.x < kPlanSums) s_carry[threadIdx.x] = 0;
+  __syncthreads();
+  for (int m0 = 0; m0 < nmesh; m0 += 1024) {
+    const int m = m0 + (int)threadIdx.x;
+    unsigned long long v[kPlanSums] = {};
+    if (m < nmesh) {
+      const MeshStats &st = *md[m].stats;
+      const bool has = md[m].has_l2 != 0;
+      const unsigned long long b = st.boundary, p = st.pairs;
+      const unsigned long long cells =
+          (unsigned long long)md[m].g.n2[0] * md[m].g.n2[1] * md[m].g.n2[2];
+      v[0] = b;
+      v[1] = has ? b : 0ull;
+      v[2] = has ? b * cells : 0ull;
+      v[3] = has ? (p + kSortTileItems - 1) / kSortTileItems : 0ull;
+      v[4] = has ? p : 0ull;
+      v[5] = (has && st.xycells >= 64ull * p) ? p : 0ull;
+      v[6] = st.status != 0u;
+    }
+    unsigned long long x[kPlanSums];
+#pragma unroll
+    for (int k = 0; k < kPlanSums; ++k) {
+      x[k] = v[k];
+#pragma unroll
+      for (int d = 1; d < 32; d <<= 1) {
+        const unsigned long long o = __shfl_up_sync(FULL, x[k], d);
+        if (lane >= (unsigned)d) x[k] += o;
+      }
+      if (lane == 31) s_w[warp][k] = x[k];
+    }
+    __syncthreads();
+    if (warp == 0) {
+#pragma unroll
+      for (int k = 0; k < kPlanSums; ++k) {
+        unsigned long long w = s_w[lane][k];
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+          const unsigned long long o = __shfl_up_sync(FULL, w, d);
+          if (lane >= (unsigned)d) w += o;
+        }
+        s_w[lane][k] = w;
+      }
+    }
+    __syncthreads();
+    if (m < nmesh) {
+      unsigned long long e[kPlanSums];
+#pragma unroll
+      for (int k = 0; k < kPlanSums; ++k)
+        e[k] = s_carry[k] + (warp ? s_w[warp - 1][k] : 0ull) + x[k] - v[k];
+      md[m].u_base = (int64_t)e[1];
+      md[m].pair_base = (int64_t)e[4];
+      md[m].stile_base = (int64_t)e[3];
+      md[m].bindex = bindex + min((long long)e[0], (long long)caps.B);
+      md[m].l2 = l2 + min((long long)e[2], (long long)caps.l2bytes);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0)
+#pragma unroll
+      for (int k = 0; k < kPlanSums; ++k) s_carry[k] += s_w[31][k];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    const unsigned long long *t = s_carry;
+    DevPlan p;
+    p.ok = t[6] == 0 && t[0] <= (unsigned long long)caps.B && t[1] <= (unsigned long long)caps.U &&
+           t[2] <= (unsigned long long)caps.l2bytes && t[3] <= (unsigned long long)caps.tiles &&
+           t[4] <= (unsigned long long)caps.P;
+    p.qsel = mode == GPV_LEVEL2_QUEUED   ? 1u
+             : mode == GPV_LEVEL2_INLINE ? 0u
+                                         : ((double)t[5] > 0.9 * (double)t[4] ? 1u : 0u);
+    p.ub = (uint32_t)min(t[1], 0xffffffffull);
+    p.ntiles = (uint32_t)min(t[3], 0xffffffffull);
+    p.P2 = t[4];
+    p.Btot = t[0];
+    p.l2bytes = t[2];
+    *plan = p;
   }
 }
 
@@ -673,6 +753,8 @@ __global__ void __launch_bounds__(kExpandWarps * 32) k_expand(BatchDev bd,
   __shared__ int s_mesh;
   __shared__ int s_m[kExpandWarps];
   __shared__ unsigned long long s_nin[kExpandWarps];
+  // one-graph calls whose sizes did not fit: the call is re-run
+  if (bd.plan && !bd.plan->ok) return;
   const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
   const int64_t c0 = (int64_t)blockIdx.x * kExpandWarps * iters;
   if (threadIdx.x == 0) s_mesh = find_mesh<&MeshDesc::xc_base>(bd.md, bd.nmesh, c0);
@@ -817,6 +899,12 @@ void StageList::launch() {
 void launch_pair_bases(const BatchDev &bd, MeshDesc *d_md, uint32_t *keys, uint32_t *vals,
                        int64_t cap, cudaStream_t s) {
   k_pair_bases<<<1, 1024, 0, s>>>(bd.nmesh, d_md, keys, vals, cap);
+  count_launch();
+}
+
+void launch_plan(const BatchDev &bd, MeshDesc *d_md, int32_t *bindex, uint8_t *l2,
+                 const PlanCaps &caps, int level2_mode, DevPlan *plan, cudaStream_t s) {
+  k_plan<<<1, 1024, 0, s>>>(bd.nmesh, d_md, bindex, l2, caps, level2_mode, plan);
   count_launch();
 }
 

@@ -156,9 +156,12 @@ struct WarpScratch {
                       // the triangle's topmost voxel
   uint32_t zrec[32];  // SAT: (triangle slot, p, q) of a sub-column item
   uint32_t seg[33];   // SAT: first pair of each voxel of the chunk, and the end
-  uint32_t zown[64];  // SAT: (record lane, cell) of each (triangle, cell) item of a window
+  uint32_t zown[64];  // SAT: (record lane, cell) of each (triangle, cell) item of a window;
+                      // queued fill: Tx of each record
   uint32_t brec[64];  // SAT: queued (triangle slot, p, q) records of sub-columns passing the
-                      // z-invariant axes
+                      // z-invariant axes; queued fill: (triangle slot, sub-column) records of
+                      // sub-columns passing u/v
+  float fty[64];      // queued fill: Ty of each record
 };
 
 // ---- item construction -----------------------------------------------------------------------
@@ -171,22 +174,38 @@ __device__ __forceinline__ int mesh_of_u(const MeshDesc *md, int nmesh, int64_t 
   return lo;
 }
 
+// Boundary voxels of the sorted meshes: B, or (one-graph calls, B the capacity) the device
+// plan's count, none when the plan did not fit.
+__device__ __forceinline__ int64_t sorted_voxels(const BatchDev &bd, int64_t B) {
+  if (!bd.plan) return B;
+  return bd.plan->ok ? min(B, (int64_t)bd.plan->ub) : 0;
+}
+
 // cflag[u] = 1 where a new Level1 column starts (a mesh's first boundary voxel, or a column
-// change within the mesh).
+// change within the mesh).  One-graph calls: zero past the device count (the scans run over the
+// capacity), and no work items until k_itemstarts counts them.
 __global__ void k_colflags(BatchDev bd, const uint32_t *__restrict__ keys,
-                           const uint32_t *__restrict__ useg, int64_t B,
-                           uint32_t *__restrict__ cflag) {
+                           const uint32_t *__restrict__ useg, int64_t Bcap,
+                           uint32_t *__restrict__ cflag, uint32_t *__restrict__ nitems) {
   const int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (u >= B) return;
+  if (u >= Bcap) return;
+  if (bd.plan && u == 0) *nitems = 0;
+  const int64_t B = sorted_voxels(bd, Bcap);
+  if (u >= B) {
+    cflag[u] = 0;
+    return;
+  }
   const int m = mesh_of_u(bd.md, bd.nmesh, u);
   const uint32_t nz = (uint32_t)bd.md[m].g.n[2];
   const uint32_t col = keys[useg[u]] / nz;
   cflag[u] = (u == bd.md[m].u_base || keys[useg[u - 1]] / nz != col) ? 1u : 0u;
 }
 
-__global__ void k_colheads(const uint32_t *__restrict__ cflag, const uint32_t *__restrict__ cord,
-                           int64_t B, uint32_t *__restrict__ colhead) {
+__global__ void k_colheads(BatchDev bd, const uint32_t *__restrict__ cflag,
+                           const uint32_t *__restrict__ cord, int64_t Bcap,
+                           uint32_t *__restrict__ colhead) {
   const int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t B = sorted_voxels(bd, Bcap);
   if (u >= B) return;
   if (cflag[u]) colhead[cord[u]] = (uint32_t)u;
   if (u == B - 1) colhead[cord[u] + cflag[u]] = (uint32_t)B;
@@ -197,9 +216,13 @@ __global__ void k_colheads(const uint32_t *__restrict__ cflag, const uint32_t *_
 __global__ void k_itemflags(BatchDev bd, const uint32_t *__restrict__ keys,
                             const uint32_t *__restrict__ useg, const uint32_t *__restrict__ cflag,
                             const uint32_t *__restrict__ cord, const uint32_t *__restrict__ colhead,
-                            int64_t B, int zslab, uint32_t *__restrict__ iflag) {
+                            int64_t Bcap, int zslab, uint32_t *__restrict__ iflag) {
   const int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (u >= B) return;
+  if (u >= Bcap) return;
+  if (u >= sorted_voxels(bd, Bcap)) {
+    iflag[u] = 0;
+    return;
+  }
   const MeshDesc &d = bd.md[mesh_of_u(bd.md, bd.nmesh, u)];
   const uint32_t c = cord[u] + cflag[u] - 1u;
   bool start = (u - colhead[c]) % d.ch == 0;
@@ -211,9 +234,11 @@ __global__ void k_itemflags(BatchDev bd, const uint32_t *__restrict__ keys,
   iflag[u] = (d.has_l2 && start) ? 1u : 0u;
 }
 
-__global__ void k_itemstarts(const uint32_t *__restrict__ iflag, const uint32_t *__restrict__ iord,
-                             int64_t B, uint32_t *__restrict__ istart, uint32_t *__restrict__ nitems) {
+__global__ void k_itemstarts(BatchDev bd, const uint32_t *__restrict__ iflag,
+                             const uint32_t *__restrict__ iord, int64_t Bcap,
+                             uint32_t *__restrict__ istart, uint32_t *__restrict__ nitems) {
   const int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t B = sorted_voxels(bd, Bcap);
   if (u >= B) return;
   if (iflag[u]) istart[iord[u]] = (uint32_t)u;
   if (u == B - 1) *nitems = iord[u] + iflag[u];
@@ -410,8 +435,9 @@ __global__ void __launch_bounds__(kPrefixWarps * 32) k_stencil_prefix(
 // ST: the stencil fill (ClassifyInOut2xLevel2) instead of the ray fill.  QUEUE: the (triangle,
 // sub-column) items passing the z-invariant axes are queued and their slab work done 32 records
 // at a time (pays off when a pair has many items: triangles large against the Level2 cells);
-// otherwise each item lane does its own slab work.
-template <bool ST, bool QUEUE>
+// otherwise each item lane does its own slab work.  FQ (ray fill): the (triangle, sub-column)
+// items passing u/v are queued the same way before their per-voxel work.
+template <bool ST, bool QUEUE, bool FQ>
 // Six blocks per SM for the queued organisation (80 registers); seven for the per-lane one
 // (72), measured 1.5-3% faster there (the 4096-mesh batch, a 4^3 Level2 grid).
 __global__ void __launch_bounds__(kWarps * 32, QUEUE ? 6 : 7) k_level2c(
@@ -421,6 +447,8 @@ __global__ void __launch_bounds__(kWarps * 32, QUEUE ? 6 : 7) k_level2c(
     const uint32_t *__restrict__ istart, const uint32_t *__restrict__ nitems, int per_warp,
     int slab, int zslab, const uint32_t *__restrict__ ilist, const uint32_t *__restrict__ ioff) {
   extern __shared__ uint32_t sm[];
+  // one-graph calls launch both SAT organisations; the device plan picks one
+  if (bd.plan && bd.plan->qsel != (QUEUE ? 1u : 0u)) return;
   const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
   uint32_t *base = sm + (size_t)warp * per_warp;
   // all items, or (z slabs) this launch's slab of the slab-ordered item list
@@ -955,23 +983,9 @@ __global__ void __launch_bounds__(kWarps * 32, QUEUE ? 6 : 7) k_level2c(
     ws.pre[lane] = inc - cnt;
     const uint32_t tot = __shfl_sync(FULL, inc, 31);
     __syncwarp();
-    for (uint32_t w = lane; w < tot; w += 32) {
-      const int tl = batch_search(ws.pre, w);
-      const uint32_t loc = w - ws.pre[tl];
-      const uint32_t rg = ws.rng[tl];
-      const int np = (int)((rg >> 6) & 63u);
-      const int qq = __float2int_rz(((float)loc + 0.5f) * ws.x[tl][2]);
-      const int p = (int)(rg & 63u) + (int)loc - qq * np;
-      const int q = (int)((rg >> 12) & 63u) + qq;
-      RayTri rt;
-      rt.v1x = ws.v[tl][0]; rt.v1y = ws.v[tl][1]; rt.v1z = ws.v[tl][2];
-      rt.e1x = ws.v[tl][3]; rt.e1y = ws.v[tl][4]; rt.e1z = ws.v[tl][5];
-      rt.e2x = ws.v[tl][6]; rt.e2y = ws.v[tl][7]; rt.e2z = ws.v[tl][8];
-      rt.inv_det = ws.x[tl][0];
-      rt.ok = true;
-      RayCol rc;
-      if (!ray_col(rt, __ldg(ox + p), __ldg(oy + q), rc)) continue;
-      const int pq = q * n2x + p;
+    // The toggles of one (triangle slot, sub-column pq) item that passed u/v, in the voxels of the
+    // chunk at or below the triangle's topmost voxel, top down.
+    auto item_voxels = [&](const RayTri &rt, const RayCol &rc, int tl, int pq) {
       const float E2 = ws.x[tl][1];
       const bool well = E2 > 0.f;
       for (int jv = ws.jm[tl] - 1; jv >= 0; --jv) {
@@ -1007,6 +1021,91 @@ __global__ void __launch_bounds__(kWarps * 32, QUEUE ? 6 : 7) k_level2c(
             if (ray_t(rt, rc, __ldg(oz + r), g.thr)) bits |= 1u << r;
         }
         if (bits) xor_column(par + jv * W, pq, n2z, bits);
+      }
+    };
+    // (triangle slot, p, q) of item w of this batch
+    auto item_of = [&](uint32_t w, int &tl, int &p, int &q) {
+      tl = batch_search(ws.pre, w);
+      const uint32_t loc = w - ws.pre[tl];
+      const uint32_t rg = ws.rng[tl];
+      const int np = (int)((rg >> 6) & 63u);
+      const int qq = __float2int_rz(((float)loc + 0.5f) * ws.x[tl][2]);
+      p = (int)(rg & 63u) + (int)loc - qq * np;
+      q = (int)((rg >> 12) & 63u) + qq;
+    };
+    if constexpr (!FQ) {
+      // each item lane goes on to its own voxels
+      for (uint32_t w = lane; w < tot; w += 32) {
+        int tl, p, q;
+        item_of(w, tl, p, q);
+        RayTri rt;
+        rt.v1x = ws.v[tl][0]; rt.v1y = ws.v[tl][1]; rt.v1z = ws.v[tl][2];
+        rt.e1x = ws.v[tl][3]; rt.e1y = ws.v[tl][4]; rt.e1z = ws.v[tl][5];
+        rt.e2x = ws.v[tl][6]; rt.e2y = ws.v[tl][7]; rt.e2z = ws.v[tl][8];
+        rt.inv_det = ws.x[tl][0];
+        rt.ok = true;
+        RayCol rc;
+        if (!ray_col(rt, __ldg(ox + p), __ldg(oy + q), rc)) continue;
+        item_voxels(rt, rc, tl, q * n2x + p);
+      }
+    } else {
+      // the items passing u/v are queued as (triangle slot, sub-column) records with their Tx, Ty
+      // and their voxels done 32 records at a time, so that every lane of that loop works (most
+      // items fail u/v: 34% pass on torus262k)
+      uint32_t nfr = 0;
+      for (uint32_t wb = 0; wb < tot || nfr > 0; wb += 32) {
+        const uint32_t w = wb + lane;
+        bool pass = false;
+        uint32_t frec = 0;
+        RayCol rc0;
+        if (w < tot) {
+          int tl, p, q;
+          item_of(w, tl, p, q);
+          RayTri rt;  // the fields of the u/v test
+          rt.v1x = ws.v[tl][0]; rt.v1y = ws.v[tl][1];
+          rt.e1x = ws.v[tl][3]; rt.e1y = ws.v[tl][4];
+          rt.e2x = ws.v[tl][6]; rt.e2y = ws.v[tl][7];
+          rt.inv_det = ws.x[tl][0];
+          if (ray_col(rt, __ldg(ox + p), __ldg(oy + q), rc0)) {
+            pass = true;
+            frec = (uint32_t)tl | ((uint32_t)(q * n2x + p) << 5);
+          }
+        }
+        const uint32_t fbal = __ballot_sync(FULL, pass);
+        if (pass) {
+          const uint32_t k = nfr + __popc(fbal & ((1u << lane) - 1u));
+          ws.brec[k] = frec;
+          ws.zown[k] = __float_as_uint(rc0.Tx);
+          ws.fty[k] = rc0.Ty;
+        }
+        nfr += (uint32_t)__popc(fbal);
+        __syncwarp();
+        // every 32 records, and at the end of the batch (the records name its triangle slots)
+        if (nfr < 32 && !(wb + 32 >= tot && nfr > 0)) continue;
+        const uint32_t nr = min(nfr, 32u);
+        if (lane < nr) {
+          const uint32_t fr = ws.brec[lane];
+          const int tl = (int)(fr & 31u);
+          RayTri rt;
+          rt.v1x = ws.v[tl][0]; rt.v1y = ws.v[tl][1]; rt.v1z = ws.v[tl][2];
+          rt.e1x = ws.v[tl][3]; rt.e1y = ws.v[tl][4]; rt.e1z = ws.v[tl][5];
+          rt.e2x = ws.v[tl][6]; rt.e2y = ws.v[tl][7]; rt.e2z = ws.v[tl][8];
+          rt.inv_det = ws.x[tl][0];
+          rt.ok = true;
+          RayCol rc;
+          rc.Tx = __uint_as_float(ws.zown[lane]);
+          rc.Ty = ws.fty[lane];
+          item_voxels(rt, rc, tl, (int)(fr >> 5));
+        }
+        __syncwarp();
+        // move the records beyond the first nr to the front
+        uint32_t m0 = 0, m1 = 0;
+        float m2 = 0.f;
+        if (lane + nr < nfr) { m0 = ws.brec[nr + lane]; m1 = ws.zown[nr + lane]; m2 = ws.fty[nr + lane]; }
+        __syncwarp();
+        if (lane + nr < nfr) { ws.brec[lane] = m0; ws.zown[lane] = m1; ws.fty[lane] = m2; }
+        nfr -= nr;
+        __syncwarp();
       }
     }
     __syncwarp();
@@ -1118,7 +1217,7 @@ void launch_level2(const BatchDev &bd, const uint32_t *keys, const uint32_t *val
                    const uint32_t *useg, int64_t B, uint32_t *tmp, int warp_words, int num_sms,
                    cudaStream_t s, const std::function<void()> &before_kernel, int zslab,
                    int nslab, const std::function<void(int, cudaStream_t)> &after_slab, int slab_nz,
-                   const SlabStreams *aux, bool queue) {
+                   const SlabStreams *aux, bool queue, bool fillq) {
   if (B <= 0) return;
   uint32_t *cflag = tmp, *cord = cflag + B, *colhead = cord + B, *iflag = colhead + B + 1,
            *iord = iflag + B, *istart = iord + B, *nitems = istart + B + 1,
@@ -1126,12 +1225,13 @@ void launch_level2(const BatchDev &bd, const uint32_t *keys, const uint32_t *val
            *stmp = ilist + B;
   if (nslab <= 1) zslab = 0;
   const unsigned nb = (unsigned)((B + 255) / 256);
-  k_colflags<<<nb, 256, 0, s>>>(bd, keys, useg, B, cflag);
+  // (one-graph calls: B is the capacity, the kernels read the device count)
+  k_colflags<<<nb, 256, 0, s>>>(bd, keys, useg, B, cflag, nitems);
   scan_u32(cflag, cord, B, nullptr, stmp, s);
-  k_colheads<<<nb, 256, 0, s>>>(cflag, cord, B, colhead);
+  k_colheads<<<nb, 256, 0, s>>>(bd, cflag, cord, B, colhead);
   k_itemflags<<<nb, 256, 0, s>>>(bd, keys, useg, cflag, cord, colhead, B, zslab, iflag);
   scan_u32(iflag, iord, B, nullptr, stmp, s);
-  k_itemstarts<<<nb, 256, 0, s>>>(iflag, iord, B, istart, nitems);
+  k_itemstarts<<<nb, 256, 0, s>>>(bd, iflag, iord, B, istart, nitems);
   count_launch(4);
   if (bd.fill == GPV_FILL_STENCIL && bd.stp) {
     k_stencil_prefix<<<(unsigned)((B + kPrefixWarps - 1) / kPrefixWarps), kPrefixWarps * 32, 0, s>>>(
@@ -1140,18 +1240,30 @@ void launch_level2(const BatchDev &bd, const uint32_t *keys, const uint32_t *val
   }
   const size_t smem = level2_smem_bytes(warp_words);
   const bool st = bd.fill == GPV_FILL_STENCIL;
-  auto kern = st ? (queue ? k_level2c<true, true> : k_level2c<true, false>)
-                 : (queue ? k_level2c<false, true> : k_level2c<false, false>);
-  const int kv = (st ? 2 : 0) + (queue ? 1 : 0);
-  static bool attr_set[4] = {false, false, false, false};
-  if (!attr_set[kv]) {
-    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-    attr_set[kv] = true;
-  }
-  int per_sm = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kWarps * 32, smem);
-  per_sm = std::max(per_sm, 1);
-  const int64_t grid = std::min<int64_t>((B + kWarps - 1) / kWarps, (int64_t)num_sms * per_sm);
+  using Kern = decltype(&k_level2c<false, false, false>);
+  static bool attr_set[6] = {false, false, false, false, false, false};
+  // the kernel of one SAT organisation, and its persistent grid
+  auto pick = [&](bool q, int64_t &grid) {
+    Kern k = st ? (q ? k_level2c<true, true, false> : k_level2c<true, false, false>)
+           : fillq ? (q ? k_level2c<false, true, true> : k_level2c<false, false, true>)
+                   : (q ? k_level2c<false, true, false> : k_level2c<false, false, false>);
+    const int kv = (st ? 4 : fillq ? 2 : 0) + (q ? 1 : 0);
+    if (!attr_set[kv]) {
+      cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+      attr_set[kv] = true;
+    }
+    int per_sm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, kWarps * 32, smem);
+    per_sm = std::max(per_sm, 1);
+    // (one-graph calls: B is a capacity, the queue ends the work)
+    grid = bd.plan ? (int64_t)num_sms * per_sm
+                   : std::min<int64_t>((B + kWarps - 1) / kWarps, (int64_t)num_sms * per_sm);
+    return k;
+  };
+  int64_t grid = 0, grid2 = 0;
+  const Kern kern = pick(queue, grid);
+  // one-graph calls: the other organisation too; the device plan leaves one of them empty
+  const Kern kern2 = bd.plan ? pick(!queue, grid2) : nullptr;
   const int nz = slab_nz;
   if (zslab > 0) {
     // single mesh: order the items by slab so that each launch takes only its own
@@ -1178,6 +1290,12 @@ void launch_level2(const BatchDev &bd, const uint32_t *keys, const uint32_t *val
                                                     nitems, warp_words, sl, zslab,
                                                     zslab > 0 ? ilist : nullptr, ioff);
     count_launch();
+    if (kern2) {
+      kern2<<<(unsigned)grid2, kWarps * 32, smem, ls>>>(bd, keys, vals, useg, cflag, cord, colhead,
+                                                        istart, nitems, warp_words, sl, zslab,
+                                                        zslab > 0 ? ilist : nullptr, ioff);
+      count_launch();
+    }
     if (after_slab) after_slab(sl, ls);
   }
   if (two) {

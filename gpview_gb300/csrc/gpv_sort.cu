@@ -375,12 +375,31 @@ __device__ __forceinline__ uint32_t cs_rank(const BatchDev &bd, const MeshDesc &
   return kpre[w] - kpre[0] + __popc(word & (bit - 1u));
 }
 
+// The block's pair tile: from the host's list, or (one-graph calls, tiles == nullptr) from the
+// device plan: the mesh by its sort-tile base, the count from its pairs.  False: no tile (the
+// grid was launched for the capacity, or the plan did not fit).
+__device__ __forceinline__ bool cs_tile(const BatchDev &bd, const SortTile *tiles, SortTile &st) {
+  if (tiles) {
+    st = tiles[blockIdx.x];
+    return true;
+  }
+  if (!bd.plan->ok || blockIdx.x >= bd.plan->ntiles) return false;
+  const int m = find_mesh<&MeshDesc::stile_base>(bd.md, bd.nmesh, (int64_t)blockIdx.x);
+  const int64_t j = (int64_t)blockIdx.x - bd.md[m].stile_base;
+  st.mesh = m;
+  st.j = (int32_t)j;
+  st.count = (int32_t)min((int64_t)kSortTile, (int64_t)bd.md[m].stats->pairs - j * kSortTile);
+  return true;
+}
+
 __global__ void __launch_bounds__(kSortThreads) k_cs_count(BatchDev bd,
                                                            const SortTile *__restrict__ tiles,
                                                            const uint32_t *__restrict__ keys,
                                                            const uint32_t *__restrict__ kpre,
                                                            int64_t nseg, uint32_t *__restrict__ cnt) {
-  const SortTile st = tiles[blockIdx.x];
+  SortTile st;
+  if (!cs_tile(bd, tiles, st)) return;
+  if (bd.plan) nseg = bd.plan->ub;
   const MeshDesc &d = bd.md[st.mesh];
   const int64_t in0 = d.emit_base + (int64_t)st.j * kSortTile;
   for (int i = threadIdx.x; i < st.count; i += kSortThreads) {
@@ -397,9 +416,14 @@ __global__ void __launch_bounds__(kSortThreads) k_cs_scatter(
     uint32_t *__restrict__ cnt, const uint32_t *__restrict__ useg, uint32_t *__restrict__ kout,
     uint32_t *__restrict__ vout, uint32_t *__restrict__ done) {
   __shared__ uint32_t s_done;
+  SortTile st;
+  if (!cs_tile(bd, tiles, st)) return;
+  if (bd.plan) {
+    nseg = bd.plan->ub;
+    P = (int64_t)bd.plan->P2;
+  }
   if (threadIdx.x == 0) s_done = 0;
   __syncthreads();
-  const SortTile st = tiles[blockIdx.x];
   const MeshDesc &d = bd.md[st.mesh];
   const int64_t in0 = d.emit_base + (int64_t)st.j * kSortTile;
   uint32_t fin = 0;
@@ -460,7 +484,10 @@ void count_sort_pairs(const BatchDev &bd, const SortTile *tiles, int64_t ntiles,
                       uint32_t *vout, uint32_t *done, uint32_t *temp, cudaStream_t s) {
   if (P <= 0 || ntiles <= 0 || nseg <= 0) return;
   k_cs_count<<<(unsigned)ntiles, kSortThreads, 0, s>>>(bd, tiles, keys, kpre, nseg, cnt);
-  scan_u32(cnt, useg, nseg, useg + nseg, temp, s);
+  // one-graph calls: nseg is the capacity and the counts past the device's segment count are
+  // zero (cleared, never counted), so the scan of nseg + 1 counts puts the total at useg[ub]
+  if (bd.plan) scan_u32(cnt, useg, nseg + 1, nullptr, temp, s);
+  else scan_u32(cnt, useg, nseg, useg + nseg, temp, s);
   k_cs_scatter<<<(unsigned)ntiles, kSortThreads, 0, s>>>(bd, tiles, keys, vals, kpre, nseg, P, cnt,
                                                           useg, kout, vout, done);
   count_launch(2);

@@ -165,9 +165,19 @@ int gpv_result_copy_hierarchy_to_host(gpv_ctx *ctx, const gpv_result *res, gpv_b
 #define GPV_FILL_RAY 0
 #define GPV_FILL_STENCIL 1
 int gpv_set_fill(gpv_ctx *ctx, int mode);
-/* Record the Level1 and Level2 launch sequences of each voxelization as CUDA graphs (default on;
- * the executable graphs are cached in the context and updated in place). */
-int gpv_set_graphs(gpv_ctx *ctx, int on);
+/* Record the launch sequences of each voxelization as CUDA graphs; the executable graphs are
+ * cached in the context and updated in place.
+ *   GPV_GRAPHS_ONE (default, also any other non-zero value): a call with the same meshes (counts)
+ *     and grids as the context's previous call on this path (device triangles, no normals, the
+ *     ray fill, no hierarchy) is recorded as ONE graph: its result arrays and second-half launches
+ *     are sized by that call's counts, and a planning kernel computes every per-mesh base on the
+ *     device, so no host synchronisation splits the call.  A size that does not fit re-runs the
+ *     call with the exact sizes.  Other calls run as two graphs;
+ *   GPV_GRAPHS_TWO: always two graphs (first half, host synchronisation and planning, second half);
+ *   0: launched directly. */
+#define GPV_GRAPHS_ONE 1
+#define GPV_GRAPHS_TWO 2
+int gpv_set_graphs(gpv_ctx *ctx, int mode);
 /* Autotuner: times every (tile, Level2 chunk) pair of {32,64,128,256} x {4,8,16,32} on the given
  * sample batch (CUDA events on `stream`), keeps the fastest in the context and reports it. */
 int gpv_autotune(gpv_ctx *ctx, int32_t n, const float *const *d_tris, const int64_t *num_triangles,
@@ -199,13 +209,20 @@ uint64_t gpv_kernel_launches(void);
  *   GPV_DEBUG_PAIR_CAPACITY the next call starts with this (voxel, triangle) record capacity
  *                           (one-shot): an overflow re-runs the call with the exact capacity;
  *   GPV_DEBUG_FAIL_ALLOCS   the next this-many device allocations of the context are refused
- *                           (the call returns GPV_ERR_OOM).
- * gpv_get_debug reads GPV_DEBUG_REPLANS: calls re-run after a record-buffer overflow. */
+ *                           (the call returns GPV_ERR_OOM);
+ *   GPV_DEBUG_ONE_GRAPH_CAPACITY the next one-graph call's boundary-voxel capacity (one-shot): a
+ *                           smaller one than the call needs re-runs it with the exact sizes.
+ * gpv_get_debug reads GPV_DEBUG_REPLANS (calls re-run after a record-buffer overflow),
+ * GPV_DEBUG_ONE_GRAPH_CALLS (calls completed as one graph) and GPV_DEBUG_ONE_GRAPH_REPLANS
+ * (one-graph calls re-run because a size did not fit). */
 #define GPV_DEBUG_WAIT_LIMIT 1
 #define GPV_DEBUG_FAIL_WAIT 2
 #define GPV_DEBUG_PAIR_CAPACITY 3
 #define GPV_DEBUG_FAIL_ALLOCS 4
 #define GPV_DEBUG_REPLANS 5
+#define GPV_DEBUG_ONE_GRAPH_CAPACITY 6
+#define GPV_DEBUG_ONE_GRAPH_CALLS 7
+#define GPV_DEBUG_ONE_GRAPH_REPLANS 8
 int gpv_set_debug(gpv_ctx *ctx, int what, int64_t value);
 int64_t gpv_get_debug(gpv_ctx *ctx, int what);
 
