@@ -554,7 +554,6 @@ int run_batch(gpv_ctx *ctx, int n, const float *const *d_tris, const int64_t *T,
                        res_hier[n] == 0;
   if (og_path && ctx->og_key == key && ctx->og_caps.B > 0) {
     PlanCaps cap = ctx->og_caps;
-    cap.P = pair_cap;
     if (ctx->debug_og_cap > 0) {  // failure-detection hook: a boundary capacity that overflows
       cap.B = ctx->debug_og_cap;
       ctx->debug_og_cap = 0;
@@ -564,8 +563,8 @@ int run_batch(gpv_ctx *ctx, int n, const float *const *d_tris, const int64_t *T,
              *l2tmp = nullptr;
     CK(ws.get(&d_plan, 1));
     if (any_l2) {
-      CK(ws.get(&kalt, (size_t)pair_cap));
-      CK(ws.get(&valt, (size_t)pair_cap));
+      CK(ws.get(&kalt, (size_t)cap.P));
+      CK(ws.get(&valt, (size_t)cap.P));
       CK(ws.get(&cnt, (size_t)cap.U + 1));
       CK(ws.get(&useg, (size_t)cap.U + 1));
       CK(ws.get(&sortmp, (size_t)scan_temp_words(cap.U + 1)));
@@ -577,6 +576,7 @@ int run_batch(gpv_ctx *ctx, int n, const float *const *d_tris, const int64_t *T,
     bdp.plan = d_plan;
     std::vector<uint64_t> sig2 = sig0;
     for (uint64_t x : {(uint64_t)cap.B, (uint64_t)cap.U, (uint64_t)cap.l2bytes, (uint64_t)cap.tiles,
+                       (uint64_t)cap.P,
                        (uint64_t)(uintptr_t)d_plan, (uint64_t)(uintptr_t)kalt,
                        (uint64_t)(uintptr_t)valt, (uint64_t)(uintptr_t)cnt, (uint64_t)(uintptr_t)useg,
                        (uint64_t)(uintptr_t)sortmp, (uint64_t)(uintptr_t)l2tmp,
@@ -594,7 +594,7 @@ int run_batch(gpv_ctx *ctx, int n, const float *const *d_tris, const int64_t *T,
       launch_expand(bdp, wpre, s);
       mark(6);
       if (any_l2) {
-        count_sort_pairs(bdp, nullptr, cap.tiles, keys, vals, wpre + words, cap.U, pair_cap, cnt,
+        count_sort_pairs(bdp, nullptr, cap.tiles, keys, vals, wpre + words, cap.U, cap.P, cnt,
                          useg, kalt, valt, wtot + 1, sortmp, s);
         mark(7);
         launch_level2(bdp, kalt, valt, useg, cap.U, l2tmp, warp_words, ctx->num_sms, s,
@@ -979,6 +979,7 @@ int run_batch(gpv_ctx *ctx, int n, const float *const *d_tris, const int64_t *T,
     ctx->og_caps.U = ub + ub / 64 + 64;
     ctx->og_caps.l2bytes = l2bytes + l2bytes / 64 + 4096;
     ctx->og_caps.tiles = ntiles + ntiles / 64 + 4;
+    ctx->og_caps.P = P2 + P2 / 64 + 1024;
   }
   take_host_times();
   return GPV_OK;

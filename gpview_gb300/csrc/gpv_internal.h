@@ -181,7 +181,7 @@ void launch_slab_offsets(const uint32_t *wpre, const uint32_t *wtot, int64_t wor
 // (u_base, pair_base, stile_base, and the bindex and l2 slices of the given result arenas) and
 // the DevPlan, checked against the capacities the second half was recorded with.  level2_mode is
 // GPV_LEVEL2_*; the automatic choice is the host's level2_queue_pays, evaluated on the device.
-struct PlanCaps { int64_t B, U, l2bytes, tiles, P; };
+struct PlanCaps { int64_t B, U, l2bytes, tiles, P; };  // boundary, sorted, Level2 bytes, tiles, pairs
 void launch_plan(const BatchDev &bd, MeshDesc *d_md, int32_t *bindex, uint8_t *l2,
                  const PlanCaps &caps, int level2_mode, DevPlan *plan, cudaStream_t s);
 // Device-side per-mesh pair segments (emit_base, pair_cap, keys, vals) from prep's sat1 counts.
