@@ -438,9 +438,11 @@ __global__ void __launch_bounds__(kPrefixWarps * 32) k_stencil_prefix(
 // otherwise each item lane does its own slab work.  FQ (ray fill): the (triangle, sub-column)
 // items passing u/v are queued the same way before their per-voxel work.
 template <bool ST, bool QUEUE, bool FQ>
-// Six blocks per SM for the queued organisation (80 registers); seven for the per-lane one
-// (72), measured 1.5-3% faster there (the 4096-mesh batch, a 4^3 Level2 grid).
-__global__ void __launch_bounds__(kWarps * 32, QUEUE ? 6 : 7) k_level2c(
+// Six blocks per SM for the queued organisation (80 registers); five with the queued fill (96
+// registers, no spills: torus262k 0.535 -> 0.526 ms, a 16k sphere at 4^3 0.136 -> 0.130 ms, while
+// five blocks made star1310k, which keeps the inline fill, 3.6% slower); seven for the per-lane
+// organisation (72), measured 1.5-3% faster there (the 4096-mesh batch, a 4^3 Level2 grid).
+__global__ void __launch_bounds__(kWarps * 32, QUEUE ? (FQ ? 5 : 6) : 7) k_level2c(
     BatchDev bd, const uint32_t *__restrict__ keys, const uint32_t *__restrict__ vals,
     const uint32_t *__restrict__ useg, const uint32_t *__restrict__ cflag,
     const uint32_t *__restrict__ cord, const uint32_t *__restrict__ colhead,
