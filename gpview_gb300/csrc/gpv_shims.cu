@@ -24,6 +24,7 @@
 #include <cstdio>
 #include <cstring>
 #include <mutex>
+#include <thread>
 #include <vector>
 
 #include "gpv_internal.h"
@@ -235,6 +236,33 @@ __device__ __forceinline__ void face_normal(const float *V, float n[3]) {
   }
 }
 
+// The SAT's z-invariant axes (sat_col) with the box x and y axes first.  The result is the same
+// conjunction of the same axis tests, each evaluated with the same operations, so it is
+// identical; a voxel's list is tested against every sub-column of the voxel, and most
+// (triangle, sub-column) pairs already fail the box axes.
+__device__ __forceinline__ bool box_range_fails(float a, float b, float c, float h) {
+  float mn = a, mx = a;
+  if (b < mn) mn = b;
+  if (b > mx) mx = b;
+  if (c < mn) mn = c;
+  if (c > mx) mx = c;
+  return mn > h || mx < -h;
+}
+__device__ __forceinline__ bool sat_col_box_first(const float *V, float cx, float cy,
+                                                  const float h[3], SatCol &s) {
+  s.v0x = fs(V[0], cx); s.v1x = fs(V[3], cx); s.v2x = fs(V[6], cx);
+  if (box_range_fails(s.v0x, s.v1x, s.v2x, h[0])) return false;
+  s.v0y = fs(V[1], cy); s.v1y = fs(V[4], cy); s.v2y = fs(V[7], cy);
+  if (box_range_fails(s.v0y, s.v1y, s.v2y, h[1])) return false;
+  return sat_col(V, cx, cy, h, s);
+}
+// The z-dependent part (sat_z) with the box z axis first, identical for the same reason.
+__device__ __forceinline__ bool sat_z_box_first(const SatCol &s, const float *V, float cz,
+                                                const float h[3]) {
+  if (box_range_fails(fs(V[2], cz), fs(V[5], cz), fs(V[8], cz), h[2])) return false;
+  return sat_z(s, V, cz, h);
+}
+
 // CUDAClassifyTessellationLevel2Kernel (.cu:403-448), one thread per (boundary voxel,
 // sub-column) instead of per cell: the SAT's z-invariant axes run once per (triangle,
 // sub-column) and the z-dependent part per cell (the split is exact: the test is the conjunction
@@ -262,11 +290,11 @@ __global__ void k_shim_level2_sat(const float *__restrict__ tris, float *__restr
     float V[9];
     for (int j = 0; j < 9; ++j) V[j] = tris[9 * (size_t)t + j];
     SatCol sc;
-    if (!sat_col(V, cx, cy, h, sc)) continue;
+    if (!sat_col_box_first(V, cx, cy, h, sc)) continue;
     bool have_fn = false;
     float fn[3];
     for (int r = 0; r < n2.z; ++r) {
-      if (!sat_z(sc, V, cz[r], h)) continue;
+      if (!sat_z_box_first(sc, V, cz[r], h)) continue;
       if (!have_fn) {
         face_normal(V, fn);
         have_fn = true;
@@ -281,16 +309,48 @@ __global__ void k_shim_level2_sat(const float *__restrict__ tris, float *__restr
   }
 }
 
+// End of the x/y-column lists (the largest xyTriFlatIndex + xyTriCount over the columns).
+__global__ void k_shim_list_end(const int *__restrict__ cnt, const int *__restrict__ index,
+                                int ncols, int *__restrict__ end) {
+  int e = 0;
+  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < ncols; c += gridDim.x * blockDim.x)
+    if (cnt[c] > 0) e = max(e, index[c] + cnt[c]);
+  e = __reduce_max_sync(0xffffffffu, e);
+  if ((threadIdx.x & 31u) == 0 && e) atomicMax(end, e);
+}
+
+// The +z ray test's per-triangle constants (RayTri: v1, the edges, 1/det and the |det| test) of
+// every entry of the x/y-column lists, once per entry instead of once per (entry, sub-column):
+// three float4 per entry, the w of the second holding the det test.  One warp per column walks
+// the column's own entries, so only entries a column references are read (as the fill does).
+__global__ void k_shim_ray_entries(const float *__restrict__ tris, const int *__restrict__ cnt,
+                                   const int *__restrict__ index, const int *__restrict__ flat,
+                                   int ncols, float thr, float4 *__restrict__ out) {
+  const int64_t c = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (c >= ncols) return;
+  const int n = cnt[c], f0 = index[c];
+  for (int k = (int)(threadIdx.x & 31u); k < n; k += 32) {
+    const int64_t e = (int64_t)f0 + k;
+    const int t = flat[e];
+    float V[9];
+    for (int j = 0; j < 9; ++j) V[j] = tris[9 * (size_t)t + j];
+    RayTri rt;
+    ray_tri(V, thr, rt);
+    out[3 * e + 0] = make_float4(rt.v1x, rt.v1y, rt.v1z, rt.inv_det);
+    out[3 * e + 1] = make_float4(rt.e1x, rt.e1y, rt.e1z, rt.ok ? 1.f : 0.f);
+    out[3 * e + 2] = make_float4(rt.e2x, rt.e2y, rt.e2z, 0.f);
+  }
+}
+
 // CUDAClassifyInOutLevel2Kernel (.cu:450-504), one thread per (boundary voxel, sub-column)
 // instead of per cell: the ray test's u/v part depends only on the origin's x and y, so it runs
 // once per (triangle, sub-column), and t per cell; the +z parity of every cell of the sub-column
 // against the x/y-column list is kept in one bit each.  Origins: (2p+1)*ext2 + mid - ext1 in
 // float, left to right, as the reference kernel forms them.
-__global__ void k_shim_level2_fill(const float *__restrict__ tris, float *__restrict__ l2,
+__global__ void k_shim_level2_fill(const float4 *__restrict__ ray, float *__restrict__ l2,
                                    const float *__restrict__ mid, const int *__restrict__ l2index,
                                    const int *__restrict__ xycnt, const int *__restrict__ xyIndex,
-                                   const int *__restrict__ xyflat, int B, int3 nd, int3 n2,
-                                   float3 e1, float3 e2, float thr) {
+                                   int B, int3 nd, int3 n2, float3 e1, float3 e2, float thr) {
   const int64_t gid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const int ncol2 = n2.x * n2.y, cells = ncol2 * n2.z;
   if (gid >= (int64_t)B * ncol2) return;
@@ -304,12 +364,14 @@ __global__ void k_shim_level2_fill(const float *__restrict__ tris, float *__rest
   uint32_t par = 0;  // one bit per cell (n2z <= 32)
   const int n = xycnt[xy], f0 = xyIndex[xy];
   for (int k = 0; k < n; ++k) {
-    const int t = xyflat[f0 + k];
-    float V[9];
-    for (int j = 0; j < 9; ++j) V[j] = tris[9 * (size_t)t + j];
+    const float4 *re = ray + 3 * (size_t)(f0 + k);
+    const float4 a = re[0], b1 = re[1], b2 = re[2];
+    if (b1.w == 0.f) continue;  // |det| test failed
     RayTri rt;
-    ray_tri(V, thr, rt);
-    if (!rt.ok) continue;
+    rt.v1x = a.x; rt.v1y = a.y; rt.v1z = a.z; rt.inv_det = a.w;
+    rt.e1x = b1.x; rt.e1y = b1.y; rt.e1z = b1.z;
+    rt.e2x = b2.x; rt.e2y = b2.y; rt.e2z = b2.z;
+    rt.ok = true;
     RayCol rc;
     if (!ray_col(rt, ox, oy, rc)) continue;
     for (int r = 0; r < n2.z; ++r) {
@@ -477,12 +539,32 @@ int CUDAClassifyTessellationLevel2(float *trianglesCUDAData, float *level2InOutC
   const float e1[3] = {boxExtentsLevel1.x, boxExtentsLevel1.y, boxExtentsLevel1.z};
   const float e2[3] = {boxExtentsLevel2.x, boxExtentsLevel2.y, boxExtentsLevel2.z};
   const int n2[3] = {numDiv2.x, numDiv2.y, numDiv2.z};
-  for (int b = 0; b < numBoundary; ++b)
-    for (int a = 0, o = 0; a < 3; o += n2[a], ++a) {
-      const float g2 = e2[a] * 2.0f;  // gridSize2 (exact: ext2 = gridSize2 / 2)
-      for (int p = 0; p < n2[a]; ++p)
-        cen[(size_t)b * nn + o + p] = (float)((p + 0.5) * g2 + (double)mid[3 * (size_t)b + a] - e1[a]);
-    }
+  // (p + 0.5) * gridSize2 in double, per axis and cell (the same for every voxel)
+  std::vector<double> off(nn);
+  for (int a = 0, o = 0; a < 3; o += n2[a], ++a) {
+    const float g2 = e2[a] * 2.0f;  // gridSize2 (exact: ext2 = gridSize2 / 2)
+    for (int p = 0; p < n2[a]; ++p) off[o + p] = (p + 0.5) * g2;
+  }
+  auto centres = [&](int b0, int b1) {
+    for (int b = b0; b < b1; ++b)
+      for (int a = 0, o = 0; a < 3; o += n2[a], ++a) {
+        const double m = (double)mid[3 * (size_t)b + a];
+        for (int p = 0; p < n2[a]; ++p)
+          cen[(size_t)b * nn + o + p] = (float)(off[o + p] + m - e1[a]);
+      }
+  };
+  // large calls on up to 16 host threads (110k boundary voxels at 8^3: ~2.6 M centres)
+  const int hw = (int)std::max(1u, std::thread::hardware_concurrency());
+  const int nt = std::min(std::min(hw, 16), std::max(1, numBoundary / 4096));
+  if (nt <= 1) {
+    centres(0, numBoundary);
+  } else {
+    std::vector<std::thread> th;
+    for (int k = 0; k < nt; ++k)
+      th.emplace_back(centres, (int)((int64_t)numBoundary * k / nt),
+                      (int)((int64_t)numBoundary * (k + 1) / nt));
+    for (std::thread &x : th) x.join();
+  }
   float *d_cen = static_cast<float *>(g_shim.dev);
   cudaMemcpyAsync(d_cen, cen, ncen * sizeof(float), cudaMemcpyHostToDevice, 0);
   const int64_t n = (int64_t)numBoundary * numDiv2.x * numDiv2.y;  // a thread per sub-column
@@ -503,12 +585,29 @@ int CUDAClassifyInOutLevel2(float *trianglesCUDAData, float *level2InOutCUDAData
   const int cells = numDiv2.x * numDiv2.y * numDiv2.z;
   if (numBoundary <= 0 || cells <= 0) return 1;
   if (numDiv2.z > 32) return 1;  // one parity bit per cell of a sub-column
+  std::lock_guard<std::mutex> lk(g_shim.mu);
+  // the end of the column lists, then the ray constants of every list entry (workspace)
+  const int ncols = numDiv.x * numDiv.y;
+  if (ncols <= 0 || !shim_reserve(256)) return 1;
+  int *d_end = static_cast<int *>(g_shim.dev);
+  cudaMemsetAsync(d_end, 0, sizeof(int), 0);
+  k_shim_list_end<<<std::min((ncols + 255) / 256, 4 * shim_num_sms()), 256>>>(
+      xyTriCountCUDAData, xyTriFlatIndexCUDAData, ncols, d_end);
+  int nE = 0;
+  if (cudaMemcpy(&nE, d_end, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess) return 1;
+  if (!shim_reserve(256 + 48 * (size_t)std::max(nE, 1))) return 1;
+  float4 *ray = reinterpret_cast<float4 *>(static_cast<char *>(g_shim.dev) + 256);
+  const float thr = eps_threshold();
+  if (nE > 0)
+    k_shim_ray_entries<<<(unsigned)((ncols + 7) / 8), 256>>>(
+        trianglesCUDAData, xyTriCountCUDAData, xyTriFlatIndexCUDAData, xyTriFlatCUDAData, ncols,
+        thr, ray);
   const int64_t n = (int64_t)numBoundary * numDiv2.x * numDiv2.y;  // a thread per sub-column
   k_shim_level2_fill<<<(unsigned)((n + 127) / 128), 128>>>(
-      trianglesCUDAData, level2InOutCUDAData, level1MidPointCUDAData, level2IndexCUDAData,
-      xyTriCountCUDAData, xyTriFlatIndexCUDAData, xyTriFlatCUDAData, numBoundary, numDiv, numDiv2,
-      boxExtentsLevel1, boxExtentsLevel2, eps_threshold());
-  count_launch();
+      ray, level2InOutCUDAData, level1MidPointCUDAData, level2IndexCUDAData, xyTriCountCUDAData,
+      xyTriFlatIndexCUDAData, numBoundary, numDiv, numDiv2, boxExtentsLevel1, boxExtentsLevel2, thr);
+  count_launch(nE > 0 ? 3 : 2);
+  cudaStreamSynchronize(0);  // the workspace is reused by the next call
   return 1;
 }
 
