@@ -552,7 +552,9 @@ int run_batch(gpv_ctx *ctx, int n, const float *const *d_tris, const int64_t *T,
   const uint64_t key = call_key(n, T, specs);
   const bool og_path = ctx->graphs && ctx->one_graph && !sink && nmode == 0 && !stencil &&
                        res_hier[n] == 0;
-  if (og_path && ctx->og_key == key && ctx->og_caps.B > 0) {
+  const bool og_skip = ctx->og_skip;  // (one-shot: the re-run of a call that did not fit)
+  ctx->og_skip = false;
+  if (og_path && !og_skip && ctx->og_key == key && ctx->og_caps.B > 0) {
     PlanCaps cap = ctx->og_caps;
     if (ctx->debug_og_cap > 0) {  // failure-detection hook: a boundary capacity that overflows
       cap.B = ctx->debug_og_cap;
@@ -634,7 +636,8 @@ int run_batch(gpv_ctx *ctx, int n, const float *const *d_tris, const int64_t *T,
         if (raised) return fail_all(GPV_ERR_DEVICE, "device status raised in Level1");
         ctx->og_replans++;
       }
-      ctx->og_key = 0;
+      // the re-run takes two phases (the exact sizes) and records them, merged with these
+      ctx->og_skip = true;
       fail_all(GPV_OK, "");
       ctx->err.clear();
       return run_batch(ctx, n, d_tris, T, specs, out, s);
@@ -973,13 +976,23 @@ int run_batch(gpv_ctx *ctx, int n, const float *const *d_tris, const int64_t *T,
   }
   if (og_path) {
     // this call's sizes, for a next call with the same meshes and grids as one graph (a little
-    // room for triangles that move between calls)
+    // room for triangles that move between calls; with the key unchanged, the larger of the old
+    // and new sizes, so that two meshes sharing a key do not re-run each other's calls)
+    PlanCaps c;
+    c.B = Btot + Btot / 64 + 64;
+    c.U = ub + ub / 64 + 64;
+    c.l2bytes = l2bytes + l2bytes / 64 + 4096;
+    c.tiles = ntiles + ntiles / 64 + 4;
+    c.P = P2 + P2 / 64 + 1024;
+    if (ctx->og_key == key) {
+      c.B = std::max(c.B, ctx->og_caps.B);
+      c.U = std::max(c.U, ctx->og_caps.U);
+      c.l2bytes = std::max(c.l2bytes, ctx->og_caps.l2bytes);
+      c.tiles = std::max(c.tiles, ctx->og_caps.tiles);
+      c.P = std::max(c.P, ctx->og_caps.P);
+    }
     ctx->og_key = key;
-    ctx->og_caps.B = Btot + Btot / 64 + 64;
-    ctx->og_caps.U = ub + ub / 64 + 64;
-    ctx->og_caps.l2bytes = l2bytes + l2bytes / 64 + 4096;
-    ctx->og_caps.tiles = ntiles + ntiles / 64 + 4;
-    ctx->og_caps.P = P2 + P2 / 64 + 1024;
+    ctx->og_caps = c;
   }
   take_host_times();
   return GPV_OK;

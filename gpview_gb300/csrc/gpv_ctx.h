@@ -75,6 +75,7 @@ struct gpv_ctx {
   gpv::PlanCaps og_caps = {};
   int64_t og_calls = 0, og_replans = 0;
   int64_t debug_og_cap = 0;            // the next one-graph call's boundary capacity (one-shot)
+  bool og_skip = false;                // the next call runs as two graphs (a re-run, one-shot)
   int normals = 0;                     // GPV_NORMALS_* for the next voxelizations
   bool hierarchy = false;              // build the voxel box hierarchy
   int fill = GPV_FILL_RAY;             // inside fill of both levels
