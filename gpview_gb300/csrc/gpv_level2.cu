@@ -339,42 +339,42 @@ __device__ __forceinline__ uint32_t column_bits(const uint32_t *m, int off, int 
 // A triangle whose topmost record in a Level1 column lies below voxel v is not recorded in any
 // voxel from v up, so within the column's x/y extent it lies below v's bottom face (up to the
 // SAT's rounding, far less than the half Level2 cell to v's first clip height): every covered
-// sample keeps it in every slice of v and above.  One warp per column walks the column's records
-// in z order once, XOR-ing each triangle's sample coverage into a running mask, and stores the
-// mask reached at each boundary voxel; a Level2 chunk then starts from its first voxel's mask and
-// draws only the triangles recorded from that voxel up (otherwise every chunk of a tall column
-// would draw all the triangles below it again).
+// sample keeps it in every slice of v and above.  A Level2 chunk therefore starts from the XOR of
+// the sample coverage of the column's triangles whose topmost record lies below its first voxel,
+// and draws only the triangles recorded from that voxel up (otherwise every chunk of a tall
+// column would draw all the triangles below it again).  Two passes, since the XOR is order-free:
+//   k_stencil_segment  one warp per work item: the coverage XOR of the triangles whose topmost
+//                      record lies in the item's own voxels (items that end their column skip it),
+//                      stored at the item's first voxel;
+//   k_stencil_scan     one warp per column with more than one item: those masks turned in place
+//                      into exclusive XOR prefixes, the mask each item starts from.
+// (One warp per column walking all of its records was latency-bound on the few long columns:
+// 186 us on torus262k at 22% warps active.)
 constexpr int kPrefixWarps = 4;
 constexpr int kPrefixMaskWords = 128;  // 4 * 32 * 32 samples / 32
 
-__global__ void __launch_bounds__(kPrefixWarps * 32) k_stencil_prefix(
+__global__ void __launch_bounds__(kPrefixWarps * 32) k_stencil_segment(
     BatchDev bd, const uint32_t *__restrict__ keys, const uint32_t *__restrict__ vals,
     const uint32_t *__restrict__ useg, const uint32_t *__restrict__ cflag,
     const uint32_t *__restrict__ cord, const uint32_t *__restrict__ colhead,
-    const uint32_t *__restrict__ iflag, int64_t B) {
+    const uint32_t *__restrict__ istart, const uint32_t *__restrict__ nitems, int64_t B) {
   __shared__ uint32_t s_mask[kPrefixWarps][kPrefixMaskWords];
   __shared__ StTri s_t[kPrefixWarps][32];
   __shared__ uint32_t s_pre[kPrefixWarps][32];
   const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
-  const int64_t c = (int64_t)blockIdx.x * kPrefixWarps + warp;
-  const int64_t ncols = (int64_t)cord[B - 1] + cflag[B - 1];
-  if (c >= ncols) return;
-  const uint32_t u0 = colhead[c], u1 = colhead[c + 1];
-  const MeshDesc &d = bd.md[mesh_of_u(bd.md, bd.nmesh, u0)];
+  const int64_t it = (int64_t)blockIdx.x * kPrefixWarps + warp;
+  const int64_t NI = (int64_t)*nitems;
+  if (it >= NI) return;
+  const uint32_t ua = istart[it];
+  const uint32_t ue = it + 1 < NI ? istart[it + 1] : (uint32_t)B;  // the item's voxels [ua, ue)
+  if (ue >= colhead[cord[ua] + cflag[ua]]) return;  // the column's last item: no item reads it
+  const MeshDesc &d = bd.md[mesh_of_u(bd.md, bd.nmesh, ua)];
   if (!d.has_l2) return;
-  // only the column's later work-item starts read a mask: a one-item column needs none, and
-  // the records from the last start up are not needed
-  uint32_t ulast = u0;
-  for (uint32_t u = u0 + 1 + lane; u < u1; u += 32)
-    if (iflag[u]) ulast = max(ulast, u);
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) ulast = max(ulast, __shfl_xor_sync(FULL, ulast, o));
-  if (ulast == u0) return;
   const GridDev &g = d.g;
   const int n2x = g.n2[0], n2y = g.n2[1], nz = g.n[2], nx = g.n[0];
   const int SW = 2 * n2x, SH = 2 * n2y;
   const int FWS = (4 * n2x * n2y + 31) >> 5;
-  const uint32_t col = keys[useg[u0]] / (uint32_t)nz;
+  const uint32_t col = keys[useg[ua]] / (uint32_t)nz;
   const int ci = (int)(col % (uint32_t)nx), cj = (int)(col / (uint32_t)nx);
   const float lx = fa(fm((float)ci, g.g[0]), g.bmin[0]), hx = fa(lx, g.g[0]);
   const float ly = fa(fm((float)cj, g.g[1]), g.bmin[1]), hy = fa(ly, g.g[1]);
@@ -382,51 +382,83 @@ __global__ void __launch_bounds__(kPrefixWarps * 32) k_stencil_prefix(
   for (int w = lane; w < FWS; w += 32) mask[w] = 0;
   __syncwarp();
   const float4 *__restrict__ ptri = d.ptri;
-  for (uint32_t u = u0; u <= ulast; ++u) {
-    if (u == u0 || iflag[u]) {
-      uint32_t *out = bd.stp + (size_t)u * bd.stp_words;
-      for (int w = lane; w < FWS; w += 32) out[w] = mask[w];
+  const uint32_t e0 = useg[ua], e1 = useg[ue];
+  for (uint32_t b0 = e0; b0 < e1; b0 += 32) {
+    const uint32_t e = b0 + lane;
+    const uint32_t vv = e < e1 ? vals[e] : 0u;
+    uint32_t cnt = 0;
+    if (vv & 0x80000000u) {  // the triangle's topmost record in the column
+      const uint32_t t = vv & 0x7fffffffu;
+      const float4 a0 = __ldg(ptri + 3 * (size_t)t), a1 = __ldg(ptri + 3 * (size_t)t + 1),
+                   a2 = __ldg(ptri + 3 * (size_t)t + 2);
+      const float V[9] = {a0.x, a0.y, a0.z, a1.x, a1.y, a1.z, a2.x, a2.y, a2.z};
+      StTri st;
+      if (st_setup(V, lx, hx, ly, hy, SW, SH, st)) {
+        s_t[warp][lane] = st;
+        cnt = (uint32_t)((st.sx1 - st.sx0 + 1) * (st.sy1 - st.sy0 + 1));
+      }
     }
-    if (u == ulast) break;
-    const uint32_t e0 = useg[u], e1 = useg[u + 1];
-    for (uint32_t b0 = e0; b0 < e1; b0 += 32) {
-      const uint32_t e = b0 + lane;
-      const uint32_t vv = e < e1 ? vals[e] : 0u;
-      uint32_t cnt = 0;
-      if (vv & 0x80000000u) {  // the triangle's topmost record in the column
-        const uint32_t t = vv & 0x7fffffffu;
-        const float4 a0 = __ldg(ptri + 3 * (size_t)t), a1 = __ldg(ptri + 3 * (size_t)t + 1),
-                     a2 = __ldg(ptri + 3 * (size_t)t + 2);
-        const float V[9] = {a0.x, a0.y, a0.z, a1.x, a1.y, a1.z, a2.x, a2.y, a2.z};
-        StTri st;
-        if (st_setup(V, lx, hx, ly, hy, SW, SH, st)) {
-          s_t[warp][lane] = st;
-          cnt = (uint32_t)((st.sx1 - st.sx0 + 1) * (st.sy1 - st.sy0 + 1));
-        }
-      }
-      uint32_t inc = cnt;
+    uint32_t inc = cnt;
 #pragma unroll
-      for (int o = 1; o < 32; o <<= 1) {
-        const uint32_t x = __shfl_up_sync(FULL, inc, o);
-        if (lane >= (unsigned)o) inc += x;
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t x = __shfl_up_sync(FULL, inc, o);
+      if (lane >= (unsigned)o) inc += x;
+    }
+    s_pre[warp][lane] = inc - cnt;
+    const uint32_t tot = __shfl_sync(FULL, inc, 31);
+    __syncwarp();
+    for (uint32_t w = lane; w < tot; w += 32) {
+      const int tl = batch_search(s_pre[warp], w);
+      const StTri &st = s_t[warp][tl];
+      const uint32_t loc = w - s_pre[warp][tl];
+      const uint32_t nsx = (uint32_t)(st.sx1 - st.sx0 + 1);
+      const uint32_t row = loc / nsx;
+      const int sx = st.sx0 + (int)(loc - row * nsx), sy = st.sy0 + (int)row;
+      float zs;
+      if (st_cover(st, sx, sy, zs)) {
+        const int sidx = sy * SW + sx;
+        atomicXor(&mask[sidx >> 5], 1u << (sidx & 31));
       }
-      s_pre[warp][lane] = inc - cnt;
-      const uint32_t tot = __shfl_sync(FULL, inc, 31);
-      __syncwarp();
-      for (uint32_t w = lane; w < tot; w += 32) {
-        const int tl = batch_search(s_pre[warp], w);
-        const StTri &st = s_t[warp][tl];
-        const uint32_t loc = w - s_pre[warp][tl];
-        const uint32_t nsx = (uint32_t)(st.sx1 - st.sx0 + 1);
-        const uint32_t row = loc / nsx;
-        const int sx = st.sx0 + (int)(loc - row * nsx), sy = st.sy0 + (int)row;
-        float zs;
-        if (st_cover(st, sx, sy, zs)) {
-          const int sidx = sy * SW + sx;
-          atomicXor(&mask[sidx >> 5], 1u << (sidx & 31));
+    }
+    __syncwarp();
+  }
+  uint32_t *out = bd.stp + (size_t)ua * bd.stp_words;
+  for (int w = lane; w < FWS; w += 32) out[w] = mask[w];
+}
+
+__global__ void __launch_bounds__(kPrefixWarps * 32) k_stencil_scan(
+    BatchDev bd, const uint32_t *__restrict__ cflag, const uint32_t *__restrict__ cord,
+    const uint32_t *__restrict__ colhead, const uint32_t *__restrict__ iflag, int64_t B) {
+  const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+  const int64_t c = (int64_t)blockIdx.x * kPrefixWarps + warp;
+  const int64_t ncols = (int64_t)cord[B - 1] + cflag[B - 1];
+  if (c >= ncols) return;
+  const uint32_t u0 = colhead[c], u1 = colhead[c + 1];
+  const MeshDesc &d = bd.md[mesh_of_u(bd.md, bd.nmesh, u0)];
+  if (!d.has_l2) return;
+  // a one-item column has nothing to scan
+  bool more = false;
+  for (uint32_t u = u0 + 1 + lane; u < u1 && !more; u += 32) more = iflag[u] != 0u;
+  if (!__any_sync(FULL, more)) return;
+  const int FWS = (4 * d.g.n2[0] * d.g.n2[1] + 31) >> 5;  // <= kPrefixMaskWords
+  uint32_t acc[kPrefixMaskWords / 32] = {};
+  // the column's item starts 32 voxels at a time (one flag load per lane), then each in order
+  for (uint32_t base = u0; base < u1; base += 32) {
+    const uint32_t uu = base + lane;
+    uint32_t starts = __ballot_sync(FULL, uu < u1 && (uu == u0 || iflag[uu] != 0u));
+    while (starts) {
+      const uint32_t u = base + (uint32_t)(__ffs(starts) - 1);
+      starts &= starts - 1u;
+      uint32_t *m = bd.stp + (size_t)u * bd.stp_words;
+#pragma unroll
+      for (int k = 0; k < kPrefixMaskWords / 32; ++k) {
+        const int w = (int)lane + 32 * k;
+        if (w < FWS) {
+          const uint32_t seg = m[w];  // (the column's last item wrote none: its value goes unused)
+          m[w] = acc[k];
+          acc[k] ^= seg;
         }
       }
-      __syncwarp();
     }
   }
 }
@@ -1232,9 +1264,11 @@ void launch_level2(const BatchDev &bd, const uint32_t *keys, const uint32_t *val
   k_itemstarts<<<nb, 256, 0, s>>>(bd, iflag, iord, B, istart, nitems);
   count_launch(4);
   if (bd.fill == GPV_FILL_STENCIL && bd.stp) {
-    k_stencil_prefix<<<(unsigned)((B + kPrefixWarps - 1) / kPrefixWarps), kPrefixWarps * 32, 0, s>>>(
-        bd, keys, vals, useg, cflag, cord, colhead, iflag, B);
-    count_launch();
+    const unsigned nbp = (unsigned)((B + kPrefixWarps - 1) / kPrefixWarps);  // items, columns <= B
+    k_stencil_segment<<<nbp, kPrefixWarps * 32, 0, s>>>(bd, keys, vals, useg, cflag, cord, colhead,
+                                                         istart, nitems, B);
+    k_stencil_scan<<<nbp, kPrefixWarps * 32, 0, s>>>(bd, cflag, cord, colhead, iflag, B);
+    count_launch(2);
   }
   const size_t smem = level2_smem_bytes(warp_words);
   const bool st = bd.fill == GPV_FILL_STENCIL;

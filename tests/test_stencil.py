@@ -247,6 +247,22 @@ def test_gpu_stencil_small_cases(ctx, case):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("cap", [1, 2, 5])
+def test_gpu_stencil_short_chunks(ctx, cap):
+    """Level2 work items of 1, 2 and 5 boundary voxels split every column into many items: each
+    starts from the sample-coverage XOR of the column's triangles recorded only below it (the
+    segment masks and their per-column prefix)."""
+    import workloads as W
+
+    tris, spec = W.make(W.C1)
+    ctx.set_level2_chunk(cap)
+    try:
+        _check_stencil(ctx, tris, spec)
+    finally:
+        ctx.set_level2_chunk(16)
+
+
+@pytest.mark.gpu
 def test_gpu_stencil_torus_nonuniform(ctx):
     import gpview_gb300 as gpv
 
